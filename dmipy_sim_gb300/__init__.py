@@ -1,0 +1,24 @@
+"""dmipy_sim_gb300 — GB300-native Monte-Carlo diffusion-MRI forward walk.
+
+Drop-in for dmipy-sim's ``simulate`` / ``simulate_cpmg`` / ``simulate_trajectories`` /
+``replay`` path: the same Waveform and geometry objects and signatures, with the per-walker step
+loop executed by hand-written sm_103a CUDA kernels (``libdmsim.so``, C ABI in include/dmsim.h).
+"""
+from .constants import GAMMA, DEFAULT_SLEW_RATE
+from .waveforms import (Waveform, pgse, pgste, ogse, cpmg, calc_b, calc_btensor, set_b,
+                        rotate_waveform, tile_waveform)
+from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, pack_cylinders,
+                         PackedCylinders, pack_spheres, PackedSpheres)
+from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
+                   permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
+                   fused_sub_steps)
+from .trajectories import replay
+
+__all__ = [
+    "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
+    "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "Geometry", "FreeDiffusion",
+    "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres",
+    "simulate", "simulate_cpmg", "simulate_trajectories", "replay", "run_walk", "WalkResult",
+    "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
+    "fused_sub_steps",
+]

@@ -1,0 +1,118 @@
+"""ctypes binding of ``libdmsim.so`` (the C ABI declared in ``include/dmsim.h``).
+
+The structures below mirror the C structs field for field.  Device memory is owned by PyTorch;
+only raw pointers cross the boundary.  There is no CPU fallback: a missing library or a missing
+GPU raises.
+"""
+import ctypes as C
+import os
+from pathlib import Path
+
+import torch
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libdmsim.so"
+
+DMSIM_ABI_VERSION = 1
+
+GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
+WALL_REFLECT, WALL_RELAX, WALL_PERMEATE = range(3)
+
+STATUS_NAMES = ("nonfinite", "clamped", "init_fail", "bounce_budget", "escape_reject",
+                "wait_timeout", "graze_fp64", "transmit")
+STATUS_WORDS = len(STATUS_NAMES)
+
+# Symbols every build of the library exports (the C ABI of include/dmsim.h).
+EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "dmsim_walk",
+            "dmsim_replay_workspace_bytes", "dmsim_replay")
+
+
+class Geometry(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("wall_mode", C.c_int32),
+        ("radius", C.c_float), ("eps_detect", C.c_float), ("nudge", C.c_float),
+        ("kappa_over_D", C.c_float), ("rho_over_D", C.c_float), ("L", C.c_float),
+        ("n_objects", C.c_int32), ("grid_n", C.c_int32), ("cell_h", C.c_float),
+        ("reach", C.c_float), ("n_cand", C.c_int32), ("pad0", C.c_int32),
+        ("cell_start", C.c_void_p), ("cand", C.c_void_p), ("cand_obj", C.c_void_p),
+        ("n_tri", C.c_int32), ("mesh_dims", C.c_int32 * 3), ("periodic", C.c_int32 * 3),
+        ("max_bounces", C.c_int32), ("grid_min", C.c_float * 3), ("mesh_cell", C.c_float),
+        ("vmin", C.c_float * 3), ("box", C.c_float * 3), ("mesh_eps", C.c_float),
+        ("mesh_nudge", C.c_float), ("mesh_graze", C.c_float), ("rho_mult_intra", C.c_float),
+        ("rho_mult_extra", C.c_float), ("kappa_mult_out", C.c_float),
+        ("kappa_mult_in", C.c_float), ("reject_escape", C.c_int32),
+        ("tri", C.c_void_p), ("tri_vn", C.c_void_p), ("mesh_cell_start", C.c_void_p),
+        ("mesh_cell_tri", C.c_void_p),
+    ]
+
+
+class WalkParams(C.Structure):
+    _fields_ = [
+        ("n_walkers", C.c_int64), ("walker_offset", C.c_int64), ("seed", C.c_uint64),
+        ("n_t", C.c_int32), ("n_meas", C.c_int32), ("sub_steps", C.c_int32),
+        ("phase_per_substep", C.c_int32), ("step_length", C.c_float), ("gamma_dt", C.c_float),
+        ("t2_decay", C.c_float), ("t1_decay", C.c_float), ("has_weight", C.c_int32),
+        ("n_echo", C.c_int32), ("echo_idx", C.POINTER(C.c_int32)), ("G", C.c_void_p),
+        ("chi", C.c_void_p), ("r0", C.c_void_p),
+    ]
+
+
+class WalkOutputs(C.Structure):
+    _fields_ = [
+        ("sums", C.c_void_p), ("status", C.c_void_p), ("final_pos", C.c_void_p),
+        ("log_w", C.c_void_p), ("phi", C.c_void_p), ("comp0", C.c_void_p),
+        ("comp_end", C.c_void_p), ("traj", C.c_void_p), ("traj_f16", C.c_int32),
+        ("pad0", C.c_int32), ("dlog_unit", C.c_void_p), ("comp_occ", C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load():
+    """Load libdmsim.so (building it first if it is missing); raises if that is impossible."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists() or os.environ.get("DMSIM_REBUILD"):
+        from .build import build
+        build()
+    lib = C.CDLL(str(LIB_PATH))
+    lib.dmsim_version.restype = C.c_int
+    lib.dmsim_last_error.restype = C.c_char_p
+    lib.dmsim_walk_workspace_bytes.restype = C.c_size_t
+    lib.dmsim_walk_workspace_bytes.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry)]
+    lib.dmsim_walk.restype = C.c_int
+    lib.dmsim_walk.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry), C.POINTER(WalkOutputs),
+                               C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.dmsim_replay_workspace_bytes.restype = C.c_size_t
+    lib.dmsim_replay_workspace_bytes.argtypes = [C.c_int64, C.c_int32, C.c_int32]
+    lib.dmsim_replay.restype = C.c_int
+    lib.dmsim_replay.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int32, C.c_void_p,
+                                 C.c_int32, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_size_t, C.c_void_p]
+    if lib.dmsim_version() != DMSIM_ABI_VERSION:
+        raise RuntimeError(f"libdmsim ABI {lib.dmsim_version()} != {DMSIM_ABI_VERSION}")
+    _lib = lib
+    return lib
+
+
+def device():
+    """The CUDA device the walk runs on; raises when no GPU is visible (no CPU fallback)."""
+    if not torch.cuda.is_available():
+        raise RuntimeError("dmipy_sim_gb300 needs a CUDA GPU: the Monte-Carlo walk has no CPU path")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def check(rc, what):
+    if rc != 0:
+        msg = load().dmsim_last_error().decode(errors="replace")
+        raise RuntimeError(f"{what} failed (code {rc}): {msg}")
+
+
+def stream_handle():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)

@@ -1,0 +1,491 @@
+"""Simulation entry points: ``simulate``, ``simulate_cpmg``, ``simulate_trajectories``.
+
+Same signatures, routing and return conventions as dmipy-sim's core.py (simulate 193-762,
+_replay_gap 77-106, _simulate_via_replay 115-190, _simulate_in_walker_batches 765-818,
+simulate_cpmg 861-969, simulate_trajectories 972-1529), with the walk itself executed by the CUDA
+kernels of libdmsim.so (one persistent launch per call; no JAX, no CPU fallback).
+
+Engine semantics reproduced here:
+  * ``engine="replay"`` (and "auto" where the reference routes to replay): the walk uses the
+    producer's sub-step rule (step <= R/6, or R/25 when permeable; core.py:1089-1120) and the phase
+    samples the position once per waveform sample, phi = gamma*dt*sum_t G(t).r(t)
+    (trajectories.py:550-552).  The walk-once/replay split of the reference is fused into one
+    kernel pass; no trajectory is materialised.
+  * ``engine="fused"``: sub-steps from make_step_fn (physics.py:276-415: permeable R/25, surface
+    relaxivity pore/8, meshes the collision rule, otherwise 1) and the phase accumulated at every
+    sub-step with gamma*dt_sub.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import GAMMA
+
+_REPLAY_AUTO_GEOM_NAMES = frozenset({
+    "FreeDiffusion", "Box1D", "Sphere", "Cylinder", "Ellipsoid", "PackedCylinders",
+    "PackedSpheres", "Mesh",
+})
+
+
+# ------------------------------------------------------------------------------------------------
+# Sub-step rules (physics.py:15-188, core.py:1089-1120)
+# ------------------------------------------------------------------------------------------------
+def _geometry_radius(geometry):
+    """Smallest geometric radius of a geometry, or None (physics.py:15-32)."""
+    R = getattr(geometry, 'radius', None)
+    if R is None:
+        R = getattr(geometry, 'sphere_radius', None)
+    if R is None:
+        radii = getattr(geometry, '_radii_np', None)
+        if radii is not None and len(radii) > 0:
+            R = float(np.min(radii))
+    if R is None:
+        inner = getattr(geometry, '_inner_radii_np', None)
+        if inner is not None and len(inner) > 0 and np.any(inner > 0):
+            R = float(np.min(inner[inner > 0]))
+    return float(R) if R is not None else None
+
+
+def permeable_sub_steps(geometry, diffusivity, dt):
+    """Sub-steps so a permeable walk has step <= R/25 (physics.py:35-48)."""
+    R = _geometry_radius(geometry)
+    if R is None:
+        return 1
+    return max(1, int(np.ceil(dt / (R ** 2 / (3750.0 * diffusivity)))))
+
+
+def _surface_char_radius(geometry):
+    """Extra-axonal pore radius (cell area minus axons over their perimeter), else R
+    (physics.py:51-69)."""
+    outer = getattr(geometry, '_outer_radii_np', None)
+    cell = getattr(geometry, '_cell_size', None)
+    if outer is not None and cell is not None:
+        outer = np.asarray(outer, float)
+        outer = outer[outer > 0]
+        area = float(cell) ** 2 - float(np.sum(np.pi * outer ** 2))
+        perim = float(np.sum(2.0 * np.pi * outer))
+        if perim > 0 and area > 0:
+            return area / perim
+    return _geometry_radius(geometry)
+
+
+def collision_sub_steps(geometry, diffusivity, dt, frac=0.9):
+    """Sub-steps so a step cannot outrun a mesh's 27-cell candidate gather (physics.py:72-95)."""
+    cs = getattr(geometry, "cell_size", None)
+    if cs is None or not np.isfinite(cs) or cs <= 0:
+        return 1
+    L = float(np.sqrt(6.0 * float(diffusivity) * float(dt)))
+    ratio = L / (float(frac) * float(cs))
+    return int(max(1, np.ceil(ratio ** 2))) if ratio > 1.0 else 1
+
+
+def surface_sub_steps(geometry, diffusivity, dt, frac=8.0):
+    """Sub-steps so the surface-relaxivity walk has step <= pore/frac (physics.py:163-188)."""
+    g_frac = getattr(geometry, 'surface_substep_frac', None)
+    if g_frac is not None:
+        frac = g_frac
+    if not frac or frac <= 0:
+        return 1
+    Rc = _surface_char_radius(geometry)
+    if Rc is None:
+        return 1
+    return max(1, int(np.ceil(dt / ((Rc / frac) ** 2 / (6.0 * diffusivity)))))
+
+
+def replay_sub_steps(geometry, diffusivity, dt):
+    """Producer-walk sub-steps: step <= R/6 (216), or R/25 (3750) when permeable (core.py:1089-1120)."""
+    R = getattr(geometry, 'radius', None)
+    if R is None:
+        R = getattr(geometry, 'sphere_radius', None)
+    if R is None:
+        R = getattr(geometry, 'length', None)
+    if R is None:
+        radii = getattr(geometry, '_radii_np', None)
+        if radii is not None and len(radii) > 0:
+            R = float(np.min(radii))
+    if R is None:
+        inner = getattr(geometry, '_inner_radii_np', None)
+        if inner is not None and len(inner) > 0:
+            R = float(np.min(inner[inner > 0])) if np.any(inner > 0) else None
+    if R is None:
+        return 1
+    div = 3750.0 if getattr(geometry, 'permeability', None) is not None else 216.0
+    return max(1, int(np.ceil(dt / (float(R) ** 2 / (div * diffusivity)))))
+
+
+def fused_sub_steps(geometry, diffusivity, dt):
+    """The fused engine's sub-step count for this geometry (physics.py:276-415 branch order)."""
+    if getattr(geometry, 'permeability', None) is not None:
+        return permeable_sub_steps(geometry, diffusivity, dt)
+    if getattr(geometry, 'surface_relaxivity_t2', None) is not None:
+        return surface_sub_steps(geometry, diffusivity, dt)
+    return collision_sub_steps(geometry, diffusivity, dt)
+
+
+# ------------------------------------------------------------------------------------------------
+# Routing (core.py:77-112)
+# ------------------------------------------------------------------------------------------------
+def _replay_gap(geometry, *, return_positions, return_compartments, return_walker_signals,
+                diffusivity):
+    if return_positions is not False:
+        return "return_positions is a fused single-pass internal (no replay equivalent)"
+    if return_compartments is not False:
+        return "return_compartments is a fused single-pass internal (no replay equivalent)"
+    if return_walker_signals:
+        return "return_walker_signals is a fused single-pass internal (no replay equivalent)"
+    if getattr(geometry, '_is_myelinated', False):
+        return "MyelinatedCylinder uses a dedicated fused step kernel (no replay walk)"
+    if getattr(geometry, '_is_packed_myelinated', False):
+        return ("PackedMyelinatedCylinders fused single-reflection kernel is not "
+                "position-parity with the multi-bounce replay walk")
+    if getattr(geometry, 'permeability', None) is not None:
+        return ("membrane permeability is single-pass walk semantics "
+                "(fused-only; scalar replay has no exchange reservoir)")
+    if getattr(geometry, '_D_comp', None) is not None:
+        return "per-compartment diffusivity (Mesh intra/extra D) alters the walk (fused-only)"
+    if diffusivity is None:
+        return "replay needs an explicit diffusivity for the sub-step auto-tune"
+    return None
+
+
+def _replay_auto_allowed(geometry):
+    return type(geometry).__name__ in _REPLAY_AUTO_GEOM_NAMES
+
+
+# ------------------------------------------------------------------------------------------------
+# The walk call
+# ------------------------------------------------------------------------------------------------
+class WalkResult:
+    """Raw result of one device walk: FP64 ensemble sums and optional per-walker outputs."""
+
+    def __init__(self, sums, n_walkers, status, extras):
+        self.sums = sums              # (n_echo, M, 3) float64: sum w cos, sum w sin, sum (w cos)^2
+        self.n_walkers = n_walkers
+        self.status = status          # dict of anomaly counters
+        self.extras = extras          # dict of device tensors
+
+    @property
+    def signal(self):
+        return self.sums[..., 0] / max(self.n_walkers, 1)
+
+    @property
+    def stderr(self):
+        n = max(self.n_walkers, 1)
+        m = self.sums[..., 0] / n
+        return np.sqrt(np.maximum(self.sums[..., 2] / n - m * m, 0.0) / n)
+
+
+def _waveform_arrays(waveform, geometry):
+    G = np.asarray(waveform.G, dtype=np.float32)                  # (M, n_t, 3)
+    orient = getattr(geometry, '_orient_R', None)                 # Mesh placement (core.py:417-419)
+    if orient is not None:
+        G = G @ np.asarray(orient, dtype=np.float32)
+    frame = geometry._frame()
+    if frame is not None:                                         # g.r_lab = (R g).r_frame
+        G = (G.astype(np.float64) @ frame.T).astype(np.float32)
+    n_meas, n_t, _ = G.shape
+    chi = getattr(waveform, 'chi_perp', None)
+    chi = None if chi is None else np.asarray(chi, dtype=np.float32).reshape(n_t)
+    return G, chi
+
+
+def run_walk(geometry, *, n_walkers, diffusivity, G, dt, sub_steps, phase_per_substep, seed,
+             chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
+             want_positions=False, want_walker_signals=False, want_compartments=False,
+             traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False):
+    """One device walk.  ``G`` is (M, n_t, 3) in the geometry's walk frame; ``r0`` (n, 3) in the
+    walk frame.  Returns a :class:`WalkResult`."""
+    lib = _lib.load()
+    dev = _lib.device()
+    G = np.asarray(G, dtype=np.float32)
+    n_meas, n_t, _ = G.shape
+    dt = float(dt)
+    S = int(sub_steps)
+    dt_sub = dt / S
+    D = float(diffusivity)
+    step_l = np.float32(np.sqrt(6.0 * D * dt_sub))
+    gamma_dt = np.float32(GAMMA * (dt_sub if phase_per_substep else dt))
+
+    rho = getattr(geometry, 'surface_relaxivity_t2', None)
+    kappa = getattr(geometry, 'permeability', None)
+    rho_over_D = np.float32(rho / D) if rho is not None else np.float32(0.0)
+    kappa_over_D = np.float32(kappa / D) if kappa is not None else np.float32(0.0)
+    want_w = (rho is not None) or (kappa is not None) or (T2 is not None) or (T1 is not None)
+    wall = geometry._wall_mode(rho is not None or want_dlog)
+    gdesc, keep = geometry._desc(float(step_l), wall, rho_over_D if rho is not None else 0.0,
+                                 kappa_over_D, dev)
+
+    echo = np.asarray([n_t - 1] if echo_idx is None else echo_idx, dtype=np.int32).ravel()
+    echo_c = (ctypes.c_int32 * len(echo))(*echo.tolist())
+
+    G_dev = torch.from_numpy(np.ascontiguousarray(G.transpose(1, 0, 2))).to(dev)   # (n_t, M, 3)
+    chi_dev = None if chi is None else torch.from_numpy(np.asarray(chi, np.float32)).to(dev)
+    r0_dev = None
+    if r0 is not None:
+        r0 = np.asarray(r0, dtype=np.float32)
+        if r0.shape != (n_walkers, 3):
+            raise ValueError(f"r0 must have shape ({n_walkers}, 3), got {r0.shape}")
+        r0_dev = torch.from_numpy(np.ascontiguousarray(r0)).to(dev)
+
+    p = _lib.WalkParams()
+    p.n_walkers = int(n_walkers)
+    p.walker_offset = int(walker_offset)
+    p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    p.n_t = n_t
+    p.n_meas = n_meas
+    p.sub_steps = S
+    p.phase_per_substep = 1 if phase_per_substep else 0
+    p.step_length = step_l
+    p.gamma_dt = gamma_dt
+    p.t2_decay = np.float32(dt_sub / T2) if T2 is not None else 0.0
+    p.t1_decay = np.float32(dt_sub / T1) if T1 is not None else 0.0
+    p.has_weight = 1 if want_w else 0
+    p.n_echo = len(echo)
+    p.echo_idx = echo_c
+    p.G = G_dev.data_ptr()
+    p.chi = None if chi_dev is None else chi_dev.data_ptr()
+    p.r0 = None if r0_dev is None else r0_dev.data_ptr()
+
+    sums = torch.zeros((len(echo), n_meas, 3), dtype=torch.float64, device=dev)
+    status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+    o = _lib.WalkOutputs()
+    o.sums = sums.data_ptr()
+    o.status = status.data_ptr()
+    extras = {}
+    if want_positions:
+        extras["pos"] = torch.empty((n_walkers, 3), dtype=torch.float32, device=dev)
+        o.final_pos = extras["pos"].data_ptr()
+    if want_walker_signals:
+        extras["log_w"] = torch.zeros(n_walkers, dtype=torch.float32, device=dev)
+        extras["phi"] = torch.empty((n_walkers, n_meas), dtype=torch.float32, device=dev)
+        o.log_w = extras["log_w"].data_ptr()
+        o.phi = extras["phi"].data_ptr()
+    if want_compartments:
+        extras["comp0"] = torch.empty(n_walkers, dtype=torch.int32, device=dev)
+        extras["comp_end"] = torch.empty(n_walkers, dtype=torch.int32, device=dev)
+        o.comp0 = extras["comp0"].data_ptr()
+        o.comp_end = extras["comp_end"].data_ptr()
+    if traj is not None:
+        o.traj = traj.data_ptr()
+        o.traj_f16 = 1 if traj_f16 else 0
+    if want_dlog:
+        extras["dlog"] = torch.empty((n_walkers, n_t), dtype=torch.float32, device=dev)
+        o.dlog_unit = extras["dlog"].data_ptr()
+    if want_comp_occ:
+        extras["comp_occ"] = torch.empty((n_walkers, n_t), dtype=torch.float32, device=dev)
+        o.comp_occ = extras["comp_occ"].data_ptr()
+
+    nbytes = lib.dmsim_walk_workspace_bytes(p, gdesc)
+    if nbytes == 0:
+        _lib.check(-1, "dmsim_walk_workspace_bytes")
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    rc = lib.dmsim_walk(p, gdesc, o, _lib.ptr(ws), nbytes, _lib.stream_handle())
+    _lib.check(rc, "dmsim_walk")
+    torch.cuda.synchronize(dev)
+    st = status.cpu().numpy().astype(np.uint32)
+    del keep
+    return WalkResult(sums.cpu().numpy(), int(n_walkers),
+                      dict(zip(_lib.STATUS_NAMES, st.tolist())), extras)
+
+
+def _to_lab(geometry, pos):
+    frame = geometry._frame()
+    if frame is None:
+        return pos
+    return (pos.astype(np.float64) @ frame).astype(np.float32)
+
+
+def _to_frame(geometry, r):
+    frame = geometry._frame()
+    r = np.asarray(r, dtype=np.float32)
+    if frame is None:
+        return r
+    return (r.astype(np.float64) @ frame.T).astype(np.float32)
+
+
+def _check_gpu(require_gpu):
+    if require_gpu is False:
+        return
+    _lib.device()
+
+
+# ------------------------------------------------------------------------------------------------
+# Public API
+# ------------------------------------------------------------------------------------------------
+def simulate(n_walkers, diffusivity=None, waveform=None, geometry=None, seed=123, T2=None, T1=None,
+             return_positions=False, return_compartments=False, return_walker_signals=False,
+             r0=None, walker_batch_size=None, require_gpu=None, engine="auto"):
+    """Monte-Carlo diffusion signal (core.py:193-762).
+
+    Returns ``signals`` (n_meas,) float32 = Re<exp(log_w) exp(i phi)> (x0.5 for a stimulated echo),
+    followed, as requested, by positions ((n, 3) final or (n, n_t, 3) 'full'), compartment
+    (origin, final or full) and per-walker (log_w (n,), phi (n, n_meas)).
+    """
+    if return_compartments not in (False, 'final', 'full'):
+        raise ValueError("return_compartments must be False, 'final', or 'full'; "
+                         f"got {return_compartments!r}")
+    if return_positions not in (False, True, 'full'):
+        raise ValueError(f"return_positions must be False, True, or 'full'; got {return_positions!r}")
+    if engine not in ("auto", "replay", "fused"):
+        raise ValueError(f"engine must be 'auto', 'replay', or 'fused'; got {engine!r}")
+    if hasattr(waveform, 'waveform'):
+        waveform = waveform.waveform
+    if diffusivity is None:
+        raise NotImplementedError(
+            "simulate() without an explicit diffusivity (myelin geometries carrying their own D) "
+            "is not supported by this engine")
+    if return_compartments == 'full':
+        raise NotImplementedError("return_compartments='full' is not supported by this engine")
+
+    gap = _replay_gap(geometry, return_positions=return_positions,
+                      return_compartments=return_compartments,
+                      return_walker_signals=return_walker_signals, diffusivity=diffusivity)
+    if engine == "replay" and gap is not None:
+        raise NotImplementedError(f"engine='replay' cannot serve this run: {gap}. "
+                                  "Use engine='fused' (or 'auto').")
+    use_replay = engine == "replay" or (engine == "auto" and gap is None
+                                        and _replay_auto_allowed(geometry))
+    _check_gpu(require_gpu)
+
+    G, chi = _waveform_arrays(waveform, geometry)
+    dt = float(waveform.dt)
+    if use_replay:
+        S = replay_sub_steps(geometry, diffusivity, dt)
+    else:
+        S = fused_sub_steps(geometry, diffusivity, dt)
+        if walker_batch_size is not None and walker_batch_size < n_walkers:
+            return _simulate_in_walker_batches(
+                n_walkers, walker_batch_size, seed=seed, diffusivity=diffusivity,
+                waveform=waveform, geometry=geometry, T2=T2, T1=T1, r0=r0,
+                return_positions=return_positions, return_compartments=return_compartments,
+                return_walker_signals=return_walker_signals)
+
+    n_t = G.shape[1]
+    traj = None
+    if return_positions == 'full':
+        traj = torch.empty((n_walkers, n_t, 3), dtype=torch.float32, device=_lib.device())
+    res = run_walk(geometry, n_walkers=n_walkers, diffusivity=diffusivity, G=G, dt=dt,
+                   sub_steps=S, phase_per_substep=not use_replay, seed=seed, chi=chi, T2=T2, T1=T1,
+                   r0=None if r0 is None else _to_frame(geometry, r0),
+                   want_positions=return_positions is True,
+                   want_walker_signals=bool(return_walker_signals),
+                   want_compartments=return_compartments is not False, traj=traj, traj_f16=False)
+    signals = res.signal[0].astype(np.float32)
+    if getattr(waveform, 'stimulated_echo', False):
+        signals = signals * np.float32(0.5)
+    out = [signals]
+    if return_positions == 'full':
+        out.append(_to_lab(geometry, traj.cpu().numpy().reshape(-1, 3)).reshape(n_walkers, n_t, 3))
+    elif return_positions:
+        out.append(_to_lab(geometry, res.extras["pos"].cpu().numpy()))
+    if return_compartments is not False:
+        out.append(res.extras["comp0"].cpu().numpy())
+        out.append(res.extras["comp_end"].cpu().numpy())
+    if return_walker_signals:
+        out.append(res.extras["log_w"].cpu().numpy())
+        out.append(res.extras["phi"].cpu().numpy())
+    return out[0] if len(out) == 1 else tuple(out)
+
+
+def _simulate_in_walker_batches(n_walkers, walker_batch_size, *, seed, diffusivity, waveform,
+                                geometry, T2, T1, r0, return_positions, return_compartments,
+                                return_walker_signals):
+    """Walker chunks with sub-seeds seed + 1 + b, recombined as a size-weighted mean
+    (core.py:765-818)."""
+    n_b = (n_walkers + walker_batch_size - 1) // walker_batch_size
+    acc = None
+    extra = []
+    for b in range(n_b):
+        s0 = b * walker_batch_size
+        nb = min(walker_batch_size, n_walkers - s0)
+        out = simulate(nb, diffusivity, waveform, geometry, seed=seed + 1 + b, T2=T2, T1=T1,
+                       return_positions=return_positions,
+                       return_compartments=return_compartments,
+                       return_walker_signals=return_walker_signals,
+                       r0=None if r0 is None else r0[s0:s0 + nb], walker_batch_size=None,
+                       require_gpu=False, engine="fused")
+        items = list(out) if isinstance(out, tuple) else [out]
+        sig = np.asarray(items.pop(0))
+        acc = sig * nb if acc is None else acc + sig * nb
+        extra.append(items)
+    res = [acc / n_walkers]
+    for k in range(len(extra[0])):
+        res.append(np.concatenate([e[k] for e in extra], axis=0))
+    return res[0] if len(res) == 1 else tuple(res)
+
+
+def simulate_cpmg(n_walkers, diffusivity, waveform, geometry, *, T2=None, seed=123,
+                  walker_batch_size=None, require_gpu=None):
+    """Multi-echo CPMG signal (n_echoes, n_meas) from one walk (core.py:861-969): the ensemble is
+    reduced only at the echo samples instead of materialising the (n, n_t, n_meas) trace."""
+    _check_gpu(require_gpu)
+    if hasattr(waveform, 'waveform'):
+        waveform = waveform.waveform
+    echo = getattr(waveform, 'echo_indices', None)
+    if echo is None:
+        raise ValueError("simulate_cpmg needs a multi-echo waveform with echo_indices set; "
+                         "build it with dmipy_sim.cpmg(...).")
+    echo = np.asarray(echo, dtype=int)
+    if walker_batch_size is not None and walker_batch_size < n_walkers:
+        n_b = (n_walkers + walker_batch_size - 1) // walker_batch_size
+        acc = None
+        for b in range(n_b):
+            nb = min(walker_batch_size, n_walkers - b * walker_batch_size)
+            s = simulate_cpmg(nb, diffusivity, waveform, geometry, T2=T2, seed=seed + 1 + b,
+                              walker_batch_size=None, require_gpu=False)
+            acc = s * nb if acc is None else acc + s * nb
+        return acc / n_walkers
+    G, chi = _waveform_arrays(waveform, geometry)
+    S = fused_sub_steps(geometry, diffusivity, float(waveform.dt))
+    order = np.argsort(echo, kind="stable")
+    uniq, inv = np.unique(echo[order], return_inverse=True)
+    res = run_walk(geometry, n_walkers=n_walkers, diffusivity=diffusivity, G=G,
+                   dt=float(waveform.dt), sub_steps=S, phase_per_substep=True, seed=seed, chi=chi,
+                   T2=T2, echo_idx=uniq)
+    sig = res.signal.astype(np.float32)                 # (n_unique, M)
+    out = np.empty((len(echo), G.shape[0]), dtype=np.float32)
+    out[order] = sig[inv]
+    return out
+
+
+def simulate_trajectories(n_walkers, diffusivity, geometry, T_max, dt_save, seed=42,
+                          walker_batch_size=50_000, save_relaxation_data=False, require_gpu=None,
+                          r0=None, kappa_MT=0.0, dwell_time=0.0, equilibrate_binding="auto",
+                          compress=None):
+    """Walk once and return the positions after every saved step (core.py:972-1529).
+
+    Returns ``(trajectories (n, n_t, 3) float16, dt_actual, sub_steps, dt_sim)`` and, with
+    ``save_relaxation_data``, also ``dlog_boundary_unit (n, n_t) float16`` and ``comp_traj``
+    (float16 occupancy of compartment 1 for a permeable Cylinder/Sphere, int8 zeros otherwise).
+    """
+    if kappa_MT and kappa_MT > 0:
+        raise NotImplementedError("magnetisation-transfer binding walks are not supported")
+    if compress is not None:
+        raise NotImplementedError("compressed (DCT) trajectory export is not supported")
+    _check_gpu(require_gpu)
+    n_t = int(round(T_max / dt_save)) + 1
+    dt_actual = T_max / (n_t - 1)
+    S = replay_sub_steps(geometry, diffusivity, dt_actual)
+    dt_sim = dt_actual / S
+    dev = _lib.device()
+    traj = torch.empty((n_walkers, n_t, 3), dtype=torch.float16, device=dev)
+    perm2 = (getattr(geometry, 'permeability', None) is not None
+             and type(geometry).__name__ in ("Cylinder", "Sphere"))
+    G = np.zeros((1, n_t, 3), dtype=np.float32)
+    res = run_walk(geometry, n_walkers=n_walkers, diffusivity=diffusivity, G=G, dt=dt_actual,
+                   sub_steps=S, phase_per_substep=False, seed=seed,
+                   r0=None if r0 is None else _to_frame(geometry, r0), traj=traj, traj_f16=True,
+                   want_dlog=save_relaxation_data and hasattr(geometry, "_desc"),
+                   want_comp_occ=save_relaxation_data and perm2)
+    t = traj.float().cpu().numpy()
+    t = _to_lab(geometry, t.reshape(-1, 3)).reshape(n_walkers, n_t, 3).astype(np.float16)
+    if not save_relaxation_data:
+        return t, dt_actual, S, dt_sim
+    dlog = res.extras["dlog"].cpu().numpy().astype(np.float16)
+    if perm2:
+        comp = res.extras["comp_occ"].cpu().numpy().astype(np.float16)
+    else:
+        comp = np.zeros((n_walkers, n_t), dtype=np.int8)
+    return t, dt_actual, S, dt_sim, dlog, comp

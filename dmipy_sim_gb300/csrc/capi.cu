@@ -1,0 +1,420 @@
+// Host side of the C ABI (include/dmsim.h): argument checks, launch planning, workspace layout,
+// the waveform re-layout kernel, the deterministic cross-block reduction, and the replay kernel.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "dmsim.h"
+#include "walk_kernel.cuh"
+
+namespace dmsim {
+WalkFn walk_fn_free(int wall, int mt, bool tsm);
+WalkFn walk_fn_cyl(int wall, int mt, bool tsm);
+WalkFn walk_fn_sph(int wall, int mt, bool tsm);
+WalkFn walk_fn_pcyl(int wall, int mt, bool tsm);
+WalkFn walk_fn_psph(int wall, int mt, bool tsm);
+}  // namespace dmsim
+
+using namespace dmsim;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+size_t pad16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// Largest shared-memory footprint for which the cell list is staged into shared memory; larger
+// lists are read through L1 from global memory.
+constexpr size_t kTabSmemBudget = 96 * 1024;
+
+int pick_mt(int M) {
+  if (M <= 4) return 4;
+  if (M <= 16) return 16;
+  if (M <= 32) return 32;
+  return 64;
+}
+
+size_t smem_fixed(int mt) {
+  switch (mt) {
+    case 4: return walk_smem_fixed<4>();
+    case 16: return walk_smem_fixed<16>();
+    case 32: return walk_smem_fixed<32>();
+    default: return walk_smem_fixed<64>();
+  }
+}
+
+struct Plan {
+  WalkFn fn = nullptr;
+  int mt = 0, n_pass = 0, n_chunks = 0, grid = 0;
+  bool tsm = false;
+  size_t smem = 0, tab_cs = 0, tab_cand = 0;
+  size_t off_gp = 0, off_act = 0, off_part = 0, total = 0;
+};
+
+int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
+  if (!p || !g) return fail(DMSIM_EINVAL, "null params or geometry");
+  if (p->n_walkers < 0) return fail(DMSIM_EINVAL, "n_walkers < 0");
+  if (p->n_t < 1 || p->n_meas < 1 || p->sub_steps < 1)
+    return fail(DMSIM_EINVAL, "n_t, n_meas and sub_steps must be >= 1");
+  if (p->n_echo < 1 || p->n_echo > kMaxEcho)
+    return fail(DMSIM_ETOOBIG, "n_echo must be in [1, %d]", kMaxEcho);
+  if (!p->echo_idx) return fail(DMSIM_EINVAL, "echo_idx is null");
+  for (int e = 0; e < p->n_echo; ++e) {
+    if (p->echo_idx[e] < 0 || p->echo_idx[e] >= p->n_t)
+      return fail(DMSIM_EINVAL, "echo index %d out of range", p->echo_idx[e]);
+    if (e > 0 && p->echo_idx[e] <= p->echo_idx[e - 1])
+      return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
+  }
+  const bool packed = g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
+  if (g->kind < 0 || g->kind > DMSIM_GEOM_PACKED_SPHERES)
+    return fail(DMSIM_EINVAL, "unsupported geometry kind %d", g->kind);
+  if (g->wall_mode < 0 || g->wall_mode > 2) return fail(DMSIM_EINVAL, "bad wall_mode");
+  if (g->kind == DMSIM_GEOM_FREE && g->wall_mode != DMSIM_WALL_REFLECT)
+    return fail(DMSIM_EINVAL, "free diffusion has no walls");
+  if (packed) {
+    if (!g->cell_start || !g->cand || g->grid_n < 1 || g->n_cand < 0 || !(g->L > 0.f))
+      return fail(DMSIM_EINVAL, "packed geometry needs a cell list");
+    if (!(g->reach >= p->step_length))
+      return fail(DMSIM_EINVAL, "cell list reach %g is shorter than the step %g", g->reach,
+                  p->step_length);
+    if (((uintptr_t)g->cell_start & 15) || ((uintptr_t)g->cand & 15))
+      return fail(DMSIM_EINVAL, "cell list arrays must be 16-byte aligned");
+  }
+  if (p->G == nullptr) return fail(DMSIM_EINVAL, "G is null");
+
+  pl->mt = pick_mt(p->n_meas);
+  pl->n_pass = (p->n_meas + pl->mt - 1) / pl->mt;
+  pl->n_chunks = (p->n_t + kTC - 1) / kTC;
+  size_t cells = 0;
+  if (packed) {
+    cells = (size_t)g->grid_n * g->grid_n * (g->kind == DMSIM_GEOM_PACKED_SPHERES ? g->grid_n : 1);
+    pl->tab_cs = pad16((cells + 1) * 4);
+    pl->tab_cand = (size_t)g->n_cand * 16;
+    pl->tsm = pl->tab_cs + pl->tab_cand <= kTabSmemBudget;
+  }
+  switch (g->kind) {
+    case DMSIM_GEOM_FREE: pl->fn = walk_fn_free(g->wall_mode, pl->mt, false); break;
+    case DMSIM_GEOM_CYLINDER: pl->fn = walk_fn_cyl(g->wall_mode, pl->mt, false); break;
+    case DMSIM_GEOM_SPHERE: pl->fn = walk_fn_sph(g->wall_mode, pl->mt, false); break;
+    case DMSIM_GEOM_PACKED_CYLINDERS: pl->fn = walk_fn_pcyl(g->wall_mode, pl->mt, pl->tsm); break;
+    case DMSIM_GEOM_PACKED_SPHERES: pl->fn = walk_fn_psph(g->wall_mode, pl->mt, pl->tsm); break;
+  }
+  if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
+  pl->smem = smem_fixed(pl->mt) + (pl->tsm ? pl->tab_cs + pl->tab_cand : 0);
+
+  int dev = 0, n_sm = 0, nb = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(DMSIM_ECUDA, "cudaGetDevice failed");
+  if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "cudaDeviceGetAttribute failed");
+  if (cudaFuncSetAttribute((const void*)pl->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)pl->smem) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "cudaFuncSetAttribute(%zu B shared) failed", pl->smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)pl->fn, kBlock, pl->smem) !=
+          cudaSuccess ||
+      nb < 1)
+    return fail(DMSIM_ECUDA, "kernel does not fit on an SM (%zu B shared)", pl->smem);
+  const int64_t n_tiles = (p->n_walkers + kBlock - 1) / kBlock;
+  int64_t grid = (int64_t)nb * n_sm;
+  if (grid > n_tiles) grid = n_tiles;
+  if (grid < 1) grid = 1;
+  pl->grid = (int)grid;
+
+  size_t off = 0;
+  pl->off_gp = off;
+  off = align256(off + (size_t)pl->n_pass * pl->n_chunks * kTC * pl->mt * 3 * 4);
+  pl->off_act = off;
+  off = align256(off + (size_t)pl->n_pass * p->n_t);
+  pl->off_part = off;
+  off = align256(off + (size_t)pl->grid * p->n_echo * pl->n_pass * pl->mt * 3 * 8);
+  pl->total = off;
+  return DMSIM_OK;
+}
+
+// Waveform re-layout: G (n_t, M, 3) -> per pass (n_chunks*kTC, MT, 3), zero padded, plus a
+// per-sample flag telling whether any gradient of the pass is on (the walk skips the phase
+// update otherwise).
+__global__ void k_prep(const float* __restrict__ G, int n_t, int M, int mt, int n_pass, int t_pad,
+                       float* __restrict__ Gp, uint8_t* __restrict__ act) {
+  const int64_t n = (int64_t)n_pass * t_pad;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int pass = (int)(i / t_pad), t = (int)(i % t_pad);
+    float* dst = Gp + ((size_t)pass * t_pad + t) * mt * 3;
+    bool any = false;
+    for (int j = 0; j < mt; ++j) {
+      const int m = pass * mt + j;
+      for (int k = 0; k < 3; ++k) {
+        float v = 0.f;
+        if (t < n_t && m < M) v = G[((size_t)t * M + m) * 3 + k];
+        dst[j * 3 + k] = v;
+        any |= (v != 0.f);
+      }
+    }
+    if (t < n_t) act[(size_t)pass * n_t + t] = any ? 1 : 0;
+  }
+}
+
+// Deterministic reduction of the per-block FP64 partials (fixed block order).
+__global__ void k_reduce(const double* __restrict__ part, int grid, int n_echo, int Mp, int M,
+                         double* __restrict__ sums) {
+  const int n = n_echo * M * 3;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int e = i / (M * 3), r = i % (M * 3);
+    double acc = 0.0;
+    for (int b = 0; b < grid; ++b) acc += part[((size_t)b * n_echo + e) * Mp * 3 + r];
+    sums[i] = acc;
+  }
+}
+
+// ---- replay (trajectories.py:550-552, 634): phase of saved trajectories ------------------------
+constexpr int kRB = 128;   // walkers per block
+constexpr int kRT = 8;     // samples per staged step
+constexpr int kRM = 16;    // measurements per register tile
+
+template <bool F16>
+__global__ void __launch_bounds__(kRB) k_replay(const void* __restrict__ traj, int64_t n_walkers,
+                                                int n_t, const float* __restrict__ G, int M,
+                                                float gamma_dt, const float* __restrict__ log_w,
+                                                double* __restrict__ part, float* __restrict__ phi_out) {
+  __shared__ float Gs[kRT * kRM * 3];
+  __shared__ float red[kRB / 32][kRM * 3];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_mt = (M + kRM - 1) / kRM;
+  const int64_t n_tiles = (n_walkers + kRB - 1) / kRB;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t w = tile * kRB + tid;
+    const bool act = w < n_walkers;
+    const float wgt = act ? (log_w ? expf(log_w[w]) : 1.f) : 0.f;
+    for (int mt = 0; mt < n_mt; ++mt) {
+      float phi[kRM], kc[kRM];
+#pragma unroll
+      for (int j = 0; j < kRM; ++j) phi[j] = kc[j] = 0.f;
+      for (int t0 = 0; t0 < n_t; t0 += kRT) {
+        __syncthreads();
+        for (int i = tid; i < kRT * kRM * 3; i += kRB) {
+          const int tt = i / (kRM * 3), r = i % (kRM * 3), m = mt * kRM + r / 3;
+          Gs[i] = (t0 + tt < n_t && m < M) ? G[((size_t)(t0 + tt) * M + m) * 3 + r % 3] : 0.f;
+        }
+        __syncthreads();
+        for (int tt = 0; tt < kRT && t0 + tt < n_t; ++tt) {
+          float rx = 0.f, ry = 0.f, rz = 0.f;
+          if (act) {
+            const size_t o = ((size_t)w * n_t + t0 + tt) * 3;
+            if (F16) {
+              const __half* tp = reinterpret_cast<const __half*>(traj);
+              rx = __half2float(tp[o]);
+              ry = __half2float(tp[o + 1]);
+              rz = __half2float(tp[o + 2]);
+            } else {
+              const float* tp = reinterpret_cast<const float*>(traj);
+              rx = tp[o];
+              ry = tp[o + 1];
+              rz = tp[o + 2];
+            }
+          }
+          rx *= gamma_dt;
+          ry *= gamma_dt;
+          rz *= gamma_dt;
+#pragma unroll
+          for (int j = 0; j < kRM; ++j) {
+            const float* gg = Gs + (tt * kRM + j) * 3;
+            const float d = fmaf(gg[2], rz, fmaf(gg[1], ry, gg[0] * rx));
+            const float yk = d - kc[j];
+            const float tk = phi[j] + yk;
+            kc[j] = (tk - phi[j]) - yk;
+            phi[j] = tk;
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kRM; ++j) {
+        const int m = mt * kRM + j;
+        float sn, cs;
+        sincosf(phi[j], &sn, &cs);
+        const float c1 = warp_sum(wgt * cs), c2 = warp_sum(wgt * sn),
+                    c3 = warp_sum((wgt * cs) * (wgt * cs));
+        if (lane == 0) {
+          red[warp][3 * j] = c1;
+          red[warp][3 * j + 1] = c2;
+          red[warp][3 * j + 2] = c3;
+        }
+        if (act && phi_out && m < M) phi_out[(size_t)w * M + m] = phi[j];
+      }
+      __syncthreads();
+      for (int i = tid; i < kRM * 3; i += kRB) {
+        const int m = mt * kRM + i / 3;
+        if (m >= M) continue;
+        double acc = 0.0;
+        for (int ww = 0; ww < kRB / 32; ++ww) acc += (double)red[ww][i];
+        part[(size_t)blockIdx.x * M * 3 + (size_t)m * 3 + i % 3] += acc;
+      }
+    }
+  }
+}
+
+__global__ void k_zero(double* p, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = 0.0;
+}
+
+int replay_grid(int64_t n_walkers) {
+  int dev = 0, n_sm = 0, nb = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_replay<true>, kRB, 0);
+  int64_t grid = (int64_t)(nb > 0 ? nb : 1) * (n_sm > 0 ? n_sm : 1);
+  const int64_t n_tiles = (n_walkers + kRB - 1) / kRB;
+  if (grid > n_tiles) grid = n_tiles;
+  return (int)(grid < 1 ? 1 : grid);
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmsim_version(void) { return DMSIM_ABI_VERSION; }
+
+const char* dmsim_last_error(void) { return g_err; }
+
+size_t dmsim_walk_workspace_bytes(const dmsim_walk_params* p, const dmsim_geometry* g) {
+  Plan pl;
+  if (make_plan(p, g, &pl) != DMSIM_OK) return 0;
+  return pl.total;
+}
+
+int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
+               void* workspace, size_t workspace_bytes, void* stream) {
+  Plan pl;
+  int rc = make_plan(p, g, &pl);
+  if (rc != DMSIM_OK) return rc;
+  if (!o || !o->sums || !o->status) return fail(DMSIM_EINVAL, "outputs need sums and status");
+  if (!workspace || workspace_bytes < pl.total)
+    return fail(DMSIM_EWORKSPACE, "workspace %zu B < required %zu B", workspace_bytes, pl.total);
+  if (((uintptr_t)workspace & 255) != 0) return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
+  if (p->n_walkers == 0) {
+    cudaMemsetAsync(o->sums, 0, sizeof(double) * p->n_echo * p->n_meas * 3, (cudaStream_t)stream);
+    return DMSIM_OK;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* ws = static_cast<uint8_t*>(workspace);
+  float* Gp = reinterpret_cast<float*>(ws + pl.off_gp);
+  uint8_t* act = ws + pl.off_act;
+  double* part = reinterpret_cast<double*>(ws + pl.off_part);
+  const int t_pad = pl.n_chunks * kTC;
+
+  k_prep<<<64, 256, 0, st>>>(p->G, p->n_t, p->n_meas, pl.mt, pl.n_pass, t_pad, Gp, act);
+
+  KArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n_walkers = p->n_walkers;
+  a.walker_offset = p->walker_offset;
+  a.seed = p->seed;
+  a.n_t = p->n_t;
+  a.n_chunks = pl.n_chunks;
+  a.S = p->sub_steps;
+  a.phase_sub = p->phase_per_substep ? 1 : 0;
+  a.has_weight = p->has_weight ? 1 : 0;
+  a.n_echo = p->n_echo;
+  a.Mp = pl.n_pass * pl.mt;
+  a.M = p->n_meas;
+  a.step_l = p->step_length;
+  a.gamma_dt = p->gamma_dt;
+  a.t2dec = p->t2_decay;
+  a.t1dec = p->t1_decay;
+  a.rho = g->rho_over_D;
+  GeoK gk;
+  memset(&gk, 0, sizeof(gk));
+  const bool packed =
+      g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
+  gk.R = g->radius;
+  gk.R2 = g->radius * g->radius;
+  gk.invR = g->radius > 0.f ? 1.f / g->radius : 0.f;
+  gk.eps = g->eps_detect;
+  gk.nudge = g->nudge;
+  gk.kod = g->kappa_over_D;
+  gk.L = packed ? g->L : 0.f;
+  gk.halfL = packed ? 0.5f * g->L : 0.f;
+  gk.inv_h = packed ? (float)g->grid_n / g->L : 0.f;
+  gk.n = packed ? g->grid_n : 1;
+  a.g = gk;
+  a.tab_cs_bytes = (uint32_t)pl.tab_cs;
+  a.tab_cand_bytes = (uint32_t)pl.tab_cand;
+  a.cs = g->cell_start;
+  a.cand = reinterpret_cast<const float4*>(g->cand);
+  a.cand_obj = g->cand_obj;
+  a.active = nullptr;
+  a.chi = p->chi;
+  a.r0 = p->r0;
+  a.part = part;
+  a.status = o->status;
+  a.final_pos = o->final_pos;
+  a.log_w = o->log_w;
+  a.phi_out = o->phi;
+  a.comp0 = o->comp0;
+  a.comp_end = o->comp_end;
+  a.traj = o->traj;
+  a.traj_f16 = o->traj_f16;
+  a.dlog_unit = o->dlog_unit;
+  a.comp_occ = o->comp_occ;
+  if ((o->comp0 || o->comp_end || o->comp_occ) && packed && !g->cand_obj)
+    return fail(DMSIM_EINVAL, "classification of packed objects needs cand_obj");
+  for (int e = 0; e < p->n_echo; ++e) a.echo[e] = p->echo_idx[e];
+
+  for (int pass = 0; pass < pl.n_pass; ++pass) {
+    a.pass = pass;
+    a.Gp = Gp + (size_t)pass * t_pad * pl.mt * 3;
+    a.active = act + (size_t)pass * p->n_t;
+    pl.fn<<<pl.grid, kBlock, pl.smem, st>>>(a);
+  }
+  const int nred = p->n_echo * p->n_meas * 3;
+  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, pl.grid, p->n_echo, pl.n_pass * pl.mt,
+                                               p->n_meas, o->sums);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
+size_t dmsim_replay_workspace_bytes(int64_t n_walkers, int32_t n_t, int32_t n_meas) {
+  (void)n_t;
+  if (n_walkers <= 0 || n_meas <= 0) return 256;
+  return align256((size_t)replay_grid(n_walkers) * n_meas * 3 * 8);
+}
+
+int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t n_t,
+                 const float* G, int32_t n_meas, float gamma_dt, const float* log_w, double* sums,
+                 float* phi_out, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!traj || !G || !sums || n_walkers < 1 || n_t < 1 || n_meas < 1)
+    return fail(DMSIM_EINVAL, "replay: bad arguments");
+  const int grid = replay_grid(n_walkers);
+  const size_t need = align256((size_t)grid * n_meas * 3 * 8);
+  if (!workspace || workspace_bytes < need)
+    return fail(DMSIM_EWORKSPACE, "replay workspace %zu B < required %zu B", workspace_bytes, need);
+  cudaStream_t st = (cudaStream_t)stream;
+  double* part = static_cast<double*>(workspace);
+  k_zero<<<64, 256, 0, st>>>(part, (size_t)grid * n_meas * 3);
+  if (traj_f16)
+    k_replay<true><<<grid, kRB, 0, st>>>(traj, n_walkers, n_t, G, n_meas, gamma_dt, log_w, part,
+                                         phi_out);
+  else
+    k_replay<false><<<grid, kRB, 0, st>>>(traj, n_walkers, n_t, G, n_meas, gamma_dt, log_w, part,
+                                          phi_out);
+  const int nred = n_meas * 3;
+  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, grid, 1, n_meas, n_meas, sums);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(DMSIM_ECUDA, "replay launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
+}  // extern "C"

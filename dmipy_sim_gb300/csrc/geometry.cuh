@@ -1,0 +1,612 @@
+// Device-side geometry step functions of the walk.
+//
+// Each function advances one walker by one physics sub-step against one geometry and returns the
+// unit boundary log-weight (-2 * sum of perpendicular overshoots d_perp, i.e. the reference's
+// dlog_w at rho/D = 1; the kernel scales it by rho/D and by the transverse mask).  The arithmetic
+// follows the reference's per-walker JAX functions statement by statement (same epsilons, nudges,
+// clamps, root choices and argmin rules) so that the walk is the same random process:
+//   Cylinder.reflect / reflect_with_log_weight / permeate   geometries.py:493-563, 565-653, 655-801
+//   Sphere.reflect / reflect_with_log_weight / permeate     geometries.py:197-264, 266-318, 320-424
+//   PackedCylinders.reflect / reflect_with_log_weight / permeate   geometries.py:1746-1884,
+//                                                           1886-2016, 2018-2183
+//   PackedSpheres.reflect / reflect_with_log_weight / permeate     geometries.py:2445-2537,
+//                                                           2539-2631, 2633-2756
+// What differs is the data layout, not the process:
+//   * Cylinders walk in their own frame (axis = z): an isotropic step is isotropic in any frame, so
+//     the per-step frame rotation of the reference (geometries.py:510-515) is folded into the
+//     gradient once on the host.
+//   * Packed substrates keep the position folded into the periodic cell plus integer image
+//     counters (the reference keeps an unfolded FP32 position and min-images every object,
+//     geometries.py:1782-1783).  The unfolded position for the phase is x + L*image.
+//   * Packed substrates test only the objects listed for the walker's cell of a uniform cell list
+//     (every object within reach of the cell), instead of all K objects; a candidate counts only if
+//     it is the minimum image of its object, which is exactly the reference's min-image rule.
+//   * A wall root whose discriminant is within 1e-4*R^2 of grazing is re-solved in FP64.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#include "dmsim.h"
+
+namespace dmsim {
+
+enum { kReflect = DMSIM_WALL_REFLECT, kRelax = DMSIM_WALL_RELAX, kPermeate = DMSIM_WALL_PERMEATE };
+
+constexpr float kGrazeTol = 1e-4f;
+
+struct Tally {
+  uint32_t clamp = 0, graze = 0, transmit = 0;
+};
+
+// Geometry constants in registers/param space (a trimmed copy of dmsim_geometry).
+struct GeoK {
+  float R, R2, invR, eps, nudge, kod;  // single objects: R; packed: eps/nudge from R_min
+  float L, halfL, inv_h;
+  int n;  // cells per axis
+};
+
+// ------------------------------------------------------------------------------------------------
+// Single cylinder, axis z, centred at the origin.
+// ------------------------------------------------------------------------------------------------
+template <int WALL>
+__device__ __forceinline__ float cylinder_step(float& x, float& y, float sx, float sy, float u,
+                                               const GeoK& g, Tally& tl) {
+  const float lxy = sqrtf(sx * sx + sy * sy);
+  float dx = 0.f, dy = 0.f;
+  if (lxy > 0.f) {
+    dx = sx / lxy;
+    dy = sy / lxy;
+  }
+  float dsum = 0.f;  // sum of d_perp
+  if constexpr (WALL != kPermeate) {
+    // Up to 10 specular bounces (geometries.py:523-559).  An iteration without a crossing leaves
+    // the state unchanged, so the loop stops at the first one.
+    float rem = lxy;
+    if (lxy > 0.f) {
+#pragma unroll 1
+      for (int it = 0; it < 10; ++it) {
+        const float dp = dx * x + dy * y;
+        float disc = fmaxf(dp * dp - ((x * x + y * y) - g.R2), 0.f);
+        float d = -dp + sqrtf(disc);
+        if (disc < kGrazeTol * g.R2) {
+          const double dpd = (double)dx * x + (double)dy * y;
+          const double dd = fmax(dpd * dpd - (((double)x * x + (double)y * y) - (double)g.R * g.R), 0.0);
+          disc = (float)dd;
+          d = (float)(-dpd + sqrt(dd));
+          ++tl.graze;
+        }
+        if (!(d > g.eps && d < rem)) break;
+        const float hx = x + d * dx, hy = y + d * dy;
+        const float nx = hx / g.R, ny = hy / g.R;
+        const float dn = dx * nx + dy * ny;
+        float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
+        const float rn = sqrtf(rx * rx + ry * ry);
+        rx /= rn;
+        ry /= rn;
+        if constexpr (WALL == kRelax) dsum += (rem - d) * (sqrtf(disc) / g.R);
+        x = hx - g.nudge * nx;
+        y = hy - g.nudge * ny;
+        dx = rx;
+        dy = ry;
+        rem = rem - d - g.nudge;
+      }
+    }
+    const float f = fmaxf(rem, 0.f);
+    x += dx * f;
+    y += dy * f;
+    const float rr = sqrtf(x * x + y * y);
+    if (rr >= g.R) {  // safety clamp, geometries.py:555-559
+      const float s = (g.R - g.nudge) / rr;
+      x *= s;
+      y *= s;
+      ++tl.clamp;
+    }
+    return -2.f * dsum;
+  } else {
+    // Powles crossing, one decision per sub-step (geometries.py:705-801).
+    const float dp = dx * x + dy * y;
+    const float q2 = x * x + y * y;
+    float disc = dp * dp - (q2 - g.R2);
+    const bool inside = q2 < g.R2;
+    float sq = sqrtf(fmaxf(disc, 0.f));
+    float t = inside ? -dp + sq : -dp - sq;
+    if (fabsf(disc) < kGrazeTol * g.R2) {
+      const double dpd = (double)dx * x + (double)dy * y;
+      const double dd = dpd * dpd - (((double)x * x + (double)y * y) - (double)g.R * g.R);
+      const double sd = sqrt(fmax(dd, 0.0));
+      disc = (float)dd;
+      sq = (float)sd;
+      t = (float)(inside ? -dpd + sd : -dpd - sd);
+      ++tl.graze;
+    }
+    const bool hit = (disc > 0.f) && (t > g.eps) && (t < lxy) && (lxy > 0.f);
+    if (!hit) {
+      x += sx;
+      y += sy;
+      return 0.f;
+    }
+    const float hrx = x + t * dx, hry = y + t * dy;
+    const float hl = fmaxf(sqrtf(hrx * hrx + hry * hry), 1e-30f);
+    const float nx = hrx / hl, ny = hry / hl;
+    const float hx = g.R * nx, hy = g.R * ny;  // snapped to the wall
+    const float rem = lxy - t;
+    const float dperp = rem * (sq / g.R);
+    const float p = fminf(1.f, 2.f * g.kod * dperp);
+    if (u < p) {
+      x += sx;
+      y += sy;
+      ++tl.transmit;
+      return 0.f;
+    }
+    const float dn = dx * nx + dy * ny;
+    float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
+    const float rn = sqrtf(rx * rx + ry * ry);
+    rx /= rn;
+    ry /= rn;
+    const float sgn = inside ? -1.f : 1.f;
+    const float f = fmaxf(rem - g.nudge, 0.f);
+    float ox = hx + g.nudge * sgn * nx + rx * f;
+    float oy = hy + g.nudge * sgn * ny + ry * f;
+    const float on = sqrtf(ox * ox + oy * oy);
+    const bool wrong = inside ? (on >= g.R) : (on <= g.R);
+    if (wrong) {
+      const float s = (inside ? g.R - g.nudge : g.R + g.nudge) / fmaxf(on, 1e-30f);
+      ox *= s;
+      oy *= s;
+      ++tl.clamp;
+    }
+    x = ox;
+    y = oy;
+    return -2.f * dperp;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Single sphere centred at the origin.
+// ------------------------------------------------------------------------------------------------
+template <int WALL>
+__device__ __forceinline__ float sphere_step(float& x, float& y, float& z, float sx, float sy,
+                                             float sz, float u, const GeoK& g, Tally& tl) {
+  const float l = sqrtf(sx * sx + sy * sy + sz * sz);
+  float dx = sx / l, dy = sy / l, dz = sz / l;
+  if constexpr (WALL != kPermeate) {
+    // geometries.py:236-264
+    float rem = l;
+    float dsum = 0.f;
+#pragma unroll 1
+    for (int it = 0; it < 10; ++it) {
+      const float dp = dx * x + dy * y + dz * z;
+      float disc = fmaxf(dp * dp - ((x * x + y * y + z * z) - g.R2), 0.f);
+      float d = -dp + sqrtf(disc);
+      if (disc < kGrazeTol * g.R2) {
+        const double dpd = (double)dx * x + (double)dy * y + (double)dz * z;
+        const double dd = fmax(dpd * dpd - (((double)x * x + (double)y * y + (double)z * z) -
+                                            (double)g.R * g.R), 0.0);
+        disc = (float)dd;
+        d = (float)(-dpd + sqrt(dd));
+        ++tl.graze;
+      }
+      if (!(d > g.eps && d < rem)) break;
+      const float hx = x + d * dx, hy = y + d * dy, hz = z + d * dz;
+      const float nx = hx / g.R, ny = hy / g.R, nz = hz / g.R;
+      const float dn = dx * nx + dy * ny + dz * nz;
+      float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny, rz = dz - 2.f * dn * nz;
+      const float rn = sqrtf(rx * rx + ry * ry + rz * rz);
+      rx /= rn;
+      ry /= rn;
+      rz /= rn;
+      if constexpr (WALL == kRelax) dsum += (rem - d) * (sqrtf(disc) / g.R);
+      x = hx - g.nudge * nx;
+      y = hy - g.nudge * ny;
+      z = hz - g.nudge * nz;
+      dx = rx;
+      dy = ry;
+      dz = rz;
+      rem = rem - d - g.nudge;
+    }
+    const float f = fmaxf(rem, 0.f);
+    x += dx * f;
+    y += dy * f;
+    z += dz * f;
+    const float rr = sqrtf(x * x + y * y + z * z);
+    if (rr >= g.R) {  // geometries.py:260-263
+      const float s = (g.R - g.nudge) / rr;
+      x *= s;
+      y *= s;
+      z *= s;
+      ++tl.clamp;
+    }
+    return -2.f * dsum;
+  } else {
+    // geometries.py:367-424 (no snapping and no side clamp, unlike the cylinder)
+    const float dp = dx * x + dy * y + dz * z;
+    const float q2 = x * x + y * y + z * z;
+    float disc = dp * dp - (q2 - g.R2);
+    const bool inside = q2 < g.R2;
+    float sq = sqrtf(fmaxf(disc, 0.f));
+    float t = inside ? -dp + sq : -dp - sq;
+    if (fabsf(disc) < kGrazeTol * g.R2) {
+      const double dpd = (double)dx * x + (double)dy * y + (double)dz * z;
+      const double dd = dpd * dpd - (((double)x * x + (double)y * y + (double)z * z) - (double)g.R * g.R);
+      const double sd = sqrt(fmax(dd, 0.0));
+      disc = (float)dd;
+      sq = (float)sd;
+      t = (float)(inside ? -dpd + sd : -dpd - sd);
+      ++tl.graze;
+    }
+    const bool hit = (disc > 0.f) && (t > g.eps) && (t < l) && (l > 0.f);
+    if (!hit) {
+      x += sx;
+      y += sy;
+      z += sz;
+      return 0.f;
+    }
+    const float hx = x + t * dx, hy = y + t * dy, hz = z + t * dz;
+    const float nx = hx / g.R, ny = hy / g.R, nz = hz / g.R;
+    const float rem = l - t;
+    const float dperp = rem * (sq / g.R);
+    const float p = fminf(1.f, 2.f * g.kod * dperp);
+    if (u < p) {
+      x += sx;
+      y += sy;
+      z += sz;
+      ++tl.transmit;
+      return 0.f;
+    }
+    const float dn = dx * nx + dy * ny + dz * nz;
+    float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny, rz = dz - 2.f * dn * nz;
+    const float rn = sqrtf(rx * rx + ry * ry + rz * rz);
+    rx /= rn;
+    ry /= rn;
+    rz /= rn;
+    const float sgn = inside ? -1.f : 1.f;
+    const float f = fmaxf(rem - g.nudge, 0.f);
+    x = hx + g.nudge * sgn * nx + rx * f;
+    y = hy + g.nudge * sgn * ny + ry * f;
+    z = hz + g.nudge * sgn * nz + rz * f;
+    return -2.f * dperp;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Packed objects: cell lookup of the walker's candidate list.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ int cell_of(float v, const GeoK& g) {
+  int i = (int)floorf((v + g.halfL) * g.inv_h);
+  return min(max(i, 0), g.n - 1);
+}
+
+__device__ __forceinline__ bool min_image(float q, const GeoK& g) {
+  return q >= -g.halfL && q < g.halfL;
+}
+
+__device__ __forceinline__ void fold(float& v, int& img, const GeoK& g) {
+  if (v >= g.halfL) {
+    v -= g.L;
+    ++img;
+  } else if (v < -g.halfL) {
+    v += g.L;
+    --img;
+  }
+}
+
+// Packed cylinders (2-D cross-section; z is free).  cs/cand point at the cell list (shared or
+// global memory).
+template <int WALL>
+__device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, int& iy, float sx,
+                                                 float sy, float u, const GeoK& g,
+                                                 const uint32_t* __restrict__ cs,
+                                                 const float4* __restrict__ cand, Tally& tl) {
+  const float lxy = sqrtf(sx * sx + sy * sy);
+  float dx = 0.f, dy = 0.f;
+  if (lxy > 0.f) {
+    dx = sx / lxy;
+    dy = sy / lxy;
+  }
+  const int c = cell_of(y, g) * g.n + cell_of(x, g);
+  const uint32_t kb = cs[c], ke = cs[c + 1];
+
+  // Nearest wall crossing over the candidates (geometries.py:1777-1805 / 2054-2081).
+  float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hR = 1.f;
+  bool hit_in = false;
+#pragma unroll 1
+  for (uint32_t k = kb; k < ke; ++k) {
+    const float4 C = cand[k];
+    const float qx = x - C.x, qy = y - C.y;
+    if (!(min_image(qx, g) && min_image(qy, g))) continue;
+    const float R2 = C.w * C.w;
+    const float dp = dx * qx + dy * qy;
+    const float q2 = qx * qx + qy * qy;
+    float disc = dp * dp - (q2 - R2);
+    const bool ins = (WALL == kPermeate) && (q2 < R2);
+    if (!ins && dp >= 0.f) continue;  // entry root -dp - sqrt(disc) <= 0: no forward crossing
+    float sq = sqrtf(fmaxf(disc, 0.f));
+    float t = ins ? -dp + sq : -dp - sq;
+    if (fabsf(disc) < kGrazeTol * R2 && t > 0.f && t < 1.01f * lxy) {
+      const double dpd = (double)dx * qx + (double)dy * qy;
+      const double dd = dpd * dpd - (((double)qx * qx + (double)qy * qy) - (double)C.w * C.w);
+      const double sd = sqrt(fmax(dd, 0.0));
+      disc = (float)dd;
+      t = (float)(ins ? -dpd + sd : -dpd - sd);
+      ++tl.graze;
+    }
+    const bool valid = (disc > 0.f) && (t > g.eps) && (t < lxy) && (lxy > 0.f);
+    if (valid && t < tbest) {
+      tbest = t;
+      disc_hit = disc;
+      hcx = C.x;
+      hcy = C.y;
+      hR = C.w;
+      hit_in = ins;
+    }
+  }
+
+  float nxp, nyp;  // new position in the start cell's frame
+  float dlog = 0.f;
+  if (tbest < INFINITY) {
+    const float qcx = x - hcx, qcy = y - hcy;
+    if constexpr (WALL != kPermeate) {
+      // geometries.py:1810-1842 / 1943-1967
+      const float nx = (qcx + tbest * dx) / hR, ny = (qcy + tbest * dy) / hR;
+      const float dn = dx * nx + dy * ny;
+      float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
+      const float rn = sqrtf(rx * rx + ry * ry);
+      if (rn > 0.f) {
+        rx /= fmaxf(rn, 1e-30f);
+        ry /= fmaxf(rn, 1e-30f);
+      } else {
+        rx = 0.f;
+        ry = 0.f;
+      }
+      const float remr = lxy - tbest;
+      const float f = fmaxf(remr - g.nudge, 0.f);
+      nxp = (x + tbest * dx) + g.nudge * nx + rx * f;
+      nyp = (y + tbest * dy) + g.nudge * ny + ry * f;
+      if constexpr (WALL == kRelax) dlog = -2.f * (remr * (sqrtf(fmaxf(disc_hit, 0.f)) / hR));
+    } else {
+      // geometries.py:2083-2165
+      const float hrx = qcx + tbest * dx, hry = qcy + tbest * dy;
+      const float hl = fmaxf(sqrtf(hrx * hrx + hry * hry), 1e-30f);
+      const float nx = hrx / hl, ny = hry / hl;
+      const float rem = lxy - tbest;
+      const float dperp = rem * (sqrtf(fmaxf(disc_hit, 0.f)) / hR);
+      const float p = fminf(1.f, 2.f * g.kod * dperp);
+      if (u < p) {
+        nxp = x + sx;
+        nyp = y + sy;
+        ++tl.transmit;
+      } else {
+        const float dn = dx * nx + dy * ny;
+        float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
+        const float rn = sqrtf(rx * rx + ry * ry);
+        if (rn > 0.f) {
+          rx /= fmaxf(rn, 1e-30f);
+          ry /= fmaxf(rn, 1e-30f);
+        } else {
+          rx = 0.f;
+          ry = 0.f;
+        }
+        const float sgn = hit_in ? -1.f : 1.f;
+        const float f = fmaxf(rem - g.nudge, 0.f);
+        float ox = hR * nx + g.nudge * sgn * nx + rx * f;
+        float oy = hR * ny + g.nudge * sgn * ny + ry * f;
+        const float on = sqrtf(ox * ox + oy * oy);
+        const bool wrong = hit_in ? (on >= hR) : (on <= hR);
+        if (wrong) {
+          const float s = (hit_in ? hR - g.nudge : hR + g.nudge) / fmaxf(on, 1e-30f);
+          ox *= s;
+          oy *= s;
+          ++tl.clamp;
+        }
+        nxp = x + (ox - qcx);
+        nyp = y + (oy - qcy);
+        dlog = -2.f * dperp;
+      }
+    }
+  } else {
+    nxp = x + sx;
+    nyp = y + sy;
+  }
+
+  if constexpr (WALL != kPermeate) {
+    // Fold-first safety clamp (geometries.py:1851-1877): push the walker out of the object it
+    // penetrates most deeply (relative to R^2).  The start cell's list covers every object within
+    // reach of the end point.
+    float pbest = 1.f, qbx = 0.f, qby = 0.f, Rb = 1.f;
+#pragma unroll 1
+    for (uint32_t k = kb; k < ke; ++k) {
+      const float4 C = cand[k];
+      const float qx = nxp - C.x, qy = nyp - C.y;
+      if (!(min_image(qx, g) && min_image(qy, g))) continue;
+      const float d2 = qx * qx + qy * qy, R2 = C.w * C.w;
+      if (d2 < R2) {
+        const float pen = d2 / R2;
+        if (pen < pbest) {
+          pbest = pen;
+          qbx = qx;
+          qby = qy;
+          Rb = C.w;
+        }
+      }
+    }
+    if (pbest < 1.f) {
+      const float dcl = sqrtf(qbx * qbx + qby * qby);
+      const float s = (Rb + g.nudge) / fmaxf(dcl, g.nudge);
+      nxp += qbx * (s - 1.f);
+      nyp += qby * (s - 1.f);
+      ++tl.clamp;
+    }
+  }
+  x = nxp;
+  y = nyp;
+  fold(x, ix, g);
+  fold(y, iy, g);
+  return dlog;
+}
+
+// Packed spheres (3-D periodic cell).
+template <int WALL>
+__device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, int& ix, int& iy,
+                                                 int& iz, float sx, float sy, float sz, float u,
+                                                 const GeoK& g, const uint32_t* __restrict__ cs,
+                                                 const float4* __restrict__ cand, Tally& tl) {
+  const float l = sqrtf(sx * sx + sy * sy + sz * sz);
+  float dx = 0.f, dy = 0.f, dz = 0.f;
+  if (l > 0.f) {
+    dx = sx / l;
+    dy = sy / l;
+    dz = sz / l;
+  }
+  const int c = (cell_of(z, g) * g.n + cell_of(y, g)) * g.n + cell_of(x, g);
+  const uint32_t kb = cs[c], ke = cs[c + 1];
+
+  float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hcz = 0.f, hR = 1.f;
+  bool hit_in = false;
+#pragma unroll 1
+  for (uint32_t k = kb; k < ke; ++k) {
+    const float4 C = cand[k];
+    const float qx = x - C.x, qy = y - C.y, qz = z - C.z;
+    if (!(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
+    const float R2 = C.w * C.w;
+    const float dp = dx * qx + dy * qy + dz * qz;
+    const float q2 = qx * qx + qy * qy + qz * qz;
+    float disc = dp * dp - (q2 - R2);
+    const bool ins = (WALL == kPermeate) && (q2 < R2);
+    if (!ins && dp >= 0.f) continue;
+    float sq = sqrtf(fmaxf(disc, 0.f));
+    float t = ins ? -dp + sq : -dp - sq;
+    if (fabsf(disc) < kGrazeTol * R2 && t > 0.f && t < 1.01f * l) {
+      const double dpd = (double)dx * qx + (double)dy * qy + (double)dz * qz;
+      const double dd = dpd * dpd - (((double)qx * qx + (double)qy * qy + (double)qz * qz) -
+                                     (double)C.w * C.w);
+      const double sd = sqrt(fmax(dd, 0.0));
+      disc = (float)dd;
+      t = (float)(ins ? -dpd + sd : -dpd - sd);
+      ++tl.graze;
+    }
+    const bool valid = (disc > 0.f) && (t > g.eps) && (t < l) && (l > 0.f);
+    if (valid && t < tbest) {
+      tbest = t;
+      disc_hit = disc;
+      hcx = C.x;
+      hcy = C.y;
+      hcz = C.z;
+      hR = C.w;
+      hit_in = ins;
+    }
+  }
+
+  float nxp, nyp, nzp;
+  float dlog = 0.f;
+  if (tbest < INFINITY) {
+    const float qcx = x - hcx, qcy = y - hcy, qcz = z - hcz;
+    if constexpr (WALL != kPermeate) {
+      // geometries.py:2490-2515 / 2584-2604
+      const float nx = (qcx + tbest * dx) / hR, ny = (qcy + tbest * dy) / hR,
+                  nz = (qcz + tbest * dz) / hR;
+      const float dn = dx * nx + dy * ny + dz * nz;
+      float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny, rz = dz - 2.f * dn * nz;
+      const float rn = sqrtf(rx * rx + ry * ry + rz * rz);
+      if (rn > 0.f) {
+        const float inv = 1.f / fmaxf(rn, 1e-30f);
+        rx *= inv;
+        ry *= inv;
+        rz *= inv;
+      } else {
+        rx = ry = rz = 0.f;
+      }
+      const float remr = l - tbest;
+      const float f = fmaxf(remr - g.nudge, 0.f);
+      nxp = (x + tbest * dx) + g.nudge * nx + rx * f;
+      nyp = (y + tbest * dy) + g.nudge * ny + ry * f;
+      nzp = (z + tbest * dz) + g.nudge * nz + rz * f;
+      if constexpr (WALL == kRelax) dlog = -2.f * (remr * (sqrtf(fmaxf(disc_hit, 0.f)) / hR));
+    } else {
+      // geometries.py:2690-2745
+      const float hrx = qcx + tbest * dx, hry = qcy + tbest * dy, hrz = qcz + tbest * dz;
+      const float hl = fmaxf(sqrtf(hrx * hrx + hry * hry + hrz * hrz), 1e-30f);
+      const float nx = hrx / hl, ny = hry / hl, nz = hrz / hl;
+      const float rem = l - tbest;
+      const float dperp = rem * (sqrtf(fmaxf(disc_hit, 0.f)) / hR);
+      const float p = fminf(1.f, 2.f * g.kod * dperp);
+      if (u < p) {
+        nxp = x + sx;
+        nyp = y + sy;
+        nzp = z + sz;
+        ++tl.transmit;
+      } else {
+        const float dn = dx * nx + dy * ny + dz * nz;
+        float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny, rz = dz - 2.f * dn * nz;
+        const float rn = sqrtf(rx * rx + ry * ry + rz * rz);
+        if (rn > 0.f) {
+          const float inv = 1.f / fmaxf(rn, 1e-30f);
+          rx *= inv;
+          ry *= inv;
+          rz *= inv;
+        } else {
+          rx = ry = rz = 0.f;
+        }
+        const float sgn = hit_in ? -1.f : 1.f;
+        const float f = fmaxf(rem - g.nudge, 0.f);
+        float ox = hR * nx + g.nudge * sgn * nx + rx * f;
+        float oy = hR * ny + g.nudge * sgn * ny + ry * f;
+        float oz = hR * nz + g.nudge * sgn * nz + rz * f;
+        const float on = sqrtf(ox * ox + oy * oy + oz * oz);
+        const bool wrong = hit_in ? (on >= hR) : (on <= hR);
+        if (wrong) {
+          const float s = (hit_in ? hR - g.nudge : hR + g.nudge) / fmaxf(on, 1e-30f);
+          ox *= s;
+          oy *= s;
+          oz *= s;
+          ++tl.clamp;
+        }
+        nxp = x + (ox - qcx);
+        nyp = y + (oy - qcy);
+        nzp = z + (oz - qcz);
+        dlog = -2.f * dperp;
+      }
+    }
+  } else {
+    nxp = x + sx;
+    nyp = y + sy;
+    nzp = z + sz;
+  }
+
+  if constexpr (WALL != kPermeate) {
+    float pbest = 1.f, qbx = 0.f, qby = 0.f, qbz = 0.f, Rb = 1.f;
+#pragma unroll 1
+    for (uint32_t k = kb; k < ke; ++k) {
+      const float4 C = cand[k];
+      const float qx = nxp - C.x, qy = nyp - C.y, qz = nzp - C.z;
+      if (!(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
+      const float d2 = qx * qx + qy * qy + qz * qz, R2 = C.w * C.w;
+      if (d2 < R2) {
+        const float pen = d2 / R2;
+        if (pen < pbest) {
+          pbest = pen;
+          qbx = qx;
+          qby = qy;
+          qbz = qz;
+          Rb = C.w;
+        }
+      }
+    }
+    if (pbest < 1.f) {  // geometries.py:2520-2535
+      const float dcl = sqrtf(qbx * qbx + qby * qby + qbz * qbz);
+      const float s = (Rb + g.nudge) / fmaxf(dcl, g.nudge);
+      nxp += qbx * (s - 1.f);
+      nyp += qby * (s - 1.f);
+      nzp += qbz * (s - 1.f);
+      ++tl.clamp;
+    }
+  }
+  x = nxp;
+  y = nyp;
+  z = nzp;
+  fold(x, ix, g);
+  fold(y, iy, g);
+  fold(z, iz, g);
+  return dlog;
+}
+
+}  // namespace dmsim

@@ -1,0 +1,485 @@
+// The persistent walk kernel: one walker per thread, walker state in registers.
+//
+// Replaces the vmap(lax.scan(step_fn)) of dmipy-sim (core.py:700-727, physics.py:191-417) and the
+// producer walk of simulate_trajectories (core.py:1137-1155, 1246-1307).  Per block:
+//   * the packed-object cell list is staged into shared memory once with a bulk async copy
+//     (cp.async.bulk + mbarrier), when it fits;
+//   * the gradient waveform streams through shared memory in chunks of kTC samples, double
+//     buffered with bulk async copies, so every walker of the block reads each G(t) as a
+//     broadcast;
+//   * each thread walks its walker for all n_t samples x S sub-steps, drawing from a Philox
+//     stream keyed by (seed, global walker index);
+//   * the phase of MT measurements is accumulated in FP32 registers with Kahan compensation:
+//       phi_m += gamma_dt * g_m(t) . R(t)
+//     where R(t) is the sample's last position (walk-once + replay, trajectories.py:550-552) or the
+//     sum of the S sub-step positions (fused engine: G is constant over the sub-steps of a sample,
+//     physics.py:293-317, so sum_s g.r_s = g . sum_s r_s);
+//   * at every echo sample the block reduces w*cos(phi), w*sin(phi) and (w*cos(phi))^2 with warp
+//     shuffles and adds them, in FP64 and in a fixed order, into the block's own partial slice.
+// Blocks loop over walker tiles (grid = SMs x resident blocks), so the partial buffer is
+// independent of n_walkers.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dmsim.h"
+#include "geometry.cuh"
+#include "philox.cuh"
+
+namespace dmsim {
+
+constexpr int kBlock = 128;  // walkers per tile
+constexpr int kWarps = kBlock / 32;
+constexpr int kTC = 16;  // samples per staged waveform chunk
+constexpr int kMaxEcho = 512;
+
+struct KArgs {
+  int64_t n_walkers, walker_offset;
+  uint64_t seed;
+  int n_t, n_chunks, S, phase_sub, has_weight, n_echo, Mp, pass, M;
+  float step_l, gamma_dt, t2dec, t1dec, rho;
+  GeoK g;
+  uint32_t tab_cs_bytes, tab_cand_bytes;  // shared-memory staging sizes (multiples of 16 B)
+  const uint32_t* cs;
+  const float4* cand;
+  const int32_t* cand_obj;
+  const float* Gp;          // this pass, (n_chunks*kTC, MT, 3)
+  const uint8_t* active;    // this pass, (n_t): 1 where some g_m(t) != 0
+  const float* chi;         // (n_t) or null
+  const float* r0;          // (n_walkers, 3) or null
+  double* part;             // [gridDim.x][n_echo][Mp][3]
+  uint32_t* status;
+  float* final_pos;
+  float* log_w;
+  float* phi_out;
+  int32_t* comp0;
+  int32_t* comp_end;
+  void* traj;
+  int traj_f16;
+  float* dlog_unit;
+  float* comp_occ;
+  int echo[kMaxEcho];
+};
+
+// ---- shared-memory async-copy helpers (bulk copy + mbarrier), bounded waits -------------------
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(saddr(dst)),
+      "l"(src), "r"(bytes), "r"(saddr(b))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Gives up after a bounded number of polls (well under a second) instead of spinning forever.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  for (uint32_t i = 0; i < (1u << 22); ++i)
+    if (mbar_try(b, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int MT>
+__host__ __device__ constexpr size_t walk_smem_fixed() {
+  // two waveform chunk buffers + 3 mbarriers/flags (64 B) + warp reduction scratch
+  return (size_t)2 * kTC * MT * 3 * 4 + 64 + (size_t)kWarps * MT * 3 * 4;
+}
+
+template <int GEOM>
+__device__ __forceinline__ int classify(float x, float y, float z, const GeoK& g,
+                                        const uint32_t* cs, const float4* cand,
+                                        const int32_t* cobj) {
+  if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
+    return (x * x + y * y < g.R2) ? 0 : 1;  // geometries.py:803-813
+  } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
+    return (x * x + y * y + z * z < g.R2) ? 0 : 1;  // geometries.py:161-165
+  } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES) {
+    // 0 = extra, k+1 = inside object k; the largest id wins (geometries.py:2185-2214)
+    constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
+    int c = cell_of(y, g) * g.n + cell_of(x, g);
+    if (P3) c = cell_of(z, g) * g.n * g.n + c;
+    int id = 0;
+    for (uint32_t k = cs[c]; k < cs[c + 1]; ++k) {
+      const float4 C = cand[k];
+      const float qx = x - C.x, qy = y - C.y, qz = P3 ? z - C.z : 0.f;
+      if (!(min_image(qx, g) && min_image(qy, g) && (!P3 || min_image(qz, g)))) continue;
+      if (qx * qx + qy * qy + qz * qz < C.w * C.w) id = max(id, cobj[k] + 1);
+    }
+    return id;
+  } else {
+    return 0;
+  }
+}
+
+template <int GEOM, int WALL, int MT, bool TSM>
+__global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  constexpr int GCH = kTC * MT * 3;  // floats per waveform chunk
+  float* Gs = reinterpret_cast<float*>(smem);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + (size_t)2 * GCH * 4);
+  volatile int* s_abort = reinterpret_cast<volatile int*>(smem + (size_t)2 * GCH * 4 + 32);
+  float* red = reinterpret_cast<float*>(smem + (size_t)2 * GCH * 4 + 64);
+  uint8_t* tab = smem + walk_smem_fixed<MT>();
+
+  constexpr bool PACKED = GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES;
+  constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const GeoK g = a.g;
+
+  const uint32_t* cs = a.cs;
+  const float4* cand = a.cand;
+  if constexpr (PACKED && TSM) {
+    cs = reinterpret_cast<const uint32_t*>(tab);
+    cand = reinterpret_cast<const float4*>(tab + a.tab_cs_bytes);
+  }
+
+  const int64_t n_tiles = (a.n_walkers + kBlock - 1) / kBlock;
+  const int my_tiles = (int)((n_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
+  const int64_t total_chunks = (int64_t)my_tiles * a.n_chunks;
+  const uint32_t chunk_bytes = (uint32_t)GCH * 4u;
+
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    *s_abort = 0;
+    fence_async_smem();
+  }
+  // zero this block's partial slice for this pass
+  for (int e = 0; e < a.n_echo; ++e)
+    for (int j = tid; j < MT * 3; j += kBlock)
+      a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] = 0.0;
+  __syncthreads();
+  if (tid == 0) {
+    if constexpr (PACKED && TSM) {
+      mbar_expect(&bar[2], a.tab_cs_bytes + a.tab_cand_bytes);
+      bulk_g2s(tab, a.cs, a.tab_cs_bytes, &bar[2]);
+      bulk_g2s(tab + a.tab_cs_bytes, a.cand, a.tab_cand_bytes, &bar[2]);
+    }
+    if (total_chunks > 0) {
+      mbar_expect(&bar[0], chunk_bytes);
+      bulk_g2s(Gs, a.Gp, chunk_bytes, &bar[0]);
+    }
+  }
+  if constexpr (PACKED && TSM) {
+    if (!mbar_wait(&bar[2], 0)) *s_abort = 1;
+    __syncthreads();
+    if (*s_abort) {
+      if (tid == 0) {
+        atomicAdd(&a.status[DMSIM_STATUS_WAIT_TIMEOUT], 1u);
+        if (total_chunks > 0) mbar_wait(&bar[0], 0);
+      }
+      return;
+    }
+  }
+
+  Tally tl;
+  uint32_t n_nonfinite = 0, n_initfail = 0;
+  int64_t q = 0;  // running chunk counter of this block
+
+  for (int it = 0; it < my_tiles; ++it) {
+    const int64_t tile = blockIdx.x + (int64_t)it * gridDim.x;
+    const int64_t w = tile * kBlock + tid;
+    const bool act = w < a.n_walkers;
+    const uint64_t gw = (uint64_t)(a.walker_offset + w);
+
+    // ---- initial position -----------------------------------------------------------------
+    float x = 0.f, y = 0.f, z = 0.f;
+    int ix = 0, iy = 0, iz = 0;
+    if (a.r0 != nullptr) {
+      if (act) {
+        x = a.r0[3 * w];
+        y = a.r0[3 * w + 1];
+        z = a.r0[3 * w + 2];
+      }
+      if constexpr (PACKED) {
+        ix = (int)floorf(x / g.L + 0.5f);
+        x -= g.L * ix;
+        iy = (int)floorf(y / g.L + 0.5f);
+        y -= g.L * iy;
+        if (P3) {
+          iz = (int)floorf(z / g.L + 0.5f);
+          z -= g.L * iz;
+        }
+      }
+    } else if constexpr (GEOM != DMSIM_GEOM_FREE) {
+      // Uniform seeding by rejection, as the reference's host samplers (geometries.py:186-195,
+      // 477-491, 1717-1744, 2421-2443), on the seeding stream.
+      bool ok = false;
+#pragma unroll 1
+      for (uint32_t j = 0; j < 256u && !ok; ++j) {
+        const u32x4 r = draw(a.seed, gw, 1u, j);
+        const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z), u3 = u01(r.w);
+        if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
+          float px = g.R * (2.f * u0 - 1.f), py = g.R * (2.f * u1 - 1.f);
+          if (px * px + py * py < g.R2) {
+            x = px; y = py; ok = true;
+          } else {
+            px = g.R * (2.f * u2 - 1.f);
+            py = g.R * (2.f * u3 - 1.f);
+            if (px * px + py * py < g.R2) { x = px; y = py; ok = true; }
+          }
+        } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
+          const float px = g.R * (2.f * u0 - 1.f), py = g.R * (2.f * u1 - 1.f),
+                      pz = g.R * (2.f * u2 - 1.f);
+          if (px * px + py * py + pz * pz < g.R2) { x = px; y = py; z = pz; ok = true; }
+        } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS) {
+          for (int h = 0; h < 2 && !ok; ++h) {
+            const float px = g.L * ((h ? u2 : u0) - 0.5f), py = g.L * ((h ? u3 : u1) - 0.5f);
+            const int c = cell_of(py, g) * g.n + cell_of(px, g);
+            bool out = true;
+            for (uint32_t k = cs[c]; k < cs[c + 1]; ++k) {
+              const float4 C = cand[k];
+              const float qx = px - C.x, qy = py - C.y;
+              if (qx * qx + qy * qy <= C.w * C.w) out = false;
+            }
+            if (out) { x = px; y = py; ok = true; }
+          }
+        } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
+          const float px = g.L * (u0 - 0.5f), py = g.L * (u1 - 0.5f), pz = g.L * (u2 - 0.5f);
+          const int c = (cell_of(pz, g) * g.n + cell_of(py, g)) * g.n + cell_of(px, g);
+          bool out = true;
+          for (uint32_t k = cs[c]; k < cs[c + 1]; ++k) {
+            const float4 C = cand[k];
+            const float qx = px - C.x, qy = py - C.y, qz = pz - C.z;
+            if (qx * qx + qy * qy + qz * qz <= C.w * C.w) out = false;
+          }
+          if (out) { x = px; y = py; z = pz; ok = true; }
+        }
+      }
+      if (!ok && act) ++n_initfail;
+    }
+    if (act && a.comp0 != nullptr && a.pass == 0)
+      a.comp0[w] = classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+
+    float phi[MT], kc[MT];
+#pragma unroll
+    for (int m = 0; m < MT; ++m) phi[m] = kc[m] = 0.f;
+    float logw = 0.f;
+    uint32_t s = 0;   // global sub-step counter of this walker
+    u32x4 rr{0, 0, 0, 0};
+    int e = 0;        // next echo ordinal
+    int t = 0;
+
+    for (int ch = 0; ch < a.n_chunks; ++ch, ++q) {
+      // ---- waveform chunk pipeline: prefetch q+1, wait for q ----------------------------------
+      __syncthreads();
+      if (tid == 0 && q + 1 < total_chunks) {
+        const int64_t qn = q + 1;
+        const int src_chunk = (int)(qn % a.n_chunks);
+        fence_async_smem();
+        mbar_expect(&bar[qn & 1], chunk_bytes);
+        bulk_g2s(Gs + (qn & 1) * GCH, a.Gp + (size_t)src_chunk * GCH, chunk_bytes, &bar[qn & 1]);
+      }
+      if (!mbar_wait(&bar[q & 1], (uint32_t)((q >> 1) & 1))) *s_abort = 1;
+      __syncthreads();
+      if (*s_abort) {
+        if (tid == 0) {
+          atomicAdd(&a.status[DMSIM_STATUS_WAIT_TIMEOUT], 1u);
+          if (q + 1 < total_chunks) mbar_wait(&bar[(q + 1) & 1], (uint32_t)(((q + 1) >> 1) & 1));
+        }
+        return;
+      }
+      const float* Gc = Gs + (q & 1) * GCH;
+
+      const int t_end = min(a.n_t, (ch + 1) * kTC);
+#pragma unroll 1
+      for (; t < t_end; ++t) {
+        const float chi = a.chi ? __ldg(a.chi + t) : 1.f;
+        const float rc = a.rho * chi;
+        const float dec = a.t2dec * chi + a.t1dec * (1.f - chi);
+        float Rx = 0.f, Ry = 0.f, Rz = 0.f, dls = 0.f, occ = 0.f;
+#pragma unroll 1
+        for (int sub = 0; sub < a.S; ++sub, ++s) {
+          float ua, ub, up = 0.f;
+          if constexpr (WALL == kPermeate) {
+            rr = draw(a.seed, gw, 0u, s);
+            ua = u01(rr.x);
+            ub = u01(rr.y);
+            up = u01(rr.z);
+          } else {
+            if ((s & 1u) == 0u) {
+              rr = draw(a.seed, gw, 0u, s >> 1);
+              ua = u01(rr.x);
+              ub = u01(rr.y);
+            } else {
+              ua = u01(rr.z);
+              ub = u01(rr.w);
+            }
+          }
+          // isotropic direction from two uniforms: cos(theta) = 1 - 2 ua, azimuth = pi (2 ub - 1)
+          const float cz = 1.f - 2.f * ua;
+          const float sz = sqrtf(fmaxf(0.f, 1.f - cz * cz));
+          float sn, cs_;
+          __sincosf(3.14159265358979f * (2.f * ub - 1.f), &sn, &cs_);
+          const float stx = a.step_l * sz * cs_, sty = a.step_l * sz * sn, stz = a.step_l * cz;
+
+          float dl = 0.f;
+          if constexpr (GEOM == DMSIM_GEOM_FREE) {
+            x += stx;
+            y += sty;
+            z += stz;
+          } else if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
+            dl = cylinder_step<WALL>(x, y, stx, sty, up, g, tl);
+            z += stz;
+          } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
+            dl = sphere_step<WALL>(x, y, z, stx, sty, stz, up, g, tl);
+          } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS) {
+            dl = packed_cyl_step<WALL>(x, y, ix, iy, stx, sty, up, g, cs, cand, tl);
+            z += stz;
+          } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
+            dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tl);
+          }
+          if (a.has_weight) logw += rc * dl - dec;
+          if (a.phase_sub) {
+            Rx += x + g.L * (float)ix;
+            Ry += y + g.L * (float)iy;
+            Rz += z + g.L * (float)iz;
+          }
+          if (a.dlog_unit) dls += dl;
+          if (a.comp_occ) occ += (float)classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+        }
+        const float ux = x + g.L * (float)ix, uy = y + g.L * (float)iy, uz = z + g.L * (float)iz;
+        if (!a.phase_sub) {
+          Rx = ux;
+          Ry = uy;
+          Rz = uz;
+        }
+        // ---- phase: phi_m += gamma_dt * g_m(t) . R(t), Kahan-compensated --------------------
+        if (__ldg(a.active + t)) {
+          const float px = a.gamma_dt * Rx, py = a.gamma_dt * Ry, pz = a.gamma_dt * Rz;
+          const float4* g4 = reinterpret_cast<const float4*>(Gc + (t - ch * kTC) * MT * 3);
+          float acc = 0.f;
+#pragma unroll
+          for (int j = 0; j < MT * 3 / 4; ++j) {
+            const float4 v = g4[j];
+            const float gv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              const int el = 4 * j + h, m = el / 3, k = el % 3;
+              const float pk = k == 0 ? px : (k == 1 ? py : pz);
+              acc = (k == 0) ? gv[h] * pk : fmaf(gv[h], pk, acc);
+              if (k == 2) {
+                const float yk = acc - kc[m];
+                const float tk = phi[m] + yk;
+                kc[m] = (tk - phi[m]) - yk;
+                phi[m] = tk;
+              }
+            }
+          }
+        }
+        if (act) {
+          if (a.traj != nullptr && a.pass == 0) {
+            const size_t o = ((size_t)w * a.n_t + t) * 3;
+            if (a.traj_f16) {
+              __half* tp = reinterpret_cast<__half*>(a.traj);
+              tp[o] = __float2half_rn(ux);
+              tp[o + 1] = __float2half_rn(uy);
+              tp[o + 2] = __float2half_rn(uz);
+            } else {
+              float* tp = reinterpret_cast<float*>(a.traj);
+              tp[o] = ux;
+              tp[o + 1] = uy;
+              tp[o + 2] = uz;
+            }
+          }
+          if (a.dlog_unit != nullptr && a.pass == 0) a.dlog_unit[(size_t)w * a.n_t + t] = dls;
+          if (a.comp_occ != nullptr && a.pass == 0)
+            a.comp_occ[(size_t)w * a.n_t + t] = occ / (float)a.S;
+        }
+        // ---- ensemble sums at an echo sample (block-uniform branch) --------------------------
+        if (e < a.n_echo && t == a.echo[e]) {
+          const float wgt = act ? (a.has_weight ? expf(logw) : 1.f) : 0.f;
+#pragma unroll
+          for (int m = 0; m < MT; ++m) {
+            float sn, cs_;
+            sincosf(phi[m], &sn, &cs_);
+            const float c1 = warp_sum(wgt * cs_);
+            const float c2 = warp_sum(wgt * sn);
+            const float c3 = warp_sum((wgt * cs_) * (wgt * cs_));
+            if (lane == 0) {
+              red[warp * MT * 3 + 3 * m] = c1;
+              red[warp * MT * 3 + 3 * m + 1] = c2;
+              red[warp * MT * 3 + 3 * m + 2] = c3;
+            }
+          }
+          __syncthreads();
+          for (int j = tid; j < MT * 3; j += kBlock) {
+            double acc = 0.0;
+#pragma unroll
+            for (int ww = 0; ww < kWarps; ++ww) acc += (double)red[ww * MT * 3 + j];
+            a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] += acc;
+          }
+          __syncthreads();
+          ++e;
+        }
+      }
+    }
+
+    // ---- per-walker outputs --------------------------------------------------------------------
+    const float ux = x + g.L * (float)ix, uy = y + g.L * (float)iy, uz = z + g.L * (float)iz;
+    if (act) {
+      if (!(isfinite(ux) && isfinite(uy) && isfinite(uz))) ++n_nonfinite;
+      if (a.pass == 0) {
+        if (a.final_pos) {
+          a.final_pos[3 * w] = ux;
+          a.final_pos[3 * w + 1] = uy;
+          a.final_pos[3 * w + 2] = uz;
+        }
+        if (a.log_w) a.log_w[w] = logw;
+        if (a.comp_end) a.comp_end[w] = classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+      }
+      if (a.phi_out) {
+#pragma unroll
+        for (int m = 0; m < MT; ++m)
+          if (a.pass * MT + m < a.M) a.phi_out[(size_t)w * a.M + a.pass * MT + m] = phi[m];
+      }
+    }
+  }
+
+  // ---- anomaly tallies ------------------------------------------------------------------------
+  const uint32_t v0 = __reduce_add_sync(0xffffffffu, n_nonfinite);
+  const uint32_t v1 = __reduce_add_sync(0xffffffffu, tl.clamp);
+  const uint32_t v2 = __reduce_add_sync(0xffffffffu, n_initfail);
+  const uint32_t v3 = __reduce_add_sync(0xffffffffu, tl.graze);
+  const uint32_t v4 = __reduce_add_sync(0xffffffffu, tl.transmit);
+  if (lane == 0 && a.pass == 0) {
+    if (v0) atomicAdd(&a.status[DMSIM_STATUS_NONFINITE], v0);
+    if (v1) atomicAdd(&a.status[DMSIM_STATUS_CLAMPED], v1);
+    if (v2) atomicAdd(&a.status[DMSIM_STATUS_INIT_FAIL], v2);
+    if (v3) atomicAdd(&a.status[DMSIM_STATUS_GRAZE_FP64], v3);
+    if (v4) atomicAdd(&a.status[DMSIM_STATUS_TRANSMIT], v4);
+  }
+}
+
+using WalkFn = void (*)(KArgs);
+
+}  // namespace dmsim

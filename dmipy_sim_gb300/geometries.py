@@ -1,0 +1,491 @@
+"""Substrate geometries: host-side objects that describe the walls and build the device descriptor.
+
+Same constructors, attribute names and conventions as dmipy-sim's geometries.py (FreeDiffusion
+34-45, Sphere 143-424, Cylinder 427-844, pack_cylinders 1502-1601, PackedCylinders 1604-2242,
+pack_spheres 2249-2340, PackedSpheres 2343-2786, _rotation_to_z 1466-1495).  The per-walker
+``reflect`` / ``reflect_with_log_weight`` / ``permeate`` plug-ins of the reference are not Python
+functions here: each geometry compiles to a POD ``dmsim_geometry`` descriptor (include/dmsim.h)
+consumed by the CUDA step functions, and packed substrates additionally get a uniform cell list
+(every object within reach of each cell, pre-shifted to its periodic image) on the device.
+"""
+import itertools
+
+import numpy as np
+import torch
+
+from . import _lib
+
+__all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders",
+           "pack_spheres", "PackedSpheres"]
+
+
+def _rotation_to_z(v):
+    """Rotation matrix R with R @ v = [0, 0, 1] (Rodrigues; geometries.py:1466-1495)."""
+    v = np.asarray(v, dtype=np.float64)
+    v = v / np.linalg.norm(v)
+    k = np.array([0.0, 0.0, 1.0])
+    dot = float(np.dot(v, k))
+    if abs(dot - 1.0) < 1e-10:
+        return np.eye(3)
+    if abs(dot + 1.0) < 1e-10:
+        return np.diag([1.0, -1.0, -1.0])
+    axis = np.cross(v, k)
+    axis = axis / np.linalg.norm(axis)
+    ang = np.arccos(np.clip(dot, -1.0, 1.0))
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * (K @ K)
+
+
+class Geometry:
+    """Base class.  Subclasses provide ``_desc(...)`` (the device descriptor) and ``_frame()``
+    (the lab -> walk-frame rotation, or None when the walk runs in the lab frame)."""
+
+    surface_relaxivity_t2 = None
+    permeability = None
+
+    def _frame(self):
+        return None
+
+    def _wall_mode(self, with_weight_channel):
+        if self.permeability is not None:
+            return _lib.WALL_PERMEATE
+        if with_weight_channel:
+            return _lib.WALL_RELAX
+        return _lib.WALL_REFLECT
+
+    def _base_desc(self, kind, wall_mode, rho_over_D, kappa_over_D):
+        g = _lib.Geometry()
+        g.kind = kind
+        g.wall_mode = wall_mode
+        g.rho_over_D = float(rho_over_D)
+        g.kappa_over_D = float(kappa_over_D)
+        return g
+
+
+class FreeDiffusion(Geometry):
+    """Unbounded free diffusion; walkers start at the origin (geometries.py:34-45)."""
+
+    def classify_position(self, r):
+        return np.zeros(np.shape(r)[:-1], dtype=np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        return np.zeros((n_walkers, 3), dtype=np.float32)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        return self._base_desc(_lib.GEOM_FREE, _lib.WALL_REFLECT, 0.0, 0.0), ()
+
+
+def _opt_float(v):
+    return float(v) if v is not None else None
+
+
+def _host_rng(key):
+    return np.random.default_rng(None if key is None else int(np.asarray(key).ravel()[-1]))
+
+
+class Sphere(Geometry):
+    """Reflecting (optionally relaxing / permeable) sphere of radius R at the origin
+    (geometries.py:143-424).  Exchange time R/(3 kappa); surface T2 = R/(3 rho)."""
+
+    def __init__(self, radius, surface_relaxivity_t2=None, permeability=None):
+        self.radius = float(radius)
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+        self.permeability = _opt_float(permeability)
+
+    def volume(self):
+        return (4.0 / 3.0) * np.pi * self.radius ** 3
+
+    def surface_area(self):
+        return 4.0 * np.pi * self.radius ** 2
+
+    def classify_position(self, r):
+        r = np.asarray(r, dtype=np.float32)
+        return np.where(np.sum(r * r, axis=-1) < np.float32(self.radius) ** 2, 0, 1).astype(np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        """Uniform inside the sphere (host rejection sampling, geometries.py:186-195)."""
+        rng = _host_rng(key)
+        out = []
+        while sum(len(a) for a in out) < n_walkers:
+            p = rng.uniform(-self.radius, self.radius, (n_walkers * 4, 3))
+            out.append(p[np.linalg.norm(p, axis=1) < self.radius])
+        return np.concatenate(out)[:n_walkers].astype(np.float32)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        g = self._base_desc(_lib.GEOM_SPHERE, wall_mode, rho_over_D, kappa_over_D)
+        g.radius = self.radius
+        g.eps_detect = np.float32(1e-7 * self.radius)
+        g.nudge = np.float32(1e-4 * self.radius)
+        return g, ()
+
+
+class Cylinder(Geometry):
+    """Infinite cylinder of radius R along ``orientation`` (geometries.py:427-844).
+
+    The walk runs in the cylinder frame (``_R @ orientation = z``); gradients are rotated into it
+    and positions out of it by the engine.
+    """
+
+    def __init__(self, radius, orientation, surface_relaxivity_t2=None, permeability=None):
+        self.radius = float(radius)
+        o = np.asarray(orientation, dtype=np.float64)
+        self.orientation = (o / np.linalg.norm(o)).astype(np.float32)
+        R = _rotation_to_z(self.orientation)
+        self._R = R.astype(np.float32)
+        self._R_inv = R.T.astype(np.float32)
+        self._is_identity_rotation = bool(np.allclose(R, np.eye(3)))
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+        self.permeability = _opt_float(permeability)
+
+    def _frame(self):
+        return None if self._is_identity_rotation else self._R.astype(np.float64)
+
+    def classify_position(self, r):
+        r = np.asarray(r, dtype=np.float32)
+        rc = r if self._is_identity_rotation else r @ self._R.T
+        return np.where(np.sum(rc[..., :2] ** 2, axis=-1) < np.float32(self.radius) ** 2,
+                        0, 1).astype(np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        """Uniform in the cross-section, z = 0 in the cylinder frame (geometries.py:477-491)."""
+        rng = _host_rng(key)
+        out = []
+        while sum(len(a) for a in out) < n_walkers:
+            xy = rng.uniform(-self.radius, self.radius, (n_walkers * 2, 2))
+            out.append(xy[np.linalg.norm(xy, axis=1) < self.radius])
+        xy = np.concatenate(out)[:n_walkers].astype(np.float32)
+        rc = np.concatenate([xy, np.zeros((n_walkers, 1), np.float32)], axis=1)
+        return (rc @ self._R).astype(np.float32)
+
+    def volume(self, L=1.0):
+        return np.pi * self.radius ** 2 * float(L)
+
+    def surface_area(self, L=1.0, include_caps=False):
+        a = 2.0 * np.pi * self.radius * float(L)
+        if include_caps:
+            a += 2.0 * np.pi * self.radius ** 2
+        return a
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        g = self._base_desc(_lib.GEOM_CYLINDER, wall_mode, rho_over_D, kappa_over_D)
+        g.radius = self.radius
+        g.eps_detect = np.float32(1e-7 * self.radius)
+        g.nudge = np.float32(1e-4 * self.radius)
+        return g, ()
+
+
+# ------------------------------------------------------------------------------------------------
+# Random sequential addition packers
+# ------------------------------------------------------------------------------------------------
+def _rsa(radii, dim, L, seed, max_attempts, what):
+    """RSA in a periodic box, largest objects first; the same draws as geometries.py:1570-1595 so a
+    seed gives the same packing."""
+    rng = np.random.default_rng(int(seed))
+    order = np.argsort(radii)[::-1]
+    rs = radii[order]
+    cs = np.zeros((len(radii), dim))
+    for i, r_new in enumerate(rs):
+        placed = False
+        for _ in range(max_attempts):
+            c = rng.uniform(-L / 2.0, L / 2.0, dim)
+            if i:
+                dq = c - cs[:i]
+                dq -= L * np.round(dq / L)
+                if np.any(np.linalg.norm(dq, axis=1) < r_new + rs[:i]):
+                    continue
+            cs[i] = c
+            placed = True
+            break
+        if not placed:
+            raise RuntimeError(
+                f"RSA failed after {max_attempts} attempts placing {what} {i} "
+                f"(r = {r_new * 1e6:.2f} µm).  The target packing fraction may exceed what RSA can "
+                f"achieve; try reducing target_vf or increasing max_attempts.")
+    out = np.empty_like(cs)
+    out[order] = cs
+    return out
+
+
+def _check_pack_args(radii, target_vf, L):
+    radii = np.asarray(radii, dtype=np.float64).ravel()
+    if len(radii) == 0:
+        raise ValueError("radii must contain at least one element.")
+    if np.any(radii <= 0):
+        raise ValueError("All radii must be positive.")
+    if (target_vf is None) == (L is None):
+        raise ValueError("Provide exactly one of target_vf or L.")
+    if target_vf is not None and not 0.0 < float(target_vf) < 1.0:
+        raise ValueError(f"target_vf must be in (0, 1), got {target_vf}.")
+    return radii
+
+
+def pack_cylinders(radii, target_vf=None, L=None, seed=0, max_attempts=100_000):
+    """Pack parallel cylinders in a periodic square (geometries.py:1502-1601).
+
+    Returns ``(centers (N, 2), L, achieved_vf)``.
+    """
+    radii = _check_pack_args(radii, target_vf, L)
+    L = float(np.sqrt(np.pi * np.sum(radii ** 2) / float(target_vf))) if target_vf is not None \
+        else float(L)
+    if np.any(radii > L / 2.0):
+        raise ValueError(f"Largest radius ({np.max(radii) * 1e6:.2f} µm) exceeds L/2 "
+                         f"({L / 2.0 * 1e6:.2f} µm).  Reduce target_vf or supply a larger L.")
+    centers = _rsa(radii, 2, L, seed, max_attempts, "cylinder")
+    return centers, L, float(np.pi * np.sum(radii ** 2) / L ** 2)
+
+
+def pack_spheres(radii, target_vf=None, L=None, seed=0, max_attempts=100_000):
+    """Pack spheres in a periodic cube (geometries.py:2249-2340).
+
+    Returns ``(centers (N, 3), L, achieved_vf)``.
+    """
+    radii = _check_pack_args(radii, target_vf, L)
+    L = float(((4.0 / 3.0) * np.pi * np.sum(radii ** 3) / float(target_vf)) ** (1.0 / 3.0)) \
+        if target_vf is not None else float(L)
+    if np.any(radii > L / 2.0):
+        raise ValueError(f"Largest radius ({np.max(radii) * 1e6:.2f} µm) exceeds L/2 "
+                         f"({L / 2.0 * 1e6:.2f} µm).  Reduce target_vf or supply a larger L.")
+    centers = _rsa(radii, 3, L, seed, max_attempts, "sphere")
+    return centers, L, float((4.0 / 3.0) * np.pi * np.sum(radii ** 3) / L ** 3)
+
+
+def _min_gap(centers, radii, L):
+    n = len(radii)
+    gap = float("inf")
+    for i in range(n):
+        dq = centers[i] - centers[i + 1:]
+        dq -= L * np.round(dq / L)
+        if len(dq):
+            gap = min(gap, float(np.min(np.linalg.norm(dq, axis=1) - radii[i] - radii[i + 1:])))
+    return min(gap, float(np.min(L - 2.0 * radii)))
+
+
+def build_cell_list(centers, radii, L, reach, max_bytes=64 * 1024, min_cell=None):
+    """Uniform cell list over the periodic cell [-L/2, L/2)^d.
+
+    Cell c lists every periodic image (within one box) of every object whose disc/ball of radius
+    R + reach meets the cell, ordered by object index then image, as float32 (cx, cy, cz, R).
+    The grid is as fine as the table budget ``max_bytes`` allows (no finer than ``min_cell``).
+    Returns ``(n, cell_start uint32 (padded to 16 B), cand float32 (n_cand, 4), cand_obj int32)``.
+    """
+    centers = np.asarray(centers, dtype=np.float64)
+    radii = np.asarray(radii, dtype=np.float64)
+    K, dim = centers.shape
+    c0 = centers - L * np.floor(centers / L + 0.5)
+    Rr = radii + reach
+    shifts = np.array(list(itertools.product((-1, 0, 1), repeat=dim)), dtype=np.float64)
+    if min_cell is None:
+        min_cell = max(reach, 0.25 * float(np.mean(radii)))
+    n = max(1, int(L // min_cell))
+    while True:
+        h = L / n
+        cells, objs, imgs = [], [], []
+        for si, s in enumerate(shifts):
+            cs = c0 + L * s                                           # (K, dim)
+            lo = np.floor((cs - Rr[:, None] + L / 2) / h).astype(np.int64)
+            hi = np.floor((cs + Rr[:, None] + L / 2) / h).astype(np.int64)
+            lo = np.clip(lo, 0, n - 1)
+            hi = np.clip(hi, 0, n - 1)
+            inside_box = np.all((cs + Rr[:, None] + L / 2 >= 0) & (cs - Rr[:, None] + L / 2 <= L),
+                                axis=1)
+            span = int(np.max(hi - lo + 1)) if K else 1
+            grids = np.stack(np.meshgrid(*[np.arange(span)] * dim, indexing="ij"),
+                             axis=-1).reshape(-1, dim)                 # (B, dim)
+            idx = lo[:, None, :] + grids[None, :, :]                   # (K, B, dim)
+            ok = np.all(idx <= hi[:, None, :], axis=2) & inside_box[:, None]
+            edge_lo = -L / 2 + idx * h
+            d = np.maximum(np.maximum(edge_lo - cs[:, None, :], 0.0),
+                           cs[:, None, :] - (edge_lo + h))
+            ok &= np.sum(d * d, axis=2) <= (Rr[:, None] * (1 + 1e-9)) ** 2
+            kk, bb = np.nonzero(ok)
+            cid = np.zeros(len(kk), dtype=np.int64)
+            for a in reversed(range(dim)):
+                cid = cid * n + idx[kk, bb, a]
+            cells.append(cid)
+            objs.append(kk)
+            imgs.append(np.full(len(kk), si))
+        cells = np.concatenate(cells)
+        objs = np.concatenate(objs)
+        imgs = np.concatenate(imgs)
+        n_cells = n ** dim
+        nbytes = (n_cells + 4) * 4 + len(cells) * 16
+        if nbytes <= max_bytes or n == 1:
+            break
+        n = max(1, int(n / 1.25))
+    order = np.lexsort((imgs, objs, cells))
+    cells, objs, imgs = cells[order], objs[order], imgs[order]
+    counts = np.bincount(cells, minlength=n_cells)
+    start = np.zeros(((n_cells + 1 + 3) // 4) * 4, dtype=np.uint32)
+    start[1:n_cells + 1] = np.cumsum(counts)
+    start[n_cells + 1:] = start[n_cells]
+    pos = c0[objs] + L * shifts[imgs]
+    cand = np.zeros((len(objs), 4), dtype=np.float32)
+    cand[:, :dim] = pos
+    cand[:, 3] = radii[objs]
+    return n, start, cand, objs.astype(np.int32)
+
+
+class _Packed(Geometry):
+    """Shared machinery of PackedCylinders / PackedSpheres (periodic objects + cell list)."""
+
+    _dim = 2
+    _kind = None
+
+    def _setup(self, radii, centers, L, surface_relaxivity_t2, permeability):
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+        self.permeability = _opt_float(permeability)
+        self._L_float = float(L)
+        self._radii_np = radii.copy()
+        self._centers_np = centers.copy()
+        self._centers_jax = centers.astype(np.float32)    # name kept for duck-typed callers
+        self._radii_jax = radii.astype(np.float32)
+        self._L_jax = np.float32(L)
+        min_r = float(np.min(radii))
+        self._eps_detect = np.float32(1e-7 * min_r)
+        self._nudge = np.float32(1e-4 * min_r)
+        self.min_gap = _min_gap(centers, radii, float(L))
+        self._dev_cache = {}
+
+    def _classify_frame(self, rc):
+        L = np.float32(self._L_float)
+        q = rc[..., None, :self._dim] - self._centers_jax
+        q = q - L * np.floor(q / L + np.float32(0.5))
+        inside = np.sum(q * q, axis=-1) < self._radii_jax ** 2
+        ids = np.arange(1, len(self._radii_np) + 1, dtype=np.int32)
+        return np.max(np.where(inside, ids, 0), axis=-1).astype(np.int32)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        reach = float(step_length) * 1.05 + 8.0 * float(self._nudge)
+        key = (round(reach, 15), str(dev))
+        if key not in self._dev_cache:
+            n, start, cand, obj = build_cell_list(self._centers_np, self._radii_np, self._L_float,
+                                                  reach)
+            t_start = torch.from_numpy(start.view(np.int32)).to(dev)
+            t_cand = torch.from_numpy(cand).to(dev)
+            t_obj = torch.from_numpy(obj if len(obj) else np.zeros(1, np.int32)).to(dev)
+            self._dev_cache = {key: (n, reach, t_start, t_cand, t_obj, len(obj))}
+        n, reach, t_start, t_cand, t_obj, n_cand = self._dev_cache[key]
+        g = self._base_desc(self._kind, wall_mode, rho_over_D, kappa_over_D)
+        g.radius = float(np.min(self._radii_np))
+        g.eps_detect = self._eps_detect
+        g.nudge = self._nudge
+        g.L = np.float32(self._L_float)
+        g.n_objects = len(self._radii_np)
+        g.grid_n = n
+        g.cell_h = self._L_float / n
+        g.reach = reach
+        g.n_cand = n_cand
+        g.cell_start = t_start.data_ptr()
+        g.cand = t_cand.data_ptr()
+        g.cand_obj = t_obj.data_ptr()
+        return g, (t_start, t_cand, t_obj)
+
+    def volume_fraction(self):
+        if self._dim == 2:
+            return float(np.pi * np.sum(self._radii_np ** 2) / self._L_float ** 2)
+        return float((4.0 / 3.0) * np.pi * np.sum(self._radii_np ** 3) / self._L_float ** 3)
+
+
+class PackedCylinders(_Packed):
+    """Extra-axonal diffusion among parallel cylinders in a periodic square (geometries.py:1604-2242).
+
+    Positions stay unfolded for the phase; detection uses the minimum image; one specular
+    reflection per sub-step plus the fold-first safety clamp; permeable walls transmit with the
+    Powles probability.
+    """
+
+    _dim = 2
+    _kind = _lib.GEOM_PACKED_CYLINDERS
+
+    def __init__(self, radii, centers, L, orientation=(0., 0., 1.), surface_relaxivity_t2=None,
+                 permeability=None):
+        radii = np.asarray(radii, dtype=np.float64).ravel()
+        centers = np.asarray(centers, dtype=np.float64)
+        if centers.shape != (len(radii), 2):
+            raise ValueError(f"centers shape {centers.shape} does not match ({len(radii)}, 2) for "
+                             f"{len(radii)} cylinders.")
+        if np.any(radii <= 0):
+            raise ValueError("All radii must be positive.")
+        o = np.asarray(orientation, dtype=np.float64)
+        self.orientation = (o / np.linalg.norm(o)).astype(np.float32)
+        R = _rotation_to_z(self.orientation)
+        self._R = R.astype(np.float32)
+        self._R_inv = R.T.astype(np.float32)
+        self._is_identity_rotation = bool(np.allclose(R, np.eye(3)))
+        self._setup(radii, centers, L, surface_relaxivity_t2, permeability)
+
+    def _frame(self):
+        return None if self._is_identity_rotation else self._R.astype(np.float64)
+
+    def classify_position(self, r):
+        """0 = extra-axonal, k = inside cylinder k (1-based)."""
+        r = np.asarray(r, dtype=np.float32)
+        rc = r if self._is_identity_rotation else r @ self._R.T
+        return self._classify_frame(rc)
+
+    def init_positions(self, n_walkers, key=None):
+        """Uniform in the periodic box outside every cylinder, z = 0 (geometries.py:1717-1744)."""
+        rng = _host_rng(key)
+        L = self._L_float
+        out, have = [], 0
+        while have < n_walkers:
+            xy = rng.uniform(-L / 2.0, L / 2.0, (max(n_walkers * 4, 1024), 2))
+            ok = np.ones(len(xy), bool)
+            for k in range(len(self._radii_np)):
+                d = xy - self._centers_np[k]
+                d -= L * np.round(d / L)
+                ok &= np.sum(d * d, axis=1) > self._radii_np[k] ** 2
+            out.append(xy[ok])
+            have = sum(len(a) for a in out)
+        xy = np.concatenate(out)[:n_walkers].astype(np.float32)
+        rc = np.concatenate([xy, np.zeros((n_walkers, 1), np.float32)], axis=1)
+        return (rc @ self._R).astype(np.float32)
+
+    def volume(self, L=1.0):
+        return float(np.pi * np.sum(self._radii_np ** 2) * float(L))
+
+    def surface_area(self, L=1.0):
+        return float(2.0 * np.pi * np.sum(self._radii_np) * float(L))
+
+
+class PackedSpheres(_Packed):
+    """Extra-cellular diffusion among spheres in a periodic cube (geometries.py:2343-2786)."""
+
+    _dim = 3
+    _kind = _lib.GEOM_PACKED_SPHERES
+
+    def __init__(self, radii, centers, L, surface_relaxivity_t2=None, permeability=None):
+        radii = np.asarray(radii, dtype=np.float64).ravel()
+        centers = np.asarray(centers, dtype=np.float64)
+        if centers.shape != (len(radii), 3):
+            raise ValueError(f"centers shape {centers.shape} does not match ({len(radii)}, 3) for "
+                             f"{len(radii)} spheres.")
+        if np.any(radii <= 0):
+            raise ValueError("All radii must be positive.")
+        self._setup(radii, centers, L, surface_relaxivity_t2, permeability)
+
+    def classify_position(self, r):
+        """0 = extra-cellular, k = inside sphere k (1-based)."""
+        return self._classify_frame(np.asarray(r, dtype=np.float32))
+
+    def init_positions(self, n_walkers, key=None):
+        """Uniform in the periodic cube outside every sphere (geometries.py:2421-2443)."""
+        rng = _host_rng(key)
+        L = self._L_float
+        out, have = [], 0
+        while have < n_walkers:
+            p = rng.uniform(-L / 2.0, L / 2.0, (max(n_walkers * 4, 1024), 3))
+            ok = np.ones(len(p), bool)
+            for k in range(len(self._radii_np)):
+                d = p - self._centers_np[k]
+                d -= L * np.round(d / L)
+                ok &= np.sum(d * d, axis=1) > self._radii_np[k] ** 2
+            out.append(p[ok])
+            have = sum(len(a) for a in out)
+        return np.concatenate(out)[:n_walkers].astype(np.float32)
+
+    def volume(self):
+        return float((4.0 / 3.0) * np.pi * np.sum(self._radii_np ** 3))
+
+    def surface_area(self):
+        return float(4.0 * np.pi * np.sum(self._radii_np ** 2))

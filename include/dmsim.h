@@ -1,0 +1,195 @@
+/*
+ * dmsim.h — C ABI of the GB300 Monte-Carlo diffusion-MRI forward walk.
+ *
+ * The library replaces the per-walker JAX step loop of dmipy-sim:
+ *   - the fused scan body   physics.py:191-417 (make_step_fn) driven by core.py:572-727 (simulate)
+ *     and core.py:861-969 (simulate_cpmg),
+ *   - the walk-once producer core.py:972-1529 (simulate_trajectories),
+ *   - the replay operator    trajectories.py:360-641 (replay),
+ *   - the per-walker geometry plug-ins geometries.py:14-31 (reflect / reflect_with_log_weight /
+ *     permeate / classify_position / init_positions) of Sphere (143-424), Cylinder (427-844),
+ *     PackedCylinders (1604-2242), PackedSpheres (2343-2786) and mesh.py:257-907 (Mesh).
+ *
+ * Conventions
+ *   - Every pointer inside the structs is a DEVICE pointer unless the field says otherwise.
+ *     The caller allocates and owns every buffer, including the workspace sized by
+ *     dmsim_walk_workspace_bytes(); the library allocates nothing.
+ *   - Geometry-frame coordinates: the kernels walk in the geometry's native frame (cylinder axis
+ *     along z, mesh native frame).  The caller rotates gradients INTO that frame and positions out
+ *     of it (dmipy-sim does the same for meshes, core.py:417-419).
+ *   - Return value: 0 on success, a negative DMSIM_E* code on failure; dmsim_last_error() gives a
+ *     thread-local message.  Device-side anomalies never trap: they are counted in the status
+ *     words (DMSIM_STATUS_*) that the caller reads back.
+ *   - Streams: every call is asynchronous on the given cudaStream_t (passed as void*), re-entrant,
+ *     and touches no global mutable state except the thread-local error string.
+ */
+#ifndef DMSIM_H
+#define DMSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DMSIM_ABI_VERSION 1
+
+/* ---- error codes ---------------------------------------------------------------------------- */
+#define DMSIM_OK 0
+#define DMSIM_EINVAL (-1)     /* bad argument (sizes, null pointers, unsupported combination)   */
+#define DMSIM_ECUDA (-2)      /* a CUDA runtime call failed                                     */
+#define DMSIM_EWORKSPACE (-3) /* workspace smaller than dmsim_walk_workspace_bytes()            */
+#define DMSIM_ETOOBIG (-4)    /* a size beyond a documented maximum                             */
+
+/* ---- device status words (uint32 counters written by the kernels) --------------------------- */
+#define DMSIM_STATUS_NONFINITE 0      /* walkers whose position became NaN/Inf                  */
+#define DMSIM_STATUS_CLAMPED 1        /* safety-clamp projections (geometries.py:556-559 etc.)  */
+#define DMSIM_STATUS_INIT_FAIL 2      /* walkers whose rejection seeding ran out of attempts    */
+#define DMSIM_STATUS_BOUNCE_BUDGET 3  /* mesh steps whose bounce budget ran out (mesh.py:662)   */
+#define DMSIM_STATUS_ESCAPE_REJECT 4  /* mesh steps rejected by the leak guard (mesh.py:669)    */
+#define DMSIM_STATUS_WAIT_TIMEOUT 5   /* bounded mbarrier waits that gave up                    */
+#define DMSIM_STATUS_GRAZE_FP64 6     /* wall roots re-solved in FP64 at a grazing hit          */
+#define DMSIM_STATUS_TRANSMIT 7       /* membrane transmissions (Powles crossings)              */
+#define DMSIM_STATUS_WORDS 8
+
+/* ---- geometry descriptor -------------------------------------------------------------------- */
+enum dmsim_geom_kind {
+  DMSIM_GEOM_FREE = 0,             /* geometries.py:34-45                                      */
+  DMSIM_GEOM_CYLINDER = 1,         /* geometries.py:427-844, axis along frame z                */
+  DMSIM_GEOM_SPHERE = 2,           /* geometries.py:143-424, centred at the origin             */
+  DMSIM_GEOM_PACKED_CYLINDERS = 3, /* geometries.py:1604-2242, periodic square cell, axis z    */
+  DMSIM_GEOM_PACKED_SPHERES = 4,   /* geometries.py:2343-2786, periodic cubic cell             */
+  DMSIM_GEOM_MESH = 5              /* mesh.py:257-907                                          */
+};
+
+enum dmsim_wall_mode {
+  DMSIM_WALL_REFLECT = 0,  /* reflect()                  */
+  DMSIM_WALL_RELAX = 1,    /* reflect_with_log_weight()  */
+  DMSIM_WALL_PERMEATE = 2  /* permeate()                 */
+};
+
+typedef struct dmsim_geometry {
+  int32_t kind;      /* enum dmsim_geom_kind */
+  int32_t wall_mode; /* enum dmsim_wall_mode */
+  float radius;      /* Cylinder/Sphere R; packed: R_min (m) */
+  float eps_detect;  /* crossing threshold, 1e-7*R (geometries.py:219)        */
+  float nudge;       /* post-collision nudge, 1e-4*R (geometries.py:220)      */
+  float kappa_over_D;
+  float rho_over_D; /* used only by the RELAX/PERMEATE weight channel; the walk kernel scales
+                       the unit (rho/D = 1) boundary log-weight by this value */
+  float L;          /* packed: periodic cell side (m) */
+
+  /* packed objects: uniform cell list over the periodic cell [-L/2, L/2)^d.  cell c covers
+     candidates cand[cell_start[c] .. cell_start[c+1]); each candidate is a float4
+     (cx, cy, cz, R) already shifted to the periodic image nearest the cell.  Every object whose
+     disc/ball comes within `reach` of the cell is listed. */
+  int32_t n_objects;
+  int32_t grid_n; /* cells per axis */
+  float cell_h;   /* L / grid_n */
+  float reach;    /* maximum step length + margin the lists were built for */
+  int32_t n_cand;
+  int32_t pad0;
+  const uint32_t* cell_start; /* grid_n^d + 1 */
+  const float* cand;          /* n_cand x 4 */
+  const int32_t* cand_obj;    /* n_cand: object index of each candidate (classification) */
+
+  /* mesh (DMSIM_GEOM_MESH): triangles incl. periodic ghosts, uniform grid (CSR) */
+  int32_t n_tri;
+  int32_t mesh_dims[3];
+  int32_t periodic[3];
+  int32_t max_bounces;
+  float grid_min[3];
+  float mesh_cell;
+  float vmin[3];
+  float box[3];
+  float mesh_eps;
+  float mesh_nudge;
+  float mesh_graze;
+  float rho_mult_intra;
+  float rho_mult_extra;
+  float kappa_mult_out;
+  float kappa_mult_in;
+  int32_t reject_escape;
+  const float* tri;              /* n_tri x 12: v0 v1 v2 (9) + geometric normal (3)        */
+  const float* tri_vn;           /* n_tri x 9: smooth vertex normals of v0 v1 v2            */
+  const uint32_t* mesh_cell_start; /* dims product + 1                                      */
+  const uint32_t* mesh_cell_tri;   /* triangle indices                                        */
+} dmsim_geometry;
+
+/* ---- walk parameters -------------------------------------------------------------------------- */
+typedef struct dmsim_walk_params {
+  int64_t n_walkers;     /* walkers in this call                                                */
+  int64_t walker_offset; /* global index of the first walker (Philox counter; shard offset)   */
+  uint64_t seed;
+  int32_t n_t;               /* waveform samples                                               */
+  int32_t n_meas;            /* measurements M                                                 */
+  int32_t sub_steps;         /* physics sub-steps per waveform sample, S                       */
+  int32_t phase_per_substep; /* 1: phi += gamma*dt_sub*g.r after every sub-step (fused engine,
+                                physics.py:313); 0: phi += gamma*dt*g.r at the sample's last
+                                sub-step only (walk-once + replay, trajectories.py:550-552)    */
+  float step_length;         /* sqrt(6 D dt_sub)                                               */
+  float gamma_dt;            /* gamma*dt_sub (fused) or gamma*dt (replay)                       */
+  float t2_decay;            /* dt_sub/T2 per sub-step, 0 if none                               */
+  float t1_decay;            /* dt_sub/T1 per sub-step, 0 if none                               */
+  int32_t has_weight;        /* track log_w (surface relaxivity, permeability, T2, T1)          */
+  int32_t n_echo;            /* emitted samples: 1 for simulate (the last), n_echoes for CPMG   */
+  const int32_t* echo_idx;   /* HOST array of n_echo ascending sample indices                   */
+  const float* G;            /* (n_t, n_meas, 3) float, geometry frame, T/m                     */
+  const float* chi;          /* (n_t) transverse mask or NULL (all ones)                        */
+  const float* r0;           /* (n_walkers, 3) geometry-frame start positions or NULL           */
+} dmsim_walk_params;
+
+/* ---- outputs ---------------------------------------------------------------------------------- */
+typedef struct dmsim_walk_outputs {
+  double* sums;      /* (n_echo, n_meas, 3): sum w cos(phi), sum w sin(phi), sum (w cos(phi))^2 */
+  uint32_t* status;  /* DMSIM_STATUS_WORDS counters (accumulated, not cleared)                 */
+  float* final_pos;  /* optional (n_walkers, 3) geometry frame, unfolded                         */
+  float* log_w;      /* optional (n_walkers)                                                     */
+  float* phi;        /* optional (n_walkers, n_meas)                                             */
+  int32_t* comp0;    /* optional (n_walkers) compartment at t=0                                 */
+  int32_t* comp_end; /* optional (n_walkers) compartment at the end                              */
+  void* traj;        /* optional (n_walkers, n_t, 3) positions after each sample                 */
+  int32_t traj_f16;  /* 1: traj is float16 (as core.py:1426-1449), 0: float32                   */
+  int32_t pad0;
+  float* dlog_unit;  /* optional (n_walkers, n_t) boundary log-weight per sample at rho/D = 1     */
+  float* comp_occ;   /* optional (n_walkers, n_t) mean compartment id over the sample's sub-steps */
+} dmsim_walk_outputs;
+
+/* ---- entry points ----------------------------------------------------------------------------- */
+
+/* Library ABI version (DMSIM_ABI_VERSION). */
+int dmsim_version(void);
+
+/* Thread-local message for the last failing call on this thread. */
+const char* dmsim_last_error(void);
+
+/* Workspace bytes dmsim_walk() needs for these parameters on the current device
+   (per-block FP64 partials of the ensemble sums).  Replaces the device memory XLA allocated for
+   the vmapped scan carry (core.py:700-727). */
+size_t dmsim_walk_workspace_bytes(const dmsim_walk_params* p, const dmsim_geometry* g);
+
+/* One Monte-Carlo walk of p->n_walkers walkers through g, accumulating the ensemble sums at
+   every echo sample.  Replaces the vmap(lax.scan(step_fn)) of core.py:700-727 (simulate),
+   core.py:944-969 (simulate_cpmg, n_echo > 1) and the producer walk of core.py:1243-1309
+   (simulate_trajectories, when o->traj is set).  o->sums is overwritten; the signal for echo e,
+   measurement m is sums[(e*M+m)*3+0] / n_walkers (core.py:426-429). */
+int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
+               void* workspace, size_t workspace_bytes, void* stream);
+
+/* Replay operator on saved trajectories, trajectories.py:360-641 without relaxation terms:
+   phi[m,w] = gamma_dt * sum_t G[t,m,:] . traj[w,t,:]  (trajectories.py:550-552) and
+   sums[m] = (sum_w e^{log_w[w]} cos phi, sum e^{log_w} sin phi, sum (e^{log_w} cos phi)^2).
+   traj is (n_walkers, n_t, 3) float16 (traj_f16=1) or float32; log_w is (n_walkers) or NULL
+   (all zero); phi_out is optional (n_walkers, n_meas).  Workspace from
+   dmsim_replay_workspace_bytes(). */
+size_t dmsim_replay_workspace_bytes(int64_t n_walkers, int32_t n_t, int32_t n_meas);
+int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t n_t,
+                 const float* G, int32_t n_meas, float gamma_dt, const float* log_w,
+                 double* sums, float* phi_out, void* workspace, size_t workspace_bytes,
+                 void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMSIM_H */
