@@ -290,6 +290,35 @@ def run_walk(geometry, *, n_walkers, diffusivity, G, dt, sub_steps, phase_per_su
                       dict(zip(_lib.STATUS_NAMES, st.tolist())), extras)
 
 
+def step_kat(geometry, r, steps, u=None, wall=None, diffusivity=2e-9):
+    """One device sub-step (the walk kernel's step functions) for each (r, step, u) in the walk
+    frame; returns ``(r_new (n, 3), dlog_unit (n,))``.  The known-answer counterpart of one
+    reference plug-in call (reflect / reflect_with_log_weight / permeate)."""
+    lib = _lib.load()
+    dev = _lib.device()
+    r = np.ascontiguousarray(r, dtype=np.float32)
+    steps = np.ascontiguousarray(steps, dtype=np.float32)
+    n = len(r)
+    rho = getattr(geometry, 'surface_relaxivity_t2', None)
+    kappa = getattr(geometry, 'permeability', None)
+    if wall is None:
+        wall = geometry._wall_mode(rho is not None)
+    kod = np.float32(kappa / diffusivity) if kappa is not None else 0.0
+    reach = float(np.max(np.linalg.norm(steps, axis=1))) if n else 0.0
+    gdesc, keep = geometry._desc(reach, wall, 0.0, kod, dev)
+    t_r = torch.from_numpy(r).to(dev)
+    t_s = torch.from_numpy(steps).to(dev)
+    t_u = None if u is None else torch.from_numpy(np.ascontiguousarray(u, np.float32)).to(dev)
+    out = torch.empty_like(t_r)
+    dl = torch.empty(n, dtype=torch.float32, device=dev)
+    rc = lib.dmsim_step_kat(gdesc, n, _lib.ptr(t_r), _lib.ptr(t_s), _lib.ptr(t_u), _lib.ptr(out),
+                            _lib.ptr(dl), _lib.stream_handle())
+    _lib.check(rc, "dmsim_step_kat")
+    torch.cuda.synchronize(dev)
+    del keep
+    return out.cpu().numpy(), dl.cpu().numpy()
+
+
 def _to_lab(geometry, pos):
     frame = geometry._frame()
     if frame is None:

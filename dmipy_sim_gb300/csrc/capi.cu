@@ -269,6 +269,82 @@ __global__ void k_zero(double* p, size_t n) {
     p[i] = 0.0;
 }
 
+// ---- known-answer kernel: one sub-step of the device step functions per input triple ---------
+template <int GEOM, int WALL>
+__global__ void k_step_kat(const GeoK g, int64_t n, const float* __restrict__ rin,
+                           const float* __restrict__ st, const float* __restrict__ uin,
+                           const uint32_t* __restrict__ cs, const float4* __restrict__ cand,
+                           float* __restrict__ rout, float* __restrict__ dlog) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float x = rin[3 * i], y = rin[3 * i + 1], z = rin[3 * i + 2];
+    const float sx = st[3 * i], sy = st[3 * i + 1], sz = st[3 * i + 2];
+    const float u = uin ? uin[i] : 0.f;
+    Tally tl;
+    float dl = 0.f;
+    int ix = 0, iy = 0, iz = 0;
+    if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES) {
+      ix = (int)floorf(x / g.L + 0.5f);
+      x -= g.L * ix;
+      iy = (int)floorf(y / g.L + 0.5f);
+      y -= g.L * iy;
+      if (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
+        iz = (int)floorf(z / g.L + 0.5f);
+        z -= g.L * iz;
+      }
+    }
+    if constexpr (GEOM == DMSIM_GEOM_FREE) {
+      x += sx; y += sy; z += sz;
+    } else if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
+      dl = cylinder_step<WALL>(x, y, sx, sy, u, g, tl);
+      z += sz;
+    } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
+      dl = sphere_step<WALL>(x, y, z, sx, sy, sz, u, g, tl);
+    } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS) {
+      dl = packed_cyl_step<WALL>(x, y, ix, iy, sx, sy, u, g, cs, cand, tl);
+      z += sz;
+    } else {
+      dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, sx, sy, sz, u, g, cs, cand, tl);
+    }
+    rout[3 * i] = x + g.L * (float)ix;
+    rout[3 * i + 1] = y + g.L * (float)iy;
+    rout[3 * i + 2] = z + g.L * (float)iz;
+    dlog[i] = dl;
+  }
+}
+
+using KatFn = void (*)(GeoK, int64_t, const float*, const float*, const float*, const uint32_t*,
+                       const float4*, float*, float*);
+
+template <int GEOM>
+KatFn kat_fn(int wall) {
+  if constexpr (GEOM == DMSIM_GEOM_FREE) {
+    return k_step_kat<GEOM, 0>;
+  } else {
+    if (wall == 0) return k_step_kat<GEOM, 0>;
+    if (wall == 1) return k_step_kat<GEOM, 1>;
+    return k_step_kat<GEOM, 2>;
+  }
+}
+
+GeoK make_geok(const dmsim_geometry* g) {
+  GeoK gk;
+  memset(&gk, 0, sizeof(gk));
+  const bool packed =
+      g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
+  gk.R = g->radius;
+  gk.R2 = g->radius * g->radius;
+  gk.invR = g->radius > 0.f ? 1.f / g->radius : 0.f;
+  gk.eps = g->eps_detect;
+  gk.nudge = g->nudge;
+  gk.kod = g->kappa_over_D;
+  gk.L = packed ? g->L : 0.f;
+  gk.halfL = packed ? 0.5f * g->L : 0.f;
+  gk.inv_h = packed ? (float)g->grid_n / g->L : 0.f;
+  gk.n = packed ? g->grid_n : 1;
+  return gk;
+}
+
 int replay_grid(int64_t n_walkers) {
   int dev = 0, n_sm = 0, nb = 0;
   cudaGetDevice(&dev);
@@ -334,21 +410,9 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
   a.t2dec = p->t2_decay;
   a.t1dec = p->t1_decay;
   a.rho = g->rho_over_D;
-  GeoK gk;
-  memset(&gk, 0, sizeof(gk));
   const bool packed =
       g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  gk.R = g->radius;
-  gk.R2 = g->radius * g->radius;
-  gk.invR = g->radius > 0.f ? 1.f / g->radius : 0.f;
-  gk.eps = g->eps_detect;
-  gk.nudge = g->nudge;
-  gk.kod = g->kappa_over_D;
-  gk.L = packed ? g->L : 0.f;
-  gk.halfL = packed ? 0.5f * g->L : 0.f;
-  gk.inv_h = packed ? (float)g->grid_n / g->L : 0.f;
-  gk.n = packed ? g->grid_n : 1;
-  a.g = gk;
+  a.g = make_geok(g);
   a.tab_cs_bytes = (uint32_t)pl.tab_cs;
   a.tab_cand_bytes = (uint32_t)pl.tab_cand;
   a.cs = g->cell_start;
@@ -383,6 +447,35 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
                                                p->n_meas, o->sums);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
+int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const float* steps,
+                   const float* u, float* r_out, float* dlog_unit, void* stream) {
+  if (!g || n < 0 || (n > 0 && (!r_in || !steps || !r_out || !dlog_unit)))
+    return fail(DMSIM_EINVAL, "step_kat: bad arguments");
+  if (g->wall_mode == DMSIM_WALL_PERMEATE && n > 0 && !u)
+    return fail(DMSIM_EINVAL, "step_kat: permeate needs the uniforms");
+  const bool packed =
+      g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
+  if (packed && (!g->cell_start || !g->cand || g->grid_n < 1))
+    return fail(DMSIM_EINVAL, "step_kat: packed geometry needs a cell list");
+  KatFn fn = nullptr;
+  switch (g->kind) {
+    case DMSIM_GEOM_FREE: fn = kat_fn<DMSIM_GEOM_FREE>(g->wall_mode); break;
+    case DMSIM_GEOM_CYLINDER: fn = kat_fn<DMSIM_GEOM_CYLINDER>(g->wall_mode); break;
+    case DMSIM_GEOM_SPHERE: fn = kat_fn<DMSIM_GEOM_SPHERE>(g->wall_mode); break;
+    case DMSIM_GEOM_PACKED_CYLINDERS: fn = kat_fn<DMSIM_GEOM_PACKED_CYLINDERS>(g->wall_mode); break;
+    case DMSIM_GEOM_PACKED_SPHERES: fn = kat_fn<DMSIM_GEOM_PACKED_SPHERES>(g->wall_mode); break;
+    default: return fail(DMSIM_EINVAL, "step_kat: unsupported geometry kind %d", g->kind);
+  }
+  if (n == 0) return DMSIM_OK;
+  const int blocks = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+  fn<<<blocks, 256, 0, (cudaStream_t)stream>>>(make_geok(g), n, r_in, steps, u, g->cell_start,
+                                                 reinterpret_cast<const float4*>(g->cand), r_out,
+                                                 dlog_unit);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(DMSIM_ECUDA, "step_kat launch failed: %s", cudaGetErrorString(err));
   return DMSIM_OK;
 }
 

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     }
   }
 
-  Tally tl;
+  Tally tl, tl_idle;  // tallies of real walkers / of the idle threads of the last tile
   uint32_t n_nonfinite = 0, n_initfail = 0;
   int64_t q = 0;  // running chunk counter of this block
 
@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     const int64_t w = tile * kBlock + tid;
     const bool act = w < a.n_walkers;
     const uint64_t gw = (uint64_t)(a.walker_offset + w);
+    Tally& tw = act ? tl : tl_idle;
 
     // ---- initial position -----------------------------------------------------------------
     float x = 0.f, y = 0.f, z = 0.f;
@@ -348,15 +349,15 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
             y += sty;
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
-            dl = cylinder_step<WALL>(x, y, stx, sty, up, g, tl);
+            dl = cylinder_step<WALL>(x, y, stx, sty, up, g, tw);
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
-            dl = sphere_step<WALL>(x, y, z, stx, sty, stz, up, g, tl);
+            dl = sphere_step<WALL>(x, y, z, stx, sty, stz, up, g, tw);
           } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS) {
-            dl = packed_cyl_step<WALL>(x, y, ix, iy, stx, sty, up, g, cs, cand, tl);
+            dl = packed_cyl_step<WALL>(x, y, ix, iy, stx, sty, up, g, cs, cand, tw);
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
-            dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tl);
+            dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
           }
           if (a.has_weight) logw += rc * dl - dec;
           if (a.phase_sub) {

@@ -177,6 +177,16 @@ size_t dmsim_walk_workspace_bytes(const dmsim_walk_params* p, const dmsim_geomet
 int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
                void* workspace, size_t workspace_bytes, void* stream);
 
+/* Known-answer entry point of the device step functions: one geometry sub-step for each of n
+   (position, step, uniform) triples, through exactly the code the walk kernel runs.  Counterpart
+   of a single reference plug-in call (geometries.py: Cylinder/Sphere/PackedCylinders/PackedSpheres
+   .reflect / .reflect_with_log_weight / .permeate) applied to a batch.  r_in (n, 3) are unfolded
+   geometry-frame positions, steps (n, 3), u (n) the Powles uniforms (PERMEATE; may be NULL
+   otherwise); writes r_out (n, 3) and dlog_unit (n) = -2 * sum of d_perp (rho/D = 1).  The cell
+   list of a packed geometry must have been built with reach >= every |step|. */
+int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const float* steps,
+                   const float* u, float* r_out, float* dlog_unit, void* stream);
+
 /* Replay operator on saved trajectories, trajectories.py:360-641 without relaxation terms:
    phi[m,w] = gamma_dt * sum_t G[t,m,:] . traj[w,t,:]  (trajectories.py:550-552) and
    sums[m] = (sum_w e^{log_w[w]} cos phi, sum e^{log_w} sin phi, sum (e^{log_w} cos phi)^2).

@@ -1,0 +1,79 @@
+/*
+ * CPU oracle of the dmipy-sim Monte-Carlo walk — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's per-walker algorithm, used by tests/, smoke() and the
+ * bench's CPU baseline as the checker; the product (libdmsim.so) never links or calls it.
+ * Compiled twice: *_f32 restates the reference's FP32 arithmetic statement by statement, *_f64
+ * is the same algorithm in FP64 (the "FP64 rerun" that the GPU's FP32 error is stated against).
+ *
+ * What it follows (paths inside the dmipy-sim source tree):
+ *   step direction / sub-steps / phase / log-weight   physics.py:191-417
+ *   Sphere reflect / reflect_with_log_weight / permeate   geometries.py:197-264, 266-318, 320-424
+ *   Cylinder reflect / reflect_with_log_weight / permeate geometries.py:493-563, 565-653, 655-801
+ *   PackedCylinders reflect / rwlw / permeate             geometries.py:1746-1884, 1886-2016, 2018-2183
+ *   PackedSpheres reflect / rwlw / permeate               geometries.py:2445-2537, 2539-2631, 2633-2756
+ *   ensemble Re<w e^{i phi}>                              core.py:426-429; replay FP64 phase
+ *                                                         trajectories.py:550-552, 634
+ * It tests every object of a packed substrate (no cell list) with the reference's min-image
+ * arithmetic on unfolded positions, exactly as the reference does.  Random numbers come from the
+ * Philox stream contract of dmipy_sim_gb300/csrc/philox.cuh so a walk here and on the GPU is the
+ * same walk, walker for walker.
+ */
+#ifndef DMSIM_ORACLE_H
+#define DMSIM_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4 };
+enum { OR_REFLECT = 0, OR_RELAX = 1, OR_PERMEATE = 2 };
+
+typedef struct {
+  int32_t kind;
+  int32_t n_objects;
+  double radius;      /* Cylinder/Sphere radius */
+  double L;           /* packed cell side */
+  double rmin;        /* packed: smallest radius (sets EPS and NUDGE) */
+  const double* objects; /* n_objects x 4: (cx, cy, cz, R) */
+  double rot[9];      /* lab -> cylinder frame (row-major), used by or_plugin only */
+  int32_t rot_identity;
+  int32_t pad;
+} or_geom;
+
+typedef struct {
+  int64_t n_walkers, walker_offset;
+  uint64_t seed;
+  int32_t n_t, n_meas, sub_steps, phase_per_substep;
+  int32_t has_weight, wall, n_echo, f16_positions; /* f16: replay phase from float16-rounded positions */
+  const int32_t* echo_idx;
+  double step_length, gamma_dt, t2_decay, t1_decay, rho_over_D, kappa_over_D;
+} or_walk_params;
+
+/* One reference plug-in call in the LAB frame: mode OR_REFLECT (reflect), OR_RELAX
+   (reflect_with_log_weight with rho_over_D) or OR_PERMEATE (permeate with kappa_over_D,
+   rho_over_D and the Bernoulli uniform u).  Returns 0 on success. */
+int or_plugin_f32(const or_geom* g, int mode, const double* r, const double* step,
+                  double rho_over_D, double kappa_over_D, double u, double* r_out, double* dlog);
+int or_plugin_f64(const or_geom* g, int mode, const double* r, const double* step,
+                  double rho_over_D, double kappa_over_D, double u, double* r_out, double* dlog);
+
+/* A full walk in the geometry frame.  G is (n_t, n_meas, 3) float32, chi (n_t) or NULL, r0
+   (n_walkers, 3) or NULL (seeded on the Philox seeding stream).  sums (n_echo, n_meas, 3) is
+   overwritten with sum w cos(phi), sum w sin(phi), sum (w cos(phi))^2.  final_pos (n, 3), log_w
+   (n), phi (n, n_meas) are optional.  n_threads <= 0 uses every core. */
+int or_walk_f32(const or_geom* g, const or_walk_params* p, const float* G, const float* chi,
+                const float* r0, double* sums, float* final_pos, float* log_w, float* phi,
+                int n_threads);
+int or_walk_f64(const or_geom* g, const or_walk_params* p, const float* G, const float* chi,
+                const float* r0, double* sums, float* final_pos, float* log_w, float* phi,
+                int n_threads);
+
+/* Philox4x32-10 draw (for cross-checking the stream contract). */
+void or_philox(uint64_t seed, uint64_t walker, uint32_t stream, uint32_t j, uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

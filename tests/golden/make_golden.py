@@ -1,0 +1,410 @@
+"""Generate the golden fixtures of the parity tests from the dmipy-sim reference itself.
+
+Runs the reference's own ``waveforms.py``, ``geometries.py``, ``physics.py``, ``trajectories.py``
+and ``core.py`` unmodified, under the numpy stand-in for JAX in ``jaxstub.py`` (JAX is not
+installed where the fixtures are made), and writes:
+
+  kat.npz  known-answer vectors: waveform constructors / calc_b / set_b, the sub-step rules, the
+           RSA packers, every geometry plug-in call (reflect / reflect_with_log_weight / permeate)
+           on seeded inputs with the Powles uniform injected, and the replay operator.
+  mc.json  the reference's own Monte-Carlo signals (core.simulate / simulate_cpmg, numpy random
+           numbers in place of threefry) on small configurations, with their standard errors,
+           for the 3-standard-error statistical parity tests.
+
+Usage:  python tests/golden/make_golden.py [--kat] [--mc] [--ref /path/to/dmipy-sim]
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import jaxstub  # noqa: E402
+
+D = 2e-9
+
+
+def _ref(root):
+    return jaxstub.load_reference(root)
+
+
+# ------------------------------------------------------------------------------------------------
+# Known-answer vectors
+# ------------------------------------------------------------------------------------------------
+def _unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def _plugin_cases(m, rng, out):
+    geo = m["geometries"]
+    R = 5e-6
+    n = 256
+
+    def run(tag, g, mode, rs, steps, rho=0.0, kappa=0.0, us=None):
+        ro = np.zeros((len(rs), 3), np.float64)
+        dl = np.zeros(len(rs), np.float64)
+        for i, (r, s) in enumerate(zip(rs, steps)):
+            r32 = np.asarray(r, np.float32)
+            s32 = np.asarray(s, np.float32)
+            if mode == 0:
+                o, d = g.reflect(r32, s32), 0.0
+            elif mode == 1:
+                o, d = g.reflect_with_log_weight(r32, s32, np.float32(rho))
+            else:
+                o, d = g.permeate(r32, s32, np.float32(kappa), np.float32(rho),
+                                  jaxstub.Injected(us[i]))
+            ro[i] = np.asarray(o, np.float64)
+            dl[i] = float(d)
+        out[f"pl_{tag}_r"] = np.asarray(rs, np.float32)
+        out[f"pl_{tag}_step"] = np.asarray(steps, np.float32)
+        out[f"pl_{tag}_out"] = ro
+        out[f"pl_{tag}_dlog"] = dl
+        out[f"pl_{tag}_mode"] = np.array(mode)
+        out[f"pl_{tag}_rho"] = np.array(rho)
+        out[f"pl_{tag}_kappa"] = np.array(kappa)
+        if us is not None:
+            out[f"pl_{tag}_u"] = np.asarray(us, np.float32)
+
+    # single cylinder: identity and tilted frames
+    for tag, ori in (("cyl", (0, 0, 1)), ("cyltilt", (1.0, 1.0, 0.3))):
+        c = geo.Cylinder(R, ori)
+        Rm = np.asarray(c._R, np.float64)
+        rad = R * np.sqrt(rng.uniform(0.2, 0.9999, n))
+        ang = rng.uniform(0, 2 * np.pi, n)
+        rc = np.stack([rad * np.cos(ang), rad * np.sin(ang), rng.uniform(-R, R, n)], 1)
+        rl = rc @ Rm                                   # lab = R^T r_c
+        st = _unit(rng, n) * (R * rng.uniform(0.02, 1.5, n))[:, None]
+        out[f"geo_{tag}_R"] = np.array(R)
+        out[f"geo_{tag}_ori"] = np.array(ori, np.float64)
+        run(tag + "_reflect", c, 0, rl, st)
+        run(tag + "_relax", c, 1, rl, st, rho=500.0)
+        cp = geo.Cylinder(R, ori, permeability=1e-5)
+        rad2 = R * rng.uniform(0.6, 1.4, n)
+        rc2 = np.stack([rad2 * np.cos(ang), rad2 * np.sin(ang), rng.uniform(-R, R, n)], 1)
+        st2 = _unit(rng, n) * (R * rng.uniform(0.01, 0.5, n))[:, None]
+        run(tag + "_perm", cp, 2, rc2 @ Rm, st2, rho=500.0, kappa=5000.0,
+            us=rng.uniform(0, 1, n))
+    # single sphere
+    s = geo.Sphere(R)
+    dirs = _unit(rng, n)
+    rs = dirs * (R * rng.uniform(0.2, 0.9999, n) ** (1 / 3))[:, None]
+    st = _unit(rng, n) * (R * rng.uniform(0.02, 1.5, n))[:, None]
+    out["geo_sph_R"] = np.array(R)
+    run("sph_reflect", s, 0, rs, st)
+    run("sph_relax", s, 1, rs, st, rho=500.0)
+    sp = geo.Sphere(R, permeability=1e-5)
+    rs2 = dirs * (R * rng.uniform(0.6, 1.4, n))[:, None]
+    st2 = _unit(rng, n) * (R * rng.uniform(0.01, 0.5, n))[:, None]
+    run("sph_perm", sp, 2, rs2, st2, rho=500.0, kappa=5000.0, us=rng.uniform(0, 1, n))
+
+    # packed cylinders / spheres (RSA), unfolded positions several boxes away
+    radii = np.clip(rng.lognormal(np.log(2e-6), 0.25, 16), 0.9e-6, 3.5e-6)
+    cen, L, vf = geo.pack_cylinders(radii, target_vf=0.45, seed=11)
+    pc = geo.PackedCylinders(radii, cen, L)
+    pts = []
+    while len(pts) < n:
+        p = rng.uniform(-L / 2, L / 2, 2)
+        d = p - cen
+        d -= L * np.round(d / L)
+        if np.all(np.sum(d * d, 1) > (radii * 1.0001) ** 2):
+            pts.append(p)
+    pts = np.array(pts)
+    # walkers start next to a wall half of the time
+    k = rng.integers(0, len(radii), n)
+    near = rng.uniform(size=n) < 0.5
+    a2 = rng.uniform(0, 2 * np.pi, n)
+    pn = cen[k] + (radii[k] * rng.uniform(1.0005, 1.2, n))[:, None] * np.stack(
+        [np.cos(a2), np.sin(a2)], 1)
+    pts = np.where(near[:, None], pn, pts)
+    img = rng.integers(-3, 4, (n, 2)) * L
+    rl = np.concatenate([pts + img, rng.uniform(-R, R, (n, 1))], 1)
+    st = _unit(rng, n) * (radii.min() * rng.uniform(0.05, 0.6, n))[:, None]
+    out["geo_pcyl_radii"] = radii
+    out["geo_pcyl_centers"] = cen
+    out["geo_pcyl_L"] = np.array(L)
+    run("pcyl_reflect", pc, 0, rl, st)
+    run("pcyl_relax", pc, 1, rl, st, rho=500.0)
+    pcp = geo.PackedCylinders(radii, cen, L, permeability=2e-5)
+    inside = rng.uniform(size=n) < 0.5
+    pin = cen[k] + (radii[k] * rng.uniform(0.7, 0.9995, n))[:, None] * np.stack(
+        [np.cos(a2), np.sin(a2)], 1)
+    rl2 = np.concatenate([np.where(inside[:, None], pin, pts) + img, rl[:, 2:]], 1)
+    run("pcyl_perm", pcp, 2, rl2, st, rho=500.0, kappa=10000.0, us=rng.uniform(0, 1, n))
+
+    sr = np.clip(rng.lognormal(np.log(1.5e-6), 0.2, 12), 0.8e-6, 2.5e-6)
+    scen, sL, svf = geo.pack_spheres(sr, target_vf=0.25, seed=5)
+    ps = geo.PackedSpheres(sr, scen, sL)
+    pts = []
+    while len(pts) < n:
+        p = rng.uniform(-sL / 2, sL / 2, 3)
+        d = p - scen
+        d -= sL * np.round(d / sL)
+        if np.all(np.sum(d * d, 1) > (sr * 1.0001) ** 2):
+            pts.append(p)
+    pts = np.array(pts)
+    k = rng.integers(0, len(sr), n)
+    dd = _unit(rng, n)
+    pn = scen[k] + (sr[k] * rng.uniform(1.0005, 1.2, n))[:, None] * dd
+    near = rng.uniform(size=n) < 0.5
+    pts = np.where(near[:, None], pn, pts)
+    img = rng.integers(-3, 4, (n, 3)) * sL
+    st = _unit(rng, n) * (sr.min() * rng.uniform(0.05, 0.6, n))[:, None]
+    out["geo_psph_radii"] = sr
+    out["geo_psph_centers"] = scen
+    out["geo_psph_L"] = np.array(sL)
+    run("psph_reflect", ps, 0, pts + img, st)
+    run("psph_relax", ps, 1, pts + img, st, rho=500.0)
+    psp = geo.PackedSpheres(sr, scen, sL, permeability=2e-5)
+    pin = scen[k] + (sr[k] * rng.uniform(0.7, 0.9995, n))[:, None] * dd
+    inside = rng.uniform(size=n) < 0.5
+    run("psph_perm", psp, 2, np.where(inside[:, None], pin, pts) + img, st, rho=500.0,
+        kappa=10000.0, us=rng.uniform(0, 1, n))
+
+
+def _waveform_cases(m, out):
+    wf = m["waveforms"]
+    bv3 = [[1, 0, 0]] * 3
+    w = wf.pgse(0.01, 0.04, 0.05, bv3, 300)
+    w = wf.set_b(w, [0, 1e9, 2e9])
+    out["wf_pgse_G"] = np.asarray(w.G)
+    out["wf_pgse_dt"] = np.array(w.dt)
+    out["wf_pgse_b"] = wf.calc_b(w)
+    rng = np.random.default_rng(0)
+    bv = rng.normal(size=(30, 3))
+    bv /= np.linalg.norm(bv, axis=1, keepdims=True)
+    w = wf.set_b(wf.pgse(0.01, 0.04, 0.05, bv, 300), 1e9)
+    out["wf_pgse30_G"] = np.asarray(w.G)
+    out["wf_pgse30_bvecs"] = bv
+    w = wf.pgse(0.008, 0.03, 0.1, [[0, 1, 0], [0, 0, 1]], 101, slew_rate=np.inf)
+    out["wf_square_G"] = np.asarray(w.G)
+    out["wf_square_btensor"] = wf.calc_btensor(w)
+    w = wf.pgste(0.005, 0.02, 0.08, [[1, 0, 0]], 121)
+    out["wf_pgste_G"] = np.asarray(w.G)
+    out["wf_pgste_chi"] = np.asarray(w.chi_perp, np.float32)
+    out["wf_pgste_dt"] = np.array(w.dt)
+    for f in (10.0, 50.0, 100.0):
+        w = wf.ogse(f, 0.05, 0.06, [[1, 0, 0], [0.6, 0.8, 0]], 1000)
+        out[f"wf_ogse{int(f)}_G"] = np.asarray(w.G)
+    w = wf.cpmg(16, 5e-3, 0.02, [[1, 0, 0], [0, 0, 1]], n_t_per_echo=100)
+    out["wf_cpmg_G"] = np.asarray(w.G)
+    out["wf_cpmg_echo"] = np.asarray(w.echo_indices)
+    out["wf_cpmg_dt"] = np.array(w.dt)
+
+
+def _substep_cases(m, out):
+    geo, ph, core = m["geometries"], m["physics"], m["core"]
+    rows = []
+    for R in (0.8e-6, 2e-6, 5e-6):
+        for dt in (1.6722408e-4, 5.005e-5, 1e-3):
+            s = geo.Sphere(R, permeability=1e-5)
+            c = geo.Cylinder(R, (0, 0, 1), surface_relaxivity_t2=1e-6)
+            rows.append([R, dt, ph.permeable_sub_steps(s, D, dt), ph.surface_sub_steps(c, D, dt)])
+    out["sub_perm_surf"] = np.array(rows, np.float64)
+
+    class _Grid:
+        def __init__(self, cs):
+            self.cell_size = cs
+    rows = []
+    for cs in (0.1e-6, 0.5e-6, 2e-6):
+        for dt in (5e-5, 1.6722408e-4, 1e-3):
+            rows.append([cs, dt, ph.collision_sub_steps(_Grid(cs), D, dt)])
+    out["sub_collision"] = np.array(rows, np.float64)
+    # the replay producer's rule, read back from simulate_trajectories itself on a tiny walk
+    rows = []
+    for name, g in (("cyl", geo.Cylinder(5e-6, (0, 0, 1))),
+                    ("sphk", geo.Sphere(3e-6, permeability=1e-5)),
+                    ("pcyl", geo.PackedCylinders([1.1e-6, 2e-6], [[-2e-6, -2e-6], [2.5e-6, 2.5e-6]],
+                                                 9e-6))):
+        for dt in (1.6722408e-4, 5e-5):
+            out_ = core.simulate_trajectories(2, D, g, dt * 2, dt, seed=1, require_gpu=False)
+            rows.append([dt, out_[2]])
+        out[f"sub_replay_{name}"] = np.array(rows[-2:], np.float64)
+
+
+def _pack_cases(m, out):
+    geo = m["geometries"]
+    rng = np.random.default_rng(7)
+    radii = np.clip(rng.lognormal(np.log(2e-6), 0.25, 40), 0.8e-6, 4e-6)
+    c, L, vf = geo.pack_cylinders(radii, target_vf=0.5, seed=3)
+    out["pack_cyl_radii"], out["pack_cyl_centers"], out["pack_cyl_L"] = radii, c, np.array(L)
+    sr = rng.uniform(1e-6, 2e-6, 25)
+    c, L, vf = geo.pack_spheres(sr, target_vf=0.3, seed=4)
+    out["pack_sph_radii"], out["pack_sph_centers"], out["pack_sph_L"] = sr, c, np.array(L)
+
+
+def _replay_cases(m, out):
+    tr, wf = m["trajectories"], m["waveforms"]
+    rng = np.random.default_rng(3)
+    n, n_t = 400, 121
+    traj = np.cumsum(rng.normal(scale=0.3e-6, size=(n, n_t, 3)), axis=1).astype(np.float16)
+    w = wf.set_b(wf.pgste(0.005, 0.02, 0.08, [[1, 0, 0], [0, 1, 0], [0.6, 0, 0.8]], n_t), 1e9)
+    dlog = -np.abs(rng.normal(scale=1e-9, size=(n, n_t))).astype(np.float16)
+    sig = tr.replay(traj, w.dt, np.asarray(w.G), w.dt, chi_perp=w.chi_perp,
+                    dlog_boundary_unit=dlog, T2=0.08, T1=0.9, surface_relaxivity=1e-5, D=D,
+                    stimulated_echo=True)
+    out["rep_traj"], out["rep_G"], out["rep_chi"] = traj, np.asarray(w.G), np.asarray(
+        w.chi_perp, np.float32)
+    out["rep_dt"], out["rep_dlog"], out["rep_signal"] = np.array(w.dt), dlog, np.asarray(sig)
+    sig2 = tr.replay(traj, w.dt, np.asarray(w.G), w.dt)
+    out["rep_signal_plain"] = np.asarray(sig2)
+
+
+def make_kat(root):
+    m = _ref(root)
+    out = {}
+    rng = np.random.default_rng(2024)
+    _waveform_cases(m, out)
+    _substep_cases(m, out)
+    _pack_cases(m, out)
+    _replay_cases(m, out)
+    _plugin_cases(m, rng, out)
+    np.savez_compressed(HERE / "kat.npz", **out)
+    print(f"kat.npz: {len(out)} arrays")
+
+
+# ------------------------------------------------------------------------------------------------
+# Reference Monte-Carlo signals (statistical fixtures)
+# ------------------------------------------------------------------------------------------------
+def _mc_configs():
+    """name -> (kind, kwargs).  Small enough for the reference's per-walker Python walk."""
+    return {
+        "free_pgse": dict(geom=("free",), wf=("pgse3",), n=8000, api="simulate"),
+        "free_pgse_fused": dict(geom=("free",), wf=("pgse3",), n=6000, api="simulate",
+                                engine="fused"),
+        "cyl_rho": dict(geom=("cyl", 5e-6, 1e-6, None), wf=("pgse6",), n=3200, api="simulate"),
+        "cyl_rho_fused": dict(geom=("cyl", 5e-6, 1e-6, None), wf=("pgse6",), n=1600,
+                              api="simulate", engine="fused"),
+        "sph_kappa": dict(geom=("sph", 5e-6, None, 1e-5), wf=("pgse_short",), n=960,
+                          api="simulate"),
+        "cyl_kappa": dict(geom=("cyl", 5e-6, None, 1e-5), wf=("pgse_short",), n=960,
+                          api="simulate"),
+        "sph_t2": dict(geom=("sph", 5e-6, None, None), wf=("pgse6",), n=4000, api="simulate",
+                       T2=0.06),
+        "lattice_fused": dict(geom=("lattice", 0.6), wf=("pgse_lat",), n=6400, api="simulate",
+                              engine="fused"),
+        "rsa_fused": dict(geom=("rsa",), wf=("pgse_lat",), n=4000, api="simulate",
+                          engine="fused"),
+        "psph_fused": dict(geom=("psph",), wf=("pgse_lat",), n=4000, api="simulate",
+                           engine="fused"),
+        "cpmg_sph": dict(geom=("sph", 5e-6, None, None), wf=("cpmg",), n=4000, api="cpmg",
+                         T2=0.06),
+        "cpmg_free": dict(geom=("free",), wf=("cpmg_g",), n=4000, api="cpmg", T2=0.08),
+    }
+
+
+def build_waveform(wfm, spec):
+    name = spec[0]
+    if name == "pgse3":
+        return wfm.set_b(wfm.pgse(0.01, 0.04, 0.05, [[1, 0, 0]] * 3, 300), [0, 1e9, 2e9])
+    rng = np.random.default_rng(0)
+    bv = rng.normal(size=(6, 3))
+    bv /= np.linalg.norm(bv, axis=1, keepdims=True)
+    if name == "pgse6":
+        return wfm.set_b(wfm.pgse(0.01, 0.04, 0.05, bv, 300), 1e9)
+    if name == "pgse_short":
+        return wfm.set_b(wfm.pgse(0.003, 0.008, 0.2, bv[:4], 60), 1e9)
+    if name == "pgse_lat":
+        return wfm.set_b(wfm.pgse(0.005, 0.02, 0.1, [[1, 0, 0], [0, 1, 0], [0, 0, 1],
+                                                     [0.6, 0.8, 0]], 200), 1.5e9)
+    if name == "cpmg":
+        return wfm.cpmg(8, 12e-3, 0.0, [[1, 0, 0]], n_t_per_echo=60)
+    if name == "cpmg_g":
+        return wfm.cpmg(6, 10e-3, 0.02, [[1, 0, 0], [0, 0, 1]], n_t_per_echo=50)
+    raise KeyError(name)
+
+
+def build_geometry(geo, spec):
+    kind = spec[0]
+    if kind == "free":
+        return geo.FreeDiffusion()
+    if kind == "cyl":
+        return geo.Cylinder(spec[1], (0, 0, 1), surface_relaxivity_t2=spec[2], permeability=spec[3])
+    if kind == "sph":
+        return geo.Sphere(spec[1], surface_relaxivity_t2=spec[2], permeability=spec[3])
+    if kind == "lattice":
+        a = 4e-6
+        r = a * np.sqrt(spec[1] / np.pi)
+        cen = np.array([[(i + 0.5) * a - a, (j + 0.5) * a - a] for i in range(2) for j in range(2)])
+        return geo.PackedCylinders(np.full(4, r), cen, 2 * a)
+    if kind == "rsa":
+        rng = np.random.default_rng(1)
+        radii = np.clip(rng.lognormal(np.log(1.5e-6), 0.25, 20), 0.8e-6, 3e-6)
+        cen, L, _ = geo.pack_cylinders(radii, target_vf=0.45, seed=2)
+        return geo.PackedCylinders(radii, cen, L)
+    if kind == "psph":
+        sr = np.full(10, 1.5e-6)
+        cen, L, _ = geo.pack_spheres(sr, target_vf=0.25, seed=3)
+        return geo.PackedSpheres(sr, cen, L)
+    raise KeyError(kind)
+
+
+def _mc_worker(args):
+    root, name, cfg, seed, n = args
+    m = _ref(root)
+    import contextlib
+    import io
+    wf = build_waveform(m["waveforms"], cfg["wf"])
+    g = build_geometry(m["geometries"], cfg["geom"])
+    with contextlib.redirect_stdout(io.StringIO()):
+        if cfg["api"] == "cpmg":
+            s = m["core"].simulate_cpmg(n, D, wf, g, T2=cfg.get("T2"), seed=seed,
+                                        require_gpu=False)
+        else:
+            s = m["core"].simulate(n, D, wf, g, seed=seed, T2=cfg.get("T2"), require_gpu=False,
+                                   engine=cfg.get("engine", "auto"))
+    return name, n, np.asarray(s, np.float64)
+
+
+def make_mc(root, procs, only=None):
+    cfgs = _mc_configs()
+    jobs = []
+    for name, cfg in cfgs.items():
+        if only and name not in only:
+            continue
+        per = cfg["n"] // procs
+        for k in range(procs):
+            jobs.append((root, name, cfg, 1000 + 17 * k, per))
+    t0 = time.time()
+    res = {}
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for name, n, s in pool.imap_unordered(_mc_worker, jobs):
+            res.setdefault(name, []).append((n, s))
+            print(f"  {name}: chunk of {n} done ({time.time() - t0:.0f}s)", flush=True)
+    path = HERE / "mc.json"
+    out = json.loads(path.read_text()) if path.exists() else {}
+    for name, chunks in res.items():
+        arr = np.stack([s for _, s in chunks])                 # (procs, ...)
+        ns = np.array([n for n, _ in chunks], float)
+        mean = np.tensordot(ns, arr, axes=1) / ns.sum()
+        # standard error from the spread of the independent chunks
+        se = np.sqrt(np.sum(ns[:, None] * (arr.reshape(len(ns), -1) - mean.reshape(1, -1)) ** 2,
+                            axis=0) / ns.sum() / (len(ns) - 1)).reshape(mean.shape)
+        out[name] = dict(config=_jsonable(cfgs[name]), n_walkers=int(ns.sum()),
+                         chunks=len(ns), signal=mean.tolist(), stderr=se.tolist())
+    path.write_text(json.dumps(out, indent=1))
+    print(f"mc.json: {sorted(out)}")
+
+
+def _jsonable(cfg):
+    return {k: (list(v) if isinstance(v, tuple) else v) for k, v in cfg.items()}
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=os.environ.get("DMIPY_SIM_SRC", "/root/reference"))
+    ap.add_argument("--kat", action="store_true")
+    ap.add_argument("--mc", action="store_true")
+    ap.add_argument("--only", nargs="*")
+    ap.add_argument("--procs", type=int, default=os.cpu_count() or 4)
+    a = ap.parse_args()
+    if a.kat:
+        make_kat(a.ref)
+    if a.mc:
+        make_mc(a.ref, a.procs, a.only)

