@@ -1,0 +1,305 @@
+"""Benchmark of the Monte-Carlo forward walk on one GB300 (or N, one process per GPU).
+
+Workload (the packed-substrate configuration): PackedCylinders on a periodic 16 x 16 square
+lattice, volume fraction 0.6, lognormal radii (mean 2 um, sd 0.5 um, seed 0, clipped to 0.95 of
+the half spacing), impermeable, D = 2e-9 m^2/s, 1,000,000 walkers per GPU, 64 measurements
+(32 PGSE delta = 10 ms / DELTA = 40 ms at b = 0.5-3 ms/um^2 + 32 cosine OGSE 10-100 Hz snapped to
+40/80 Hz, b = 1 ms/um^2), n_t = 1000 over 50 ms, walked as dmipy-sim's default engine does
+(walk-once + replay semantics: step <= R_min/6, i.e. 27 sub-steps per sample).
+
+One step = one complete walk of that workload (all walkers, all samples, all sub-steps, ensemble
+reduction).  Metric: walker-steps/s, a walker-step being one walker advanced one physics sub-step
+with every measurement's phase updated.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference`` times the CPU restatement of the reference walk (oracle/, all host cores) on
+a bounded walker sample of the same workload: dmipy-sim is pure Python/JAX and JAX is not
+installed, so its own CPU path cannot run here.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+D = 2e-9
+N_WALKERS = 1_000_000
+N_T = 1000
+METRIC = "walker-steps/s/GPU (plain MC); signals/s at <=0.005 err (batched+surrogate)"
+UNIT = "walker-steps/s"
+WORKLOAD = "PackedCylinders 16x16 square lattice f=0.6 lognormal r (2.0+-0.5 um), kappa=0"
+
+
+def build_workload():
+    import dmipy_sim_gb300 as d
+    radii, centers, L = d.lattice_cylinders(16, 0.6, 2e-6, 0.5e-6, seed=0)
+    geom = d.PackedCylinders(radii, centers, L)
+    rng = np.random.default_rng(0)
+    bv = rng.normal(size=(8, 3))
+    bv /= np.linalg.norm(bv, axis=1, keepdims=True)
+    pg = d.pgse(0.01, 0.04, 0.05, np.tile(bv, (4, 1)), N_T)
+    pg = d.set_b(pg, np.repeat([0.5e9, 1e9, 2e9, 3e9], 8))
+    import warnings
+    Gs = [pg.G]
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for f in (10.0, 40.0, 70.0, 100.0):
+            og = d.set_b(d.ogse(f, 0.05, 0.05, bv, N_T), 1e9)
+            Gs.append(og.G)
+    wf = d.Waveform(G=np.concatenate(Gs, 0).astype(np.float32), dt=pg.dt, echo_idx=N_T - 1)
+    return geom, wf
+
+
+def _clock_sampler(stop, samples):
+    cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+           "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+           "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+           "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"]
+    try:
+        p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            samples.append([x.strip() for x in line.split(",")])
+    finally:
+        p.terminate()
+        try:
+            p.wait(timeout=5)
+        except Exception:
+            p.kill()
+
+
+def _clock_summary(samples, dev_index):
+    rows = [s for s in samples if s and s[0] == str(dev_index)]
+    if not rows:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[i] for r in rows for i in range(4)
+                      if len(r) > 5 + i and r[5 + i].lower().startswith("active")})
+    return {"sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+            "samples": len(rows)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def algorithmic_flops_per_walker_step(n_meas, sub_steps, k_alg=4):
+    """FP32 FLOPs per walker-step of the walk: direction from two uniforms (20), the packed
+    cylinder wall test (22 per candidate object, 4 objects within reach of a step) and the phase
+    3 FMAs per measurement per waveform sample, spread over the sample's sub-steps."""
+    return 20.0 + 22.0 * k_alg + 6.0 * n_meas / sub_steps
+
+
+def cpu_baseline(geom, wf, S, threads, budget_s=15.0):
+    """The CPU restatement of the reference walk (oracle/, FP32) on a bounded sample of walkers of
+    the same workload, every host thread; returns (walker-steps/s, sample description)."""
+    from dmipy_sim_gb300 import core
+    from oracle import oracle as O
+    G, _ = core._waveform_arrays(wf, geom)
+    og = O.geom_from(geom)
+    n = 64
+    t0 = time.perf_counter()
+    O.walk(og, n_walkers=n, G=G, dt=wf.dt, sub_steps=S, phase_per_substep=False, seed=1,
+           n_threads=threads)
+    dt1 = time.perf_counter() - t0
+    n2 = int(max(threads, min(1_000_000, n * budget_s / max(dt1, 1e-3))))
+    t0 = time.perf_counter()
+    O.walk(og, n_walkers=n2, G=G, dt=wf.dt, sub_steps=S, phase_per_substep=False, seed=2,
+           n_threads=threads)
+    el = time.perf_counter() - t0
+    steps = n2 * wf.G.shape[1] * S
+    return steps / el, f"{n2} walkers x {wf.G.shape[1]} samples x {S} sub-steps in {el:.1f} s"
+
+
+def gpu_arm(a):
+    import torch
+    import dmipy_sim_gb300 as d
+    from dmipy_sim_gb300 import core
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    geom, wf = build_workload()
+    G, chi = core._waveform_arrays(wf, geom)
+    S = core.replay_sub_steps(geom, D, wf.dt)
+    n = N_WALKERS
+    walk = core.PreparedWalk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                             phase_per_substep=False, seed=1234, walker_offset=rank * n)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(a.warmup):
+        walk.launch()
+    barrier()
+    stop, samples = threading.Event(), []
+    th = threading.Thread(target=_clock_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    time.sleep(0.3)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(a.steps)]
+    t_wall = time.perf_counter()
+    for k in range(a.steps):
+        flush.fill_(float(k))                       # evict L2 between timed walks
+        ev[k][0].record()
+        walk.launch()
+        ev[k][1].record()
+    barrier()
+    t_wall = time.perf_counter() - t_wall
+    ms = [s.elapsed_time(e) for s, e in ev]
+    kernel_s = sum(ms) / 1e3
+    t = torch.tensor([kernel_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    kernel_s = float(t.item())
+    res = walk.result()
+
+    # end to end through the public API: host waveform in, host signals out, every step
+    e2e_s = None
+    e2e_steps = max(2, min(a.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sig = d.simulate(n, D, wf, geom, seed=1234)
+    torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    stop.set()
+    th.join(timeout=5)
+    clocks = _clock_summary(samples, local)
+
+    walker_steps = float(n) * wf.G.shape[1] * S
+    value = walker_steps * world * a.steps / kernel_s
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    m = wf.G.shape[0]
+    F = algorithmic_flops_per_walker_step(m, S)
+    per_launch_s = kernel_s / a.steps
+    achieved = walker_steps * F / per_launch_s / 1e12
+    sm_max = clocks.get("sm_max_mhz") or 2070.0
+    peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12          # FP32 FMA pipes at the max SM clock
+    traffic = None
+    tpath = ROOT / "profiles" / "walk_packed_cylinders_traffic.txt"
+    if tpath.exists():
+        for line in tpath.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * kernel_s / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic substrate and waveforms (seeded), no dataset",
+        "config": {"workload": WORKLOAD, "n_walkers_per_gpu": n, "n_t": int(wf.G.shape[1]),
+                   "n_meas": int(m), "sub_steps": int(S), "engine": "replay semantics (auto)",
+                   "walker_steps_per_step": walker_steps * world,
+                   "l2": "512 MB buffer written between timed walks",
+                   "parallelism": f"walker shards x{world}"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "flops_per_walker_step": F,
+                     "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the "
+                                    "sampled max SM clock; MEASURED_PEAKS.json has no FP32 "
+                                    "figure"},
+        "e2e": {"value": walker_steps * world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(wf.G.nbytes + 4 * wf.G.shape[1]),
+                "d2h_bytes_per_step": int(8 * 3 * m + 4 * 8)},
+        "gpu_launches": walk.launches_per_call * a.steps,
+        "clocks": clocks,
+        "signal_b1_pgse_x": float(res.signal[0, 8]),
+        "status": res.status,
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        v, sample = cpu_baseline(geom, wf, S, os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                               "sample": sample}
+    print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_arm(a):
+    world, rank, local = _dist()
+    if rank != 0:
+        return
+    from dmipy_sim_gb300 import core
+    from oracle import oracle as O
+    geom, wf = build_workload()
+    G, _ = core._waveform_arrays(wf, geom)
+    S = core.replay_sub_steps(geom, D, wf.dt)
+    og = O.geom_from(geom)
+    threads = os.cpu_count() or 1
+    n = max(threads, 16 * threads)
+    for _ in range(a.warmup):
+        O.walk(og, n_walkers=n, G=G, dt=wf.dt, sub_steps=S, phase_per_substep=False, seed=7,
+               n_threads=threads)
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        O.walk(og, n_walkers=n, G=G, dt=wf.dt, sub_steps=S, phase_per_substep=False, seed=8 + k,
+               n_threads=threads)
+    el = time.perf_counter() - t0
+    walker_steps = float(n) * wf.G.shape[1] * S
+    v = walker_steps * a.steps / el
+    sample = f"{n} walkers x {wf.G.shape[1]} samples x {S} sub-steps per step"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic substrate and waveforms (seeded), no dataset",
+        "config": {"workload": WORKLOAD, "n_walkers_per_step": n, "n_t": int(wf.G.shape[1]),
+                   "n_meas": int(wf.G.shape[0]), "sub_steps": int(S),
+                   "engine": "CPU restatement of the reference walk (dmipy-sim is Python+JAX; "
+                             "JAX is not installed)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gpu_arm(a)
+
+
+if __name__ == "__main__":
+    main()

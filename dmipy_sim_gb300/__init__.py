@@ -8,7 +8,7 @@ from .constants import GAMMA, DEFAULT_SLEW_RATE
 from .waveforms import (Waveform, pgse, pgste, ogse, cpmg, calc_b, calc_btensor, set_b,
                         rotate_waveform, tile_waveform)
 from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, pack_cylinders,
-                         PackedCylinders, pack_spheres, PackedSpheres)
+                         PackedCylinders, pack_spheres, PackedSpheres, lattice_cylinders)
 from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
                    fused_sub_steps)
@@ -17,7 +17,7 @@ from .trajectories import replay
 __all__ = [
     "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
     "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "Geometry", "FreeDiffusion",
-    "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres",
+    "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
     "simulate", "simulate_cpmg", "simulate_trajectories", "replay", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
     "fused_sub_steps",

@@ -191,103 +191,123 @@ def _waveform_arrays(waveform, geometry):
     return G, chi
 
 
-def run_walk(geometry, *, n_walkers, diffusivity, G, dt, sub_steps, phase_per_substep, seed,
-             chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
-             want_positions=False, want_walker_signals=False, want_compartments=False,
-             traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False):
-    """One device walk.  ``G`` is (M, n_t, 3) in the geometry's walk frame; ``r0`` (n, 3) in the
-    walk frame.  Returns a :class:`WalkResult`."""
-    lib = _lib.load()
-    dev = _lib.device()
-    G = np.asarray(G, dtype=np.float32)
-    n_meas, n_t, _ = G.shape
-    dt = float(dt)
-    S = int(sub_steps)
-    dt_sub = dt / S
-    D = float(diffusivity)
-    step_l = np.float32(np.sqrt(6.0 * D * dt_sub))
-    gamma_dt = np.float32(GAMMA * (dt_sub if phase_per_substep else dt))
+class PreparedWalk:
+    """A walk with every device buffer allocated once: ``launch()`` enqueues the kernels on the
+    current stream (asynchronous, CUDA-graph capturable), ``result()`` synchronises and reads
+    the sums back.  ``G`` is (M, n_t, 3) in the geometry's walk frame; ``r0`` (n, 3) in the walk
+    frame."""
 
-    rho = getattr(geometry, 'surface_relaxivity_t2', None)
-    kappa = getattr(geometry, 'permeability', None)
-    rho_over_D = np.float32(rho / D) if rho is not None else np.float32(0.0)
-    kappa_over_D = np.float32(kappa / D) if kappa is not None else np.float32(0.0)
-    want_w = (rho is not None) or (kappa is not None) or (T2 is not None) or (T1 is not None)
-    wall = geometry._wall_mode(rho is not None or want_dlog)
-    gdesc, keep = geometry._desc(float(step_l), wall, rho_over_D if rho is not None else 0.0,
-                                 kappa_over_D, dev)
+    def __init__(self, geometry, *, n_walkers, diffusivity, G, dt, sub_steps, phase_per_substep,
+                 seed, chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
+                 want_positions=False, want_walker_signals=False, want_compartments=False,
+                 traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False):
+        self.lib = _lib.load()
+        dev = self.dev = _lib.device()
+        G = np.asarray(G, dtype=np.float32)
+        n_meas, n_t, _ = G.shape
+        dt = float(dt)
+        S = int(sub_steps)
+        dt_sub = dt / S
+        D = float(diffusivity)
+        step_l = np.float32(np.sqrt(6.0 * D * dt_sub))
+        gamma_dt = np.float32(GAMMA * (dt_sub if phase_per_substep else dt))
+        rho = getattr(geometry, 'surface_relaxivity_t2', None)
+        kappa = getattr(geometry, 'permeability', None)
+        rho_over_D = np.float32(rho / D) if rho is not None else np.float32(0.0)
+        kappa_over_D = np.float32(kappa / D) if kappa is not None else np.float32(0.0)
+        want_w = (rho is not None) or (kappa is not None) or (T2 is not None) or (T1 is not None)
+        wall = geometry._wall_mode(rho is not None or want_dlog)
+        self.gdesc, self._keep = geometry._desc(float(step_l), wall, rho_over_D, kappa_over_D,
+                                                dev)
+        echo = np.asarray([n_t - 1] if echo_idx is None else echo_idx, dtype=np.int32).ravel()
+        self._echo_c = (ctypes.c_int32 * len(echo))(*echo.tolist())
+        self.G_dev = torch.from_numpy(np.ascontiguousarray(G.transpose(1, 0, 2))).to(dev)
+        self.chi_dev = None if chi is None else torch.from_numpy(
+            np.asarray(chi, np.float32)).to(dev)
+        self.r0_dev = None
+        if r0 is not None:
+            r0 = np.asarray(r0, dtype=np.float32)
+            if r0.shape != (n_walkers, 3):
+                raise ValueError(f"r0 must have shape ({n_walkers}, 3), got {r0.shape}")
+            self.r0_dev = torch.from_numpy(np.ascontiguousarray(r0)).to(dev)
+        p = self.p = _lib.WalkParams()
+        p.n_walkers = int(n_walkers)
+        p.walker_offset = int(walker_offset)
+        p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        p.n_t = n_t
+        p.n_meas = n_meas
+        p.sub_steps = S
+        p.phase_per_substep = 1 if phase_per_substep else 0
+        p.step_length = step_l
+        p.gamma_dt = gamma_dt
+        p.t2_decay = np.float32(dt_sub / T2) if T2 is not None else 0.0
+        p.t1_decay = np.float32(dt_sub / T1) if T1 is not None else 0.0
+        p.has_weight = 1 if want_w else 0
+        p.n_echo = len(echo)
+        p.echo_idx = self._echo_c
+        p.G = self.G_dev.data_ptr()
+        p.chi = None if self.chi_dev is None else self.chi_dev.data_ptr()
+        p.r0 = None if self.r0_dev is None else self.r0_dev.data_ptr()
+        self.sums = torch.zeros((len(echo), n_meas, 3), dtype=torch.float64, device=dev)
+        self.status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+        o = self.o = _lib.WalkOutputs()
+        o.sums = self.sums.data_ptr()
+        o.status = self.status.data_ptr()
+        ex = self.extras = {}
+        if want_positions:
+            ex["pos"] = torch.empty((n_walkers, 3), dtype=torch.float32, device=dev)
+            o.final_pos = ex["pos"].data_ptr()
+        if want_walker_signals:
+            ex["log_w"] = torch.zeros(n_walkers, dtype=torch.float32, device=dev)
+            ex["phi"] = torch.empty((n_walkers, n_meas), dtype=torch.float32, device=dev)
+            o.log_w = ex["log_w"].data_ptr()
+            o.phi = ex["phi"].data_ptr()
+        if want_compartments:
+            ex["comp0"] = torch.empty(n_walkers, dtype=torch.int32, device=dev)
+            ex["comp_end"] = torch.empty(n_walkers, dtype=torch.int32, device=dev)
+            o.comp0 = ex["comp0"].data_ptr()
+            o.comp_end = ex["comp_end"].data_ptr()
+        if traj is not None:
+            o.traj = traj.data_ptr()
+            o.traj_f16 = 1 if traj_f16 else 0
+        if want_dlog:
+            ex["dlog"] = torch.empty((n_walkers, n_t), dtype=torch.float32, device=dev)
+            o.dlog_unit = ex["dlog"].data_ptr()
+        if want_comp_occ:
+            ex["comp_occ"] = torch.empty((n_walkers, n_t), dtype=torch.float32, device=dev)
+            o.comp_occ = ex["comp_occ"].data_ptr()
+        self.ws_bytes = self.lib.dmsim_walk_workspace_bytes(p, self.gdesc)
+        if self.ws_bytes == 0:
+            _lib.check(-1, "dmsim_walk_workspace_bytes")
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        self.n_walkers = int(n_walkers)
+        self.n_meas, self.n_t, self.sub_steps = n_meas, n_t, S
 
-    echo = np.asarray([n_t - 1] if echo_idx is None else echo_idx, dtype=np.int32).ravel()
-    echo_c = (ctypes.c_int32 * len(echo))(*echo.tolist())
+    @property
+    def launches_per_call(self):
+        """Kernels one launch() enqueues: waveform re-layout, one walk per 64-measurement pass,
+        and the cross-block reduction."""
+        mt = 4 if self.n_meas <= 4 else 16 if self.n_meas <= 16 else 32 if self.n_meas <= 32 else 64
+        return 2 + (self.n_meas + mt - 1) // mt
 
-    G_dev = torch.from_numpy(np.ascontiguousarray(G.transpose(1, 0, 2))).to(dev)   # (n_t, M, 3)
-    chi_dev = None if chi is None else torch.from_numpy(np.asarray(chi, np.float32)).to(dev)
-    r0_dev = None
-    if r0 is not None:
-        r0 = np.asarray(r0, dtype=np.float32)
-        if r0.shape != (n_walkers, 3):
-            raise ValueError(f"r0 must have shape ({n_walkers}, 3), got {r0.shape}")
-        r0_dev = torch.from_numpy(np.ascontiguousarray(r0)).to(dev)
+    def launch(self):
+        rc = self.lib.dmsim_walk(self.p, self.gdesc, self.o, _lib.ptr(self.ws), self.ws_bytes,
+                                 _lib.stream_handle())
+        _lib.check(rc, "dmsim_walk")
 
-    p = _lib.WalkParams()
-    p.n_walkers = int(n_walkers)
-    p.walker_offset = int(walker_offset)
-    p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
-    p.n_t = n_t
-    p.n_meas = n_meas
-    p.sub_steps = S
-    p.phase_per_substep = 1 if phase_per_substep else 0
-    p.step_length = step_l
-    p.gamma_dt = gamma_dt
-    p.t2_decay = np.float32(dt_sub / T2) if T2 is not None else 0.0
-    p.t1_decay = np.float32(dt_sub / T1) if T1 is not None else 0.0
-    p.has_weight = 1 if want_w else 0
-    p.n_echo = len(echo)
-    p.echo_idx = echo_c
-    p.G = G_dev.data_ptr()
-    p.chi = None if chi_dev is None else chi_dev.data_ptr()
-    p.r0 = None if r0_dev is None else r0_dev.data_ptr()
+    def result(self):
+        torch.cuda.synchronize(self.dev)
+        st = self.status.cpu().numpy().astype(np.uint32)
+        return WalkResult(self.sums.cpu().numpy(), self.n_walkers,
+                          dict(zip(_lib.STATUS_NAMES, st.tolist())), self.extras)
 
-    sums = torch.zeros((len(echo), n_meas, 3), dtype=torch.float64, device=dev)
-    status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
-    o = _lib.WalkOutputs()
-    o.sums = sums.data_ptr()
-    o.status = status.data_ptr()
-    extras = {}
-    if want_positions:
-        extras["pos"] = torch.empty((n_walkers, 3), dtype=torch.float32, device=dev)
-        o.final_pos = extras["pos"].data_ptr()
-    if want_walker_signals:
-        extras["log_w"] = torch.zeros(n_walkers, dtype=torch.float32, device=dev)
-        extras["phi"] = torch.empty((n_walkers, n_meas), dtype=torch.float32, device=dev)
-        o.log_w = extras["log_w"].data_ptr()
-        o.phi = extras["phi"].data_ptr()
-    if want_compartments:
-        extras["comp0"] = torch.empty(n_walkers, dtype=torch.int32, device=dev)
-        extras["comp_end"] = torch.empty(n_walkers, dtype=torch.int32, device=dev)
-        o.comp0 = extras["comp0"].data_ptr()
-        o.comp_end = extras["comp_end"].data_ptr()
-    if traj is not None:
-        o.traj = traj.data_ptr()
-        o.traj_f16 = 1 if traj_f16 else 0
-    if want_dlog:
-        extras["dlog"] = torch.empty((n_walkers, n_t), dtype=torch.float32, device=dev)
-        o.dlog_unit = extras["dlog"].data_ptr()
-    if want_comp_occ:
-        extras["comp_occ"] = torch.empty((n_walkers, n_t), dtype=torch.float32, device=dev)
-        o.comp_occ = extras["comp_occ"].data_ptr()
 
-    nbytes = lib.dmsim_walk_workspace_bytes(p, gdesc)
-    if nbytes == 0:
-        _lib.check(-1, "dmsim_walk_workspace_bytes")
-    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
-    rc = lib.dmsim_walk(p, gdesc, o, _lib.ptr(ws), nbytes, _lib.stream_handle())
-    _lib.check(rc, "dmsim_walk")
-    torch.cuda.synchronize(dev)
-    st = status.cpu().numpy().astype(np.uint32)
-    del keep
-    return WalkResult(sums.cpu().numpy(), int(n_walkers),
-                      dict(zip(_lib.STATUS_NAMES, st.tolist())), extras)
+def run_walk(geometry, **kw):
+    """One device walk (see :class:`PreparedWalk` for the arguments); returns a
+    :class:`WalkResult`."""
+    w = PreparedWalk(geometry, **kw)
+    w.launch()
+    return w.result()
 
 
 def step_kat(geometry, r, steps, u=None, wall=None, diffusivity=2e-9):

