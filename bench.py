@@ -145,7 +145,7 @@ def gpu_arm(a):
     geom, wf = build_workload()
     G, chi = core._waveform_arrays(wf, geom)
     S = core.replay_sub_steps(geom, D, wf.dt)
-    n = N_WALKERS
+    n = a.walkers
     walk = core.PreparedWalk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
                              phase_per_substep=False, seed=1234, walker_offset=rank * n)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -294,6 +294,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--walkers", type=int, default=N_WALKERS,
+                    help="walkers per GPU (smaller only for profiling captures)")
     a = ap.parse_args()
     if a.impl == "reference":
         reference_arm(a)
