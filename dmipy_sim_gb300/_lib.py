@@ -24,7 +24,8 @@ STATUS_WORDS = len(STATUS_NAMES)
 
 # Symbols every build of the library exports (the C ABI of include/dmsim.h).
 EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "dmsim_walk",
-            "dmsim_step_kat", "dmsim_replay_workspace_bytes", "dmsim_replay")
+            "dmsim_walk_noalloc", "dmsim_step_kat", "dmsim_replay_workspace_bytes",
+            "dmsim_replay")
 
 
 class Geometry(C.Structure):
@@ -85,6 +86,9 @@ def load():
     lib.dmsim_walk.restype = C.c_int
     lib.dmsim_walk.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry), C.POINTER(WalkOutputs),
                                C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.dmsim_walk_noalloc.restype = C.c_int
+    lib.dmsim_walk_noalloc.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
+                                       C.POINTER(WalkOutputs), C.c_void_p]
     lib.dmsim_step_kat.restype = C.c_int
     lib.dmsim_step_kat.argtypes = [C.POINTER(Geometry), C.c_int64, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

@@ -358,6 +358,11 @@ int replay_grid(int64_t n_walkers) {
 
 }  // namespace
 
+namespace dmsim {
+// Records an error for dmsim_last_error() on behalf of entry points in other translation units.
+int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace dmsim
+
 extern "C" {
 
 int dmsim_version(void) { return DMSIM_ABI_VERSION; }

@@ -177,6 +177,19 @@ size_t dmsim_walk_workspace_bytes(const dmsim_walk_params* p, const dmsim_geomet
 int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
                void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same walk as dmsim_walk for callers that cannot allocate device memory (an XLA custom call
+   that only gets the buffers XLA hands it, a plug-in under a fixed device-memory budget).  It has
+   no counterpart in the reference.  The caller passes inputs and outputs only; the scratch lives
+   in one library-owned device array of DMSIM_NOALLOC_SCRATCH_BYTES (16 MiB) that every GPU which
+   loads the library keeps until exit.  The first call on a device (with that device current)
+   looks the array's address up once: make it before any stream capture.  Calls share the array
+   and it keeps the last call's contents, so calls that overlap on the GPU race: serialise them.
+   A walk whose workspace (dmsim_walk_workspace_bytes) exceeds the array returns DMSIM_ETOOBIG
+   without launching anything.  Allocates nothing. */
+#define DMSIM_NOALLOC_SCRATCH_BYTES (16u << 20)
+int dmsim_walk_noalloc(const dmsim_walk_params* p, const dmsim_geometry* g,
+                       const dmsim_walk_outputs* o, void* stream);
+
 /* Known-answer entry point of the device step functions: one geometry sub-step for each of n
    (position, step, uniform) triples, through exactly the code the walk kernel runs.  Counterpart
    of a single reference plug-in call (geometries.py: Cylinder/Sphere/PackedCylinders/PackedSpheres
