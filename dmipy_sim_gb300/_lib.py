@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 1
+DMSIM_ABI_VERSION = 2
 
 GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
 WALL_REFLECT, WALL_RELAX, WALL_PERMEATE = range(3)
@@ -34,7 +34,7 @@ class Geometry(C.Structure):
         ("radius", C.c_float), ("eps_detect", C.c_float), ("nudge", C.c_float),
         ("kappa_over_D", C.c_float), ("rho_over_D", C.c_float), ("L", C.c_float),
         ("n_objects", C.c_int32), ("grid_n", C.c_int32), ("cell_h", C.c_float),
-        ("reach", C.c_float), ("n_cand", C.c_int32), ("pad0", C.c_int32),
+        ("reach", C.c_float), ("n_cand", C.c_int32), ("need_min_image", C.c_int32),
         ("cell_start", C.c_void_p), ("cand", C.c_void_p), ("cand_obj", C.c_void_p),
         ("n_tri", C.c_int32), ("mesh_dims", C.c_int32 * 3), ("periodic", C.c_int32 * 3),
         ("max_bounces", C.c_int32), ("grid_min", C.c_float * 3), ("mesh_cell", C.c_float),
@@ -54,7 +54,8 @@ class WalkParams(C.Structure):
         ("phase_per_substep", C.c_int32), ("step_length", C.c_float), ("gamma_dt", C.c_float),
         ("t2_decay", C.c_float), ("t1_decay", C.c_float), ("has_weight", C.c_int32),
         ("n_echo", C.c_int32), ("echo_idx", C.POINTER(C.c_int32)), ("G", C.c_void_p),
-        ("chi", C.c_void_p), ("r0", C.c_void_p),
+        ("chi", C.c_void_p), ("r0", C.c_void_p), ("basis_rank", C.c_int32),
+        ("pad1", C.c_int32), ("basis_V", C.c_void_p), ("basis_C", C.c_void_p),
     ]
 
 

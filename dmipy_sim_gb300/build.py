@@ -20,6 +20,7 @@ LIB = PKG / "libdmsim.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-prec-div=false", "-prec-sqrt=false",
               "-Xptxas", "-warn-spills"]
 
 

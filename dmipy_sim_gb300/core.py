@@ -191,6 +191,47 @@ def _waveform_arrays(waveform, geometry):
     return G, chi
 
 
+def waveform_basis(G, max_rank=8, tol=1e-5):
+    """Factor a measurement set into a few time shapes: G[m, t, k] = sum_j C[m, k, j] V[j, t].
+
+    Protocols are built from a handful of waveform shapes (one PGSE lobe pair scaled and rotated
+    per direction and b-value, one OGSE per frequency), so the (measurement, axis) rows of G are
+    scalar multiples of at most ``max_rank`` shapes.  Each nonzero row is normalised by its value
+    at its largest-magnitude sample and matched to the shapes found so far (max deviation
+    <= tol).  Returns ``(V (n_t, r) float32, C (M, 3, r) float32)``, or None when more shapes are
+    needed or the reconstruction misses G by more than tol * max|G| (the walk then accumulates
+    every measurement's phase directly).
+    """
+    G = np.asarray(G, dtype=np.float64)
+    M, n_t, _ = G.shape
+    rows = G.transpose(0, 2, 1).reshape(M * 3, n_t)
+    gmax = float(np.max(np.abs(rows))) if rows.size else 0.0
+    if gmax == 0.0:
+        return np.zeros((n_t, 1), np.float32), np.zeros((M, 3, 1), np.float32)
+    shapes, coef = [], np.zeros((M * 3, max_rank))
+    for i in range(M * 3):
+        r = rows[i]
+        piv = int(np.argmax(np.abs(r)))
+        if abs(r[piv]) <= 1e-12 * gmax:
+            continue
+        s = r / r[piv]
+        for j, v in enumerate(shapes):
+            if np.max(np.abs(s - v)) <= tol:
+                coef[i, j] = r[piv]
+                break
+        else:
+            if len(shapes) == max_rank:
+                return None
+            shapes.append(s)
+            coef[i, len(shapes) - 1] = r[piv]
+    r_ = len(shapes)
+    V = np.stack(shapes, 1)                                           # (n_t, r)
+    C = coef[:, :r_]                                                  # (M*3, r)
+    if np.max(np.abs(C @ V.T - rows)) > tol * gmax:
+        return None
+    return V.astype(np.float32), C.reshape(M, 3, r_).astype(np.float32)
+
+
 class PreparedWalk:
     """A walk with every device buffer allocated once: ``launch()`` enqueues the kernels on the
     current stream (asynchronous, CUDA-graph capturable), ``result()`` synchronises and reads
@@ -200,7 +241,8 @@ class PreparedWalk:
     def __init__(self, geometry, *, n_walkers, diffusivity, G, dt, sub_steps, phase_per_substep,
                  seed, chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
                  want_positions=False, want_walker_signals=False, want_compartments=False,
-                 traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False):
+                 traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False,
+                 use_basis=True):
         self.lib = _lib.load()
         dev = self.dev = _lib.device()
         G = np.asarray(G, dtype=np.float32)
@@ -246,6 +288,15 @@ class PreparedWalk:
         p.n_echo = len(echo)
         p.echo_idx = self._echo_c
         p.G = self.G_dev.data_ptr()
+        basis = waveform_basis(G) if use_basis else None
+        self.basis_rank = 0
+        if basis is not None:
+            V, Cb = basis
+            self.V_dev = torch.from_numpy(np.ascontiguousarray(V)).to(dev)
+            self.C_dev = torch.from_numpy(np.ascontiguousarray(Cb)).to(dev)
+            p.basis_rank = self.basis_rank = V.shape[1]
+            p.basis_V = self.V_dev.data_ptr()
+            p.basis_C = self.C_dev.data_ptr()
         p.chi = None if self.chi_dev is None else self.chi_dev.data_ptr()
         p.r0 = None if self.r0_dev is None else self.r0_dev.data_ptr()
         self.sums = torch.zeros((len(echo), n_meas, 3), dtype=torch.float64, device=dev)
@@ -285,9 +336,11 @@ class PreparedWalk:
 
     @property
     def launches_per_call(self):
-        """Kernels one launch() enqueues: waveform re-layout, one walk per 64-measurement pass,
-        and the cross-block reduction."""
-        mt = 4 if self.n_meas <= 4 else 16 if self.n_meas <= 16 else 32 if self.n_meas <= 32 else 64
+        """Kernels one launch() enqueues: waveform re-layout, the walk (one per 64-measurement
+        pass in the direct form) and the cross-block reduction."""
+        if self.basis_rank:
+            return 3
+        mt = 16 if self.n_meas <= 16 else 32 if self.n_meas <= 32 else 64
         return 2 + (self.n_meas + mt - 1) // mt
 
     def launch(self):

@@ -10,11 +10,11 @@
 #include "walk_kernel.cuh"
 
 namespace dmsim {
-WalkFn walk_fn_free(int wall, int mt, bool tsm);
-WalkFn walk_fn_cyl(int wall, int mt, bool tsm);
-WalkFn walk_fn_sph(int wall, int mt, bool tsm);
-WalkFn walk_fn_pcyl(int wall, int mt, bool tsm);
-WalkFn walk_fn_psph(int wall, int mt, bool tsm);
+WalkFn walk_fn_free(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_cyl(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_sph(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_pcyl(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_psph(int wall, int pm, int width, bool tsm);
 }  // namespace dmsim
 
 using namespace dmsim;
@@ -38,28 +38,27 @@ size_t pad16(size_t v) { return (v + 15) & ~(size_t)15; }
 // lists are read through L1 from global memory.
 constexpr size_t kTabSmemBudget = 96 * 1024;
 
+// Direct form: measurements per pass.  Basis form: shapes held per thread.
 int pick_mt(int M) {
-  if (M <= 4) return 4;
   if (M <= 16) return 16;
   if (M <= 32) return 32;
   return 64;
 }
-
-size_t smem_fixed(int mt) {
-  switch (mt) {
-    case 4: return walk_smem_fixed<4>();
-    case 16: return walk_smem_fixed<16>();
-    case 32: return walk_smem_fixed<32>();
-    default: return walk_smem_fixed<64>();
-  }
-}
+int pick_rt(int r) { return r <= 2 ? 2 : (r <= 4 ? 4 : 8); }
+constexpr int kMaxBasisRank = 8;
+constexpr int kMaxBasisMeas = 512;
 
 struct Plan {
   WalkFn fn = nullptr;
-  int mt = 0, n_pass = 0, n_chunks = 0, grid = 0;
+  int pm = 0;      // 0 direct, 1 basis
+  int width = 0;   // MT (direct) or RT (basis)
+  int mt = 0;      // measurements per pass (direct) or 1 (basis: a single pass of all M)
+  int row = 0;     // floats per staged waveform sample
+  int n_pass = 0, n_chunks = 0, grid = 0;
   bool tsm = false;
   size_t smem = 0, tab_cs = 0, tab_cand = 0;
-  size_t off_gp = 0, off_act = 0, off_part = 0, total = 0;
+  size_t off_gp = 0, off_act = 0, off_cp = 0, off_part = 0, total = 0;
+  SmemLayout lay;
 };
 
 int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
@@ -91,10 +90,24 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
     if (((uintptr_t)g->cell_start & 15) || ((uintptr_t)g->cand & 15))
       return fail(DMSIM_EINVAL, "cell list arrays must be 16-byte aligned");
   }
-  if (p->G == nullptr) return fail(DMSIM_EINVAL, "G is null");
-
-  pl->mt = pick_mt(p->n_meas);
-  pl->n_pass = (p->n_meas + pl->mt - 1) / pl->mt;
+  if (p->basis_rank < 0 || p->basis_rank > kMaxBasisRank)
+    return fail(DMSIM_EINVAL, "basis_rank must be in [0, %d]", kMaxBasisRank);
+  if (p->basis_rank > 0) {
+    if (!p->basis_V || !p->basis_C) return fail(DMSIM_EINVAL, "basis_V / basis_C is null");
+    if (p->n_meas > kMaxBasisMeas)
+      return fail(DMSIM_ETOOBIG, "the basis form handles at most %d measurements", kMaxBasisMeas);
+    pl->pm = 1;
+    pl->width = pick_rt(p->basis_rank);
+    pl->mt = 1;
+    pl->n_pass = 1;
+    pl->row = pl->width;
+  } else {
+    if (p->G == nullptr) return fail(DMSIM_EINVAL, "G is null");
+    pl->pm = 0;
+    pl->width = pl->mt = pick_mt(p->n_meas);
+    pl->n_pass = (p->n_meas + pl->mt - 1) / pl->mt;
+    pl->row = 3 * pl->mt;
+  }
   pl->n_chunks = (p->n_t + kTC - 1) / kTC;
   size_t cells = 0;
   if (packed) {
@@ -104,14 +117,19 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
     pl->tsm = pl->tab_cs + pl->tab_cand <= kTabSmemBudget;
   }
   switch (g->kind) {
-    case DMSIM_GEOM_FREE: pl->fn = walk_fn_free(g->wall_mode, pl->mt, false); break;
-    case DMSIM_GEOM_CYLINDER: pl->fn = walk_fn_cyl(g->wall_mode, pl->mt, false); break;
-    case DMSIM_GEOM_SPHERE: pl->fn = walk_fn_sph(g->wall_mode, pl->mt, false); break;
-    case DMSIM_GEOM_PACKED_CYLINDERS: pl->fn = walk_fn_pcyl(g->wall_mode, pl->mt, pl->tsm); break;
-    case DMSIM_GEOM_PACKED_SPHERES: pl->fn = walk_fn_psph(g->wall_mode, pl->mt, pl->tsm); break;
+    case DMSIM_GEOM_FREE: pl->fn = walk_fn_free(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_CYLINDER: pl->fn = walk_fn_cyl(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_SPHERE: pl->fn = walk_fn_sph(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_PACKED_CYLINDERS:
+      pl->fn = walk_fn_pcyl(g->wall_mode, pl->pm, pl->width, pl->tsm);
+      break;
+    case DMSIM_GEOM_PACKED_SPHERES:
+      pl->fn = walk_fn_psph(g->wall_mode, pl->pm, pl->width, pl->tsm);
+      break;
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
-  pl->smem = smem_fixed(pl->mt) + (pl->tsm ? pl->tab_cs + pl->tab_cand : 0);
+  pl->lay = walk_smem_layout(pl->pm, pl->width, p->n_meas);
+  pl->smem = pl->lay.off_tab + (pl->tsm ? pl->tab_cs + pl->tab_cand : 0);
 
   int dev = 0, n_sm = 0, nb = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(DMSIM_ECUDA, "cudaGetDevice failed");
@@ -130,13 +148,16 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
   if (grid < 1) grid = 1;
   pl->grid = (int)grid;
 
+  const int Mp = pl->pm ? p->n_meas : pl->n_pass * pl->mt;
   size_t off = 0;
   pl->off_gp = off;
-  off = align256(off + (size_t)pl->n_pass * pl->n_chunks * kTC * pl->mt * 3 * 4);
+  off = align256(off + (size_t)pl->n_pass * pl->n_chunks * kTC * pl->row * 4);
   pl->off_act = off;
   off = align256(off + (size_t)pl->n_pass * p->n_t);
+  pl->off_cp = off;
+  off = align256(off + (pl->pm ? (size_t)p->n_meas * 3 * pl->width * 4 : 0));
   pl->off_part = off;
-  off = align256(off + (size_t)pl->grid * p->n_echo * pl->n_pass * pl->mt * 3 * 8);
+  off = align256(off + (size_t)pl->grid * p->n_echo * Mp * 3 * 8);
   pl->total = off;
   return DMSIM_OK;
 }
@@ -162,6 +183,30 @@ __global__ void k_prep(const float* __restrict__ G, int n_t, int M, int mt, int 
       }
     }
     if (t < n_t) act[(size_t)pass * n_t + t] = any ? 1 : 0;
+  }
+}
+
+// Basis form: V (n_t, r) -> (n_chunks*kTC, RT) and C (M, 3, r) -> (M, 3, RT), zero padded, plus
+// the per-sample activity flag.
+__global__ void k_prep_basis(const float* __restrict__ V, const float* __restrict__ C, int n_t,
+                             int M, int r, int rt, int t_pad, float* __restrict__ Vp,
+                             uint8_t* __restrict__ act, float* __restrict__ Cp) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t_pad; i += stride) {
+    const int t = (int)i;
+    bool any = false;
+    for (int j = 0; j < rt; ++j) {
+      const float v = (t < n_t && j < r) ? V[(size_t)t * r + j] : 0.f;
+      Vp[(size_t)t * rt + j] = v;
+      any |= (v != 0.f);
+    }
+    if (t < n_t) act[t] = any ? 1 : 0;
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)M * 3 * rt;
+       i += stride) {
+    const int j = (int)(i % rt);
+    const int64_t mk = i / rt;
+    Cp[i] = j < r ? C[mk * r + j] : 0.f;
   }
 }
 
@@ -342,6 +387,7 @@ GeoK make_geok(const dmsim_geometry* g) {
   gk.halfL = packed ? 0.5f * g->L : 0.f;
   gk.inv_h = packed ? (float)g->grid_n / g->L : 0.f;
   gk.n = packed ? g->grid_n : 1;
+  gk.mi = packed ? (g->need_min_image != 0) : 0;
   return gk;
 }
 
@@ -395,7 +441,12 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
   double* part = reinterpret_cast<double*>(ws + pl.off_part);
   const int t_pad = pl.n_chunks * kTC;
 
-  k_prep<<<64, 256, 0, st>>>(p->G, p->n_t, p->n_meas, pl.mt, pl.n_pass, t_pad, Gp, act);
+  float* Cp = reinterpret_cast<float*>(ws + pl.off_cp);
+  if (pl.pm)
+    k_prep_basis<<<64, 256, 0, st>>>(p->basis_V, p->basis_C, p->n_t, p->n_meas, p->basis_rank,
+                                     pl.width, t_pad, Gp, act, Cp);
+  else
+    k_prep<<<64, 256, 0, st>>>(p->G, p->n_t, p->n_meas, pl.mt, pl.n_pass, t_pad, Gp, act);
 
   KArgs a;
   memset(&a, 0, sizeof(a));
@@ -408,7 +459,11 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
   a.phase_sub = p->phase_per_substep ? 1 : 0;
   a.has_weight = p->has_weight ? 1 : 0;
   a.n_echo = p->n_echo;
-  a.Mp = pl.n_pass * pl.mt;
+  a.Mp = pl.pm ? p->n_meas : pl.n_pass * pl.mt;
+  a.Cp = Cp;
+  a.off_cs = (uint32_t)pl.lay.off_cs;
+  a.off_red = (uint32_t)pl.lay.off_red;
+  a.off_tab = (uint32_t)pl.lay.off_tab;
   a.M = p->n_meas;
   a.step_l = p->step_length;
   a.gamma_dt = p->gamma_dt;
@@ -443,13 +498,13 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
 
   for (int pass = 0; pass < pl.n_pass; ++pass) {
     a.pass = pass;
-    a.Gp = Gp + (size_t)pass * t_pad * pl.mt * 3;
+    a.Gp = Gp + (size_t)pass * t_pad * pl.row;
     a.active = act + (size_t)pass * p->n_t;
     pl.fn<<<pl.grid, kBlock, pl.smem, st>>>(a);
   }
   const int nred = p->n_echo * p->n_meas * 3;
-  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, pl.grid, p->n_echo, pl.n_pass * pl.mt,
-                                               p->n_meas, o->sums);
+  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, pl.grid, p->n_echo, a.Mp, p->n_meas,
+                                               o->sums);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));
   return DMSIM_OK;

@@ -42,7 +42,8 @@ struct Tally {
 struct GeoK {
   float R, R2, invR, eps, nudge, kod;  // single objects: R; packed: eps/nudge from R_min
   float L, halfL, inv_h;
-  int n;  // cells per axis
+  int n;   // cells per axis
+  int mi;  // 1 when some cell lists two images of one object: candidates need the min-image test
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -300,36 +301,47 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
   const float lxy = sqrtf(sx * sx + sy * sy);
   float dx = 0.f, dy = 0.f;
   if (lxy > 0.f) {
-    dx = sx / lxy;
-    dy = sy / lxy;
+    const float inv = 1.f / lxy;
+    dx = sx * inv;
+    dy = sy * inv;
   }
   const int c = cell_of(y, g) * g.n + cell_of(x, g);
   const uint32_t kb = cs[c], ke = cs[c + 1];
 
-  // Nearest wall crossing over the candidates (geometries.py:1777-1805 / 2054-2081).
+  // Nearest wall crossing over the candidates (geometries.py:1777-1805 / 2054-2081).  The same
+  // pass also evaluates the fold-first safety clamp (geometries.py:1851-1877) for the straight
+  // end point x + s, which is the end point whenever no wall is hit.  A grazing root of the
+  // winning candidate is re-solved in FP64 after the pass.
   float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hR = 1.f;
   bool hit_in = false;
+  const float ex = x + sx, ey = y + sy;
+  float pe = 1.f, pqx = 0.f, pqy = 0.f, pR = 1.f;
 #pragma unroll 1
   for (uint32_t k = kb; k < ke; ++k) {
     const float4 C = cand[k];
-    const float qx = x - C.x, qy = y - C.y;
-    if (!(min_image(qx, g) && min_image(qy, g))) continue;
     const float R2 = C.w * C.w;
+    if constexpr (WALL != kPermeate) {
+      const float fx = ex - C.x, fy = ey - C.y;
+      const float d2 = fx * fx + fy * fy;
+      if (d2 < R2 && (!g.mi || (min_image(fx, g) && min_image(fy, g)))) {
+        const float pen = d2 / R2;
+        if (pen < pe) {
+          pe = pen;
+          pqx = fx;
+          pqy = fy;
+          pR = C.w;
+        }
+      }
+    }
+    const float qx = x - C.x, qy = y - C.y;
+    if (g.mi && !(min_image(qx, g) && min_image(qy, g))) continue;
     const float dp = dx * qx + dy * qy;
     const float q2 = qx * qx + qy * qy;
     float disc = dp * dp - (q2 - R2);
     const bool ins = (WALL == kPermeate) && (q2 < R2);
     if (!ins && dp >= 0.f) continue;  // entry root -dp - sqrt(disc) <= 0: no forward crossing
-    float sq = sqrtf(fmaxf(disc, 0.f));
-    float t = ins ? -dp + sq : -dp - sq;
-    if (fabsf(disc) < kGrazeTol * R2 && t > 0.f && t < 1.01f * lxy) {
-      const double dpd = (double)dx * qx + (double)dy * qy;
-      const double dd = dpd * dpd - (((double)qx * qx + (double)qy * qy) - (double)C.w * C.w);
-      const double sd = sqrt(fmax(dd, 0.0));
-      disc = (float)dd;
-      t = (float)(ins ? -dpd + sd : -dpd - sd);
-      ++tl.graze;
-    }
+    const float sq = sqrtf(fmaxf(disc, 0.f));
+    const float t = ins ? -dp + sq : -dp - sq;
     const bool valid = (disc > 0.f) && (t > g.eps) && (t < lxy) && (lxy > 0.f);
     if (valid && t < tbest) {
       tbest = t;
@@ -339,6 +351,16 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
       hR = C.w;
       hit_in = ins;
     }
+  }
+  if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR) {
+    const double qxd = (double)(x - hcx), qyd = (double)(y - hcy);
+    const double dpd = (double)dx * qxd + (double)dy * qyd;
+    const double dd = dpd * dpd - ((qxd * qxd + qyd * qyd) - (double)hR * hR);
+    const double sd = sqrt(fmax(dd, 0.0));
+    const float t = (float)(hit_in ? -dpd + sd : -dpd - sd);
+    disc_hit = (float)dd;
+    tbest = ((dd > 0.0) && (t > g.eps) && (t < lxy)) ? t : INFINITY;
+    ++tl.graze;
   }
 
   float nxp, nyp;  // new position in the start cell's frame
@@ -410,30 +432,32 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
 
   if constexpr (WALL != kPermeate) {
     // Fold-first safety clamp (geometries.py:1851-1877): push the walker out of the object it
-    // penetrates most deeply (relative to R^2).  The start cell's list covers every object within
-    // reach of the end point.
-    float pbest = 1.f, qbx = 0.f, qby = 0.f, Rb = 1.f;
+    // penetrates most deeply (relative to R^2).  Without a hit the end point is x + s, already
+    // tested above; after a reflection the start cell's list (which covers every object within
+    // reach of the end point) is scanned again.
+    if (tbest < INFINITY) {
+      pe = 1.f;
 #pragma unroll 1
-    for (uint32_t k = kb; k < ke; ++k) {
-      const float4 C = cand[k];
-      const float qx = nxp - C.x, qy = nyp - C.y;
-      if (!(min_image(qx, g) && min_image(qy, g))) continue;
-      const float d2 = qx * qx + qy * qy, R2 = C.w * C.w;
-      if (d2 < R2) {
-        const float pen = d2 / R2;
-        if (pen < pbest) {
-          pbest = pen;
-          qbx = qx;
-          qby = qy;
-          Rb = C.w;
+      for (uint32_t k = kb; k < ke; ++k) {
+        const float4 C = cand[k];
+        const float qx = nxp - C.x, qy = nyp - C.y;
+        const float d2 = qx * qx + qy * qy, R2 = C.w * C.w;
+        if (d2 < R2 && (!g.mi || (min_image(qx, g) && min_image(qy, g)))) {
+          const float pen = d2 / R2;
+          if (pen < pe) {
+            pe = pen;
+            pqx = qx;
+            pqy = qy;
+            pR = C.w;
+          }
         }
       }
     }
-    if (pbest < 1.f) {
-      const float dcl = sqrtf(qbx * qbx + qby * qby);
-      const float s = (Rb + g.nudge) / fmaxf(dcl, g.nudge);
-      nxp += qbx * (s - 1.f);
-      nyp += qby * (s - 1.f);
+    if (pe < 1.f) {
+      const float dcl = sqrtf(pqx * pqx + pqy * pqy);
+      const float s = (pR + g.nudge) / fmaxf(dcl, g.nudge);
+      nxp += pqx * (s - 1.f);
+      nyp += pqy * (s - 1.f);
       ++tl.clamp;
     }
   }
@@ -462,28 +486,35 @@ __device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, i
 
   float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hcz = 0.f, hR = 1.f;
   bool hit_in = false;
+  const float ex = x + sx, ey = y + sy, ez = z + sz;
+  float pe = 1.f, pqx = 0.f, pqy = 0.f, pqz = 0.f, pR = 1.f;
 #pragma unroll 1
   for (uint32_t k = kb; k < ke; ++k) {
     const float4 C = cand[k];
-    const float qx = x - C.x, qy = y - C.y, qz = z - C.z;
-    if (!(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
     const float R2 = C.w * C.w;
+    if constexpr (WALL != kPermeate) {
+      const float fx = ex - C.x, fy = ey - C.y, fz = ez - C.z;
+      const float d2 = fx * fx + fy * fy + fz * fz;
+      if (d2 < R2 && (!g.mi || (min_image(fx, g) && min_image(fy, g) && min_image(fz, g)))) {
+        const float pen = d2 / R2;
+        if (pen < pe) {
+          pe = pen;
+          pqx = fx;
+          pqy = fy;
+          pqz = fz;
+          pR = C.w;
+        }
+      }
+    }
+    const float qx = x - C.x, qy = y - C.y, qz = z - C.z;
+    if (g.mi && !(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
     const float dp = dx * qx + dy * qy + dz * qz;
     const float q2 = qx * qx + qy * qy + qz * qz;
     float disc = dp * dp - (q2 - R2);
     const bool ins = (WALL == kPermeate) && (q2 < R2);
     if (!ins && dp >= 0.f) continue;
-    float sq = sqrtf(fmaxf(disc, 0.f));
-    float t = ins ? -dp + sq : -dp - sq;
-    if (fabsf(disc) < kGrazeTol * R2 && t > 0.f && t < 1.01f * l) {
-      const double dpd = (double)dx * qx + (double)dy * qy + (double)dz * qz;
-      const double dd = dpd * dpd - (((double)qx * qx + (double)qy * qy + (double)qz * qz) -
-                                     (double)C.w * C.w);
-      const double sd = sqrt(fmax(dd, 0.0));
-      disc = (float)dd;
-      t = (float)(ins ? -dpd + sd : -dpd - sd);
-      ++tl.graze;
-    }
+    const float sq = sqrtf(fmaxf(disc, 0.f));
+    const float t = ins ? -dp + sq : -dp - sq;
     const bool valid = (disc > 0.f) && (t > g.eps) && (t < l) && (l > 0.f);
     if (valid && t < tbest) {
       tbest = t;
@@ -494,6 +525,16 @@ __device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, i
       hR = C.w;
       hit_in = ins;
     }
+  }
+  if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR) {
+    const double qxd = (double)(x - hcx), qyd = (double)(y - hcy), qzd = (double)(z - hcz);
+    const double dpd = (double)dx * qxd + (double)dy * qyd + (double)dz * qzd;
+    const double dd = dpd * dpd - ((qxd * qxd + qyd * qyd + qzd * qzd) - (double)hR * hR);
+    const double sd = sqrt(fmax(dd, 0.0));
+    const float t = (float)(hit_in ? -dpd + sd : -dpd - sd);
+    disc_hit = (float)dd;
+    tbest = ((dd > 0.0) && (t > g.eps) && (t < l)) ? t : INFINITY;
+    ++tl.graze;
   }
 
   float nxp, nyp, nzp;
@@ -573,30 +614,32 @@ __device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, i
   }
 
   if constexpr (WALL != kPermeate) {
-    float pbest = 1.f, qbx = 0.f, qby = 0.f, qbz = 0.f, Rb = 1.f;
+    if (tbest < INFINITY) {  // geometries.py:2520-2535, after a reflection
+      pe = 1.f;
 #pragma unroll 1
-    for (uint32_t k = kb; k < ke; ++k) {
-      const float4 C = cand[k];
-      const float qx = nxp - C.x, qy = nyp - C.y, qz = nzp - C.z;
-      if (!(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
-      const float d2 = qx * qx + qy * qy + qz * qz, R2 = C.w * C.w;
-      if (d2 < R2) {
-        const float pen = d2 / R2;
-        if (pen < pbest) {
-          pbest = pen;
-          qbx = qx;
-          qby = qy;
-          qbz = qz;
-          Rb = C.w;
+      for (uint32_t k = kb; k < ke; ++k) {
+        const float4 C = cand[k];
+        const float qx = nxp - C.x, qy = nyp - C.y, qz = nzp - C.z;
+        const float d2 = qx * qx + qy * qy + qz * qz, R2 = C.w * C.w;
+        if (d2 < R2 &&
+            (!g.mi || (min_image(qx, g) && min_image(qy, g) && min_image(qz, g)))) {
+          const float pen = d2 / R2;
+          if (pen < pe) {
+            pe = pen;
+            pqx = qx;
+            pqy = qy;
+            pqz = qz;
+            pR = C.w;
+          }
         }
       }
     }
-    if (pbest < 1.f) {  // geometries.py:2520-2535
-      const float dcl = sqrtf(qbx * qbx + qby * qby + qbz * qbz);
-      const float s = (Rb + g.nudge) / fmaxf(dcl, g.nudge);
-      nxp += qbx * (s - 1.f);
-      nyp += qby * (s - 1.f);
-      nzp += qbz * (s - 1.f);
+    if (pe < 1.f) {
+      const float dcl = sqrtf(pqx * pqx + pqy * pqy + pqz * pqz);
+      const float s = (pR + g.nudge) / fmaxf(dcl, g.nudge);
+      nxp += pqx * (s - 1.f);
+      nyp += pqy * (s - 1.f);
+      nzp += pqz * (s - 1.f);
       ++tl.clamp;
     }
   }

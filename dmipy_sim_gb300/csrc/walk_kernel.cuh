@@ -9,11 +9,15 @@
 //     broadcast;
 //   * each thread walks its walker for all n_t samples x S sub-steps, drawing from a Philox
 //     stream keyed by (seed, global walker index);
-//   * the phase of MT measurements is accumulated in FP32 registers with Kahan compensation:
-//       phi_m += gamma_dt * g_m(t) . R(t)
-//     where R(t) is the sample's last position (walk-once + replay, trajectories.py:550-552) or the
-//     sum of the S sub-step positions (fused engine: G is constant over the sub-steps of a sample,
-//     physics.py:293-317, so sum_s g.r_s = g . sum_s r_s);
+//   * the phase is accumulated in FP32 registers with Kahan compensation, from R(t), the sample's
+//     last position (walk-once + replay, trajectories.py:550-552) or the sum of its S sub-step
+//     positions (fused engine: G is constant over the sub-steps of a sample, physics.py:293-317,
+//     so sum_s g.r_s = g . sum_s r_s), in one of two forms:
+//       direct (PM = 0): phi_m += gamma_dt * g_m(t) . R(t) for MT measurements per pass;
+//       basis  (PM = 1): when the measurement set is built from RT waveform shapes,
+//         G[t, m, k] = sum_j C[m, k, j] V[t, j], the kernel accumulates only
+//         Q[j, k] += gamma_dt * V[t, j] R_k(t) (3 RT registers, 3 RT FMAs per sample) and forms
+//         phi_m = sum_jk C[m, k, j] Q[j, k] at the echo samples;
 //   * at every echo sample the block reduces w*cos(phi), w*sin(phi) and (w*cos(phi))^2 with warp
 //     shuffles and adds them, in FP64 and in a fixed order, into the block's own partial slice.
 // Blocks loop over walker tiles (grid = SMs x resident blocks), so the partial buffer is
@@ -29,7 +33,7 @@
 
 namespace dmsim {
 
-constexpr int kBlock = 128;  // walkers per tile
+constexpr int kBlock = 320;  // walkers per tile (10 warps share one staged cell list)
 constexpr int kWarps = kBlock / 32;
 constexpr int kTC = 16;  // samples per staged waveform chunk
 constexpr int kMaxEcho = 512;
@@ -41,10 +45,13 @@ struct KArgs {
   float step_l, gamma_dt, t2dec, t1dec, rho;
   GeoK g;
   uint32_t tab_cs_bytes, tab_cand_bytes;  // shared-memory staging sizes (multiples of 16 B)
+  uint32_t off_cs, off_red, off_tab;      // shared-memory offsets of C, the reduction scratch
+                                          // and the cell list (host-computed layout)
+  const float* Cp;                        // basis mode: (M, 3, RT) coefficients
   const uint32_t* cs;
   const float4* cand;
   const int32_t* cand_obj;
-  const float* Gp;          // this pass, (n_chunks*kTC, MT, 3)
+  const float* Gp;          // this pass: direct (n_chunks*kTC, MT, 3); basis (n_chunks*kTC, RT)
   const uint8_t* active;    // this pass, (n_t): 1 where some g_m(t) != 0
   const float* chi;         // (n_t) or null
   const float* r0;          // (n_walkers, 3) or null
@@ -107,10 +114,23 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-template <int MT>
-__host__ __device__ constexpr size_t walk_smem_fixed() {
-  // two waveform chunk buffers + 3 mbarriers/flags (64 B) + warp reduction scratch
-  return (size_t)2 * kTC * MT * 3 * 4 + 64 + (size_t)kWarps * MT * 3 * 4;
+// Floats per sample of the staged waveform: 3 per measurement (direct) or 1 per shape (basis).
+__host__ __device__ constexpr int walk_row(int pm, int w) { return pm ? w : 3 * w; }
+
+__host__ __device__ inline size_t pad16z(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// Shared-memory layout: [waveform chunk ring (2 x kTC x row)] [3 mbarriers + abort flag, 64 B]
+// [basis coefficients C (M x 3 x RT)] [warp reduction scratch (warps x M_red x 3)] [cell list].
+struct SmemLayout {
+  size_t off_bar, off_cs, off_red, off_tab;
+};
+__host__ __device__ inline SmemLayout walk_smem_layout(int pm, int w, int M) {
+  SmemLayout L;
+  L.off_bar = (size_t)2 * kTC * walk_row(pm, w) * 4;
+  L.off_cs = L.off_bar + 64;
+  L.off_red = L.off_cs + (pm ? pad16z((size_t)M * 3 * w * 4) : 0);
+  L.off_tab = L.off_red + pad16z((size_t)kWarps * (pm ? M : w) * 3 * 4);
+  return L;
 }
 
 template <int GEOM>
@@ -139,15 +159,20 @@ __device__ __forceinline__ int classify(float x, float y, float z, const GeoK& g
   }
 }
 
-template <int GEOM, int WALL, int MT, bool TSM>
+template <int GEOM, int WALL, int PM, int W, bool TSM>
 __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a) {
   extern __shared__ __align__(128) uint8_t smem[];
-  constexpr int GCH = kTC * MT * 3;  // floats per waveform chunk
+  constexpr int ROW = walk_row(PM, W);
+  constexpr int GCH = kTC * ROW;  // floats per waveform chunk
+  constexpr int MT = PM ? 1 : W;  // measurements held per thread in the direct form
   float* Gs = reinterpret_cast<float*>(smem);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + (size_t)2 * GCH * 4);
-  volatile int* s_abort = reinterpret_cast<volatile int*>(smem + (size_t)2 * GCH * 4 + 32);
-  float* red = reinterpret_cast<float*>(smem + (size_t)2 * GCH * 4 + 64);
-  uint8_t* tab = smem + walk_smem_fixed<MT>();
+  const SmemLayout lay = walk_smem_layout(PM, W, a.M);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.off_bar);
+  volatile int* s_abort = reinterpret_cast<volatile int*>(smem + lay.off_bar + 32);
+  float* Cs = reinterpret_cast<float*>(smem + lay.off_cs);
+  float* red = reinterpret_cast<float*>(smem + lay.off_red);
+  uint8_t* tab = smem + lay.off_tab;
+  const int MR = PM ? a.M : W;  // measurements reduced per emission by this launch
 
   constexpr bool PACKED = GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
@@ -173,16 +198,18 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     *s_abort = 0;
     fence_async_smem();
   }
-  // zero this block's partial slice for this pass
+  // zero this block's partial slice for this pass; stage the basis coefficients
   for (int e = 0; e < a.n_echo; ++e)
-    for (int j = tid; j < MT * 3; j += kBlock)
+    for (int j = tid; j < MR * 3; j += kBlock)
       a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] = 0.0;
+  if constexpr (PM == 1)
+    for (int j = tid; j < a.M * 3 * W; j += kBlock) Cs[j] = a.Cp[j];
   __syncthreads();
   if (tid == 0) {
     if constexpr (PACKED && TSM) {
       mbar_expect(&bar[2], a.tab_cs_bytes + a.tab_cand_bytes);
       bulk_g2s(tab, a.cs, a.tab_cs_bytes, &bar[2]);
-      bulk_g2s(tab + a.tab_cs_bytes, a.cand, a.tab_cand_bytes, &bar[2]);
+      if (a.tab_cand_bytes) bulk_g2s(tab + a.tab_cs_bytes, a.cand, a.tab_cand_bytes, &bar[2]);
     }
     if (total_chunks > 0) {
       mbar_expect(&bar[0], chunk_bytes);
@@ -281,9 +308,11 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     if (act && a.comp0 != nullptr && a.pass == 0)
       a.comp0[w] = classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
 
-    float phi[MT], kc[MT];
+    // phase accumulators: direct form phi[m] (+ Kahan), basis form Q[j][k] (+ Kahan)
+    constexpr int NACC = PM ? 3 * W : W;
+    float acc[NACC], kc[NACC];
 #pragma unroll
-    for (int m = 0; m < MT; ++m) phi[m] = kc[m] = 0.f;
+    for (int i = 0; i < NACC; ++i) acc[i] = kc[i] = 0.f;
     float logw = 0.f;
     uint32_t s = 0;   // global sub-step counter of this walker
     u32x4 rr{0, 0, 0, 0};
@@ -374,25 +403,44 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
           Ry = uy;
           Rz = uz;
         }
-        // ---- phase: phi_m += gamma_dt * g_m(t) . R(t), Kahan-compensated --------------------
+        // ---- phase, Kahan-compensated ------------------------------------------------------
         if (__ldg(a.active + t)) {
           const float px = a.gamma_dt * Rx, py = a.gamma_dt * Ry, pz = a.gamma_dt * Rz;
-          const float4* g4 = reinterpret_cast<const float4*>(Gc + (t - ch * kTC) * MT * 3);
-          float acc = 0.f;
+          const float* gt = Gc + (t - ch * kTC) * ROW;
+          if constexpr (PM == 0) {
+            // direct: phi_m += g_m(t) . R
+            const float4* g4 = reinterpret_cast<const float4*>(gt);
+            float d = 0.f;
 #pragma unroll
-          for (int j = 0; j < MT * 3 / 4; ++j) {
-            const float4 v = g4[j];
-            const float gv[4] = {v.x, v.y, v.z, v.w};
+            for (int j = 0; j < W * 3 / 4; ++j) {
+              const float4 v = g4[j];
+              const float gv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-              const int el = 4 * j + h, m = el / 3, k = el % 3;
-              const float pk = k == 0 ? px : (k == 1 ? py : pz);
-              acc = (k == 0) ? gv[h] * pk : fmaf(gv[h], pk, acc);
-              if (k == 2) {
-                const float yk = acc - kc[m];
-                const float tk = phi[m] + yk;
-                kc[m] = (tk - phi[m]) - yk;
-                phi[m] = tk;
+              for (int h = 0; h < 4; ++h) {
+                const int el = 4 * j + h, m = el / 3, k = el % 3;
+                const float pk = k == 0 ? px : (k == 1 ? py : pz);
+                d = (k == 0) ? gv[h] * pk : fmaf(gv[h], pk, d);
+                if (k == 2) {
+                  const float yk = d - kc[m];
+                  const float tk = acc[m] + yk;
+                  kc[m] = (tk - acc[m]) - yk;
+                  acc[m] = tk;
+                }
+              }
+            }
+          } else {
+            // basis: Q[j][k] += V_j(t) * R_k
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+              const float v = gt[j];
+              const float pv[3] = {v * px, v * py, v * pz};
+#pragma unroll
+              for (int k = 0; k < 3; ++k) {
+                const int i = 3 * j + k;
+                const float yk = pv[k] - kc[i];
+                const float tk = acc[i] + yk;
+                kc[i] = (tk - acc[i]) - yk;
+                acc[i] = tk;
               }
             }
           }
@@ -419,25 +467,39 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
         // ---- ensemble sums at an echo sample (block-uniform branch) --------------------------
         if (e < a.n_echo && t == a.echo[e]) {
           const float wgt = act ? (a.has_weight ? expf(logw) : 1.f) : 0.f;
-#pragma unroll
-          for (int m = 0; m < MT; ++m) {
+          auto emit = [&](int m, float ph) {
             float sn, cs_;
-            sincosf(phi[m], &sn, &cs_);
+            sincosf(ph, &sn, &cs_);
             const float c1 = warp_sum(wgt * cs_);
             const float c2 = warp_sum(wgt * sn);
             const float c3 = warp_sum((wgt * cs_) * (wgt * cs_));
             if (lane == 0) {
-              red[warp * MT * 3 + 3 * m] = c1;
-              red[warp * MT * 3 + 3 * m + 1] = c2;
-              red[warp * MT * 3 + 3 * m + 2] = c3;
+              red[(warp * MR + m) * 3] = c1;
+              red[(warp * MR + m) * 3 + 1] = c2;
+              red[(warp * MR + m) * 3 + 2] = c3;
+            }
+          };
+          if constexpr (PM == 0) {
+#pragma unroll
+            for (int m = 0; m < W; ++m) emit(m, acc[m]);
+          } else {
+#pragma unroll 1
+            for (int m = 0; m < MR; ++m) {
+              const float* c = Cs + (size_t)m * 3 * W;
+              float ph = 0.f;
+#pragma unroll
+              for (int j = 0; j < W; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) ph = fmaf(c[k * W + j], acc[3 * j + k], ph);
+              emit(m, ph);
             }
           }
           __syncthreads();
-          for (int j = tid; j < MT * 3; j += kBlock) {
-            double acc = 0.0;
+          for (int j = tid; j < MR * 3; j += kBlock) {
+            double sacc = 0.0;
 #pragma unroll
-            for (int ww = 0; ww < kWarps; ++ww) acc += (double)red[ww * MT * 3 + j];
-            a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] += acc;
+            for (int ww = 0; ww < kWarps; ++ww) sacc += (double)red[ww * MR * 3 + j];
+            a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] += sacc;
           }
           __syncthreads();
           ++e;
@@ -459,9 +521,21 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
         if (a.comp_end) a.comp_end[w] = classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
       }
       if (a.phi_out) {
+        if constexpr (PM == 0) {
 #pragma unroll
-        for (int m = 0; m < MT; ++m)
-          if (a.pass * MT + m < a.M) a.phi_out[(size_t)w * a.M + a.pass * MT + m] = phi[m];
+          for (int m = 0; m < W; ++m)
+            if (a.pass * W + m < a.M) a.phi_out[(size_t)w * a.M + a.pass * W + m] = acc[m];
+        } else {
+          for (int m = 0; m < a.M; ++m) {
+            const float* c = Cs + (size_t)m * 3 * W;
+            float ph = 0.f;
+#pragma unroll
+            for (int j = 0; j < W; ++j)
+#pragma unroll
+              for (int k = 0; k < 3; ++k) ph = fmaf(c[k * W + j], acc[3 * j + k], ph);
+            a.phi_out[(size_t)w * a.M + m] = ph;
+          }
+        }
       }
     }
   }

@@ -295,7 +295,7 @@ def _min_gap(centers, radii, L):
     return min(gap, float(np.min(L - 2.0 * radii)))
 
 
-def build_cell_list(centers, radii, L, reach, max_bytes=64 * 1024, min_cell=None):
+def build_cell_list(centers, radii, L, reach, max_bytes=96 * 1024, min_cell=None):
     """Uniform cell list over the periodic cell [-L/2, L/2)^d.
 
     Cell c lists every periodic image (within one box) of every object whose disc/ball of radius
@@ -398,8 +398,13 @@ class _Packed(Geometry):
             t_start = torch.from_numpy(start.view(np.int32)).to(dev)
             t_cand = torch.from_numpy(cand).to(dev)
             t_obj = torch.from_numpy(obj if len(obj) else np.zeros(1, np.int32)).to(dev)
-            self._dev_cache = {key: (n, reach, t_start, t_cand, t_obj, len(obj))}
-        n, reach, t_start, t_cand, t_obj, n_cand = self._dev_cache[key]
+            # lists are sorted by cell then object: a repeated (cell, object) pair means two
+            # images of one object share a cell, and only then must candidates be min-image tested
+            n_cells = n ** self._dim
+            cell_of = np.repeat(np.arange(n_cells), np.diff(start[:n_cells + 1].astype(np.int64)))
+            need_mi = bool(np.any((cell_of[1:] == cell_of[:-1]) & (obj[1:] == obj[:-1])))
+            self._dev_cache = {key: (n, reach, t_start, t_cand, t_obj, len(obj), need_mi)}
+        n, reach, t_start, t_cand, t_obj, n_cand, need_mi = self._dev_cache[key]
         g = self._base_desc(self._kind, wall_mode, rho_over_D, kappa_over_D)
         g.radius = float(np.min(self._radii_np))
         g.eps_detect = self._eps_detect
@@ -410,6 +415,7 @@ class _Packed(Geometry):
         g.cell_h = self._L_float / n
         g.reach = reach
         g.n_cand = n_cand
+        g.need_min_image = 1 if need_mi else 0
         g.cell_start = t_start.data_ptr()
         g.cand = t_cand.data_ptr()
         g.cand_obj = t_obj.data_ptr()

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 1
+#define DMSIM_ABI_VERSION 2
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -89,7 +89,8 @@ typedef struct dmsim_geometry {
   float cell_h;   /* L / grid_n */
   float reach;    /* maximum step length + margin the lists were built for */
   int32_t n_cand;
-  int32_t pad0;
+  int32_t need_min_image; /* 1 if a cell lists two images of one object (then each candidate is
+                             checked to be its object's minimum image from the walker) */
   const uint32_t* cell_start; /* grid_n^d + 1 */
   const float* cand;          /* n_cand x 4 */
   const int32_t* cand_obj;    /* n_cand: object index of each candidate (classification) */
@@ -138,6 +139,13 @@ typedef struct dmsim_walk_params {
   const float* G;            /* (n_t, n_meas, 3) float, geometry frame, T/m                     */
   const float* chi;          /* (n_t) transverse mask or NULL (all ones)                        */
   const float* r0;           /* (n_walkers, 3) geometry-frame start positions or NULL           */
+  /* Shape basis of the waveform set (optional).  When basis_rank r > 0 (r <= 8, n_meas <= 512)
+     the measurements are built from r time shapes, G[t, m, k] = sum_j C[m, k, j] V[t, j], and the
+     walk accumulates 3 r phase moments instead of n_meas phases; G is then ignored. */
+  int32_t basis_rank;
+  int32_t pad1;
+  const float* basis_V;      /* (n_t, basis_rank)                                               */
+  const float* basis_C;      /* (n_meas, 3, basis_rank)                                         */
 } dmsim_walk_params;
 
 /* ---- outputs ---------------------------------------------------------------------------------- */
