@@ -13,6 +13,7 @@ from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, Wal
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
                    fused_sub_steps)
 from .trajectories import replay
+from .mesh import Mesh, load_ply, icosphere, random_ellipsoid_cells, mesh_contains
 
 __all__ = [
     "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
@@ -20,5 +21,5 @@ __all__ = [
     "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
     "simulate", "simulate_cpmg", "simulate_trajectories", "replay", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
-    "fused_sub_steps",
+    "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
 ]

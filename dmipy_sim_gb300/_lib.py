@@ -41,7 +41,8 @@ class Geometry(C.Structure):
         ("vmin", C.c_float * 3), ("box", C.c_float * 3), ("mesh_eps", C.c_float),
         ("mesh_nudge", C.c_float), ("mesh_graze", C.c_float), ("rho_mult_intra", C.c_float),
         ("rho_mult_extra", C.c_float), ("kappa_mult_out", C.c_float),
-        ("kappa_mult_in", C.c_float), ("reject_escape", C.c_int32),
+        ("kappa_mult_in", C.c_float), ("reject_escape", C.c_int32), ("seed_parity", C.c_int32),
+        ("seed_inside", C.c_int32), ("pad1", C.c_int32),
         ("tri", C.c_void_p), ("tri_vn", C.c_void_p), ("mesh_cell_start", C.c_void_p),
         ("mesh_cell_tri", C.c_void_p),
     ]

@@ -15,6 +15,7 @@ WalkFn walk_fn_cyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_sph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_pcyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_psph(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_mesh(int wall, int pm, int width, bool tsm);
 }  // namespace dmsim
 
 using namespace dmsim;
@@ -76,8 +77,18 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
       return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
   }
   const bool packed = g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  if (g->kind < 0 || g->kind > DMSIM_GEOM_PACKED_SPHERES)
+  if (g->kind < 0 || g->kind > DMSIM_GEOM_MESH)
     return fail(DMSIM_EINVAL, "unsupported geometry kind %d", g->kind);
+  if (g->kind == DMSIM_GEOM_MESH) {
+    if (!g->tri || !g->tri_vn || !g->mesh_cell_start || !g->mesh_cell_tri)
+      return fail(DMSIM_EINVAL, "mesh geometry needs its triangle and grid tables");
+    if (g->mesh_dims[0] < 1 || g->mesh_dims[1] < 1 || g->mesh_dims[2] < 1 ||
+        !(g->mesh_cell > 0.f) || g->max_bounces < 1 || g->max_bounces > 64)
+      return fail(DMSIM_EINVAL, "bad mesh grid or bounce budget");
+    for (int a = 0; a < 3; ++a)
+      if (g->periodic[a] && !(g->box[a] > 0.f))
+        return fail(DMSIM_EINVAL, "periodic mesh axis with an empty box");
+  }
   if (g->wall_mode < 0 || g->wall_mode > 2) return fail(DMSIM_EINVAL, "bad wall_mode");
   if (g->kind == DMSIM_GEOM_FREE && g->wall_mode != DMSIM_WALL_REFLECT)
     return fail(DMSIM_EINVAL, "free diffusion has no walls");
@@ -126,6 +137,7 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
     case DMSIM_GEOM_PACKED_SPHERES:
       pl->fn = walk_fn_psph(g->wall_mode, pl->pm, pl->width, pl->tsm);
       break;
+    case DMSIM_GEOM_MESH: pl->fn = walk_fn_mesh(g->wall_mode, pl->pm, pl->width, false); break;
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
   pl->lay = walk_smem_layout(pl->pm, pl->width, p->n_meas);
@@ -316,7 +328,7 @@ __global__ void k_zero(double* p, size_t n) {
 
 // ---- known-answer kernel: one sub-step of the device step functions per input triple ---------
 template <int GEOM, int WALL>
-__global__ void k_step_kat(const GeoK g, int64_t n, const float* __restrict__ rin,
+__global__ void k_step_kat(const GeoK g, const MeshK mk, int64_t n, const float* __restrict__ rin,
                            const float* __restrict__ st, const float* __restrict__ uin,
                            const uint32_t* __restrict__ cs, const float4* __restrict__ cand,
                            float* __restrict__ rout, float* __restrict__ dlog) {
@@ -348,18 +360,29 @@ __global__ void k_step_kat(const GeoK g, int64_t n, const float* __restrict__ ri
     } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS) {
       dl = packed_cyl_step<WALL>(x, y, ix, iy, sx, sy, u, g, cs, cand, tl);
       z += sz;
-    } else {
+    } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
       dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, sx, sy, sz, u, g, cs, cand, tl);
+    } else {
+      if (mk.per[0]) { ix = (int)floorf((x - mk.vmin[0]) / mk.box[0]); x -= mk.box[0] * ix; }
+      if (mk.per[1]) { iy = (int)floorf((y - mk.vmin[1]) / mk.box[1]); y -= mk.box[1] * iy; }
+      if (mk.per[2]) { iz = (int)floorf((z - mk.vmin[2]) / mk.box[2]); z -= mk.box[2] * iz; }
+      int cls = 1, pop = 0;
+      if (mk.reject && WALL != kPermeate) cls = mesh_classify(mk, x, y, z, pop);
+      uint32_t nb = 0, ne = 0;
+      dl = mesh_step<WALL>(x, y, z, ix, iy, iz, cls, pop, sx, sy, sz, u, mk, tl, nb, ne);
     }
-    rout[3 * i] = x + g.L * (float)ix;
-    rout[3 * i + 1] = y + g.L * (float)iy;
-    rout[3 * i + 2] = z + g.L * (float)iz;
+    const float Lx = GEOM == DMSIM_GEOM_MESH ? mk.box[0] : g.L;
+    const float Ly = GEOM == DMSIM_GEOM_MESH ? mk.box[1] : g.L;
+    const float Lz = GEOM == DMSIM_GEOM_MESH ? mk.box[2] : g.L;
+    rout[3 * i] = x + Lx * (float)ix;
+    rout[3 * i + 1] = y + Ly * (float)iy;
+    rout[3 * i + 2] = z + Lz * (float)iz;
     dlog[i] = dl;
   }
 }
 
-using KatFn = void (*)(GeoK, int64_t, const float*, const float*, const float*, const uint32_t*,
-                       const float4*, float*, float*);
+using KatFn = void (*)(GeoK, MeshK, int64_t, const float*, const float*, const float*,
+                       const uint32_t*, const float4*, float*, float*);
 
 template <int GEOM>
 KatFn kat_fn(int wall) {
@@ -370,6 +393,37 @@ KatFn kat_fn(int wall) {
     if (wall == 1) return k_step_kat<GEOM, 1>;
     return k_step_kat<GEOM, 2>;
   }
+}
+
+MeshK make_meshk(const dmsim_geometry* g) {
+  MeshK m;
+  memset(&m, 0, sizeof(m));
+  if (g->kind != DMSIM_GEOM_MESH) return m;
+  for (int a = 0; a < 3; ++a) {
+    m.gmin[a] = g->grid_min[a];
+    m.dims[a] = g->mesh_dims[a];
+    m.per[a] = g->periodic[a] ? 1 : 0;
+    m.vmin[a] = g->vmin[a];
+    m.box[a] = g->box[a];
+  }
+  m.cs = g->mesh_cell;
+  m.eps = g->mesh_eps;
+  m.nudge = g->mesh_nudge;
+  m.graze = g->mesh_graze;
+  m.maxb = g->max_bounces;
+  m.rmi = g->rho_mult_intra;
+  m.rme = g->rho_mult_extra;
+  m.kmo = g->kappa_mult_out;
+  m.kmi = g->kappa_mult_in;
+  m.kod = g->kappa_over_D;
+  m.reject = g->reject_escape ? 1 : 0;
+  m.seed_parity = g->seed_parity ? 1 : 0;
+  m.seed_inside = g->seed_inside ? 1 : 0;
+  m.tri = reinterpret_cast<const float4*>(g->tri);
+  m.vn = reinterpret_cast<const float4*>(g->tri_vn);
+  m.cstart = g->mesh_cell_start;
+  m.ctri = g->mesh_cell_tri;
+  return m;
 }
 
 GeoK make_geok(const dmsim_geometry* g) {
@@ -473,6 +527,7 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
   const bool packed =
       g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
   a.g = make_geok(g);
+  a.mk = make_meshk(g);
   a.tab_cs_bytes = (uint32_t)pl.tab_cs;
   a.tab_cand_bytes = (uint32_t)pl.tab_cand;
   a.cs = g->cell_start;
@@ -520,6 +575,9 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
       g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
   if (packed && (!g->cell_start || !g->cand || g->grid_n < 1))
     return fail(DMSIM_EINVAL, "step_kat: packed geometry needs a cell list");
+  if (g->kind == DMSIM_GEOM_MESH && (!g->tri || !g->tri_vn || !g->mesh_cell_start ||
+                                     !g->mesh_cell_tri || g->max_bounces < 1))
+    return fail(DMSIM_EINVAL, "step_kat: mesh geometry needs its tables");
   KatFn fn = nullptr;
   switch (g->kind) {
     case DMSIM_GEOM_FREE: fn = kat_fn<DMSIM_GEOM_FREE>(g->wall_mode); break;
@@ -527,11 +585,13 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
     case DMSIM_GEOM_SPHERE: fn = kat_fn<DMSIM_GEOM_SPHERE>(g->wall_mode); break;
     case DMSIM_GEOM_PACKED_CYLINDERS: fn = kat_fn<DMSIM_GEOM_PACKED_CYLINDERS>(g->wall_mode); break;
     case DMSIM_GEOM_PACKED_SPHERES: fn = kat_fn<DMSIM_GEOM_PACKED_SPHERES>(g->wall_mode); break;
+    case DMSIM_GEOM_MESH: fn = kat_fn<DMSIM_GEOM_MESH>(g->wall_mode); break;
     default: return fail(DMSIM_EINVAL, "step_kat: unsupported geometry kind %d", g->kind);
   }
   if (n == 0) return DMSIM_OK;
   const int blocks = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
-  fn<<<blocks, 256, 0, (cudaStream_t)stream>>>(make_geok(g), n, r_in, steps, u, g->cell_start,
+  fn<<<blocks, 256, 0, (cudaStream_t)stream>>>(make_geok(g), make_meshk(g), n, r_in, steps, u,
+                                                 g->cell_start,
                                                  reinterpret_cast<const float4*>(g->cand), r_out,
                                                  dlog_unit);
   cudaError_t err = cudaGetLastError();

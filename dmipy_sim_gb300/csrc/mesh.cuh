@@ -1,0 +1,323 @@
+// Device step function of the triangle-mesh substrate.
+//
+// Follows dmipy-sim's mesh.py statement by statement:
+//   27-cell candidate gather around the step's start (mesh.py:208-215), gathered once per step
+//   and reused for every bounce; Moller-Trumbore segment test (561-569); smooth-normal reflection
+//   lifted above the geometric plane by the graze margin, nudge along the geometric normal
+//   (607-635); at most max_bounces bounces, and when the budget runs out with a hit the leftover
+//   path is not flown (662-668); reflect (637-671), reflect_with_log_weight (673-705) with the
+//   side-dependent relaxivity multiplier; permeate (707-743) with one Powles decision at the first
+//   hit and direction-dependent permeability; nearest-centroid classification (227-254) and the
+//   leak guard that rejects a step whose decidable start and end classify differently (578-597).
+// Periodic axes keep the position folded into the box plus an integer image count (the
+// reference wraps an unfolded position each step, mesh.py:200-206).  The class and gather
+// population of the current position are carried from the previous step instead of recomputed.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#include "geometry.cuh"
+
+namespace dmsim {
+
+struct MeshK {
+  float gmin[3];
+  float cs;          // grid cell size
+  int dims[3];
+  int per[3];
+  float vmin[3], box[3];
+  float eps, nudge, graze;
+  int maxb;
+  float rmi, rme, kmo, kmi;  // side multipliers of rho (intra/extra) and kappa (out/in)
+  float kod;
+  int reject;
+  int seed_parity, seed_inside;
+  const float4* tri;  // 4 x float4 per triangle: A, E1, E2, geometric normal, centroid, 1=original
+  const float4* vn;   // 3 x float4 per triangle: smooth normals at the three vertices
+  const uint32_t* cstart;
+  const uint32_t* ctri;
+};
+
+struct Tri {
+  float ax, ay, az, e1x, e1y, e1z, e2x, e2y, e2z, nx, ny, nz;
+};
+
+__device__ __forceinline__ Tri load_tri(const MeshK& m, uint32_t k) {
+  const float4 a = m.tri[4 * k], b = m.tri[4 * k + 1], c = m.tri[4 * k + 2];
+  return Tri{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+}
+
+__device__ __forceinline__ int mesh_cell(float p, int a, const MeshK& m) {
+  const int c = (int)floorf((p - m.gmin[a]) / m.cs);
+  return min(max(c, 0), m.dims[a] - 1);
+}
+
+// Visit every candidate of the 27-cell gather around p in the reference's order.
+template <typename Fn>
+__device__ __forceinline__ void mesh_gather(const MeshK& m, float px, float py, float pz, Fn&& fn) {
+  const int cx = mesh_cell(px, 0, m), cy = mesh_cell(py, 1, m), cz = mesh_cell(pz, 2, m);
+#pragma unroll 1
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int nx = min(max(cx + dx, 0), m.dims[0] - 1);
+#pragma unroll 1
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int ny = min(max(cy + dy, 0), m.dims[1] - 1);
+#pragma unroll 1
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int nz = min(max(cz + dz, 0), m.dims[2] - 1);
+        const int cid = (nx * m.dims[1] + ny) * m.dims[2] + nz;
+        const uint32_t e = m.cstart[cid + 1];
+#pragma unroll 1
+        for (uint32_t k = m.cstart[cid]; k < e; ++k) fn(m.ctri[k]);
+      }
+    }
+  }
+}
+
+// Moller-Trumbore: ray r0 + t d against the triangle; returns t (INFINITY when the barycentric
+// test fails) and the barycentric u, v.
+__device__ __forceinline__ float mt_hit(const Tri& T, float r0x, float r0y, float r0z, float dx,
+                                        float dy, float dz, float& u, float& v) {
+  const float px = dy * T.e2z - dz * T.e2y, py = dz * T.e2x - dx * T.e2z,
+              pz = dx * T.e2y - dy * T.e2x;
+  const float det = px * T.e1x + py * T.e1y + pz * T.e1z;
+  const float tx = r0x - T.ax, ty = r0y - T.ay, tz = r0z - T.az;
+  const float qx = ty * T.e1z - tz * T.e1y, qy = tz * T.e1x - tx * T.e1z,
+              qz = tx * T.e1y - ty * T.e1x;
+  const float t = (qx * T.e2x + qy * T.e2y + qz * T.e2z) / det;
+  u = (px * tx + py * ty + pz * tz) / det;
+  v = (qx * dx + qy * dy + qz * dz) / det;
+  const bool ok = (u >= 0.f) && (u <= 1.f) && (v >= 0.f) && (u + v <= 1.f);
+  return ok ? t : INFINITY;
+}
+
+// Outgoing direction for a hit (mesh.py:599-635): reflect off the interpolated normal, then lift
+// the ray above the triangle's own plane by the graze margin.  Also returns the oriented smooth
+// normal n (for the relaxivity path length) and the oriented geometric normal nf (for the nudge).
+__device__ __forceinline__ void mesh_bounce(const MeshK& m, uint32_t k, const Tri& T, float u,
+                                            float v, float& dx, float& dy, float& dz, float& nx,
+                                            float& ny, float& nz, float& fx, float& fy,
+                                            float& fz) {
+  const float4 a = m.vn[3 * k], b = m.vn[3 * k + 1], c = m.vn[3 * k + 2];
+  const float w = 1.f - u - v;
+  float sx = w * a.x + u * a.w + v * b.z;
+  float sy = w * a.y + u * b.x + v * b.w;
+  float sz = w * a.z + u * b.y + v * c.x;
+  const float sl = sqrtf(sx * sx + sy * sy + sz * sz);
+  sx /= sl;
+  sy /= sl;
+  sz /= sl;
+  const bool flip = (dx * T.nx + dy * T.ny + dz * T.nz) > 0.f;
+  nx = flip ? -sx : sx;
+  ny = flip ? -sy : sy;
+  nz = flip ? -sz : sz;
+  fx = flip ? -T.nx : T.nx;
+  fy = flip ? -T.ny : T.ny;
+  fz = flip ? -T.nz : T.nz;
+  const float dn = dx * nx + dy * ny + dz * nz;
+  float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny, rz = dz - 2.f * dn * nz;
+  float rl = sqrtf(rx * rx + ry * ry + rz * rz);
+  rx /= rl;
+  ry /= rl;
+  rz /= rl;
+  const float cf = rx * fx + ry * fy + rz * fz;
+  if (cf < m.graze) {
+    rx += (m.graze - cf) * fx;
+    ry += (m.graze - cf) * fy;
+    rz += (m.graze - cf) * fz;
+    rl = sqrtf(rx * rx + ry * ry + rz * rz);
+    rx /= rl;
+    ry /= rl;
+    rz /= rl;
+  }
+  dx = rx;
+  dy = ry;
+  dz = rz;
+}
+
+// Nearest hit of the gathered candidates (first index on ties, like argmin).
+struct MeshHit {
+  float t, u, v;
+  uint32_t k;
+};
+
+__device__ __forceinline__ MeshHit mesh_nearest(const MeshK& m, float gx, float gy, float gz,
+                                                float r0x, float r0y, float r0z, float dx,
+                                                float dy, float dz, float rem) {
+  MeshHit h{INFINITY, 0.f, 0.f, 0u};
+  mesh_gather(m, gx, gy, gz, [&](uint32_t k) {
+    const Tri T = load_tri(m, k);
+    float u, v;
+    const float t = mt_hit(T, r0x, r0y, r0z, dx, dy, dz, u, v);
+    if (t > m.eps && t < rem && t < h.t) {
+      h.t = t;
+      h.u = u;
+      h.v = v;
+      h.k = k;
+    }
+  });
+  return h;
+}
+
+// Class of a point (0 interior, 1 exterior) and whether its gather holds any triangle.
+__device__ __forceinline__ int mesh_classify(const MeshK& m, float px, float py, float pz,
+                                             int& populated) {
+  float best = INFINITY;
+  uint32_t kb = 0;
+  int any = 0;
+  mesh_gather(m, px, py, pz, [&](uint32_t k) {
+    const float4 c = m.tri[4 * k + 3];
+    const float ddx = px - c.x, ddy = py - c.y, ddz = pz - c.z;
+    const float d = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
+    any = 1;
+    if (d < best) {
+      best = d;
+      kb = k;
+    }
+  });
+  populated = any;
+  if (!any) return 1;
+  const float4 c = m.tri[4 * kb + 3];
+  const float4 nn = m.tri[4 * kb + 2];
+  const float side = (px - c.x) * nn.y + (py - c.y) * nn.z + (pz - c.z) * nn.w;
+  return side < 0.f ? 0 : 1;
+}
+
+// Inside-ness by the parity of crossings of a ray along +x through the grid row of p (original
+// triangles only; each crossing counted in the cell that holds its hit point).
+__device__ __forceinline__ int mesh_parity(const MeshK& m, float px, float py, float pz) {
+  const int cy = mesh_cell(py, 1, m), cz = mesh_cell(pz, 2, m);
+  int parity = 0;
+#pragma unroll 1
+  for (int cx = mesh_cell(px, 0, m); cx < m.dims[0]; ++cx) {
+    const int cid = (cx * m.dims[1] + cy) * m.dims[2] + cz;
+    const uint32_t e = m.cstart[cid + 1];
+#pragma unroll 1
+    for (uint32_t i = m.cstart[cid]; i < e; ++i) {
+      const uint32_t k = m.ctri[i];
+      if (m.tri[4 * k + 3].w == 0.f) continue;  // periodic ghost
+      const Tri T = load_tri(m, k);
+      float u, v;
+      const float t = mt_hit(T, px, py, pz, 1.f, 0.f, 0.f, u, v);
+      if (t > 0.f && t < INFINITY && mesh_cell(px + t, 0, m) == cx) parity ^= 1;
+    }
+  }
+  return parity;
+}
+
+__device__ __forceinline__ void mesh_fold(float& v, int& img, int a, const MeshK& m) {
+  if (!m.per[a]) return;
+  const float hi = m.vmin[a] + m.box[a];
+  if (v >= hi) {
+    v -= m.box[a];
+    ++img;
+  } else if (v < m.vmin[a]) {
+    v += m.box[a];
+    --img;
+  }
+}
+
+// One sub-step.  (x, y, z) is the folded position; cls / pop carry the class and gather
+// population of the current position (the leak guard's start state).  Returns -2 * sum d_perp
+// including the side multipliers (rho/D = 1).
+template <int WALL>
+__device__ __forceinline__ float mesh_step(float& x, float& y, float& z, int& ix, int& iy,
+                                           int& iz, int& cls, int& pop, float sx, float sy,
+                                           float sz, float u_rand, const MeshK& m, Tally& tl,
+                                           uint32_t& n_budget, uint32_t& n_escape) {
+  const float l = sqrtf(sx * sx + sy * sy + sz * sz);
+  float dx = sx / l, dy = sy / l, dz = sz / l;
+  float r0x = x, r0y = y, r0z = z, rem = l;
+  float dsum = 0.f;
+  bool last_reflect = false;
+  bool decided = false;
+#pragma unroll 1
+  for (int it = 0; it < m.maxb; ++it) {
+    const MeshHit h = mesh_nearest(m, x, y, z, r0x, r0y, r0z, dx, dy, dz, rem);
+    const bool hit = h.t < INFINITY;
+    if constexpr (WALL != kPermeate) {
+      if (!hit) {
+        last_reflect = false;
+        break;
+      }
+      const Tri T = load_tri(m, h.k);
+      const bool outward = (dx * T.nx + dy * T.ny + dz * T.nz) > 0.f;
+      float ndx = dx, ndy = dy, ndz = dz, nx, ny, nz, fx, fy, fz;
+      mesh_bounce(m, h.k, T, h.u, h.v, ndx, ndy, ndz, nx, ny, nz, fx, fy, fz);
+      if constexpr (WALL == kRelax) {
+        const float cos_a = -(dx * nx + dy * ny + dz * nz);
+        dsum += (outward ? m.rmi : m.rme) * (rem - h.t) * cos_a;
+      }
+      r0x = r0x + h.t * dx + m.nudge * fx;
+      r0y = r0y + h.t * dy + m.nudge * fy;
+      r0z = r0z + h.t * dz + m.nudge * fz;
+      dx = ndx;
+      dy = ndy;
+      dz = ndz;
+      rem = rem - h.t - m.nudge;
+      last_reflect = true;
+    } else {
+      bool do_reflect = false;
+      if (hit) {
+        const Tri T = load_tri(m, h.k);
+        const bool outward = (dx * T.nx + dy * T.ny + dz * T.nz) > 0.f;
+        float ndx = dx, ndy = dy, ndz = dz, nx, ny, nz, fx, fy, fz;
+        mesh_bounce(m, h.k, T, h.u, h.v, ndx, ndy, ndz, nx, ny, nz, fx, fy, fz);
+        const float cos_a = -(dx * nx + dy * ny + dz * nz);
+        const float dperp = (rem - h.t) * cos_a;
+        const bool first = !decided;
+        const float p = fminf(1.f, 2.f * m.kod * (outward ? m.kmo : m.kmi) * dperp);
+        const bool transmit = first && (u_rand < p);
+        do_reflect = !transmit;
+        if (first && !transmit) dsum += (outward ? m.rmi : m.rme) * dperp;
+        if (transmit) ++tl.transmit;
+        decided = true;
+        if (do_reflect) {
+          r0x = r0x + h.t * dx + m.nudge * fx;
+          r0y = r0y + h.t * dy + m.nudge * fy;
+          r0z = r0z + h.t * dz + m.nudge * fz;
+          dx = ndx;
+          dy = ndy;
+          dz = ndz;
+          rem = rem - h.t - m.nudge;
+        }
+      }
+      last_reflect = do_reflect;
+      if (!do_reflect) {  // no hit or a transmission: fly the rest of the step straight
+        r0x += rem * dx;
+        r0y += rem * dy;
+        r0z += rem * dz;
+        rem = 0.f;
+        break;
+      }
+    }
+  }
+  if (last_reflect) ++n_budget;  // the budget ran out with a hit: the leftover is not flown
+  const float f = last_reflect ? 0.f : fmaxf(rem, 0.f);
+  float nxp = r0x + dx * f, nyp = r0y + dy * f, nzp = r0z + dz * f;
+  int jx = ix, jy = iy, jz = iz;
+  mesh_fold(nxp, jx, 0, m);
+  mesh_fold(nyp, jy, 1, m);
+  mesh_fold(nzp, jz, 2, m);
+  if constexpr (WALL != kPermeate) {
+    if (m.reject) {
+      int pop_new;
+      const int cls_new = mesh_classify(m, nxp, nyp, nzp, pop_new);
+      if (pop && pop_new && cls_new != cls) {
+        ++n_escape;  // leak guard: a decidable class change without a crossing
+        return 0.f;
+      }
+      cls = cls_new;
+      pop = pop_new;
+    }
+  }
+  x = nxp;
+  y = nyp;
+  z = nzp;
+  ix = jx;
+  iy = jy;
+  iz = jz;
+  return -2.f * dsum;
+}
+
+}  // namespace dmsim

@@ -29,6 +29,7 @@
 
 #include "dmsim.h"
 #include "geometry.cuh"
+#include "mesh.cuh"
 #include "philox.cuh"
 
 namespace dmsim {
@@ -44,6 +45,7 @@ struct KArgs {
   int n_t, n_chunks, S, phase_sub, has_weight, n_echo, Mp, pass, M;
   float step_l, gamma_dt, t2dec, t1dec, rho;
   GeoK g;
+  MeshK mk;  // GEOM_MESH only
   uint32_t tab_cs_bytes, tab_cand_bytes;  // shared-memory staging sizes (multiples of 16 B)
   uint32_t off_cs, off_red, off_tab;      // shared-memory offsets of C, the reduction scratch
                                           // and the cell list (host-computed layout)
@@ -159,6 +161,11 @@ __device__ __forceinline__ int classify(float x, float y, float z, const GeoK& g
   }
 }
 
+__device__ __forceinline__ int classify_mesh(float x, float y, float z, const MeshK& m) {
+  int pop;
+  return mesh_classify(m, x, y, z, pop);
+}
+
 template <int GEOM, int WALL, int PM, int W, bool TSM>
 __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -176,8 +183,12 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
 
   constexpr bool PACKED = GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
+  constexpr bool MESH = GEOM == DMSIM_GEOM_MESH;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const GeoK g = a.g;
+  // per-axis period used to unfold positions (packed: the cell side; mesh: the periodic box)
+  const float Lx = MESH ? a.mk.box[0] : g.L, Ly = MESH ? a.mk.box[1] : g.L,
+              Lz = MESH ? a.mk.box[2] : g.L;
 
   const uint32_t* cs = a.cs;
   const float4* cand = a.cand;
@@ -229,7 +240,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
   }
 
   Tally tl, tl_idle;  // tallies of real walkers / of the idle threads of the last tile
-  uint32_t n_nonfinite = 0, n_initfail = 0;
+  uint32_t n_nonfinite = 0, n_initfail = 0, n_budget = 0, n_escape = 0, n_idle = 0;
   int64_t q = 0;  // running chunk counter of this block
 
   for (int it = 0; it < my_tiles; ++it) {
@@ -242,6 +253,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     // ---- initial position -----------------------------------------------------------------
     float x = 0.f, y = 0.f, z = 0.f;
     int ix = 0, iy = 0, iz = 0;
+    int mcls = 1, mpop = 0;  // mesh: class and gather population of the current position
     if (a.r0 != nullptr) {
       if (act) {
         x = a.r0[3 * w];
@@ -257,6 +269,12 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
           iz = (int)floorf(z / g.L + 0.5f);
           z -= g.L * iz;
         }
+      }
+      if constexpr (MESH) {
+        const MeshK& m = a.mk;
+        if (m.per[0]) { ix = (int)floorf((x - m.vmin[0]) / m.box[0]); x -= m.box[0] * ix; }
+        if (m.per[1]) { iy = (int)floorf((y - m.vmin[1]) / m.box[1]); y -= m.box[1] * iy; }
+        if (m.per[2]) { iz = (int)floorf((z - m.vmin[2]) / m.box[2]); z -= m.box[2] * iz; }
       }
     } else if constexpr (GEOM != DMSIM_GEOM_FREE) {
       // Uniform seeding by rejection, as the reference's host samplers (geometries.py:186-195,
@@ -291,6 +309,21 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
             }
             if (out) { x = px; y = py; ok = true; }
           }
+        } else if constexpr (MESH) {
+          // uniform in the box; keep points on the requested side of the closed surface (ray
+          // parity), or by the nearest-centroid classifier for an open surface
+          // (mesh.py:746-807)
+          const MeshK& m = a.mk;
+          const float px = m.vmin[0] + m.box[0] * u0, py = m.vmin[1] + m.box[1] * u1,
+                      pz = m.vmin[2] + m.box[2] * u2;
+          int side;
+          if (m.seed_parity) {
+            side = mesh_parity(m, px, py, pz);
+          } else {
+            int pop;
+            side = mesh_classify(m, px, py, pz, pop) == 0 ? 1 : 0;
+          }
+          if (side == m.seed_inside) { x = px; y = py; z = pz; ok = true; }
         } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
           const float px = g.L * (u0 - 0.5f), py = g.L * (u1 - 0.5f), pz = g.L * (u2 - 0.5f);
           const int c = (cell_of(pz, g) * g.n + cell_of(py, g)) * g.n + cell_of(px, g);
@@ -305,8 +338,12 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
       }
       if (!ok && act) ++n_initfail;
     }
+    if constexpr (MESH) {
+      if (a.mk.reject && WALL != kPermeate) mcls = mesh_classify(a.mk, x, y, z, mpop);
+    }
     if (act && a.comp0 != nullptr && a.pass == 0)
-      a.comp0[w] = classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+      a.comp0[w] = MESH ? classify_mesh(x, y, z, a.mk)
+                        : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
 
     // phase accumulators: direct form phi[m] (+ Kahan), basis form Q[j][k] (+ Kahan)
     constexpr int NACC = PM ? 3 * W : W;
@@ -387,17 +424,22 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
             dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
+          } else if constexpr (MESH) {
+            dl = mesh_step<WALL>(x, y, z, ix, iy, iz, mcls, mpop, stx, sty, stz, up, a.mk, tw,
+                                 act ? n_budget : n_idle, act ? n_escape : n_idle);
           }
           if (a.has_weight) logw += rc * dl - dec;
           if (a.phase_sub) {
-            Rx += x + g.L * (float)ix;
-            Ry += y + g.L * (float)iy;
-            Rz += z + g.L * (float)iz;
+            Rx += x + Lx * (float)ix;
+            Ry += y + Ly * (float)iy;
+            Rz += z + Lz * (float)iz;
           }
           if (a.dlog_unit) dls += dl;
-          if (a.comp_occ) occ += (float)classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+          if (a.comp_occ)
+            occ += (float)(MESH ? classify_mesh(x, y, z, a.mk)
+                                : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
         }
-        const float ux = x + g.L * (float)ix, uy = y + g.L * (float)iy, uz = z + g.L * (float)iz;
+        const float ux = x + Lx * (float)ix, uy = y + Ly * (float)iy, uz = z + Lz * (float)iz;
         if (!a.phase_sub) {
           Rx = ux;
           Ry = uy;
@@ -508,7 +550,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     }
 
     // ---- per-walker outputs --------------------------------------------------------------------
-    const float ux = x + g.L * (float)ix, uy = y + g.L * (float)iy, uz = z + g.L * (float)iz;
+    const float ux = x + Lx * (float)ix, uy = y + Ly * (float)iy, uz = z + Lz * (float)iz;
     if (act) {
       if (!(isfinite(ux) && isfinite(uy) && isfinite(uz))) ++n_nonfinite;
       if (a.pass == 0) {
@@ -518,7 +560,9 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
           a.final_pos[3 * w + 2] = uz;
         }
         if (a.log_w) a.log_w[w] = logw;
-        if (a.comp_end) a.comp_end[w] = classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+        if (a.comp_end)
+          a.comp_end[w] = MESH ? classify_mesh(x, y, z, a.mk)
+                               : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
       }
       if (a.phi_out) {
         if constexpr (PM == 0) {
@@ -546,12 +590,16 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
   const uint32_t v2 = __reduce_add_sync(0xffffffffu, n_initfail);
   const uint32_t v3 = __reduce_add_sync(0xffffffffu, tl.graze);
   const uint32_t v4 = __reduce_add_sync(0xffffffffu, tl.transmit);
+  const uint32_t v5 = __reduce_add_sync(0xffffffffu, n_budget);
+  const uint32_t v6 = __reduce_add_sync(0xffffffffu, n_escape);
   if (lane == 0 && a.pass == 0) {
     if (v0) atomicAdd(&a.status[DMSIM_STATUS_NONFINITE], v0);
     if (v1) atomicAdd(&a.status[DMSIM_STATUS_CLAMPED], v1);
     if (v2) atomicAdd(&a.status[DMSIM_STATUS_INIT_FAIL], v2);
     if (v3) atomicAdd(&a.status[DMSIM_STATUS_GRAZE_FP64], v3);
     if (v4) atomicAdd(&a.status[DMSIM_STATUS_TRANSMIT], v4);
+    if (v5) atomicAdd(&a.status[DMSIM_STATUS_BOUNCE_BUDGET], v5);
+    if (v6) atomicAdd(&a.status[DMSIM_STATUS_ESCAPE_REJECT], v6);
   }
 }
 

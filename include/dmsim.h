@@ -112,10 +112,15 @@ typedef struct dmsim_geometry {
   float kappa_mult_out;
   float kappa_mult_in;
   int32_t reject_escape;
-  const float* tri;              /* n_tri x 12: v0 v1 v2 (9) + geometric normal (3)        */
-  const float* tri_vn;           /* n_tri x 9: smooth vertex normals of v0 v1 v2            */
-  const uint32_t* mesh_cell_start; /* dims product + 1                                      */
-  const uint32_t* mesh_cell_tri;   /* triangle indices                                        */
+  int32_t seed_parity;           /* seed by ray-crossing parity (closed surface), else by the
+                                    nearest-centroid classifier                              */
+  int32_t seed_inside;           /* seed inside (1) or outside (0) the surface                */
+  int32_t pad1;
+  const float* tri;              /* n_tri x 16: A, E1 = B - A, E2 = C - A, geometric normal,
+                                    centroid, 1 for an original / 0 for a periodic ghost      */
+  const float* tri_vn;           /* n_tri x 12: smooth normals at A, B, C (+3 padding)        */
+  const uint32_t* mesh_cell_start; /* prod(mesh_dims) + 1 (CSR)                              */
+  const uint32_t* mesh_cell_tri;   /* triangle indices, each cell in increasing order         */
 } dmsim_geometry;
 
 /* ---- walk parameters -------------------------------------------------------------------------- */

@@ -256,6 +256,57 @@ def _replay_cases(m, out):
     out["rep_signal_plain"] = np.asarray(sig2)
 
 
+def _mesh_cases(m, rng, out):
+    """Mesh.reflect / reflect_with_log_weight / permeate of the reference on a closed icosphere
+    and on a periodic box whose sphere crosses a face (ghost triangles)."""
+    import importlib
+    import warnings
+    shapes = importlib.import_module("dmipy_sim.mesh_shapes")
+    mesh_mod = importlib.import_module("dmipy_sim.mesh")
+    R = 5e-6
+    V, F = shapes.icosphere(R, 2)
+    out["mesh_V"], out["mesh_F"] = np.asarray(V, np.float64), np.asarray(F, np.int64)
+    n = 192
+    cases = {}
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        cases["msh"] = (mesh_mod.Mesh(V, F), mesh_mod.Mesh(V, F, intra={"surface_relaxivity_t2": 1e-6}),
+                        mesh_mod.Mesh(V, F, permeability=1e-5,
+                                      intra={"surface_relaxivity_t2": 1e-6}), np.zeros(3), None)
+        Vp = V * 0.6 + np.array([3.5e-6, 0.0, 0.0])
+        kw = dict(periodic=True, voxel_min=[-5e-6] * 3, voxel_max=[5e-6] * 3, feature_radius=3e-6)
+        cases["mshp"] = (mesh_mod.Mesh(Vp, F, **kw),
+                         mesh_mod.Mesh(Vp, F, intra={"surface_relaxivity_t2": 1e-6}, **kw),
+                         mesh_mod.Mesh(Vp, F, permeability=1e-5, **kw), np.array([3.5e-6, 0, 0]),
+                         kw)
+    out["mesh_Vp"] = np.asarray(V * 0.6 + np.array([3.5e-6, 0.0, 0.0]), np.float64)
+    for tag, (g0, g1, g2, c0, kw) in cases.items():
+        rr = (R if tag == "msh" else 0.6 * R)
+        d = _unit(rng, n)
+        rad = rr * rng.uniform(0.6, 1.3, n)
+        rs = (c0 + d * rad[:, None]).astype(np.float32)
+        if tag == "mshp":
+            rs = rs + (rng.integers(-2, 3, (n, 3)) * 10e-6).astype(np.float32)
+        st = (_unit(rng, n) * (rr * rng.uniform(0.02, 0.3, n))[:, None]).astype(np.float32)
+        us = rng.uniform(0, 1, n).astype(np.float32)
+        for mode, g in (("reflect", g0), ("relax", g1), ("perm", g2)):
+            ro = np.zeros((n, 3))
+            dl = np.zeros(n)
+            for i in range(n):
+                if mode == "reflect":
+                    o, dd = g.reflect(rs[i], st[i]), 0.0
+                elif mode == "relax":
+                    o, dd = g.reflect_with_log_weight(rs[i], st[i], np.float32(500.0))
+                else:
+                    o, dd = g.permeate(rs[i], st[i], np.float32(5000.0), np.float32(500.0),
+                                       jaxstub.Injected(us[i]))
+                ro[i] = np.asarray(o, np.float64)
+                dl[i] = float(dd)
+            key = f"pl_{tag}_{mode}"
+            out[key + "_r"], out[key + "_step"], out[key + "_out"] = rs, st, ro
+            out[key + "_dlog"], out[key + "_u"] = dl, us
+
+
 def make_kat(root):
     m = _ref(root)
     out = {}
@@ -265,6 +316,7 @@ def make_kat(root):
     _pack_cases(m, out)
     _replay_cases(m, out)
     _plugin_cases(m, rng, out)
+    _mesh_cases(m, np.random.default_rng(77), out)
     np.savez_compressed(HERE / "kat.npz", **out)
     print(f"kat.npz: {len(out)} arrays")
 

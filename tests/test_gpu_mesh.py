@@ -1,0 +1,76 @@
+"""Mesh substrate on the GPU: the device step (dmsim_step_kat, the walk kernel's code) against the
+reference's own Mesh.reflect / reflect_with_log_weight / permeate calls (kat.npz, closed icosphere
+and a periodic box with ghost triangles), seeding and containment, and a mesh sphere against the
+analytic sphere (the reference's tests/test_mesh_mc.py check)."""
+import warnings
+
+import numpy as np
+import pytest
+
+import dmipy_sim_gb300 as d
+from dmipy_sim_gb300 import core
+
+pytestmark = pytest.mark.gpu
+D = 2e-9
+
+
+def _mesh(kat, tag, mode):
+    kw = {}
+    if mode == "relax":
+        kw["intra"] = {"surface_relaxivity_t2": 1e-6}
+    if mode == "perm":
+        kw["permeability"] = 1e-5
+        if tag == "msh":
+            kw["intra"] = {"surface_relaxivity_t2": 1e-6}
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        if tag == "msh":
+            return d.Mesh(kat["mesh_V"], kat["mesh_F"], **kw)
+        return d.Mesh(kat["mesh_Vp"], kat["mesh_F"], periodic=True, voxel_min=[-5e-6] * 3,
+                      voxel_max=[5e-6] * 3, feature_radius=3e-6, **kw)
+
+
+@pytest.mark.parametrize("tag", ["msh", "mshp"])
+@pytest.mark.parametrize("mode", ["reflect", "relax", "perm"])
+def test_mesh_step_matches_reference(cuda, kat, tag, mode):
+    key = f"pl_{tag}_{mode}"
+    g = _mesh(kat, tag, mode)
+    wall = {"reflect": 0, "relax": 1, "perm": 2}[mode]
+    out, dl = core.step_kat(g, kat[key + "_r"], kat[key + "_step"], kat[key + "_u"], wall=wall)
+    ref = kat[key + "_out"]
+    scale = 5e-6
+    err = np.max(np.abs(out - ref), axis=1)
+    bad = err > 1e-5 * np.maximum(np.max(np.abs(ref), axis=1), scale)
+    assert bad.mean() <= 0.02, f"{bad.sum()} of {len(ref)} steps differ (worst {err.max():.3e})"
+    dref = kat[key + "_dlog"]
+    ok = np.abs(dl * 500.0 - dref) <= 1e-3 * np.abs(dref) + 1e-8
+    assert ok.mean() >= 0.97
+
+
+def test_mesh_walkers_seeded_inside_and_contained(cuda):
+    V, F = d.icosphere(5e-6, 3)
+    g = d.Mesh(V, F)
+    wf = d.set_b(d.pgse(0.01, 0.03, 0.05, [[1, 0, 0], [0, 0, 1]], 200), 1e9)
+    G, _ = core._waveform_arrays(wf, g)
+    S = core.replay_sub_steps(g, D, wf.dt)
+    res = core.run_walk(g, n_walkers=8192, diffusivity=D, G=G[:, :2], dt=wf.dt, sub_steps=S,
+                        phase_per_substep=False, seed=3, want_positions=True)
+    p0 = core.run_walk(g, n_walkers=8192, diffusivity=D, G=G[:, :1], dt=wf.dt, sub_steps=1,
+                       phase_per_substep=False, seed=3, want_positions=True)
+    assert res.status["init_fail"] == 0
+    assert d.mesh_contains(V, F, p0.extras["pos"].cpu().numpy()).mean() > 0.995
+    res = core.run_walk(g, n_walkers=8192, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                        phase_per_substep=False, seed=3, want_positions=True)
+    inside = d.mesh_contains(V, F, res.extras["pos"].cpu().numpy())
+    assert inside.mean() > 0.995, inside.mean()
+
+
+def test_mesh_sphere_matches_analytic_sphere(cuda):
+    V, F = d.icosphere(5e-6, 4)
+    rng = np.random.default_rng(1)
+    bv = rng.normal(size=(4, 3))
+    bv /= np.linalg.norm(bv, axis=1, keepdims=True)
+    wf = d.set_b(d.pgse(0.005, 0.015, 0.05, bv, 120), 1.5e9)
+    s_mesh = d.simulate(40_000, D, wf, d.Mesh(V, F), seed=2)
+    s_ana = d.simulate(200_000, D, wf, d.Sphere(5e-6), seed=2)
+    np.testing.assert_allclose(s_mesh, s_ana, atol=0.02)
