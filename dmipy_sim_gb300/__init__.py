@@ -14,6 +14,8 @@ from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, Wal
                    fused_sub_steps)
 from .trajectories import replay
 from .mesh import Mesh, load_ply, icosphere, random_ellipsoid_cells, mesh_contains
+from .batched import Instance, Tuning, PreparedBatch, simulate_batch
+from .autotune import autotune
 
 __all__ = [
     "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
@@ -22,4 +24,5 @@ __all__ = [
     "simulate", "simulate_cpmg", "simulate_trajectories", "replay", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
     "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
+    "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune",
 ]

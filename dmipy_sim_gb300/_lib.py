@@ -13,7 +13,8 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 2
+DMSIM_ABI_VERSION = 3
+TILE_WALKERS = 320
 
 GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
 WALL_REFLECT, WALL_RELAX, WALL_PERMEATE = range(3)
@@ -25,7 +26,12 @@ STATUS_WORDS = len(STATUS_NAMES)
 # Symbols every build of the library exports (the C ABI of include/dmsim.h).
 EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "dmsim_walk",
             "dmsim_walk_noalloc", "dmsim_step_kat", "dmsim_replay_workspace_bytes",
-            "dmsim_replay")
+            "dmsim_replay", "dmsim_batch_create", "dmsim_batch_bind", "dmsim_batch_launch",
+            "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_pack",
+            "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
+            "dmsim_adam_advance")
+
+EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
 
 class Geometry(C.Structure):
@@ -69,6 +75,22 @@ class WalkOutputs(C.Structure):
     ]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [
+        ("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("order", C.c_int32),
+        ("concurrent_groups", C.c_int32), ("tab_smem_bytes", C.c_int64),
+    ]
+
+
+class Gemm(C.Structure):
+    _fields_ = [
+        ("A", C.c_void_p), ("B", C.c_void_p), ("M", C.c_int64), ("N", C.c_int32),
+        ("K", C.c_int32), ("lda", C.c_int64), ("ldb", C.c_int64), ("epilogue", C.c_int32),
+        ("splits", C.c_int32), ("C", C.c_void_p), ("bias", C.c_void_p), ("P", C.c_void_p),
+        ("H", C.c_void_p), ("HT", C.c_void_p), ("ldht", C.c_int64), ("err", C.c_void_p),
+    ]
+
+
 _lib = None
 
 
@@ -100,6 +122,34 @@ def load():
     lib.dmsim_replay.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int32, C.c_void_p,
                                  C.c_int32, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.dmsim_batch_create.restype = C.c_int
+    lib.dmsim_batch_create.argtypes = [C.c_int32, C.POINTER(WalkParams), C.POINTER(Geometry),
+                                       C.POINTER(WalkOutputs), C.POINTER(BatchTuning),
+                                       C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
+    lib.dmsim_batch_bind.restype = C.c_int
+    lib.dmsim_batch_bind.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.dmsim_batch_launch.restype = C.c_int
+    lib.dmsim_batch_launch.argtypes = [C.c_void_p, C.c_void_p]
+    lib.dmsim_batch_info.restype = C.c_int
+    lib.dmsim_batch_info.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+    lib.dmsim_batch_destroy.restype = None
+    lib.dmsim_batch_destroy.argtypes = [C.c_void_p]
+    vp, i32, i64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_float
+    lib.dmsim_gemm_bf16.restype = C.c_int
+    lib.dmsim_gemm_bf16.argtypes = [C.POINTER(Gemm), vp]
+    lib.dmsim_mlp_pack.restype = C.c_int
+    lib.dmsim_mlp_pack.argtypes = [vp, i64, i32, i32, vp, vp, vp, vp, i64, vp]
+    lib.dmsim_mlp_head.restype = C.c_int
+    lib.dmsim_mlp_head.argtypes = [vp, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp]
+    lib.dmsim_rowdot_bf16.restype = C.c_int
+    lib.dmsim_rowdot_bf16.argtypes = [vp, i64, i64, i64, vp, vp, vp]
+    lib.dmsim_sum_f32.restype = C.c_int
+    lib.dmsim_sum_f32.argtypes = [vp, i64, vp, vp]
+    lib.dmsim_adamw.restype = C.c_int
+    lib.dmsim_adamw.argtypes = [vp, vp, vp, vp, i32, i64, i32, vp, vp, vp, i32, vp]
+    lib.dmsim_adam_advance.restype = C.c_int
+    lib.dmsim_adam_advance.argtypes = [vp, vp]
     if lib.dmsim_version() != DMSIM_ABI_VERSION:
         raise RuntimeError(f"libdmsim ABI {lib.dmsim_version()} != {DMSIM_ABI_VERSION}")
     _lib = lib

@@ -242,7 +242,7 @@ class PreparedWalk:
                  seed, chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
                  want_positions=False, want_walker_signals=False, want_compartments=False,
                  traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False,
-                 use_basis=True):
+                 use_basis=True, allocate_workspace=True):
         self.lib = _lib.load()
         dev = self.dev = _lib.device()
         G = np.asarray(G, dtype=np.float32)
@@ -330,7 +330,9 @@ class PreparedWalk:
         self.ws_bytes = self.lib.dmsim_walk_workspace_bytes(p, self.gdesc)
         if self.ws_bytes == 0:
             _lib.check(-1, "dmsim_walk_workspace_bytes")
-        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        # a walk that joins a batch gets its scratch from the batch's workspace instead
+        self.ws = (torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+                   if allocate_workspace else None)
         self.n_walkers = int(n_walkers)
         self.n_meas, self.n_t, self.sub_steps = n_meas, n_t, S
 

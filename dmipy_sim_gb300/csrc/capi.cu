@@ -6,6 +6,11 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <map>
+#include <tuple>
+#include <vector>
+
 #include "dmsim.h"
 #include "walk_kernel.cuh"
 
@@ -16,6 +21,12 @@ WalkFn walk_fn_sph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_pcyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_psph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_mesh(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_sph(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_pcyl(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_psph(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_mesh(int wall, int pm, int width, bool tsm);
 }  // namespace dmsim
 
 using namespace dmsim;
@@ -62,7 +73,8 @@ struct Plan {
   SmemLayout lay;
 };
 
-int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
+int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
+              size_t tab_budget = kTabSmemBudget) {
   if (!p || !g) return fail(DMSIM_EINVAL, "null params or geometry");
   if (p->n_walkers < 0) return fail(DMSIM_EINVAL, "n_walkers < 0");
   if (p->n_t < 1 || p->n_meas < 1 || p->sub_steps < 1)
@@ -125,7 +137,7 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl) {
     cells = (size_t)g->grid_n * g->grid_n * (g->kind == DMSIM_GEOM_PACKED_SPHERES ? g->grid_n : 1);
     pl->tab_cs = pad16((cells + 1) * 4);
     pl->tab_cand = (size_t)g->n_cand * 16;
-    pl->tsm = pl->tab_cs + pl->tab_cand <= kTabSmemBudget;
+    pl->tsm = pl->tab_cs + pl->tab_cand <= tab_budget;
   }
   switch (g->kind) {
     case DMSIM_GEOM_FREE: pl->fn = walk_fn_free(g->wall_mode, pl->pm, pl->width, false); break;
@@ -456,6 +468,99 @@ int replay_grid(int64_t n_walkers) {
   return (int)(grid < 1 ? 1 : grid);
 }
 
+
+int check_outputs(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o) {
+  if (!o || !o->sums || !o->status) return fail(DMSIM_EINVAL, "outputs need sums and status");
+  const bool packed =
+      g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
+  if ((o->comp0 || o->comp_end || o->comp_occ) && packed && !g->cand_obj)
+    return fail(DMSIM_EINVAL, "classification of packed objects needs cand_obj");
+  (void)p;
+  return DMSIM_OK;
+}
+
+// Kernel arguments of one walk; the per-pass fields (pass, Gp, active) and the partial buffer
+// are set by the caller.
+void fill_kargs(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
+                const Plan& pl, KArgs* a) {
+  memset(a, 0, sizeof(*a));
+  a->n_walkers = p->n_walkers;
+  a->walker_offset = p->walker_offset;
+  a->seed = p->seed;
+  a->n_t = p->n_t;
+  a->n_chunks = pl.n_chunks;
+  a->S = p->sub_steps;
+  a->phase_sub = p->phase_per_substep ? 1 : 0;
+  a->has_weight = p->has_weight ? 1 : 0;
+  a->n_echo = p->n_echo;
+  a->Mp = pl.pm ? p->n_meas : pl.n_pass * pl.mt;
+  a->M = p->n_meas;
+  a->step_l = p->step_length;
+  a->gamma_dt = p->gamma_dt;
+  a->t2dec = p->t2_decay;
+  a->t1dec = p->t1_decay;
+  a->rho = g->rho_over_D;
+  a->g = make_geok(g);
+  a->mk = make_meshk(g);
+  a->tab_cs_bytes = (uint32_t)pl.tab_cs;
+  a->tab_cand_bytes = (uint32_t)pl.tab_cand;
+  a->cs = g->cell_start;
+  a->cand = reinterpret_cast<const float4*>(g->cand);
+  a->cand_obj = g->cand_obj;
+  a->chi = p->chi;
+  a->r0 = p->r0;
+  a->status = o->status;
+  a->final_pos = o->final_pos;
+  a->log_w = o->log_w;
+  a->phi_out = o->phi;
+  a->comp0 = o->comp0;
+  a->comp_end = o->comp_end;
+  a->traj = o->traj;
+  a->traj_f16 = o->traj_f16;
+  a->dlog_unit = o->dlog_unit;
+  a->comp_occ = o->comp_occ;
+  for (int e = 0; e < p->n_echo; ++e) a->echo[e] = p->echo_idx[e];
+}
+
+// One walk on its own launches: waveform re-layout, one walk launch per pass, reduction.
+int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
+                  const Plan& pl, uint8_t* ws, cudaStream_t st) {
+  int rc = check_outputs(p, g, o);
+  if (rc != DMSIM_OK) return rc;
+  if (p->n_walkers == 0) {
+    cudaMemsetAsync(o->sums, 0, sizeof(double) * p->n_echo * p->n_meas * 3, st);
+    return DMSIM_OK;
+  }
+  float* Gp = reinterpret_cast<float*>(ws + pl.off_gp);
+  uint8_t* act = ws + pl.off_act;
+  double* part = reinterpret_cast<double*>(ws + pl.off_part);
+  float* Cp = reinterpret_cast<float*>(ws + pl.off_cp);
+  const int t_pad = pl.n_chunks * kTC;
+  if (pl.pm)
+    k_prep_basis<<<64, 256, 0, st>>>(p->basis_V, p->basis_C, p->n_t, p->n_meas, p->basis_rank,
+                                     pl.width, t_pad, Gp, act, Cp);
+  else
+    k_prep<<<64, 256, 0, st>>>(p->G, p->n_t, p->n_meas, pl.mt, pl.n_pass, t_pad, Gp, act);
+  KArgs a;
+  fill_kargs(p, g, o, pl, &a);
+  a.Cp = Cp;
+  a.part = part;
+  BatchCtl none;
+  memset(&none, 0, sizeof(none));
+  for (int pass = 0; pass < pl.n_pass; ++pass) {
+    a.pass = pass;
+    a.Gp = Gp + (size_t)pass * t_pad * pl.row;
+    a.active = act + (size_t)pass * p->n_t;
+    pl.fn<<<pl.grid, kBlock, pl.smem, st>>>(a, none);
+  }
+  const int nred = p->n_echo * p->n_meas * 3;
+  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, pl.grid, p->n_echo, a.Mp, p->n_meas,
+                                               o->sums);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
 }  // namespace
 
 namespace dmsim {
@@ -480,89 +585,12 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
   Plan pl;
   int rc = make_plan(p, g, &pl);
   if (rc != DMSIM_OK) return rc;
-  if (!o || !o->sums || !o->status) return fail(DMSIM_EINVAL, "outputs need sums and status");
+  rc = check_outputs(p, g, o);
+  if (rc != DMSIM_OK) return rc;
   if (!workspace || workspace_bytes < pl.total)
     return fail(DMSIM_EWORKSPACE, "workspace %zu B < required %zu B", workspace_bytes, pl.total);
   if (((uintptr_t)workspace & 255) != 0) return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
-  if (p->n_walkers == 0) {
-    cudaMemsetAsync(o->sums, 0, sizeof(double) * p->n_echo * p->n_meas * 3, (cudaStream_t)stream);
-    return DMSIM_OK;
-  }
-  cudaStream_t st = (cudaStream_t)stream;
-  uint8_t* ws = static_cast<uint8_t*>(workspace);
-  float* Gp = reinterpret_cast<float*>(ws + pl.off_gp);
-  uint8_t* act = ws + pl.off_act;
-  double* part = reinterpret_cast<double*>(ws + pl.off_part);
-  const int t_pad = pl.n_chunks * kTC;
-
-  float* Cp = reinterpret_cast<float*>(ws + pl.off_cp);
-  if (pl.pm)
-    k_prep_basis<<<64, 256, 0, st>>>(p->basis_V, p->basis_C, p->n_t, p->n_meas, p->basis_rank,
-                                     pl.width, t_pad, Gp, act, Cp);
-  else
-    k_prep<<<64, 256, 0, st>>>(p->G, p->n_t, p->n_meas, pl.mt, pl.n_pass, t_pad, Gp, act);
-
-  KArgs a;
-  memset(&a, 0, sizeof(a));
-  a.n_walkers = p->n_walkers;
-  a.walker_offset = p->walker_offset;
-  a.seed = p->seed;
-  a.n_t = p->n_t;
-  a.n_chunks = pl.n_chunks;
-  a.S = p->sub_steps;
-  a.phase_sub = p->phase_per_substep ? 1 : 0;
-  a.has_weight = p->has_weight ? 1 : 0;
-  a.n_echo = p->n_echo;
-  a.Mp = pl.pm ? p->n_meas : pl.n_pass * pl.mt;
-  a.Cp = Cp;
-  a.off_cs = (uint32_t)pl.lay.off_cs;
-  a.off_red = (uint32_t)pl.lay.off_red;
-  a.off_tab = (uint32_t)pl.lay.off_tab;
-  a.M = p->n_meas;
-  a.step_l = p->step_length;
-  a.gamma_dt = p->gamma_dt;
-  a.t2dec = p->t2_decay;
-  a.t1dec = p->t1_decay;
-  a.rho = g->rho_over_D;
-  const bool packed =
-      g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  a.g = make_geok(g);
-  a.mk = make_meshk(g);
-  a.tab_cs_bytes = (uint32_t)pl.tab_cs;
-  a.tab_cand_bytes = (uint32_t)pl.tab_cand;
-  a.cs = g->cell_start;
-  a.cand = reinterpret_cast<const float4*>(g->cand);
-  a.cand_obj = g->cand_obj;
-  a.active = nullptr;
-  a.chi = p->chi;
-  a.r0 = p->r0;
-  a.part = part;
-  a.status = o->status;
-  a.final_pos = o->final_pos;
-  a.log_w = o->log_w;
-  a.phi_out = o->phi;
-  a.comp0 = o->comp0;
-  a.comp_end = o->comp_end;
-  a.traj = o->traj;
-  a.traj_f16 = o->traj_f16;
-  a.dlog_unit = o->dlog_unit;
-  a.comp_occ = o->comp_occ;
-  if ((o->comp0 || o->comp_end || o->comp_occ) && packed && !g->cand_obj)
-    return fail(DMSIM_EINVAL, "classification of packed objects needs cand_obj");
-  for (int e = 0; e < p->n_echo; ++e) a.echo[e] = p->echo_idx[e];
-
-  for (int pass = 0; pass < pl.n_pass; ++pass) {
-    a.pass = pass;
-    a.Gp = Gp + (size_t)pass * t_pad * pl.row;
-    a.active = act + (size_t)pass * p->n_t;
-    pl.fn<<<pl.grid, kBlock, pl.smem, st>>>(a);
-  }
-  const int nred = p->n_echo * p->n_meas * 3;
-  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, pl.grid, p->n_echo, a.Mp, p->n_meas,
-                                               o->sums);
-  cudaError_t err = cudaGetLastError();
-  if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));
-  return DMSIM_OK;
+  return launch_single(p, g, o, pl, static_cast<uint8_t*>(workspace), (cudaStream_t)stream);
 }
 
 int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const float* steps,
@@ -628,6 +656,399 @@ int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t 
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(DMSIM_ECUDA, "replay launch failed: %s", cudaGetErrorString(err));
   return DMSIM_OK;
+}
+
+}  // extern "C"
+
+// ================================================================================================
+// Batched walks
+// ================================================================================================
+namespace {
+
+struct PrepItem {  // waveform re-layout of one batched instance
+  const float* V;
+  const float* C;
+  float* Vp;
+  uint8_t* act;
+  float* Cp;
+  int n_t, M, r, rt, t_pad, pad;
+};
+
+struct RedItem {  // reduction of one batched instance's work-item partials
+  const double* part;
+  double* sums;
+  int64_t n_items;
+  int n, pad;
+};
+
+__global__ void k_prep_basis_batch(const PrepItem* __restrict__ items) {
+  const PrepItem it = items[blockIdx.y];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int64_t i = i0; i < it.t_pad; i += stride) {
+    const int t = (int)i;
+    bool any = false;
+    for (int j = 0; j < it.rt; ++j) {
+      const float v = (t < it.n_t && j < it.r) ? it.V[(size_t)t * it.r + j] : 0.f;
+      it.Vp[(size_t)t * it.rt + j] = v;
+      any |= (v != 0.f);
+    }
+    if (t < it.n_t) it.act[t] = any ? 1 : 0;
+  }
+  for (int64_t i = i0; i < (int64_t)it.M * 3 * it.rt; i += stride) {
+    const int j = (int)(i % it.rt);
+    it.Cp[i] = j < it.r ? it.C[(i / it.rt) * it.r + j] : 0.f;
+  }
+}
+
+// Fixed-order sum of every instance's work-item partials (instance = blockIdx.y).
+__global__ void k_reduce_batch(const RedItem* __restrict__ items) {
+  const RedItem it = items[blockIdx.y];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < it.n; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int64_t b = 0; b < it.n_items; ++b) acc += it.part[(size_t)b * it.n + i];
+    it.sums[i] = acc;
+  }
+}
+
+WalkFn batch_fn(const dmsim_geometry* g, int width, bool tsm) {
+  switch (g->kind) {
+    case DMSIM_GEOM_FREE: return walk_batch_fn_free(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_CYLINDER: return walk_batch_fn_cyl(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_SPHERE: return walk_batch_fn_sph(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_PACKED_CYLINDERS: return walk_batch_fn_pcyl(g->wall_mode, 1, width, tsm);
+    case DMSIM_GEOM_PACKED_SPHERES: return walk_batch_fn_psph(g->wall_mode, 1, width, tsm);
+    case DMSIM_GEOM_MESH: return walk_batch_fn_mesh(g->wall_mode, 1, width, false);
+  }
+  return nullptr;
+}
+
+struct BatchInst {
+  dmsim_walk_params p;
+  dmsim_geometry g;
+  dmsim_walk_outputs o;
+  std::vector<int32_t> echo;
+  Plan pl;
+  bool batched = false;
+  int group = -1;
+  int64_t n_items = 0;
+  size_t off_gp = 0, off_act = 0, off_cp = 0, off_part = 0;  // batched: own slices
+  size_t off_ws = 0;                                         // plain: its dmsim_walk workspace
+};
+
+struct BatchGroup {
+  WalkFn fn = nullptr;
+  int grid = 0, max_m = 0;
+  size_t smem = 0, max_tab = 0;
+  std::vector<int> members;  // instance indices in work-queue order
+  int64_t n_items = 0;
+  size_t off_items = 0;      // (members + 1) int64 prefix sums of work items
+  size_t off_kargs = 0;      // members x KArgs
+};
+
+}  // namespace
+
+struct dmsim_batch {
+  int device = 0;
+  dmsim_batch_tuning tune{};
+  std::vector<BatchInst> inst;
+  std::vector<BatchGroup> groups;
+  std::vector<int> batched;  // instance indices with a batched walk (prep / reduce order)
+  size_t off_prep = 0, off_red = 0, off_ctr = 0, off_tables = 0, total = 0;
+  std::vector<uint8_t> blob;  // host image of [off_tables, off_ctr)
+  uint8_t* ws = nullptr;
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> ev;  // [0] fork, [1 + i] join of side stream i
+};
+
+namespace {
+
+int batch_plan(dmsim_batch* b) {
+  int n_sm = 0;
+  if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "cudaDeviceGetAttribute failed");
+  const size_t budget = b->tune.tab_smem_bytes > 0 ? (size_t)b->tune.tab_smem_bytes : kTabSmemBudget;
+  const int tpi = b->tune.tiles_per_item > 0 ? b->tune.tiles_per_item : 1;
+  std::map<std::tuple<int, int, int, bool>, int> key2group;
+  size_t off = 0;
+  for (size_t i = 0; i < b->inst.size(); ++i) {
+    BatchInst& I = b->inst[i];
+    I.p.echo_idx = I.echo.data();
+    int rc = make_plan(&I.p, &I.g, &I.pl, budget);
+    if (rc != DMSIM_OK) return rc;
+    rc = check_outputs(&I.p, &I.g, &I.o);
+    if (rc != DMSIM_OK) return rc;
+    I.batched = I.pl.pm == 1;
+    if (!I.batched) {
+      I.off_ws = off;
+      off = align256(off + I.pl.total);
+      continue;
+    }
+    const int64_t n_tiles = (I.p.n_walkers + kBlock - 1) / kBlock;
+    I.n_items = (n_tiles + tpi - 1) / tpi;
+    const int t_pad = I.pl.n_chunks * kTC;
+    I.off_gp = off;
+    off = align256(off + (size_t)t_pad * I.pl.width * 4);
+    I.off_act = off;
+    off = align256(off + (size_t)I.p.n_t);
+    I.off_cp = off;
+    off = align256(off + (size_t)I.p.n_meas * 3 * I.pl.width * 4);
+    I.off_part = off;
+    off = align256(off + (size_t)I.n_items * I.p.n_echo * I.p.n_meas * 3 * 8);
+    const auto key = std::make_tuple((int)I.g.kind, (int)I.g.wall_mode, I.pl.width, I.pl.tsm);
+    auto itg = key2group.find(key);
+    if (itg == key2group.end()) {
+      itg = key2group.emplace(key, (int)b->groups.size()).first;
+      b->groups.emplace_back();
+      b->groups.back().fn = batch_fn(&I.g, I.pl.width, I.pl.tsm);
+      if (!b->groups.back().fn) return fail(DMSIM_EINVAL, "no batched kernel for instance %zu", i);
+    }
+    I.group = itg->second;
+    BatchGroup& G = b->groups[I.group];
+    G.members.push_back((int)i);
+    G.max_m = std::max(G.max_m, I.p.n_meas);
+    if (I.pl.tsm) G.max_tab = std::max(G.max_tab, I.pl.tab_cs + I.pl.tab_cand);
+    b->batched.push_back((int)i);
+  }
+  // work-queue order inside a group: costliest tile first (longest-processing-time rule)
+  for (BatchGroup& G : b->groups) {
+    if (b->tune.order == 1)
+      std::stable_sort(G.members.begin(), G.members.end(), [&](int x, int y) {
+        const BatchInst &X = b->inst[x], &Y = b->inst[y];
+        return (double)X.p.n_t * X.p.sub_steps > (double)Y.p.n_t * Y.p.sub_steps;
+      });
+    G.n_items = 0;
+    for (int m : G.members) G.n_items += b->inst[m].n_items;
+    G.smem = walk_smem_layout(1, b->inst[G.members[0]].pl.width, G.max_m).off_tab + G.max_tab;
+    if (cudaFuncSetAttribute((const void*)G.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)G.smem) != cudaSuccess)
+      return fail(DMSIM_ECUDA, "cudaFuncSetAttribute(%zu B shared) failed", G.smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)G.fn, kBlock, G.smem) !=
+            cudaSuccess ||
+        nb < 1)
+      return fail(DMSIM_ECUDA, "batched kernel does not fit on an SM (%zu B shared)", G.smem);
+    if (b->tune.blocks_per_sm > 0) nb = std::min(nb, (int)b->tune.blocks_per_sm);
+    int64_t grid = (int64_t)nb * n_sm;
+    grid = std::min<int64_t>(grid, std::max<int64_t>(G.n_items, 1));
+    G.grid = (int)grid;
+  }
+  // tables: per group the item prefix sums and the KArgs, then prep / reduce items, counters
+  b->off_tables = off;
+  for (BatchGroup& G : b->groups) {
+    G.off_items = off;
+    off = align256(off + (G.members.size() + 1) * sizeof(int64_t));
+    G.off_kargs = off;
+    off = align256(off + G.members.size() * sizeof(KArgs));
+  }
+  b->off_prep = off;
+  off = align256(off + b->batched.size() * sizeof(PrepItem));
+  b->off_red = off;
+  off = align256(off + b->batched.size() * sizeof(RedItem));
+  b->off_ctr = off;
+  off = align256(off + std::max<size_t>(b->groups.size(), 1) * 8);
+  b->total = off;
+  return DMSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmsim_batch_create(int32_t n, const dmsim_walk_params* p, const dmsim_geometry* g,
+                       const dmsim_walk_outputs* o, const dmsim_batch_tuning* tuning,
+                       dmsim_batch** out, size_t* workspace_bytes) {
+  if (!out) return fail(DMSIM_EINVAL, "batch_create: out is null");
+  *out = nullptr;
+  if (n < 0 || (n > 0 && (!p || !g || !o))) return fail(DMSIM_EINVAL, "batch_create: bad arguments");
+  if (tuning && (tuning->blocks_per_sm < 0 || tuning->tiles_per_item < 0 || tuning->order < 0 ||
+                 tuning->order > 1 || tuning->tab_smem_bytes < 0 ||
+                 tuning->tab_smem_bytes > 200 * 1024))
+    return fail(DMSIM_EINVAL, "batch_create: bad tuning");
+  dmsim_batch* b = new dmsim_batch();
+  if (tuning) b->tune = *tuning;
+  else b->tune.concurrent_groups = 1;
+  if (cudaGetDevice(&b->device) != cudaSuccess) {
+    delete b;
+    return fail(DMSIM_ECUDA, "cudaGetDevice failed");
+  }
+  b->inst.resize(n);
+  for (int i = 0; i < n; ++i) {
+    BatchInst& I = b->inst[i];
+    I.p = p[i];
+    I.g = g[i];
+    I.o = o[i];
+    if (p[i].n_echo < 1 || p[i].n_echo > kMaxEcho || !p[i].echo_idx) {
+      delete b;
+      return fail(DMSIM_EINVAL, "batch instance %d: n_echo must be in [1, %d] with echo_idx", i,
+                  kMaxEcho);
+    }
+    I.echo.assign(p[i].echo_idx, p[i].echo_idx + p[i].n_echo);
+  }
+  const int rc = batch_plan(b);
+  if (rc != DMSIM_OK) {
+    delete b;
+    return rc;
+  }
+  if (b->tune.concurrent_groups && b->groups.size() > 1) {
+    const size_t n_side = std::min<size_t>(b->groups.size(), 4);
+    b->ev.resize(1 + n_side, nullptr);
+    bool ok = true;
+    for (auto& e : b->ev) ok &= cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    b->side.resize(n_side, nullptr);
+    for (auto& s : b->side) ok &= cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) {
+      dmsim_batch_destroy(b);
+      return fail(DMSIM_ECUDA, "batch_create: stream/event creation failed");
+    }
+  }
+  if (workspace_bytes) *workspace_bytes = b->total;
+  *out = b;
+  return DMSIM_OK;
+}
+
+int dmsim_batch_bind(dmsim_batch* b, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!b) return fail(DMSIM_EINVAL, "batch_bind: null plan");
+  if (!workspace || workspace_bytes < b->total)
+    return fail(DMSIM_EWORKSPACE, "batch workspace %zu B < required %zu B", workspace_bytes,
+                b->total);
+  if (((uintptr_t)workspace & 255) != 0)
+    return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
+  uint8_t* ws = static_cast<uint8_t*>(workspace);
+  b->blob.assign(b->off_ctr - b->off_tables, 0);
+  auto at = [&](size_t off) { return b->blob.data() + (off - b->off_tables); };
+  for (BatchGroup& G : b->groups) {
+    int64_t* starts = reinterpret_cast<int64_t*>(at(G.off_items));
+    KArgs* ka = reinterpret_cast<KArgs*>(at(G.off_kargs));
+    int64_t acc = 0;
+    for (size_t k = 0; k < G.members.size(); ++k) {
+      const BatchInst& I = b->inst[G.members[k]];
+      starts[k] = acc;
+      acc += I.n_items;
+      KArgs a;
+      fill_kargs(&I.p, &I.g, &I.o, I.pl, &a);
+      a.Cp = reinterpret_cast<const float*>(ws + I.off_cp);
+      a.Gp = reinterpret_cast<const float*>(ws + I.off_gp);
+      a.active = ws + I.off_act;
+      a.part = reinterpret_cast<double*>(ws + I.off_part);
+      a.pass = 0;
+      memcpy(&ka[k], &a, sizeof(KArgs));
+    }
+    starts[G.members.size()] = acc;
+  }
+  PrepItem* prep = reinterpret_cast<PrepItem*>(at(b->off_prep));
+  RedItem* red = reinterpret_cast<RedItem*>(at(b->off_red));
+  for (size_t k = 0; k < b->batched.size(); ++k) {
+    const BatchInst& I = b->inst[b->batched[k]];
+    PrepItem& P = prep[k];
+    P.V = I.p.basis_V;
+    P.C = I.p.basis_C;
+    P.Vp = reinterpret_cast<float*>(ws + I.off_gp);
+    P.act = ws + I.off_act;
+    P.Cp = reinterpret_cast<float*>(ws + I.off_cp);
+    P.n_t = I.p.n_t;
+    P.M = I.p.n_meas;
+    P.r = I.p.basis_rank;
+    P.rt = I.pl.width;
+    P.t_pad = I.pl.n_chunks * kTC;
+    RedItem& R = red[k];
+    R.part = reinterpret_cast<const double*>(ws + I.off_part);
+    R.sums = I.o.sums;
+    R.n_items = I.n_items;
+    R.n = I.p.n_echo * I.p.n_meas * 3;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!b->blob.empty() &&
+      cudaMemcpyAsync(ws + b->off_tables, b->blob.data(), b->blob.size(), cudaMemcpyHostToDevice,
+                      st) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "batch_bind: table upload failed");
+  if (cudaStreamSynchronize(st) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "batch_bind: %s", cudaGetErrorString(cudaGetLastError()));
+  b->ws = ws;
+  return DMSIM_OK;
+}
+
+int dmsim_batch_launch(const dmsim_batch* b, void* stream) {
+  if (!b || !b->ws) return fail(DMSIM_EINVAL, "batch_launch: plan is null or not bound");
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* ws = b->ws;
+  const int nb = (int)b->batched.size();
+  if (nb > 0) {
+    if (cudaMemsetAsync(ws + b->off_ctr, 0, b->groups.size() * 8, st) != cudaSuccess)
+      return fail(DMSIM_ECUDA, "batch_launch: counter reset failed");
+    k_prep_basis_batch<<<dim3(8, nb), 256, 0, st>>>(
+        reinterpret_cast<const PrepItem*>(ws + b->off_prep));
+  }
+  const bool fork = !b->side.empty();
+  if (fork && cudaEventRecord(b->ev[0], st) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "batch_launch: event record failed");
+  for (size_t s = 0; fork && s < b->side.size(); ++s)
+    if (cudaStreamWaitEvent(b->side[s], b->ev[0], 0) != cudaSuccess)
+      return fail(DMSIM_ECUDA, "batch_launch: stream wait failed");
+  KArgs none;
+  memset(&none, 0, sizeof(none));
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    const BatchGroup& G = b->groups[gi];
+    BatchCtl bc;
+    memset(&bc, 0, sizeof(bc));
+    bc.inst = reinterpret_cast<const KArgs*>(ws + G.off_kargs);
+    bc.item_start = reinterpret_cast<const int64_t*>(ws + G.off_items);
+    bc.n_inst = (int)G.members.size();
+    bc.max_m = G.max_m;
+    bc.tiles_per_item = b->tune.tiles_per_item > 0 ? b->tune.tiles_per_item : 1;
+    bc.total = G.n_items;
+    bc.counter = reinterpret_cast<unsigned long long*>(ws + b->off_ctr + 8 * gi);
+    cudaStream_t gs = fork ? b->side[gi % b->side.size()] : st;
+    G.fn<<<G.grid, kBlock, G.smem, gs>>>(none, bc);
+  }
+  for (const BatchInst& I : b->inst) {
+    if (I.batched) continue;
+    const int rc = launch_single(&I.p, &I.g, &I.o, I.pl, ws + I.off_ws, st);
+    if (rc != DMSIM_OK) return rc;
+  }
+  for (size_t s = 0; fork && s < b->side.size(); ++s) {
+    if (cudaEventRecord(b->ev[1 + s], b->side[s]) != cudaSuccess ||
+        cudaStreamWaitEvent(st, b->ev[1 + s], 0) != cudaSuccess)
+      return fail(DMSIM_ECUDA, "batch_launch: stream join failed");
+  }
+  if (nb > 0) {
+    int max_n = 1;
+    for (int k : b->batched) max_n = std::max(max_n, b->inst[k].p.n_echo * b->inst[k].p.n_meas * 3);
+    const int gx = std::min(64, (max_n + 255) / 256);
+    k_reduce_batch<<<dim3(gx, nb), 256, 0, st>>>(reinterpret_cast<const RedItem*>(ws + b->off_red));
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess)
+    return fail(DMSIM_ECUDA, "batch launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
+int dmsim_batch_info(const dmsim_batch* b, int32_t* n_groups, int32_t* n_single, int64_t* n_items,
+                     int32_t* n_kernels) {
+  if (!b) return fail(DMSIM_EINVAL, "batch_info: null plan");
+  int singles = 0, kern = 0;
+  int64_t items = 0;
+  for (const BatchInst& I : b->inst) {
+    if (I.batched) continue;
+    ++singles;
+    if (I.p.n_walkers > 0) kern += 2 + I.pl.n_pass;
+  }
+  for (const BatchGroup& G : b->groups) items += G.n_items;
+  if (!b->batched.empty()) kern += 2 + (int)b->groups.size();
+  if (n_groups) *n_groups = (int32_t)b->groups.size();
+  if (n_single) *n_single = singles;
+  if (n_items) *n_items = items;
+  if (n_kernels) *n_kernels = kern;
+  return DMSIM_OK;
+}
+
+void dmsim_batch_destroy(dmsim_batch* b) {
+  if (!b) return;
+  for (auto& s : b->side)
+    if (s) cudaStreamDestroy(s);
+  for (auto& e : b->ev)
+    if (e) cudaEventDestroy(e);
+  delete b;
 }
 
 }  // extern "C"

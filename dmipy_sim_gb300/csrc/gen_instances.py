@@ -1,0 +1,49 @@
+"""Writes the walk-kernel instantiation tables (walk_<kind>.cu, walk_batch_<kind>.cu).
+
+Each geometry gets one translation unit of single-instance variants (wall mode x phase form x
+cell list in shared memory) and one of batched variants (basis phase form only), so that the
+parallel build compiles them side by side.  Run after changing the variant set.
+"""
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+KINDS = [  # (file stem, enum, wall modes, has a cell list)
+    ("free", "DMSIM_GEOM_FREE", [0], False),
+    ("cyl", "DMSIM_GEOM_CYLINDER", [0, 1, 2], False),
+    ("sph", "DMSIM_GEOM_SPHERE", [0, 1, 2], False),
+    ("pcyl", "DMSIM_GEOM_PACKED_CYLINDERS", [0, 1, 2], True),
+    ("psph", "DMSIM_GEOM_PACKED_SPHERES", [0, 1, 2], True),
+    ("mesh", "DMSIM_GEOM_MESH", [0, 1, 2], False),
+]
+VARIANTS = [(0, 16), (0, 32), (0, 64), (1, 2), (1, 4), (1, 8)]  # (phase form, width)
+
+
+def _table(stem, enum, walls, packed, batch):
+    tsms = [False, True] if packed else [False]
+    fn = f"walk_{'batch_' if batch else ''}fn_{stem}"
+    what = "batched variants (basis phase form)" if batch else "wall mode x phase form (direct MT / basis RT) x cell list in shared memory"
+    lines = [f"// Instantiations of the walk kernel for {enum}: {what}.",
+             "// Written by gen_instances.py.",
+             '#include "walk_kernel.cuh"', "", "namespace dmsim {", "",
+             f"WalkFn {fn}(int wall, int pm, int width, bool tsm) {{"]
+    b = "true" if batch else "false"
+    for wall in walls:
+        for pm, width in VARIANTS:
+            if batch and pm == 0:
+                continue
+            for tsm in tsms:
+                t = "true" if tsm else "false"
+                lines.append(f"  if (wall == {wall} && pm == {pm} && width == {width} && tsm == {t}) "
+                             f"return k_walk<{enum}, {wall}, {pm}, {width}, {t}, {b}>;")
+    lines += ["  return nullptr;", "}", "", "}  // namespace dmsim", ""]
+    return "\n".join(lines)
+
+
+def main():
+    for stem, enum, walls, packed in KINDS:
+        (HERE / f"walk_{stem}.cu").write_text(_table(stem, enum, walls, packed, False))
+        (HERE / f"walk_batch_{stem}.cu").write_text(_table(stem, enum, walls, packed, True))
+
+
+if __name__ == "__main__":
+    main()

@@ -47,8 +47,6 @@ struct KArgs {
   GeoK g;
   MeshK mk;  // GEOM_MESH only
   uint32_t tab_cs_bytes, tab_cand_bytes;  // shared-memory staging sizes (multiples of 16 B)
-  uint32_t off_cs, off_red, off_tab;      // shared-memory offsets of C, the reduction scratch
-                                          // and the cell list (host-computed layout)
   const float* Cp;                        // basis mode: (M, 3, RT) coefficients
   const uint32_t* cs;
   const float4* cand;
@@ -57,7 +55,7 @@ struct KArgs {
   const uint8_t* active;    // this pass, (n_t): 1 where some g_m(t) != 0
   const float* chi;         // (n_t) or null
   const float* r0;          // (n_walkers, 3) or null
-  double* part;             // [gridDim.x][n_echo][Mp][3]
+  double* part;             // single: [gridDim.x][n_echo][Mp][3]; batched: [item][n_echo][M][3]
   uint32_t* status;
   float* final_pos;
   float* log_w;
@@ -69,6 +67,22 @@ struct KArgs {
   float* dlog_unit;
   float* comp_occ;
   int echo[kMaxEcho];
+};
+
+// Batched launch: a table of instances (one KArgs each, in global memory) walked by persistent
+// blocks that pull work items from a global counter.  A work item is up to `tiles_per_item`
+// consecutive walker tiles of one instance; item i belongs to the last instance whose
+// item_start <= i.  Each item owns one partial slice [n_echo][M][3] of its instance, so the
+// per-instance reduction runs in a fixed order whatever the schedule.
+struct BatchCtl {
+  const KArgs* inst;          // n_inst entries
+  const int64_t* item_start;  // n_inst + 1 prefix sums of work items per instance
+  int n_inst;
+  int max_m;                  // largest M of the batch (shared-memory layout)
+  int tiles_per_item;
+  int pad0;
+  int64_t total;              // total work items
+  unsigned long long* counter;
 };
 
 // ---- shared-memory async-copy helpers (bulk copy + mbarrier), bounded waits -------------------
@@ -135,6 +149,14 @@ __host__ __device__ inline SmemLayout walk_smem_layout(int pm, int w, int M) {
   return L;
 }
 
+// Resident blocks per SM the batched variants are compiled for (the register cap follows).
+#ifndef DMSIM_BATCH_MIN_BLOCKS
+#define DMSIM_BATCH_MIN_BLOCKS 2
+#endif
+__host__ __device__ constexpr int batch_min_blocks(int pm, int w) {
+  return (pm == 0 ? w <= 16 : w <= 4) ? DMSIM_BATCH_MIN_BLOCKS : 1;
+}
+
 template <int GEOM>
 __device__ __forceinline__ int classify(float x, float y, float z, const GeoK& g,
                                         const uint32_t* cs, const float4* cand,
@@ -166,40 +188,31 @@ __device__ __forceinline__ int classify_mesh(float x, float y, float z, const Me
   return mesh_classify(m, x, y, z, pop);
 }
 
-template <int GEOM, int WALL, int PM, int W, bool TSM>
-__global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a) {
+template <int GEOM, int WALL, int PM, int W, bool TSM, bool BATCH>
+__global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : 0) k_walk(const __grid_constant__ KArgs a0,
+                                                 const __grid_constant__ BatchCtl bc) {
   extern __shared__ __align__(128) uint8_t smem[];
   constexpr int ROW = walk_row(PM, W);
   constexpr int GCH = kTC * ROW;  // floats per waveform chunk
   constexpr int MT = PM ? 1 : W;  // measurements held per thread in the direct form
   float* Gs = reinterpret_cast<float*>(smem);
-  const SmemLayout lay = walk_smem_layout(PM, W, a.M);
+  const SmemLayout lay = walk_smem_layout(PM, W, BATCH ? bc.max_m : a0.M);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.off_bar);
   volatile int* s_abort = reinterpret_cast<volatile int*>(smem + lay.off_bar + 32);
   float* Cs = reinterpret_cast<float*>(smem + lay.off_cs);
   float* red = reinterpret_cast<float*>(smem + lay.off_red);
   uint8_t* tab = smem + lay.off_tab;
-  const int MR = PM ? a.M : W;  // measurements reduced per emission by this launch
+  volatile long long* s_item = reinterpret_cast<volatile long long*>(smem + lay.off_bar + 40);
 
   constexpr bool PACKED = GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool MESH = GEOM == DMSIM_GEOM_MESH;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const GeoK g = a.g;
-  // per-axis period used to unfold positions (packed: the cell side; mesh: the periodic box)
-  const float Lx = MESH ? a.mk.box[0] : g.L, Ly = MESH ? a.mk.box[1] : g.L,
-              Lz = MESH ? a.mk.box[2] : g.L;
 
-  const uint32_t* cs = a.cs;
-  const float4* cand = a.cand;
-  if constexpr (PACKED && TSM) {
-    cs = reinterpret_cast<const uint32_t*>(tab);
-    cand = reinterpret_cast<const float4*>(tab + a.tab_cs_bytes);
-  }
-
-  const int64_t n_tiles = (a.n_walkers + kBlock - 1) / kBlock;
-  const int my_tiles = (int)((n_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
-  const int64_t total_chunks = (int64_t)my_tiles * a.n_chunks;
+  // single-instance launches walk a static share of tiles; batched ones pull work items
+  const int64_t n_tiles0 = (a0.n_walkers + kBlock - 1) / kBlock;
+  const int my_tiles = BATCH ? 0 : (int)((n_tiles0 - blockIdx.x + gridDim.x - 1) / gridDim.x);
+  const int64_t total_chunks = (int64_t)my_tiles * a0.n_chunks;
   const uint32_t chunk_bytes = (uint32_t)GCH * 4u;
 
   if (tid == 0) {
@@ -209,42 +222,103 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     *s_abort = 0;
     fence_async_smem();
   }
-  // zero this block's partial slice for this pass; stage the basis coefficients
-  for (int e = 0; e < a.n_echo; ++e)
-    for (int j = tid; j < MR * 3; j += kBlock)
-      a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] = 0.0;
-  if constexpr (PM == 1)
-    for (int j = tid; j < a.M * 3 * W; j += kBlock) Cs[j] = a.Cp[j];
-  __syncthreads();
-  if (tid == 0) {
-    if constexpr (PACKED && TSM) {
-      mbar_expect(&bar[2], a.tab_cs_bytes + a.tab_cand_bytes);
-      bulk_g2s(tab, a.cs, a.tab_cs_bytes, &bar[2]);
-      if (a.tab_cand_bytes) bulk_g2s(tab + a.tab_cs_bytes, a.cand, a.tab_cand_bytes, &bar[2]);
-    }
-    if (total_chunks > 0) {
-      mbar_expect(&bar[0], chunk_bytes);
-      bulk_g2s(Gs, a.Gp, chunk_bytes, &bar[0]);
-    }
+  if constexpr (!BATCH) {
+    // zero this block's partial slice for this pass
+    for (int e = 0; e < a0.n_echo; ++e)
+      for (int j = tid; j < (PM ? a0.M : W) * 3; j += kBlock)
+        a0.part[((size_t)(blockIdx.x * a0.n_echo + e) * a0.Mp + a0.pass * MT) * 3 + j] = 0.0;
   }
-  if constexpr (PACKED && TSM) {
-    if (!mbar_wait(&bar[2], 0)) *s_abort = 1;
-    __syncthreads();
-    if (*s_abort) {
-      if (tid == 0) {
-        atomicAdd(&a.status[DMSIM_STATUS_WAIT_TIMEOUT], 1u);
-        if (total_chunks > 0) mbar_wait(&bar[0], 0);
-      }
-      return;
-    }
+  __syncthreads();
+  if (!BATCH && tid == 0 && total_chunks > 0) {
+    mbar_expect(&bar[0], chunk_bytes);
+    bulk_g2s(Gs, a0.Gp, chunk_bytes, &bar[0]);
   }
 
   Tally tl, tl_idle;  // tallies of real walkers / of the idle threads of the last tile
   uint32_t n_nonfinite = 0, n_initfail = 0, n_budget = 0, n_escape = 0, n_idle = 0;
-  int64_t q = 0;  // running chunk counter of this block
+  int64_t q = 0;      // running chunk counter of this block (parity of the chunk barriers)
+  uint32_t tabq = 0;  // staged cell lists so far (parity of the table barrier)
+  int cur_inst = -1;
 
-  for (int it = 0; it < my_tiles; ++it) {
-    const int64_t tile = blockIdx.x + (int64_t)it * gridDim.x;
+  int64_t tile = -1, tile_end = 0, item_local = 0;  // batched: current item's tile range
+  for (int it = 0;; ++it) {
+    // ---- next tile: the next of this work item, or the first of a new one ---------------------
+    int inst = 0;
+    bool fresh = false;
+    if constexpr (BATCH) {
+      inst = cur_inst < 0 ? 0 : cur_inst;
+      if (++tile >= tile_end) {
+        __syncthreads();
+        if (tid == 0) *s_item = (long long)atomicAdd(bc.counter, 1ull);
+        __syncthreads();
+        const int64_t item = *s_item;
+        if (item >= bc.total) break;
+        int lo = 0, hi = bc.n_inst;  // last instance whose first item <= item
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (bc.item_start[mid] <= item) lo = mid; else hi = mid;
+        }
+        inst = lo;
+        item_local = item - bc.item_start[inst];
+        const int64_t nt = (bc.inst[inst].n_walkers + kBlock - 1) / kBlock;
+        tile = item_local * bc.tiles_per_item;
+        tile_end = min(tile + (int64_t)bc.tiles_per_item, nt);
+        fresh = true;
+      }
+    } else {
+      if (it >= my_tiles) break;
+      tile = blockIdx.x + (int64_t)it * gridDim.x;
+    }
+    const KArgs* __restrict__ ap = BATCH ? bc.inst + inst : &a0;
+    const KArgs& a = *ap;
+    const GeoK g = a.g;
+    // per-axis period used to unfold positions (packed: the cell side; mesh: the periodic box)
+    const float Lx = MESH ? a.mk.box[0] : g.L, Ly = MESH ? a.mk.box[1] : g.L,
+                Lz = MESH ? a.mk.box[2] : g.L;
+    const int MR = PM ? a.M : W;  // measurements reduced per emission
+    const uint32_t* cs = a.cs;
+    const float4* cand = a.cand;
+    if constexpr (PACKED && TSM) {
+      cs = reinterpret_cast<const uint32_t*>(tab);
+      cand = reinterpret_cast<const float4*>(tab + a.tab_cs_bytes);
+    }
+    if (inst != cur_inst) {
+      // stage this instance's basis coefficients and cell list
+      if constexpr (PM == 1)
+        for (int j = tid; j < a.M * 3 * W; j += kBlock) Cs[j] = a.Cp[j];
+      if constexpr (PACKED && TSM) {
+        if (tid == 0) {
+          fence_async_smem();
+          mbar_expect(&bar[2], a.tab_cs_bytes + a.tab_cand_bytes);
+          bulk_g2s(tab, a.cs, a.tab_cs_bytes, &bar[2]);
+          if (a.tab_cand_bytes)
+            bulk_g2s(tab + a.tab_cs_bytes, a.cand, a.tab_cand_bytes, &bar[2]);
+        }
+        if (!mbar_wait(&bar[2], tabq & 1u)) *s_abort = 1;
+        ++tabq;
+      }
+      __syncthreads();
+      if (*s_abort) {
+        if (tid == 0) {
+          atomicAdd(&a.status[DMSIM_STATUS_WAIT_TIMEOUT], 1u);
+          if (!BATCH && total_chunks > 0) mbar_wait(&bar[0], 0);
+        }
+        return;
+      }
+      cur_inst = inst;
+    }
+    if constexpr (BATCH) {
+      if (fresh) {
+        // a work item zeroes its partial slice and starts its own waveform pipeline
+        double* pp = a.part + (size_t)item_local * a.n_echo * a.M * 3;
+        for (int j = tid; j < a.n_echo * a.M * 3; j += kBlock) pp[j] = 0.0;
+        if (tid == 0) {
+          fence_async_smem();
+          mbar_expect(&bar[q & 1], chunk_bytes);
+          bulk_g2s(Gs + (q & 1) * GCH, a.Gp, chunk_bytes, &bar[q & 1]);
+        }
+      }
+    }
     const int64_t w = tile * kBlock + tid;
     const bool act = w < a.n_walkers;
     const uint64_t gw = (uint64_t)(a.walker_offset + w);
@@ -359,9 +433,12 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
     for (int ch = 0; ch < a.n_chunks; ++ch, ++q) {
       // ---- waveform chunk pipeline: prefetch q+1, wait for q ----------------------------------
       __syncthreads();
-      if (tid == 0 && q + 1 < total_chunks) {
+      // prefetch the next chunk: of this tile, or (single instance) the next tile's first
+      const bool has_next =
+          (ch + 1 < a.n_chunks) || (BATCH ? tile + 1 < tile_end : q + 1 < total_chunks);
+      if (tid == 0 && has_next) {
         const int64_t qn = q + 1;
-        const int src_chunk = (int)(qn % a.n_chunks);
+        const int src_chunk = ch + 1 < a.n_chunks ? ch + 1 : 0;
         fence_async_smem();
         mbar_expect(&bar[qn & 1], chunk_bytes);
         bulk_g2s(Gs + (qn & 1) * GCH, a.Gp + (size_t)src_chunk * GCH, chunk_bytes, &bar[qn & 1]);
@@ -371,7 +448,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
       if (*s_abort) {
         if (tid == 0) {
           atomicAdd(&a.status[DMSIM_STATUS_WAIT_TIMEOUT], 1u);
-          if (q + 1 < total_chunks) mbar_wait(&bar[(q + 1) & 1], (uint32_t)(((q + 1) >> 1) & 1));
+          if (has_next) mbar_wait(&bar[(q + 1) & 1], (uint32_t)(((q + 1) >> 1) & 1));
         }
         return;
       }
@@ -541,7 +618,10 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
             double sacc = 0.0;
 #pragma unroll
             for (int ww = 0; ww < kWarps; ++ww) sacc += (double)red[ww * MR * 3 + j];
-            a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] += sacc;
+            if constexpr (BATCH)
+              a.part[((size_t)item_local * a.n_echo + e) * a.M * 3 + j] += sacc;
+            else
+              a.part[((size_t)(blockIdx.x * a.n_echo + e) * a.Mp + a.pass * MT) * 3 + j] += sacc;
           }
           __syncthreads();
           ++e;
@@ -582,9 +662,33 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
         }
       }
     }
+
+    if constexpr (BATCH) {
+      // flush the tallies into this instance's status words after each work item
+      const uint32_t b0 = __reduce_add_sync(0xffffffffu, n_nonfinite);
+      const uint32_t b1 = __reduce_add_sync(0xffffffffu, tl.clamp);
+      const uint32_t b2 = __reduce_add_sync(0xffffffffu, n_initfail);
+      const uint32_t b3 = __reduce_add_sync(0xffffffffu, tl.transmit);
+      const uint32_t b4 = __reduce_add_sync(0xffffffffu, n_budget);
+      const uint32_t b5 = __reduce_add_sync(0xffffffffu, n_escape);
+      const uint32_t b6 = __reduce_add_sync(0xffffffffu, tl.graze);
+      if (lane == 0 && a.pass == 0) {
+        if (b6) atomicAdd(&a.status[DMSIM_STATUS_GRAZE_FP64], b6);
+        if (b0) atomicAdd(&a.status[DMSIM_STATUS_NONFINITE], b0);
+        if (b1) atomicAdd(&a.status[DMSIM_STATUS_CLAMPED], b1);
+        if (b2) atomicAdd(&a.status[DMSIM_STATUS_INIT_FAIL], b2);
+        if (b3) atomicAdd(&a.status[DMSIM_STATUS_TRANSMIT], b3);
+        if (b4) atomicAdd(&a.status[DMSIM_STATUS_BOUNCE_BUDGET], b4);
+        if (b5) atomicAdd(&a.status[DMSIM_STATUS_ESCAPE_REJECT], b5);
+      }
+      n_nonfinite = n_initfail = n_budget = n_escape = 0;
+      tl.clamp = tl.transmit = tl.graze = 0;
+    }
   }
+  if constexpr (BATCH) return;
 
   // ---- anomaly tallies ------------------------------------------------------------------------
+  const KArgs& a = a0;
   const uint32_t v0 = __reduce_add_sync(0xffffffffu, n_nonfinite);
   const uint32_t v1 = __reduce_add_sync(0xffffffffu, tl.clamp);
   const uint32_t v2 = __reduce_add_sync(0xffffffffu, n_initfail);
@@ -603,6 +707,6 @@ __global__ void __launch_bounds__(kBlock) k_walk(const __grid_constant__ KArgs a
   }
 }
 
-using WalkFn = void (*)(KArgs);
+using WalkFn = void (*)(KArgs, BatchCtl);
 
 }  // namespace dmsim

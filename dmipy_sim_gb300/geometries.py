@@ -389,12 +389,16 @@ class _Packed(Geometry):
         ids = np.arange(1, len(self._radii_np) + 1, dtype=np.int32)
         return np.max(np.where(inside, ids, 0), axis=-1).astype(np.int32)
 
+    # Byte budget of the cell list (cell offsets + candidates): the grid is as fine as this
+    # allows.  Lists within the walk's shared-memory budget are staged on chip.
+    cell_list_bytes = 96 * 1024
+
     def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
         reach = float(step_length) * 1.05 + 8.0 * float(self._nudge)
-        key = (round(reach, 15), str(dev))
+        key = (round(reach, 15), str(dev), int(self.cell_list_bytes))
         if key not in self._dev_cache:
             n, start, cand, obj = build_cell_list(self._centers_np, self._radii_np, self._L_float,
-                                                  reach)
+                                                  reach, max_bytes=int(self.cell_list_bytes))
             t_start = torch.from_numpy(start.view(np.int32)).to(dev)
             t_cand = torch.from_numpy(cand).to(dev)
             t_obj = torch.from_numpy(obj if len(obj) else np.zeros(1, np.int32)).to(dev)

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 2
+#define DMSIM_ABI_VERSION 3
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -224,6 +224,111 @@ int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t 
                  const float* G, int32_t n_meas, float gamma_dt, const float* log_w,
                  double* sums, float* phi_out, void* workspace, size_t workspace_bytes,
                  void* stream);
+
+/* ---- batched walks ---------------------------------------------------------------------------
+   Many independent walks (instances: geometry, waveform, rho, kappa, n_walkers, n_t, seed each
+   their own) in one enqueue.  No counterpart in the reference, where each instance is one
+   simulate() call (core.py:193-762) and a study loops over them on the host.
+
+   Instances whose waveform comes as a shape basis (basis_rank > 0) are walked by persistent
+   kernels, one per (geometry kind, wall mode, basis width, cell list in shared memory) group,
+   whose blocks pull work items -- DMSIM_TILE_WALKERS x tiles_per_item walkers of one instance --
+   from a queue in device memory until it is empty; groups run on forked streams so the tail of
+   one overlaps the next.  Each work item owns a partial-sum slice, and a final kernel reduces
+   every instance's slices in a fixed order: the sums do not depend on the schedule, and an
+   instance gives exactly the sums a dmsim_walk() of the same parameters gives.  Instances
+   without a basis run as plain dmsim_walk() launches inside the same enqueue.
+
+   Lifecycle: dmsim_batch_create() validates and plans (host only; returns the workspace size),
+   dmsim_batch_bind() uploads the instance tables into the caller's workspace (once),
+   dmsim_batch_launch() enqueues the whole batch (asynchronous, no host synchronisation, no
+   allocation: capturable in a CUDA graph), dmsim_batch_destroy() frees the host plan.
+   Every device pointer of the p / g / o arrays must stay valid while the plan is in use (their
+   contents may change between launches); echo_idx is read at create time. */
+#define DMSIM_TILE_WALKERS 320
+
+typedef struct dmsim_batch_tuning {
+  int32_t blocks_per_sm;     /* resident blocks per SM of each persistent grid; 0 = occupancy max */
+  int32_t tiles_per_item;    /* walker tiles per work item; 0 = 1                               */
+  int32_t order;             /* 0 = the given instance order; 1 = costliest instances first     */
+  int32_t concurrent_groups; /* 1 = groups on forked streams; 0 = one after another            */
+  int64_t tab_smem_bytes;    /* cell lists up to this size are staged in shared memory; 0 = 96 KiB */
+} dmsim_batch_tuning;
+
+typedef struct dmsim_batch dmsim_batch; /* opaque host-side plan */
+
+int dmsim_batch_create(int32_t n, const dmsim_walk_params* p, const dmsim_geometry* g,
+                       const dmsim_walk_outputs* o, const dmsim_batch_tuning* tuning,
+                       dmsim_batch** out, size_t* workspace_bytes);
+int dmsim_batch_bind(dmsim_batch* b, void* workspace, size_t workspace_bytes, void* stream);
+int dmsim_batch_launch(const dmsim_batch* b, void* stream);
+/* Plan summary: persistent kernel groups, instances on the plain path, work items, and the
+   kernels one dmsim_batch_launch() enqueues. */
+int dmsim_batch_info(const dmsim_batch* b, int32_t* n_groups, int32_t* n_single, int64_t* n_items,
+                     int32_t* n_kernels);
+void dmsim_batch_destroy(dmsim_batch* b);
+
+/* ---- surrogate MLP ---------------------------------------------------------------------------
+   Building blocks of the learned surrogate (an MLP from substrate parameters and a waveform
+   encoding to the signal).  No counterpart in the reference.  The GEMM runs on the tcgen05 tensor
+   cores: C[M, N] = A[M, K] . B[N, K]^T with A, B row-major bf16 (K contiguous), fp32
+   accumulation in tensor memory, and one of these fused epilogues:
+     STORE_F32  C (M, N) fp32; with `splits` > 1, split s of K writes C + s*M*N;
+     BIAS_GELU  P = acc + bias[n] (fp32, stored when P is given), H = gelu(P) as bf16 (M, N) and,
+                when HT is given, its transpose (N, ldht);
+     GELU_BWD   H = acc * gelu'(P[m, n]) as bf16 (M, N) (+ transpose), P read-only (M, N) fp32.
+   GELU is x * Phi(x) with the exact normal CDF.  N must be a multiple of 128, K of 64;
+   row strides are in elements.  `err` is a device word incremented by a CTA whose bounded waits
+   gave up (zero after a healthy run). */
+#define DMSIM_EPI_STORE_F32 0
+#define DMSIM_EPI_BIAS_GELU 1
+#define DMSIM_EPI_GELU_BWD 2
+
+typedef struct dmsim_gemm {
+  const void* A;  /* bf16 (M, lda) */
+  const void* B;  /* bf16 (N, ldb) */
+  int64_t M;
+  int32_t N, K;
+  int64_t lda, ldb;
+  int32_t epilogue;
+  int32_t splits;
+  float* C;
+  const float* bias;
+  float* P;
+  void* H;   /* bf16 (M, N) */
+  void* HT;  /* bf16 (N, ldht) or NULL */
+  int64_t ldht;
+  uint32_t* err;
+} dmsim_gemm;
+
+int dmsim_gemm_bf16(const dmsim_gemm* g, void* stream);
+
+/* Input packing: out[r, c] = bf16((x[r, c] - shift[c]) * scale[c]) for c < features, 0 up to kp;
+   out_t (kp, ldt) is the optional transpose.  shift / scale may be NULL. */
+int dmsim_mlp_pack(const float* x, int64_t rows, int32_t features, int32_t kp, const float* shift,
+                   const float* scale, void* out, void* out_t, int64_t ldt, void* stream);
+
+/* Linear head y = H w + b over the last hidden layer H (rows, n) bf16.  With a target: the
+   squared-error gradient dy = 2 (y - target) / rows, sqerr = (y - target)^2 and the seed
+   gradient dP = dy * w * gelu'(P) of the last layer (bf16 (rows, n) and optional transpose). */
+int dmsim_mlp_head(const void* H, int64_t rows, int32_t n, const float* w, const float* b,
+                   float* y, const float* target, float* dy, float* sqerr, const float* P,
+                   void* dP, void* dP_t, int64_t ldt, void* stream);
+
+/* out[i] = sum_j X[i, j] * v[j] (v NULL: plain row sums) over bf16 X (rows, ld); fixed order. */
+int dmsim_rowdot_bf16(const void* X, int64_t rows, int64_t cols, int64_t ld, const float* v,
+                      float* out, void* stream);
+
+/* out[0] = sum of x[0..n) in a fixed order (FP64 accumulation). */
+int dmsim_sum_f32(const float* x, int64_t n, float* out, void* stream);
+
+/* AdamW (decoupled weight decay) on fp32 master weights p with moments m, v; the gradient is the
+   sum of `splits` consecutive partial buffers of n values.  hp (device) = [lr, beta1, beta2, eps,
+   weight_decay, step]; dmsim_adam_advance adds 1 to the step.  W (rows, cols) and WT (cols, rows)
+   receive the bf16 copies when given. */
+int dmsim_adamw(float* p, float* m, float* v, const float* grad, int32_t splits, int64_t n,
+                int32_t cols, const float* hp, void* W, void* WT, int32_t rows, void* stream);
+int dmsim_adam_advance(float* hp, void* stream);
 
 #ifdef __cplusplus
 }

@@ -48,7 +48,9 @@ def _c_layout(struct, fields):
 
 @pytest.mark.parametrize("cname,pyname", [("dmsim_geometry", "Geometry"),
                                           ("dmsim_walk_params", "WalkParams"),
-                                          ("dmsim_walk_outputs", "WalkOutputs")])
+                                          ("dmsim_walk_outputs", "WalkOutputs"),
+                                          ("dmsim_batch_tuning", "BatchTuning"),
+                                          ("dmsim_gemm", "Gemm")])
 def test_struct_layout_matches_header(cname, pyname):
     from dmipy_sim_gb300 import _lib
     py = getattr(_lib, pyname)
