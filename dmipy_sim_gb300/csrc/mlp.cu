@@ -1,0 +1,618 @@
+// Surrogate MLP kernels: a BF16 tensor-core GEMM (tcgen05.mma, accumulator in tensor memory,
+// operands staged by TMA) with fused epilogues, plus the small kernels around it (input packing,
+// the linear head with the squared-error seed gradient, row reductions, AdamW).
+//
+// GEMM: C[M, N] = A[M, K] . B[N, K]^T, A and B row-major bf16 (K contiguous, "K-major" for the
+// tensor core).  One CTA computes a 128 x BN tile (BN = 128 or 256 accumulator columns of tensor
+// memory) over its share of K:
+//   warp 0      TMA producer: 64-wide K slices of A and B into a ring of shared-memory stages
+//               (128-byte swizzle), one mbarrier per stage;
+//   warp 1      allocates the tensor memory, and one lane issues tcgen05.mma (K = 16 per
+//               instruction, 4 per stage); tcgen05.commit frees each stage and finally signals
+//               the accumulator;
+//   warps 2..5  epilogue: tcgen05.ld of 32 accumulator columns at a time (each warp owns the 32
+//               tensor-memory lanes = tile rows its warp index selects), fused bias / GELU /
+//               GELU-derivative, and stores of the row-major result and, optionally, its
+//               transpose (a warp writes 32 consecutive rows of one column: 64 contiguous bytes).
+// Every mbarrier wait is bounded; a wait that gives up sets an error word and the CTA drains,
+// frees its tensor memory and exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "dmsim.h"
+
+namespace dmsim {
+int set_error(int code, const char* msg);
+}
+
+namespace {
+
+constexpr int BM = 128;      // tile rows (tensor-memory lanes)
+constexpr int BK = 64;       // K slice per stage: 64 bf16 = 128 bytes = one swizzle row
+constexpr int kThreads = 192;
+constexpr uint32_t kWaitPolls = 1u << 24;
+
+// ---- PTX helpers --------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t s_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bar_init(uint64_t* b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_expect(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(s_addr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitPolls; ++i)
+    if (bar_try(b, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3}], [%4];" ::"r"(s_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(s_addr(b))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   s_addr(b))
+               : "memory");
+}
+// Shared-memory matrix descriptor of a K-major, 128-byte-swizzled tile whose rows are 128 bytes
+// apart and whose 8-row groups are 1024 bytes apart (the layout a TMA box of 64 bf16 columns with
+// CU_TENSOR_MAP_SWIZZLE_128B writes).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);        // start address
+  d |= (uint64_t)1 << 16;                       // leading byte offset (unused when swizzled)
+  d |= (uint64_t)(1024 >> 4) << 32;             // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                       // descriptor version
+  d |= (uint64_t)2 << 61;                       // 128-byte swizzle
+  return d;
+}
+// Instruction descriptor of kind::f16: bf16 A and B, fp32 accumulator, both K-major, M x N.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+  return (1u << 4)                    // accumulator format: f32
+         | (1u << 7)                  // A format: bf16
+         | (1u << 10)                 // B format: bf16
+         | ((uint32_t)(N >> 3) << 17)  // N / 8
+         | ((uint32_t)(M >> 4) << 24); // M / 16
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// GELU with the exact normal CDF, and its derivative.
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+struct GemmArgs {
+  int64_t M;
+  int N, K, k_per_split, epi;
+  float* C;
+  const float* bias;
+  float* P;
+  __nv_bfloat16* H;
+  __nv_bfloat16* HT;
+  int64_t ldht;
+  unsigned int* err;
+};
+
+template <int BN, int STAGES>
+struct GemmSmem {
+  static constexpr uint32_t kA = BM * BK * 2;
+  static constexpr uint32_t kB = BN * BK * 2;
+  static constexpr uint32_t kStage = kA + kB;
+  static constexpr uint32_t kBars = 1024;  // barriers + tensor-memory address, then 1 KB align
+  static constexpr uint32_t kTotal = STAGES * kStage + kBars + 1024;
+};
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+           const GemmArgs g) {
+  using L = GemmSmem<BN, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte alignment for the swizzled stages
+  uint8_t* smem = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_bar = empty + STAGES;
+  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(acc_bar + 1);
+  volatile uint32_t* abort_flag = tmem_slot + 1;
+  volatile int* consumed = reinterpret_cast<volatile int*>(tmem_slot + 2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  const int n0 = blockIdx.y * BN;
+  const int kb = blockIdx.z * g.k_per_split;
+  const int n_k = g.k_per_split / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      bar_init(&full[s], 1);
+      bar_init(&empty[s], 1);
+    }
+    bar_init(acc_bar, 1);
+    *abort_flag = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     s_addr((const void*)tmem_slot)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int issued = 0;  // warp 0 lane 0: stages whose loads were issued
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int k = 0; k < n_k && !*abort_flag; ++k) {
+        const int s = k % STAGES;
+        if (!bar_wait(&empty[s], ((k / STAGES) & 1) ^ 1)) {
+          *abort_flag = 1;
+          break;
+        }
+        uint8_t* sa = smem + s * L::kStage;
+        bar_expect(&full[s], L::kStage);
+        tma_load_2d(sa, &map_a, kb + k * BK, (int)m0, &full[s]);
+        tma_load_2d(sa + L::kA, &map_b, kb + k * BK, n0, &full[s]);
+        issued = k + 1;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = instr_desc(BM, BN);
+      bool ok = true;
+      for (int k = 0; k < n_k && ok; ++k) {
+        const int s = k % STAGES;
+        if (!bar_wait(&full[s], (k / STAGES) & 1)) {
+          *abort_flag = 1;
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = s_addr(smem + s * L::kStage);
+        const uint32_t b0 = a0 + L::kA;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk)
+          mma_bf16(tmem, smem_desc(a0 + kk * 32), smem_desc(b0 + kk * 32), idesc,
+                   (k > 0 || kk > 0) ? 1u : 0u);
+        tc_commit(&empty[s]);
+        *consumed = k + 1;
+      }
+      tc_commit(acc_bar);  // also after an abort: signals when the issued MMAs are done
+    }
+  } else {
+    // epilogue warps 2..5: tensor-memory lanes 32 * (warp % 4) .. + 31
+    const int q = warp & 3;
+    const int64_t row = m0 + q * 32 + lane;
+    const bool ok = bar_wait(acc_bar, 0);
+    tc_fence_after();
+    if (!ok) {
+      *abort_flag = 1;
+    } else if (!*abort_flag) {
+      const bool in = row < g.M;
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        const int col0 = n0 + c0;
+        if (g.epi == DMSIM_EPI_STORE_F32) {
+          if (in) {
+            float* dst = g.C + ((size_t)blockIdx.z * g.M + row) * g.N + col0;
+#pragma unroll
+            for (int i = 0; i < 32; i += 4)
+              *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+          }
+          continue;
+        }
+        if (g.epi == DMSIM_EPI_BIAS_GELU) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const float p = v[i] + __ldg(g.bias + col0 + i);
+            if (in && g.P) g.P[(size_t)row * g.N + col0 + i] = p;
+            v[i] = gelu(p);
+          }
+        } else {  // DMSIM_EPI_GELU_BWD
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            v[i] = in ? v[i] * gelu_grad(g.P[(size_t)row * g.N + col0 + i]) : 0.f;
+        }
+        if (in) {
+          __nv_bfloat16* dst = g.H + (size_t)row * g.N + col0;
+#pragma unroll
+          for (int i = 0; i < 32; i += 8) {
+            uint4 pk;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(v[i], v[i + 1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(v[i + 2], v[i + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(v[i + 4], v[i + 5]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(v[i + 6], v[i + 7]);
+            pk.x = *reinterpret_cast<uint32_t*>(&h0);
+            pk.y = *reinterpret_cast<uint32_t*>(&h1);
+            pk.z = *reinterpret_cast<uint32_t*>(&h2);
+            pk.w = *reinterpret_cast<uint32_t*>(&h3);
+            *reinterpret_cast<uint4*>(dst + i) = pk;
+          }
+          if (g.HT) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i)
+              g.HT[(size_t)(col0 + i) * g.ldht + row] = __float2bfloat16_rn(v[i]);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (*abort_flag) {
+    // drain before leaving: the loads still in flight, then the issued MMAs (bounded waits)
+    if (threadIdx.x == 0) {
+      atomicAdd(g.err, 1u);
+      for (int k = *consumed; k < issued; ++k) bar_wait(&full[k % STAGES], (k / STAGES) & 1);
+    }
+    if (warp == 1 && lane == 0) bar_wait(acc_bar, 0);
+    __syncthreads();
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN)
+                 : "memory");
+  }
+}
+
+// ---- small kernels ------------------------------------------------------------------------------
+// Inputs (rows, F) fp32 -> (x - shift) * scale as bf16 (rows, Kp), zero padded; optional
+// transpose (Kp, ldt).
+__global__ void k_pack(const float* __restrict__ x, int64_t rows, int F, int Kp,
+                       const float* __restrict__ shift, const float* __restrict__ scale,
+                       __nv_bfloat16* __restrict__ out, __nv_bfloat16* __restrict__ outT,
+                       int64_t ldt) {
+  const int64_t n = rows * Kp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / Kp;
+    const int c = (int)(i % Kp);
+    float v = 0.f;
+    if (c < F) v = (x[r * F + c] - (shift ? shift[c] : 0.f)) * (scale ? scale[c] : 1.f);
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    out[i] = b;
+    if (outT) outT[(size_t)c * ldt + r] = b;
+  }
+}
+
+// Linear head y = H w + b (one warp per row; fp32 accumulation in a fixed lane order).  With a
+// target: dy = 2 (y - t) / rows, the row's squared error in sqerr, and the seed gradient of the
+// last hidden layer dP = dy * w * gelu'(P) as bf16 (rows, N) and transposed (N, ldt).
+__global__ void k_head(const __nv_bfloat16* __restrict__ H, int64_t rows, int N,
+                       const float* __restrict__ w, const float* __restrict__ b,
+                       float* __restrict__ y, const float* __restrict__ target,
+                       float* __restrict__ dy, float* __restrict__ sqerr,
+                       const float* __restrict__ P, __nv_bfloat16* __restrict__ dP,
+                       __nv_bfloat16* __restrict__ dPT, int64_t ldt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); r < rows;
+       r += warps) {
+    float acc = 0.f;
+    for (int c = lane; c < N; c += 32) acc = fmaf(__bfloat162float(H[r * N + c]), w[c], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const float yr = acc + b[0];
+    if (lane == 0 && y) y[r] = yr;
+    if (!target) continue;
+    const float e = yr - target[r];
+    const float g = 2.f * e / (float)rows;
+    if (lane == 0) {
+      if (dy) dy[r] = g;
+      if (sqerr) sqerr[r] = e * e;
+    }
+    for (int c = lane; c < N; c += 32) {
+      const __nv_bfloat16 v = __float2bfloat16_rn(g * w[c] * gelu_grad(P[r * N + c]));
+      dP[r * N + c] = v;
+      if (dPT) dPT[(size_t)c * ldt + r] = v;
+    }
+  }
+}
+
+// out[i] = sum_j X[i, j] * (v ? v[j] : 1) over a bf16 row-major (rows, cols) matrix: one block
+// per row, fixed-order tree reduction.
+__global__ void k_rowdot(const __nv_bfloat16* __restrict__ X, int64_t rows, int64_t cols,
+                         int64_t ld, const float* __restrict__ v, float* __restrict__ out) {
+  __shared__ float red[32];
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    float acc = 0.f;
+    for (int64_t c = threadIdx.x; c < cols; c += blockDim.x)
+      acc = fmaf(__bfloat162float(X[r * ld + c]), v ? v[c] : 1.f, acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      float s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0) out[r] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// AdamW on fp32 master weights; the gradient is the sum of `splits` partial buffers of n values.
+// Refreshes the bf16 copies W (rows, cols) and, if given, WT (cols, rows).
+// Hyper-parameters come from device memory hp = [lr, beta1, beta2, eps, weight_decay, step], so
+// a captured training step needs no host update (k_adam_advance bumps the step).
+__global__ void k_adamw(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                        const float* __restrict__ grad, int splits, int64_t n, int cols,
+                        const float* __restrict__ hp, __nv_bfloat16* __restrict__ W,
+                        __nv_bfloat16* __restrict__ WT, int rows) {
+  const float lr = hp[0], b1 = hp[1], b2 = hp[2], eps = hp[3], wd = hp[4], step = hp[5];
+  const float bc1 = 1.f - powf(b1, step), bc2 = 1.f - powf(b2, step);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float gsum = 0.f;
+    for (int s = 0; s < splits; ++s) gsum += grad[(size_t)s * n + i];
+    const float mi = b1 * m[i] + (1.f - b1) * gsum;
+    const float vi = b2 * v[i] + (1.f - b2) * gsum * gsum;
+    m[i] = mi;
+    v[i] = vi;
+    const float upd = (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    const float pi = p[i] * (1.f - lr * wd) - lr * upd;
+    p[i] = pi;
+    if (W) {
+      const __nv_bfloat16 bv = __float2bfloat16_rn(pi);
+      W[i] = bv;
+      if (WT) {
+        const int64_t r = i / cols, c = i % cols;
+        WT[c * rows + r] = bv;
+      }
+    }
+  }
+}
+
+__global__ void k_adam_advance(float* hp) { hp[5] += 1.f; }
+
+// Fixed-order sum of n fp32 values (one block).
+__global__ void k_sum(const float* __restrict__ x, int64_t n, float* __restrict__ out) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += (double)x[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[0] = (float)s;
+  }
+}
+
+// ---- host side ----------------------------------------------------------------------------------
+thread_local char g_msg[256];
+
+int err(int code, const char* what) {
+  snprintf(g_msg, sizeof(g_msg), "%s", what);
+  return dmsim::set_error(code, g_msg);
+}
+
+using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                              const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                              const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn encode_fn() {
+  static EncodeFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeFn>(p);
+  });
+  return fn;
+}
+
+// 2-D bf16 tensor map over a row-major (rows, cols) matrix with row stride ld elements; box of
+// 64 columns x box_rows rows, 128-byte swizzle, zero fill out of bounds.
+bool make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld,
+              int box_rows) {
+  EncodeFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, int STAGES>
+int launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, const GemmArgs& a, int64_t M, int N,
+                int splits, cudaStream_t st) {
+  using L = GemmSmem<BN, STAGES>;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute((const void*)k_gemm<BN, STAGES>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kTotal) !=
+        cudaSuccess)
+      return err(DMSIM_ECUDA, "gemm: cudaFuncSetAttribute failed");
+    attr = true;
+  }
+  dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)(N / BN), (unsigned)splits);
+  k_gemm<BN, STAGES><<<grid, kThreads, L::kTotal, st>>>(ma, mb, a);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return err(DMSIM_ECUDA, cudaGetErrorString(e));
+  return DMSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmsim_gemm_bf16(const dmsim_gemm* g, void* stream) {
+  if (!g || !g->A || !g->B || !g->err) return err(DMSIM_EINVAL, "gemm: null argument");
+  if (g->M < 1 || g->N < 128 || g->N % 128 || g->K < BK || g->K % BK)
+    return err(DMSIM_EINVAL, "gemm: need M >= 1, N a multiple of 128, K a multiple of 64");
+  if (g->lda < g->K || g->ldb < g->K || g->lda % 8 || g->ldb % 8)
+    return err(DMSIM_EINVAL, "gemm: row strides must be >= K and multiples of 8 elements");
+  if (((uintptr_t)g->A & 15) || ((uintptr_t)g->B & 15))
+    return err(DMSIM_EINVAL, "gemm: A and B must be 16-byte aligned");
+  const int splits = g->splits > 0 ? g->splits : 1;
+  if ((g->K / BK) % splits) return err(DMSIM_EINVAL, "gemm: K / 64 must divide by splits");
+  if (g->epilogue == DMSIM_EPI_STORE_F32) {
+    if (!g->C) return err(DMSIM_EINVAL, "gemm: STORE_F32 needs C");
+  } else if (g->epilogue == DMSIM_EPI_BIAS_GELU || g->epilogue == DMSIM_EPI_GELU_BWD) {
+    if (splits != 1) return err(DMSIM_EINVAL, "gemm: only STORE_F32 splits K");
+    if (!g->H || ((uintptr_t)g->H & 15)) return err(DMSIM_EINVAL, "gemm: H missing or unaligned");
+    if (g->epilogue == DMSIM_EPI_BIAS_GELU && !g->bias) return err(DMSIM_EINVAL, "gemm: no bias");
+    if (g->epilogue == DMSIM_EPI_GELU_BWD && !g->P) return err(DMSIM_EINVAL, "gemm: no P");
+    if (g->HT && g->ldht < g->M) return err(DMSIM_EINVAL, "gemm: ldht < M");
+  } else {
+    return err(DMSIM_EINVAL, "gemm: unknown epilogue");
+  }
+  const int BN = (g->N % 256 == 0) ? 256 : 128;
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, g->A, g->M, g->K, g->lda, BM) || !make_map(&mb, g->B, g->N, g->K, g->ldb, BN))
+    return err(DMSIM_ECUDA, "gemm: tensor map encoding failed");
+  GemmArgs a;
+  a.M = g->M;
+  a.N = g->N;
+  a.K = g->K;
+  a.k_per_split = g->K / splits;
+  a.epi = g->epilogue;
+  a.C = g->C;
+  a.bias = g->bias;
+  a.P = g->P;
+  a.H = static_cast<__nv_bfloat16*>(g->H);
+  a.HT = static_cast<__nv_bfloat16*>(g->HT);
+  a.ldht = g->ldht;
+  a.err = g->err;
+  cudaStream_t st = (cudaStream_t)stream;
+  return BN == 256 ? launch_gemm<256, 4>(ma, mb, a, g->M, g->N, splits, st)
+                   : launch_gemm<128, 6>(ma, mb, a, g->M, g->N, splits, st);
+}
+
+int dmsim_mlp_pack(const float* x, int64_t rows, int32_t features, int32_t kp, const float* shift,
+                   const float* scale, void* out, void* out_t, int64_t ldt, void* stream) {
+  if (!x || !out || rows < 0 || features < 1 || kp < features || (out_t && ldt < rows))
+    return err(DMSIM_EINVAL, "mlp_pack: bad arguments");
+  if (rows == 0) return DMSIM_OK;
+  k_pack<<<1024, 256, 0, (cudaStream_t)stream>>>(x, rows, features, kp, shift, scale,
+                                                  static_cast<__nv_bfloat16*>(out),
+                                                  static_cast<__nv_bfloat16*>(out_t), ldt);
+  return cudaGetLastError() == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, "mlp_pack launch");
+}
+
+int dmsim_mlp_head(const void* H, int64_t rows, int32_t n, const float* w, const float* b,
+                   float* y, const float* target, float* dy, float* sqerr, const float* P,
+                   void* dP, void* dP_t, int64_t ldt, void* stream) {
+  if (!H || !w || !b || rows < 0 || n < 1 || (target && (!P || !dP)) || (dP_t && ldt < rows))
+    return err(DMSIM_EINVAL, "mlp_head: bad arguments");
+  if (rows == 0) return DMSIM_OK;
+  int blocks = (int)((rows + 7) / 8);
+  if (blocks > 4096) blocks = 4096;
+  k_head<<<blocks, 256, 0, (cudaStream_t)stream>>>(
+      static_cast<const __nv_bfloat16*>(H), rows, n, w, b, y, target, dy, sqerr, P,
+      static_cast<__nv_bfloat16*>(dP), static_cast<__nv_bfloat16*>(dP_t), ldt);
+  return cudaGetLastError() == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, "mlp_head launch");
+}
+
+int dmsim_rowdot_bf16(const void* X, int64_t rows, int64_t cols, int64_t ld, const float* v,
+                      float* out, void* stream) {
+  if (!X || !out || rows < 0 || cols < 0 || ld < cols)
+    return err(DMSIM_EINVAL, "rowdot: bad arguments");
+  if (rows == 0) return DMSIM_OK;
+  const int blocks = (int)(rows < 65535 ? rows : 65535);
+  k_rowdot<<<blocks, 256, 0, (cudaStream_t)stream>>>(static_cast<const __nv_bfloat16*>(X), rows,
+                                                      cols, ld, v, out);
+  return cudaGetLastError() == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, "rowdot launch");
+}
+
+int dmsim_adamw(float* p, float* m, float* v, const float* grad, int32_t splits, int64_t n,
+                int32_t cols, const float* hp, void* W, void* WT, int32_t rows, void* stream) {
+  if (!p || !m || !v || !grad || !hp || n < 0 || splits < 1 || cols < 1 ||
+      (W && (int64_t)rows * cols != n))
+    return err(DMSIM_EINVAL, "adamw: bad arguments");
+  if (n == 0) return DMSIM_OK;
+  k_adamw<<<512, 256, 0, (cudaStream_t)stream>>>(p, m, v, grad, splits, n, cols, hp,
+                                                  static_cast<__nv_bfloat16*>(W),
+                                                  static_cast<__nv_bfloat16*>(WT), rows);
+  return cudaGetLastError() == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, "adamw launch");
+}
+
+int dmsim_adam_advance(float* hp, void* stream) {
+  if (!hp) return err(DMSIM_EINVAL, "adam_advance: null");
+  k_adam_advance<<<1, 1, 0, (cudaStream_t)stream>>>(hp);
+  return cudaGetLastError() == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, "adam_advance launch");
+}
+
+int dmsim_sum_f32(const float* x, int64_t n, float* out, void* stream) {
+  if (!x || !out || n < 0) return err(DMSIM_EINVAL, "sum_f32: bad arguments");
+  k_sum<<<1, 1024, 0, (cudaStream_t)stream>>>(x, n, out);
+  return cudaGetLastError() == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, "sum_f32 launch");
+}
+
+}  // extern "C"
