@@ -12,6 +12,7 @@ The walk itself (``mesh.py`` reflect 637-671 / reflect_with_log_weight 673-705 /
 707-743 / classify 227-254 / leak guard 578-597) runs in the CUDA kernels; seeding draws uniform
 points in the box and keeps those whose ray-crossing parity says inside (or outside), on the GPU.
 """
+import copy
 import itertools
 import struct
 import warnings
@@ -160,13 +161,51 @@ def icosphere(radius, subdivisions=2):
     return V, F
 
 
-def random_ellipsoid_cells(n_cells, box, radius_range, subdivisions=3, seed=0, max_tries=20000):
+def uv_sphere(radius, n_lat, n_lon):
+    """Latitude-longitude sphere: two poles and n_lat - 1 rings of n_lon vertices, 2 n_lon
+    (n_lat - 1) outward-oriented triangles."""
+    th = np.pi * np.arange(1, n_lat) / n_lat
+    ph = 2.0 * np.pi * np.arange(n_lon) / n_lon
+    ring = np.stack([np.sin(th)[:, None] * np.cos(ph)[None, :],
+                     np.sin(th)[:, None] * np.sin(ph)[None, :],
+                     np.repeat(np.cos(th)[:, None], n_lon, axis=1)], axis=-1).reshape(-1, 3)
+    V = np.concatenate([[[0.0, 0.0, 1.0]], ring, [[0.0, 0.0, -1.0]]])
+    south = len(V) - 1
+
+    def vid(i, j):
+        return 1 + i * n_lon + (j % n_lon)
+    F = []
+    for j in range(n_lon):
+        F.append((0, vid(0, j), vid(0, j + 1)))
+        F.append((south, vid(n_lat - 2, j + 1), vid(n_lat - 2, j)))
+        for i in range(n_lat - 2):
+            a, b = vid(i, j), vid(i, j + 1)
+            c, d = vid(i + 1, j), vid(i + 1, j + 1)
+            F.append((a, c, d))
+            F.append((a, d, b))
+    F = np.asarray(F, np.int64)
+    tri = V[F]
+    out = np.einsum("ij,ij->i", np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]),
+                    tri.sum(1)) < 0
+    F[out] = F[out][:, [0, 2, 1]]
+    return V * radius, F
+
+
+def random_ellipsoid_cells(n_cells, box, radius_range, subdivisions=3, seed=0, max_tries=20000,
+                           faces_per_cell=None):
     """A substrate of ``n_cells`` closed ellipsoidal cells placed without overlap inside the cubic
     box [-box/2, box/2)^3 (a margin from every face, so each surface stays closed), with random
-    semi-axes in ``radius_range`` and random orientations.  Returns ``(V, F)``."""
+    semi-axes in ``radius_range`` and random orientations.  Each cell is an icosphere of the
+    given subdivision level, or, with ``faces_per_cell``, a latitude-longitude sphere of about
+    that many triangles.  Returns ``(V, F)``."""
     rng = np.random.default_rng(int(seed))
     Vs, Fs, cent, bound = [], [], [], []
-    base_V, base_F = icosphere(1.0, subdivisions)
+    if faces_per_cell:
+        n_lat = max(3, int(round(np.sqrt(faces_per_cell / 4.0))))
+        n_lon = max(3, int(round(faces_per_cell / (2.0 * (n_lat - 1)))))
+        base_V, base_F = uv_sphere(1.0, n_lat, n_lon)
+    else:
+        base_V, base_F = icosphere(1.0, subdivisions)
     off = 0
     for _ in range(max_tries):
         if len(cent) == n_cells:
@@ -363,6 +402,17 @@ class Mesh(Geometry):
         self._MAX_BOUNCES = int(max_bounces)
         self._closed = None
         self._dev_cache = {}
+
+    def with_walls(self, surface_relaxivity_t2=None, permeability=None):
+        """The same surface with other (uniform) wall properties: a view that shares this mesh's
+        triangles, grid and device tables.  The grid stays the one this mesh was built with."""
+        m = copy.copy(self)
+        m.surface_relaxivity_t2 = (float(surface_relaxivity_t2)
+                                   if surface_relaxivity_t2 else None)
+        m._rho_mult_intra = m._rho_mult_extra = np.float32(1.0)
+        m.permeability = float(permeability) if permeability else None
+        m._kappa_mult_out = m._kappa_mult_in = np.float32(1.0)
+        return m
 
     # -------------------------------------------------------------------------------------------
     def _surface_is_closed(self):

@@ -1,0 +1,205 @@
+"""Learned surrogate of the Monte-Carlo signal, trained on signals the batched walk generates.
+
+The surrogate maps 5 substrate parameters -- mean radius, volume fraction, permeability, surface
+relaxivity, diffusivity -- plus a 64-number waveform encoding (the dephasing q(t) at 32 absolute
+times, along and across the cylinder axis; :func:`substrates.q_encoding`) to one signal, with the
+tensor-core MLP of :mod:`mlp` (4 x 256 GELU, bf16 weights, fp32 accumulation, AdamW).
+
+Scope: packed parallel cylinders (the axis is the encoding's reference axis), with the parameters
+inside the hull it was trained on (:data:`HULL`) and echo times up to ``t_max``.  Every query
+outside the hull -- another substrate kind, a parameter out of range, a longer waveform -- is
+answered by the batched Monte-Carlo walk (:meth:`Surrogate.signals` does the routing), and the
+same walk at 1e6 walkers is the judge of the surrogate's error on held-out substrates.
+"""
+import dataclasses
+import time
+
+import numpy as np
+import torch
+
+from . import substrates as S
+from .batched import Instance, PreparedBatch, Tuning
+from .mlp import MLP
+
+N_Q = 32
+T_MAX = 0.08
+HULL = {"radius": (0.5e-6, 5e-6), "f": (0.3, 0.70), "kappa": (0.0, 1e-4), "rho": (0.0, 5e-6),
+        "D": (1e-9, 3e-9), "TE": (0.03, 0.08), "b": (0.0, 3e9)}
+# substrate inputs in natural units (um, 1, 1e-5 m/s, 1e-6 m/s, 1e-9 m^2/s)
+_UNITS = np.array([1e6, 1.0, 1e5, 1e6, 1e9])
+
+
+def substrate_features(radius, f, kappa, rho, D):
+    return np.array([radius, f, kappa, rho, D], np.float64) * _UNITS
+
+
+def features(params, wf):
+    """(M, 69) inputs of the M measurements of one instance."""
+    sub = substrate_features(params["radius"], params["f"], params["kappa"], params["rho"],
+                             params["D"])
+    q = S.q_encoding(wf, N_Q, T_MAX)
+    return np.concatenate([np.repeat(sub[None, :], len(q), 0), q], axis=1).astype(np.float32)
+
+
+def in_hull(params, wf=None):
+    if params.get("kind", "PackedCylinders") != "PackedCylinders":
+        return False
+    for k in ("radius", "f", "kappa", "rho", "D"):
+        lo, hi = HULL[k]
+        if not (lo <= params[k] <= hi):
+            return False
+    if wf is not None and (np.asarray(wf.G).shape[1] - 1) * wf.dt > T_MAX:
+        return False
+    return True
+
+
+def draw_instances(n, seed, n_meas=512, n_t=200, n_walkers=8192, mesh=None):
+    """``n`` packed-cylinder instances with parameters uniform in the hull and free waveform
+    sets of ``n_meas`` measurements; returns (instances, params)."""
+    rng = np.random.default_rng(int(seed))
+    insts, params = [], []
+    for i in range(n):
+        r = rng.uniform(*HULL["radius"])
+        f = rng.uniform(*HULL["f"])
+        kappa = rng.uniform(*HULL["kappa"])
+        rho = rng.uniform(*HULL["rho"])
+        D = rng.uniform(*HULL["D"])
+        te = rng.uniform(*HULL["TE"])
+        wf, _, _, _ = S.free_waveform_set(n_meas, n_t, te, rng, b_max=HULL["b"][1])
+        geom, fa = S.packed_substrate("PackedCylinders", r, f, rng, rho=rho, kappa=kappa)
+        radius = float(np.mean(geom._radii_np))
+        insts.append(Instance(int(n_walkers), D, wf, geom, seed=int(rng.integers(1, 2 ** 62))))
+        params.append(dict(kind="PackedCylinders", radius=radius, f=fa, kappa=kappa, rho=rho,
+                           D=D, TE=te))
+    return insts, params
+
+
+def monte_carlo(insts, tuning=None, chunk=256, log=None):
+    """Signals and standard errors of ``insts`` from the batched walk, ``chunk`` instances per
+    launch; also returns the GPU seconds spent."""
+    sig, se, gpu_s = [], [], 0.0
+    for c0 in range(0, len(insts), chunk):
+        part = insts[c0:c0 + chunk]
+        b = PreparedBatch(part, tuning or Tuning())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.launch()
+        e1.record()
+        res = b.results()
+        gpu_s += e0.elapsed_time(e1) * 1e-3
+        for r in res:
+            sig.append(r.signal[0].astype(np.float32))
+            se.append(r.stderr[0].astype(np.float32))
+        b.close()
+        if log is not None:
+            log(f"  MC {c0 + len(part)}/{len(insts)} instances, {gpu_s:.1f} GPU s")
+    return sig, se, gpu_s
+
+
+class Surrogate:
+    def __init__(self, width=256, depth=4, seed=0, lr=1e-3, weight_decay=1e-5):
+        self.net = MLP(5 + 2 * N_Q, width=width, depth=depth, seed=seed, lr=lr,
+                       weight_decay=weight_decay)
+        self.lr0 = lr
+
+    # ---- training -----------------------------------------------------------------------------
+    def fit(self, X, y, epochs=40, batch=8192, val=None, log=None, seed=0):
+        """AdamW on (X, y) with a cosine learning-rate decay; the training step is a captured
+        CUDA graph.  Returns the per-epoch history (train loss, validation MAE)."""
+        X = np.asarray(X, np.float32)
+        y = np.asarray(y, np.float32)
+        mu, sd = X.mean(0), X.std(0)
+        sd[sd < 1e-12] = 1.0
+        self.net.set_normalisation(mu, 1.0 / sd)
+        dev = self.net.dev
+        Xd = torch.as_tensor(X, device=dev)
+        yd = torch.as_tensor(y, device=dev)
+        n = (len(X) // batch) * batch
+        steps = epochs * (n // batch)
+        self.net.capture_step(batch)
+        g = torch.Generator(device=dev).manual_seed(int(seed))
+        hist, step = [], 0
+        for ep in range(epochs):
+            perm = torch.randperm(len(X), device=dev, generator=g)[:n]
+            tot = torch.zeros((), device=dev)
+            for s0 in range(0, n, batch):
+                self.net.set_lr(self.lr0 * 0.5 * (1 + np.cos(np.pi * step / steps)))
+                idx = perm[s0:s0 + batch]
+                tot += self.net.train_step(Xd[idx], yd[idx])
+                step += 1
+            train = float(tot.item()) / (n // batch)
+            v = None
+            if val is not None:
+                v = float(np.mean(np.abs(self.predict(val[0]) - val[1])))
+            hist.append((train, v))
+            if log is not None:
+                log(f"  epoch {ep + 1}/{epochs}: train mse {train:.3e}" +
+                    ("" if v is None else f", val mae {v:.4f}"))
+        self.net.check_errors()
+        return hist
+
+    # ---- inference ----------------------------------------------------------------------------
+    def predict(self, X):
+        return self.net.predict(X).cpu().numpy()
+
+    def signals(self, instances, params, tuning=None):
+        """Signals of every instance: the surrogate inside the hull, the batched Monte-Carlo
+        walk outside it.  Returns (signals, used_surrogate flags)."""
+        out, flags, mc_idx = [None] * len(instances), [], []
+        feats, owners = [], []
+        for i, (inst, p) in enumerate(zip(instances, params)):
+            wf = inst.waveform.waveform if hasattr(inst.waveform, "waveform") else inst.waveform
+            ok = in_hull(p, wf)
+            flags.append(ok)
+            if ok:
+                feats.append(features(p, wf))
+                owners.append(i)
+            else:
+                mc_idx.append(i)
+        if feats:
+            y = self.predict(np.concatenate(feats))
+            o = 0
+            for i, fb in zip(owners, feats):
+                out[i] = y[o:o + len(fb)].astype(np.float32)
+                o += len(fb)
+        if mc_idx:
+            sig, _, _ = monte_carlo([instances[i] for i in mc_idx], tuning)
+            for i, s in zip(mc_idx, sig):
+                out[i] = s
+        return out, flags
+
+    def save(self, path):
+        sd = self.net.state_dict()
+        np.savez_compressed(path, **{f"W{l}": w.numpy() for l, w in enumerate(sd["W"])},
+                            **{f"b{l}": b.numpy() for l, b in enumerate(sd["b"])},
+                            w_head=sd["w_head"].numpy(), b_head=sd["b_head"].numpy(),
+                            shift=sd["shift"].numpy(), scale=sd["scale"].numpy(),
+                            shape=np.array(sd["shape"]))
+
+    @classmethod
+    def load(cls, path):
+        z = np.load(path)
+        n_in, width, depth = (int(x) for x in z["shape"])
+        s = cls(width=width, depth=depth)
+        sd = {"W": [torch.as_tensor(z[f"W{l}"]) for l in range(depth)],
+              "b": [torch.as_tensor(z[f"b{l}"]) for l in range(depth)],
+              "w_head": torch.as_tensor(z["w_head"]), "b_head": torch.as_tensor(z["b_head"]),
+              "shift": torch.as_tensor(z["shift"]), "scale": torch.as_tensor(z["scale"])}
+        s.net.load_state_dict(sd)
+        return s
+
+
+def build_training_set(n_instances, seed=0, n_meas=512, n_t=200, n_walkers=8192, log=None,
+                       tuning=None):
+    """(X, y, se, params, GPU seconds) from ``n_instances`` batched-walk instances."""
+    t0 = time.time()
+    insts, params = draw_instances(n_instances, seed, n_meas, n_t, n_walkers)
+    if log is not None:
+        log(f"  drew {n_instances} instances in {time.time() - t0:.1f} s")
+    sig, se, gpu_s = monte_carlo(insts, tuning, log=log)
+    X = np.concatenate([features(p, i.waveform) for p, i in zip(params, insts)])
+    return X, np.concatenate(sig), np.concatenate(se), params, gpu_s
+
+
+__all__ = ["Surrogate", "HULL", "features", "in_hull", "draw_instances", "monte_carlo",
+           "build_training_set"]
