@@ -11,6 +11,16 @@ One step = one complete walk of that workload (all walkers, all samples, all sub
 reduction).  Metric: walker-steps/s, a walker-step being one walker advanced one physics sub-step
 with every measurement's phase updated.
 
+The same JSON line carries the metric's second half (rank 0, N = 1):
+  "batched"    signals/s of the batched walk on the 256-instance study (packed cylinders, packed
+               spheres and a periodic mesh of 200 ellipsoid cells with ~500k triangles; radius,
+               volume fraction, permeability, relaxivity, D, n_t and free waveforms of 8-96
+               measurements drawn from seed 0), every instance at the walker count whose
+               standard error is <= 0.005 for any signal (20,000), one graph-captured launch;
+  "surrogate"  signals/s of the trained MLP surrogate on 1,000,000 queries in one batch, its
+               absolute error against the walk on held-out substrates, and its speed-up over
+               the batched walk's signals/s.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 ``--impl reference`` times the CPU restatement of the reference walk (oracle/, all host cores) on
@@ -132,6 +142,85 @@ def cpu_baseline(geom, wf, S, threads, budget_s=15.0):
     return steps / el, f"{n2} walkers x {wf.G.shape[1]} samples x {S} sub-steps in {el:.1f} s"
 
 
+N_SE_005 = 20_000   # walkers with sqrt(max var / N) <= 0.005 (var of w cos(phi) is at most 0.5)
+SURROGATE = ROOT / "dmipy_sim_gb300" / "data" / "surrogate_packed_cylinders.npz"
+SURROGATE_REPORT = ROOT / "dmipy_sim_gb300" / "data" / "surrogate_packed_cylinders.json"
+
+
+def batched_measure(dev):
+    """The 256-instance study as one captured batched launch: signals/s at <= 0.005 error."""
+    import dataclasses
+    import torch
+    from dmipy_sim_gb300 import substrates as S
+    from dmipy_sim_gb300.batched import PreparedBatch, Tuning
+    t_host = time.perf_counter()
+    mesh = S.ellipsoid_cell_mesh()
+    insts, params = S.instance_mix(256, seed=0, mesh=mesh)
+    full = [dataclasses.replace(i, n_walkers=N_SE_005) for i in insts]
+    warm = PreparedBatch([dataclasses.replace(i, n_walkers=640) for i in insts], Tuning())
+    warm.launch()
+    torch.cuda.synchronize(dev)
+    warm.close()
+    b = PreparedBatch(full, Tuning())
+    host_s = time.perf_counter() - t_host
+    b.capture()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.replay()
+    e1.record()
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) * 1e-3
+    res = b.results()
+    n_sig = sum(int(r.sums.shape[1]) for r in res)
+    max_se = max(float(np.max(r.stderr)) for r in res)
+    info = b.info()
+    kinds = {k: sum(1 for p in params if p["kind"] == k) for k in ("PackedCylinders",
+                                                                   "PackedSpheres", "Mesh")}
+    out = {"signals_per_s": n_sig / sec, "signals": n_sig, "seconds": sec,
+           "walker_steps_per_s": b.walker_steps() / sec, "instances": len(full),
+           "walkers_per_instance": N_SE_005, "max_stderr": max_se, "kinds": kinds,
+           "mesh_triangles": int(len(mesh[0].faces)), "groups": info["groups"],
+           "gpu_launches": info["kernels"], "graph": True, "host_setup_s": host_s}
+    b.close()
+    return out, params
+
+
+def surrogate_measure(dev, mc_signals_per_s):
+    """The trained surrogate: 1M queries in one batch, and its error against the walk on a few
+    held-out substrates (2e5 walkers each)."""
+    import torch
+    from dmipy_sim_gb300 import surrogate as SG
+    if not SURROGATE.exists():
+        return {"unavailable": "no trained surrogate weights in dmipy_sim_gb300/data"}
+    sur = SG.Surrogate.load(SURROGATE)
+    insts, hp = SG.draw_instances(4, 424242, n_meas=64, n_walkers=200_000)
+    X = np.concatenate([SG.features(p, i.waveform) for p, i in zip(hp, insts)])
+    ref, ref_se, _ = SG.monte_carlo(insts)
+    ref = np.concatenate(ref)
+    err = np.abs(sur.predict(X) - ref)
+    q = torch.as_tensor(np.resize(X, (1_000_000, X.shape[1])), device=dev)
+    sur.net.predict(q)                   # warm-up at the timed size (buffers, tensor maps)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    y = sur.net.predict(q)
+    e1.record()
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) * 1e-3
+    out = {"signals_per_s": 1e6 / sec, "queries": 1_000_000, "seconds": sec,
+           "live_mae_vs_mc_2e5": float(err.mean()), "live_max_err": float(err.max()),
+           "live_mc_median_se": float(np.median(np.concatenate(ref_se))),
+           "speedup_vs_batched_mc": (1e6 / sec) / mc_signals_per_s if mc_signals_per_s else None,
+           "gpu_launches_per_query_batch": 1 + 2 * sur.net.depth + 1}
+    if SURROGATE_REPORT.exists():
+        rep = json.loads(SURROGATE_REPORT.read_text())
+        out["held_out"] = {k: rep.get(k) for k in ("held_out_instances", "held_out_signals",
+                                                   "judge_walkers", "mae", "p95_abs_err",
+                                                   "max_abs_err", "signals")}
+    return out
+
+
 def gpu_arm(a):
     import torch
     import dmipy_sim_gb300 as d
@@ -244,6 +333,15 @@ def gpu_arm(a):
         v, sample = cpu_baseline(geom, wf, S, os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": sample}
+    if world == 1 and not a.no_batched:
+        try:
+            out["batched"], _ = batched_measure(dev)
+        except Exception as e:          # reported, never silently dropped
+            out["batched"] = {"error": f"{type(e).__name__}: {e}"}
+        try:
+            out["surrogate"] = surrogate_measure(dev, out["batched"].get("signals_per_s"))
+        except Exception as e:
+            out["surrogate"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -294,6 +392,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-walk and surrogate measurements")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per GPU (smaller only for profiling captures)")
     a = ap.parse_args()

@@ -3,7 +3,7 @@ fixed ranges, as batched-walk instances and as the surrogate's training set.
 
 Ranges: mean radius 0.5-5 um, volume fraction 0.3-0.8 (clamped to what the packer reaches:
 random sequential addition up to 0.5 for cylinders, a polydisperse square lattice above that up
-to 0.70; 0.38 for spheres), permeability 0-1e-4 m/s, surface relaxivity 0-5e-6 m/s, diffusivity
+to 0.70; 0.38 for spheres, stepped down where 16 spheres jam first), permeability 0-1e-4 m/s, surface relaxivity 0-5e-6 m/s, diffusivity
 1-3e-9 m^2/s, walkers log-uniform 1e4-1e6, 300-3000 waveform samples, 8-96 measurements.
 
 A free waveform set is built from a few smooth refocused shapes: q(t) = sum_k c_k sin(pi k t/TE)
@@ -101,7 +101,12 @@ def packed_substrate(kind, radius, f, rng, n_objects=16, rho=0.0, kappa=0.0):
     if kind == "PackedSpheres":
         f = min(f, F_MAX[kind])
         radii = np.clip(rng.normal(radius, 0.1 * radius, n_objects), 0.5 * radius, 1.5 * radius)
-        centers, L, fa = pack_spheres(radii, target_vf=f, seed=seed)
+        while True:   # a few spheres jam below the large-system RSA limit: step f down
+            try:
+                centers, L, fa = pack_spheres(radii, target_vf=f, seed=seed, max_attempts=20000)
+                break
+            except RuntimeError:
+                f -= 0.02
         return PackedSpheres(radii, centers, L, **kw), fa
     raise ValueError(f"unknown packed kind {kind!r}")
 
@@ -113,7 +118,7 @@ def ellipsoid_cell_mesh(n_cells=200, faces_per_cell=2500, seed=0, box=None,
     import warnings
     from .mesh import Mesh, random_ellipsoid_cells
     if box is None:
-        box = 3.2e-6 * n_cells ** (1.0 / 3.0) * 3.0
+        box = 60e-6 * (n_cells / 200.0) ** (1.0 / 3.0)
     V, F = random_ellipsoid_cells(n_cells, box, radius_range, seed=seed,
                                   faces_per_cell=faces_per_cell)
     with warnings.catch_warnings():

@@ -119,9 +119,10 @@ class Surrogate:
         self.net.capture_step(batch)
         g = torch.Generator(device=dev).manual_seed(int(seed))
         hist, step = [], 0
+        t_ep = time.time()
         for ep in range(epochs):
             perm = torch.randperm(len(X), device=dev, generator=g)[:n]
-            tot = torch.zeros((), device=dev)
+            tot = torch.zeros(1, device=dev)
             for s0 in range(0, n, batch):
                 self.net.set_lr(self.lr0 * 0.5 * (1 + np.cos(np.pi * step / steps)))
                 idx = perm[s0:s0 + batch]
@@ -134,7 +135,8 @@ class Surrogate:
             hist.append((train, v))
             if log is not None:
                 log(f"  epoch {ep + 1}/{epochs}: train mse {train:.3e}" +
-                    ("" if v is None else f", val mae {v:.4f}"))
+                    ("" if v is None else f", val mae {v:.4f}") +
+                    f" ({time.time() - t_ep:.1f} s)")
         self.net.check_errors()
         return hist
 
