@@ -195,7 +195,7 @@ def surrogate_measure(dev, mc_signals_per_s):
         return {"unavailable": "no trained surrogate weights in dmipy_sim_gb300/data"}
     sur = SG.Surrogate.load(SURROGATE)
     insts, hp = SG.draw_instances(4, 424242, n_meas=64, n_walkers=200_000)
-    X = np.concatenate([SG.features(p, i.waveform) for p, i in zip(hp, insts)])
+    X = np.concatenate([SG.features(p, i.waveform, sur.form) for p, i in zip(hp, insts)])
     ref, ref_se, _ = SG.monte_carlo(insts)
     ref = np.concatenate(ref)
     err = np.abs(sur.predict(X) - ref)
@@ -219,6 +219,47 @@ def surrogate_measure(dev, mc_signals_per_s):
                                                    "judge_walkers", "mae", "p95_abs_err",
                                                    "max_abs_err", "signals")}
     return out
+
+
+def profile_case(a):
+    """Small single-kernel cases for profiler captures (not bench values):
+    mesh      the permeable walk through the 200-cell ellipsoid mesh (~500k triangles),
+              8192 walkers x 64 samples;
+    mlp       the surrogate's forward pass on 262,144 queries (4 tensor-core GEMMs + head);
+    batched   a 32-instance slice of the batched study at 4096 walkers per instance."""
+    import dataclasses
+    import torch
+    import dmipy_sim_gb300 as d
+    from dmipy_sim_gb300 import core
+    from dmipy_sim_gb300 import substrates as S
+    dev = torch.device("cuda", 0)
+    for _ in range(max(1, a.warmup) + a.steps):
+        if a.profile_case == "mesh":
+            if _ == 0:
+                mesh, _f = S.ellipsoid_cell_mesh()
+                g = mesh.with_walls(None, 1e-5)
+                rng = np.random.default_rng(0)
+                wf, _i, _dd, _b = S.free_waveform_set(16, 64, 0.02, rng)
+                G, chi = core._waveform_arrays(wf, g)
+                Sm = core.fused_sub_steps(g, D, wf.dt)
+                walk = core.PreparedWalk(g, n_walkers=8192, diffusivity=D, G=G, dt=wf.dt,
+                                         sub_steps=Sm, phase_per_substep=True, seed=5)
+            walk.launch()
+        elif a.profile_case == "mlp":
+            if _ == 0:
+                from dmipy_sim_gb300.mlp import MLP
+                net = MLP(69, 256, 4, seed=0)
+                x = torch.randn(262_144, 69, device=dev)
+            net.predict(x)
+        else:
+            if _ == 0:
+                from dmipy_sim_gb300.batched import PreparedBatch
+                insts, _p = S.instance_mix(32, seed=0, kinds=("PackedCylinders",
+                                                              "PackedSpheres"))
+                b = PreparedBatch([dataclasses.replace(i, n_walkers=4096) for i in insts])
+            b.launch()
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"profile_case": a.profile_case, "ok": True}))
 
 
 def gpu_arm(a):
@@ -396,8 +437,12 @@ def main():
                     help="skip the batched-walk and surrogate measurements")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per GPU (smaller only for profiling captures)")
+    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched"], default=None,
+                    help="run one small kernel case for a profiler capture and exit")
     a = ap.parse_args()
-    if a.impl == "reference":
+    if a.profile_case:
+        profile_case(a)
+    elif a.impl == "reference":
         reference_arm(a)
     else:
         gpu_arm(a)

@@ -33,6 +33,7 @@ def free_shapes(n_shapes, n_t, rng, n_harm=4):
     for i in range(n_shapes):
         c = rng.normal(size=n_harm) / k
         g = np.sum(c[:, None] * (np.pi * k[:, None]) * np.cos(np.pi * k[:, None] * t[None, :]), 0)
+        g -= g.mean()            # the sampled moment sum_t g(t) dt is exactly zero
         out[i] = g / np.max(np.abs(g))
     return out
 
@@ -67,10 +68,16 @@ def q_encoding(wf, n_samples=32, t_max=0.08, axis=(0.0, 0.0, 1.0)):
     q = GAMMA * np.cumsum(G, axis=1) * wf.dt                      # q after sample i, rad/m
     tq = (np.arange(n_t) + 1.0) * wf.dt
     ts = (np.arange(n_samples) + 0.5) * (t_max / n_samples)
-    qs = np.zeros((M, n_samples, 3))
-    for k in range(3):
-        for m in range(M):
-            qs[m, :, k] = np.interp(ts, tq, q[m, :, k], left=0.0, right=0.0)
+    # linear interpolation on the shared time grid (0 before the first sample, 0 after the end)
+    i = np.searchsorted(tq, ts, side="right")
+    inside = (i > 0) & (ts <= tq[-1])
+    hi = np.clip(i, 1, n_t - 1)
+    lo = hi - 1
+    w = np.clip((ts - tq[lo]) / (tq[hi] - tq[lo]), 0.0, 1.0)
+    exact_end = ts == tq[-1]
+    w[exact_end] = 1.0
+    qs = q[:, lo] * (1.0 - w)[None, :, None] + q[:, hi] * w[None, :, None]
+    qs[:, ~inside] = 0.0
     a = np.asarray(axis, np.float64)
     a = a / np.linalg.norm(a)
     par = qs @ a

@@ -29,15 +29,25 @@ HULL = {"radius": (0.5e-6, 5e-6), "f": (0.3, 0.70), "kappa": (0.0, 1e-4), "rho":
 _UNITS = np.array([1e6, 1.0, 1e5, 1e6, 1e9])
 
 
-def substrate_features(radius, f, kappa, rho, D):
-    return np.array([radius, f, kappa, rho, D], np.float64) * _UNITS
+def substrate_features(radius, f, kappa, rho, D, form="dimensionless"):
+    """The 5 substrate inputs.  ``raw``: radius (um), f, kappa (1e-5 m/s), rho (1e-6 m/s),
+    D (1e-9 m^2/s).  ``dimensionless``: log(radius / 1 um), f, kappa R / D, rho R / D,
+    log(D / 1e-9) -- the groups the walk's physics depends on."""
+    if form == "raw":
+        return np.array([radius, f, kappa, rho, D], np.float64) * _UNITS
+    return np.array([np.log(radius * 1e6), f, kappa * radius / D, rho * radius / D,
+                     np.log(D * 1e9)], np.float64)
 
 
-def features(params, wf):
-    """(M, 69) inputs of the M measurements of one instance."""
+def features(params, wf, form="dimensionless"):
+    """(M, 69) inputs of the M measurements of one instance.  In the dimensionless form the
+    dephasing samples are scaled by sqrt(D t_max / N_Q), so that their sum of squares is the
+    attenuation exponent b D of free diffusion."""
     sub = substrate_features(params["radius"], params["f"], params["kappa"], params["rho"],
-                             params["D"])
+                             params["D"], form)
     q = S.q_encoding(wf, N_Q, T_MAX)
+    if form != "raw":
+        q = q * 1e6 * np.sqrt(params["D"] * T_MAX / N_Q)
     return np.concatenate([np.repeat(sub[None, :], len(q), 0), q], axis=1).astype(np.float32)
 
 
@@ -97,10 +107,12 @@ def monte_carlo(insts, tuning=None, chunk=256, log=None):
 
 
 class Surrogate:
-    def __init__(self, width=256, depth=4, seed=0, lr=1e-3, weight_decay=1e-5):
+    def __init__(self, width=256, depth=4, seed=0, lr=1e-3, weight_decay=1e-5,
+                 form="dimensionless"):
         self.net = MLP(5 + 2 * N_Q, width=width, depth=depth, seed=seed, lr=lr,
                        weight_decay=weight_decay)
         self.lr0 = lr
+        self.form = form
 
     # ---- training -----------------------------------------------------------------------------
     def fit(self, X, y, epochs=40, batch=8192, val=None, log=None, seed=0):
@@ -154,7 +166,7 @@ class Surrogate:
             ok = in_hull(p, wf)
             flags.append(ok)
             if ok:
-                feats.append(features(p, wf))
+                feats.append(features(p, wf, self.form))
                 owners.append(i)
             else:
                 mc_idx.append(i)
@@ -176,13 +188,13 @@ class Surrogate:
                             **{f"b{l}": b.numpy() for l, b in enumerate(sd["b"])},
                             w_head=sd["w_head"].numpy(), b_head=sd["b_head"].numpy(),
                             shift=sd["shift"].numpy(), scale=sd["scale"].numpy(),
-                            shape=np.array(sd["shape"]))
+                            shape=np.array(sd["shape"]), form=np.array(self.form))
 
     @classmethod
     def load(cls, path):
         z = np.load(path)
         n_in, width, depth = (int(x) for x in z["shape"])
-        s = cls(width=width, depth=depth)
+        s = cls(width=width, depth=depth, form=str(z["form"]) if "form" in z else "raw")
         sd = {"W": [torch.as_tensor(z[f"W{l}"]) for l in range(depth)],
               "b": [torch.as_tensor(z[f"b{l}"]) for l in range(depth)],
               "w_head": torch.as_tensor(z["w_head"]), "b_head": torch.as_tensor(z["b_head"]),
@@ -192,14 +204,14 @@ class Surrogate:
 
 
 def build_training_set(n_instances, seed=0, n_meas=512, n_t=200, n_walkers=8192, log=None,
-                       tuning=None):
+                       tuning=None, form="dimensionless"):
     """(X, y, se, params, GPU seconds) from ``n_instances`` batched-walk instances."""
     t0 = time.time()
     insts, params = draw_instances(n_instances, seed, n_meas, n_t, n_walkers)
     if log is not None:
         log(f"  drew {n_instances} instances in {time.time() - t0:.1f} s")
     sig, se, gpu_s = monte_carlo(insts, tuning, log=log)
-    X = np.concatenate([features(p, i.waveform) for p, i in zip(params, insts)])
+    X = np.concatenate([features(p, i.waveform, form) for p, i in zip(params, insts)])
     return X, np.concatenate(sig), np.concatenate(se), params, gpu_s
 
 

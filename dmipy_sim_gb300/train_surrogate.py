@@ -30,6 +30,8 @@ def main(argv=None):
     ap.add_argument("--judge-walkers", type=int, default=1_000_000)
     ap.add_argument("--judge-meas", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--form", default="dimensionless", choices=["dimensionless", "raw"])
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default="surrogate.npz")
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
@@ -40,12 +42,13 @@ def main(argv=None):
     t0 = time.time()
     log(f"training set: {a.instances} instances x {a.meas} measurements, {a.walkers} walkers")
     X, y, se, params, gpu_train_mc = SG.build_training_set(a.instances, a.seed, a.meas,
-                                                           n_walkers=a.walkers, log=log)
+                                                           n_walkers=a.walkers, log=log,
+                                                           form=a.form)
     log(f"  {len(y)} signals, median SE {np.median(se):.4f}, MC {gpu_train_mc:.1f} GPU s")
     # validation split: the last 5 % of instances
     n_val = max(1, a.instances // 20) * a.meas
     Xtr, ytr, Xva, yva = X[:-n_val], y[:-n_val], X[-n_val:], y[-n_val:]
-    sur = SG.Surrogate(seed=a.seed)
+    sur = SG.Surrogate(seed=a.seed, lr=a.lr, form=a.form)
     t1 = time.time()
     hist = sur.fit(Xtr, ytr, epochs=a.epochs, batch=a.batch, val=(Xva, yva), log=log)
     torch.cuda.synchronize()
@@ -57,7 +60,7 @@ def main(argv=None):
     insts, hp = SG.draw_instances(a.held_out, a.seed + 10_000, a.judge_meas,
                                   n_walkers=a.judge_walkers)
     ref, ref_se, gpu_judge = SG.monte_carlo(insts, chunk=8, log=log)
-    Xh = np.concatenate([SG.features(p, i.waveform) for p, i in zip(hp, insts)])
+    Xh = np.concatenate([SG.features(p, i.waveform, a.form) for p, i in zip(hp, insts)])
     pred = sur.predict(Xh)
     ref = np.concatenate(ref)
     ref_se = np.concatenate(ref_se)
@@ -74,7 +77,7 @@ def main(argv=None):
     e1.synchronize()
     sur_s = e0.elapsed_time(e1) * 1e-3
     rep = {
-        "instances": a.instances, "signals": int(len(y)), "walkers": a.walkers,
+        "instances": a.instances, "signals": int(len(y)), "walkers": a.walkers, "form": a.form,
         "train_mc_gpu_s": gpu_train_mc, "train_s": train_s, "epochs": a.epochs,
         "final_train_mse": hist[-1][0], "val_mae_vs_training_mc": hist[-1][1],
         "held_out_instances": a.held_out, "held_out_signals": int(len(ref)),

@@ -1,0 +1,81 @@
+"""The trained surrogate on the GPU: its error against the batched walk on held-out substrates,
+what it gains over the walk (signals per second at the same error), and the routing of queries
+outside its hull to the walk."""
+import time
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import dmipy_sim_gb300 as d
+from dmipy_sim_gb300 import surrogate as SG
+from dmipy_sim_gb300.batched import Instance
+
+pytestmark = pytest.mark.gpu
+WEIGHTS = Path(__file__).resolve().parent.parent / "dmipy_sim_gb300" / "data" / \
+    "surrogate_packed_cylinders.npz"
+
+
+@pytest.fixture(scope="module")
+def sur(cuda):
+    if not WEIGHTS.exists():
+        pytest.skip("no trained surrogate weights")
+    return SG.Surrogate.load(WEIGHTS)
+
+
+@pytest.fixture(scope="module")
+def held_out(cuda):
+    # substrates drawn from a seed the training set never used, walked at 2e5 walkers
+    insts, params = SG.draw_instances(6, 777, n_meas=48, n_walkers=200_000)
+    sig, se, gpu_s = SG.monte_carlo(insts)
+    return insts, params, np.concatenate(sig), np.concatenate(se), gpu_s
+
+
+def test_surrogate_error_on_held_out_substrates(sur, held_out):
+    insts, params, ref, se, _ = held_out
+    X = np.concatenate([SG.features(p, i.waveform, sur.form) for p, i in zip(params, insts)])
+    err = np.abs(sur.predict(X) - ref)
+    # the walk's own noise at 2e5 walkers (median SE) sits inside the measured error
+    assert np.median(se) < 0.003
+    assert err.mean() < 0.02, (err.mean(), np.percentile(err, 95))
+    assert np.percentile(err, 95) < 0.08
+
+
+def test_surrogate_gain_over_the_walk(sur, held_out):
+    """Signals per second at matched error: the walk needs N walkers for its standard error to
+    reach the surrogate's mean error; the surrogate answers a 1M-query batch."""
+    insts, params, ref, se, gpu_s = held_out
+    X = np.concatenate([SG.features(p, i.waveform, sur.form) for p, i in zip(params, insts)])
+    mae = float(np.mean(np.abs(sur.predict(X) - ref)))
+    walker_steps = sum(i.n_walkers * i.waveform.G.shape[1] for i in insts)   # per sub-step
+    n_sig = len(ref)
+    # walkers for SE = mae, from SE ~ sqrt(var / N) with the measured SE at 2e5 walkers
+    n_match = 2e5 * (np.median(se) / mae) ** 2
+    mc_sig_per_s = n_sig / (gpu_s * n_match / 2e5)
+    q = torch.as_tensor(np.resize(X, (1_000_000, X.shape[1])), device=sur.net.dev)
+    sur.net.predict(q)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sur.net.predict(q)
+    e1.record()
+    e1.synchronize()
+    sur_sig_per_s = 1e6 / (e0.elapsed_time(e1) * 1e-3)
+    assert walker_steps > 0
+    assert sur_sig_per_s > 100.0 * mc_sig_per_s, (sur_sig_per_s, mc_sig_per_s)
+
+
+def test_queries_outside_the_hull_go_to_the_walk(sur):
+    rng = np.random.default_rng(5)
+    from dmipy_sim_gb300 import substrates as S
+    wf, _, _, _ = S.free_waveform_set(6, 150, 0.04, rng, n_shapes=1)
+    inside, pin = SG.draw_instances(1, 99, n_meas=6, n_walkers=4096)
+    sph = d.Sphere(4e-6)
+    out_inst = Instance(4096, 2e-9, wf, sph, seed=3)
+    pout = dict(kind="Sphere", radius=4e-6, f=1.0, kappa=0.0, rho=0.0, D=2e-9)
+    sig, flags = sur.signals([inside[0], out_inst], [pin[0], pout])
+    assert flags == [True, False]
+    ref = d.simulate(4096, 2e-9, wf, sph, seed=3)
+    np.testing.assert_allclose(sig[1], ref, atol=1e-6)
+    assert sig[0].shape == (6,) and np.all(np.isfinite(sig[0]))

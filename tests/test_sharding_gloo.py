@@ -60,3 +60,50 @@ def test_two_rank_gloo_walk_equals_single_process(tmp_path):
     geom, G, dt, S = _case()
     whole = oracle_walk(geom, G, dt, S, False, N, seed=3, want_walkers=False)["sums"]
     np.testing.assert_allclose(np.load(out), whole, rtol=1e-12, atol=1e-12)
+
+
+def test_instance_shards_cover_every_instance_once_and_balance():
+    from dmipy_sim_gb300.sharding import shard_instances
+    rng = np.random.default_rng(0)
+    costs = rng.lognormal(0, 1.5, 257)
+    for w in (1, 2, 3, 8):
+        parts = [shard_instances(costs, w, r) for r in range(w)]
+        flat = sorted(i for p in parts for i in p)
+        assert flat == list(range(len(costs)))
+        loads = [sum(costs[i] for i in p) for p in parts]
+        assert max(loads) - min(loads) <= max(costs)
+
+
+def _batch_worker(rank, world, port, out):
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    import torch.distributed as dist
+    from parity_cases import oracle_walk
+    from dmipy_sim_gb300.sharding import gather_signals, shard_instances
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    geom, G, dt, S = _case()
+    sizes = [40, 200, 90, 10, 150, 60]
+    mine = shard_instances(sizes, world, rank)
+    local = [oracle_walk(geom, G, dt, S, False, sizes[i], seed=100 + i,
+                         want_walkers=False)["sums"] for i in mine]
+    allsig = gather_signals(local, mine, len(sizes))
+    if rank == 0:
+        np.save(out, np.stack(allsig))
+    dist.destroy_process_group()
+
+
+def test_two_rank_gloo_instance_shards_equal_single_process(tmp_path):
+    from parity_cases import oracle_walk
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = str(tmp_path / "sig.npy")
+    mp.start_processes(_batch_worker, args=(2, port, out), nprocs=2, join=True,
+                       start_method="spawn")
+    geom, G, dt, S = _case()
+    sizes = [40, 200, 90, 10, 150, 60]
+    ref = np.stack([oracle_walk(geom, G, dt, S, False, n, seed=100 + i,
+                                want_walkers=False)["sums"] for i, n in enumerate(sizes)])
+    np.testing.assert_array_equal(np.load(out), ref)
