@@ -63,9 +63,11 @@ def in_hull(params, wf=None):
     return True
 
 
-def draw_instances(n, seed, n_meas=512, n_t=200, n_walkers=8192, mesh=None):
+def draw_instances(n, seed, n_meas=256, n_t=200, n_walkers=8192, n_objects=64):
     """``n`` packed-cylinder instances with parameters uniform in the hull and free waveform
-    sets of ``n_meas`` measurements; returns (instances, params)."""
+    sets of ``n_meas`` measurements; returns (instances, params).  Each substrate holds
+    ``n_objects`` cylinders, enough that one packing's signal is close to the mean over packings
+    of the same radius and volume fraction (the 5 substrate inputs do not name the packing)."""
     rng = np.random.default_rng(int(seed))
     insts, params = [], []
     for i in range(n):
@@ -76,7 +78,8 @@ def draw_instances(n, seed, n_meas=512, n_t=200, n_walkers=8192, mesh=None):
         D = rng.uniform(*HULL["D"])
         te = rng.uniform(*HULL["TE"])
         wf, _, _, _ = S.free_waveform_set(n_meas, n_t, te, rng, b_max=HULL["b"][1])
-        geom, fa = S.packed_substrate("PackedCylinders", r, f, rng, rho=rho, kappa=kappa)
+        geom, fa = S.packed_substrate("PackedCylinders", r, f, rng, n_objects=n_objects, rho=rho,
+                                      kappa=kappa)
         radius = float(np.mean(geom._radii_np))
         insts.append(Instance(int(n_walkers), D, wf, geom, seed=int(rng.integers(1, 2 ** 62))))
         params.append(dict(kind="PackedCylinders", radius=radius, f=fa, kappa=kappa, rho=rho,
@@ -203,7 +206,7 @@ class Surrogate:
         return s
 
 
-def build_training_set(n_instances, seed=0, n_meas=512, n_t=200, n_walkers=8192, log=None,
+def build_training_set(n_instances, seed=0, n_meas=256, n_t=200, n_walkers=8192, log=None,
                        tuning=None, form="dimensionless"):
     """(X, y, se, params, GPU seconds) from ``n_instances`` batched-walk instances."""
     t0 = time.time()

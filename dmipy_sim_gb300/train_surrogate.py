@@ -1,9 +1,9 @@
 """Train the packed-cylinder surrogate from batched Monte-Carlo signals and judge it against the
 walk at high walker counts on held-out substrates.
 
-    python -m dmipy_sim_gb300.train_surrogate --instances 4000 --out surrogate.npz
+    python -m dmipy_sim_gb300.train_surrogate --instances 12000 --out surrogate.npz
 
-Steps: draw ``instances`` substrates uniformly in the hull (512 free measurements each), walk
+Steps: draw ``instances`` substrates uniformly in the hull (256 free measurements each), walk
 them with the batched kernel at ``walkers`` walkers, fit the MLP (graph-captured AdamW steps on
 the tensor cores), then draw ``held_out`` new substrates, walk them at ``judge_walkers`` and
 report the surrogate's absolute error against them, with the throughput of both methods.
@@ -21,17 +21,17 @@ from . import surrogate as SG
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--instances", type=int, default=4000)
-    ap.add_argument("--meas", type=int, default=512)
+    ap.add_argument("--instances", type=int, default=12000)
+    ap.add_argument("--meas", type=int, default=256)
     ap.add_argument("--walkers", type=int, default=8192)
-    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--held-out", type=int, default=24)
     ap.add_argument("--judge-walkers", type=int, default=1_000_000)
     ap.add_argument("--judge-meas", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--form", default="dimensionless", choices=["dimensionless", "raw"])
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--out", default="surrogate.npz")
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
