@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 3
+DMSIM_ABI_VERSION = 4
 TILE_WALKERS = 320
 
 GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
@@ -29,7 +29,7 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_replay", "dmsim_batch_create", "dmsim_batch_bind", "dmsim_batch_launch",
             "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_pack",
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
-            "dmsim_adam_advance")
+            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods")
 
 EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
@@ -50,7 +50,8 @@ class Geometry(C.Structure):
         ("kappa_mult_in", C.c_float), ("reject_escape", C.c_int32), ("seed_parity", C.c_int32),
         ("seed_inside", C.c_int32), ("pad1", C.c_int32),
         ("tri", C.c_void_p), ("tri_vn", C.c_void_p), ("mesh_cell_start", C.c_void_p),
-        ("mesh_cell_tri", C.c_void_p),
+        ("mesh_cell_tri", C.c_void_p), ("mesh_nb_start", C.c_void_p), ("mesh_nb_tri", C.c_void_p),
+        ("tri_bs", C.c_void_p),
     ]
 
 
@@ -148,6 +149,8 @@ def load():
     lib.dmsim_sum_f32.argtypes = [vp, i64, vp, vp]
     lib.dmsim_adamw.restype = C.c_int
     lib.dmsim_adamw.argtypes = [vp, vp, vp, vp, i32, i64, i32, vp, vp, vp, i32, vp]
+    lib.dmsim_mesh_neighbourhoods.restype = C.c_int
+    lib.dmsim_mesh_neighbourhoods.argtypes = [C.POINTER(Geometry), vp, vp, vp]
     lib.dmsim_adam_advance.restype = C.c_int
     lib.dmsim_adam_advance.argtypes = [vp, vp]
     if lib.dmsim_version() != DMSIM_ABI_VERSION:

@@ -433,9 +433,26 @@ MeshK make_meshk(const dmsim_geometry* g) {
   m.seed_inside = g->seed_inside ? 1 : 0;
   m.tri = reinterpret_cast<const float4*>(g->tri);
   m.vn = reinterpret_cast<const float4*>(g->tri_vn);
+  m.bs = reinterpret_cast<const float4*>(g->tri_bs);
   m.cstart = g->mesh_cell_start;
   m.ctri = g->mesh_cell_tri;
+  m.nbstart = g->mesh_nb_start;
+  m.nbtri = g->mesh_nb_tri;
   return m;
+}
+
+__global__ void k_mesh_nb(const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ct,
+                          int d0, int d1, int d2, const uint32_t* __restrict__ start,
+                          uint32_t* __restrict__ out) {
+  const int dims[3] = {d0, d1, d2};
+  const int64_t n = (int64_t)d0 * d1 * d2;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    if (start)
+      mesh_neighbourhood(cs, ct, dims, c, out + start[c]);
+    else
+      out[c] = mesh_neighbourhood(cs, ct, dims, c, nullptr);
+  }
 }
 
 GeoK make_geok(const dmsim_geometry* g) {
@@ -624,6 +641,22 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
                                                  dlog_unit);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(DMSIM_ECUDA, "step_kat launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
+int dmsim_mesh_neighbourhoods(const dmsim_geometry* g, uint32_t* nb_start, uint32_t* nb_tri,
+                              void* stream) {
+  if (!g || !nb_start || !g->mesh_cell_start || !g->mesh_cell_tri || g->mesh_dims[0] < 1 ||
+      g->mesh_dims[1] < 1 || g->mesh_dims[2] < 1)
+    return fail(DMSIM_EINVAL, "mesh_neighbourhoods: bad arguments");
+  const int64_t n = (int64_t)g->mesh_dims[0] * g->mesh_dims[1] * g->mesh_dims[2];
+  const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  k_mesh_nb<<<blocks, 256, 0, (cudaStream_t)stream>>>(
+      g->mesh_cell_start, g->mesh_cell_tri, g->mesh_dims[0], g->mesh_dims[1], g->mesh_dims[2],
+      nb_tri ? nb_start : nullptr, nb_tri ? nb_tri : nb_start);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess)
+    return fail(DMSIM_ECUDA, "mesh_neighbourhoods launch failed: %s", cudaGetErrorString(err));
   return DMSIM_OK;
 }
 

@@ -34,8 +34,11 @@ struct MeshK {
   int seed_parity, seed_inside;
   const float4* tri;  // 4 x float4 per triangle: A, E1, E2, geometric normal, centroid, 1=original
   const float4* vn;   // 3 x float4 per triangle: smooth normals at the three vertices
+  const float4* bs;   // optional bounding sphere per triangle (centre, radius)
   const uint32_t* cstart;
   const uint32_t* ctri;
+  const uint32_t* nbstart;  // optional neighbourhood lists (see mesh_neighbourhood): one list
+  const uint32_t* nbtri;    // per cell with the distinct triangles of its 27-cell gather
 };
 
 struct Tri {
@@ -52,10 +55,68 @@ __device__ __forceinline__ int mesh_cell(float p, int a, const MeshK& m) {
   return min(max(c, 0), m.dims[a] - 1);
 }
 
-// Visit every candidate of the 27-cell gather around p in the reference's order.
+// The neighbourhood list of grid cell `cid`: the triangles of its 27 neighbour cells (indices
+// clamped to the grid, neighbours in x-major order, each cell's triangles in increasing order)
+// with every repeat after the first dropped.  A triangle larger than a cell is listed in several
+// cells; a repeat is recognised by a binary search of the earlier neighbours' (sorted) lists.
+// Writes the list to `out` when given; returns its length.
+__device__ __forceinline__ uint32_t mesh_neighbourhood(const uint32_t* __restrict__ cs,
+                                                       const uint32_t* __restrict__ ct,
+                                                       const int* dims, int64_t cid,
+                                                       uint32_t* __restrict__ out) {
+  const int cz = (int)(cid % dims[2]);
+  const int cy = (int)((cid / dims[2]) % dims[1]);
+  const int cx = (int)(cid / ((int64_t)dims[1] * dims[2]));
+  int nb[27];
+#pragma unroll
+  for (int d = 0; d < 27; ++d) {
+    const int nx = min(max(cx + d / 9 - 1, 0), dims[0] - 1);
+    const int ny = min(max(cy + (d / 3) % 3 - 1, 0), dims[1] - 1);
+    const int nz = min(max(cz + d % 3 - 1, 0), dims[2] - 1);
+    nb[d] = (nx * dims[1] + ny) * dims[2] + nz;
+  }
+  uint32_t n = 0;
+#pragma unroll 1
+  for (int d = 0; d < 27; ++d) {
+    bool same_cell = false;
+    for (int e = 0; e < d; ++e) same_cell |= nb[e] == nb[d];
+    if (same_cell) continue;  // a clamped neighbour already visited whole
+    const uint32_t kb = cs[nb[d]], ke = cs[nb[d] + 1];
+#pragma unroll 1
+    for (uint32_t k = kb; k < ke; ++k) {
+      const uint32_t t = ct[k];
+      bool seen = false;
+#pragma unroll 1
+      for (int e = 0; e < d && !seen; ++e) {
+        uint32_t lo = cs[nb[e]], hi = cs[nb[e] + 1];  // lower bound of t in a sorted list
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (ct[mid] < t) lo = mid + 1; else hi = mid;
+        }
+        seen = lo < cs[nb[e] + 1] && ct[lo] == t;
+      }
+      if (seen) continue;
+      if (out) out[n] = t;
+      ++n;
+    }
+  }
+  return n;
+}
+
+// Visit every candidate of the 27-cell gather around p in the reference's order.  With the
+// neighbourhood lists each distinct triangle is visited once, at its first position in that
+// order; every use of the gather keeps the first of equal candidates (strict comparisons), so
+// the result is the same as visiting the repeats.
 template <typename Fn>
 __device__ __forceinline__ void mesh_gather(const MeshK& m, float px, float py, float pz, Fn&& fn) {
   const int cx = mesh_cell(px, 0, m), cy = mesh_cell(py, 1, m), cz = mesh_cell(pz, 2, m);
+  if (m.nbstart != nullptr) {
+    const int cid = (cx * m.dims[1] + cy) * m.dims[2] + cz;
+    const uint32_t e = m.nbstart[cid + 1];
+#pragma unroll 1
+    for (uint32_t k = m.nbstart[cid]; k < e; ++k) fn(m.nbtri[k]);
+    return;
+  }
 #pragma unroll 1
   for (int dx = -1; dx <= 1; ++dx) {
     const int nx = min(max(cx + dx, 0), m.dims[0] - 1);
@@ -146,6 +207,15 @@ __device__ __forceinline__ MeshHit mesh_nearest(const MeshK& m, float gx, float 
                                                 float dy, float dz, float rem) {
   MeshHit h{INFINITY, 0.f, 0.f, 0u};
   mesh_gather(m, gx, gy, gz, [&](uint32_t k) {
+    if (m.bs != nullptr) {
+      // a triangle whose bounding sphere misses the segment r0 + s d, s in [0, rem], cannot
+      // be hit within the step (the sphere covers the float32 triangle with a margin)
+      const float4 b = __ldg(m.bs + k);
+      const float cx = b.x - r0x, cy = b.y - r0y, cz = b.z - r0z;
+      const float s = fminf(fmaxf(cx * dx + cy * dy + cz * dz, 0.f), rem);
+      const float ex = cx - s * dx, ey = cy - s * dy, ez = cz - s * dz;
+      if (ex * ex + ey * ey + ez * ez > b.w * b.w) return;
+    }
     const Tri T = load_tri(m, k);
     float u, v;
     const float t = mt_hit(T, r0x, r0y, r0z, dx, dy, dz, u, v);

@@ -406,6 +406,7 @@ class Mesh(Geometry):
     def with_walls(self, surface_relaxivity_t2=None, permeability=None):
         """The same surface with other (uniform) wall properties: a view that shares this mesh's
         triangles, grid and device tables.  The grid stays the one this mesh was built with."""
+        self._surface_is_closed()   # computed once, shared by every view
         m = copy.copy(self)
         m.surface_relaxivity_t2 = (float(surface_relaxivity_t2)
                                    if surface_relaxivity_t2 else None)
@@ -434,15 +435,49 @@ class Mesh(Geometry):
             rec[:, 15] = (np.arange(len(t)) < self._n_orig).astype(np.float32)  # 1 = not a ghost
             vn = np.zeros((len(t), 12), np.float32)
             vn[:, 0:9] = self._vn_all.reshape(-1, 9)
+            # bounding sphere of each float32 triangle about its float32 centroid, widened so
+            # that rounding in the walk's segment test can never reject a true hit
+            c64 = cent.astype(np.float64)
+            rb = np.max(np.linalg.norm(t.astype(np.float64) - c64[:, None, :], axis=2), axis=1)
+            bs = np.zeros((len(t), 4), np.float32)
+            bs[:, 0:3] = cent
+            bs[:, 3] = (rb * (1.0 + 1e-3) + 1e-9).astype(np.float32)
             tt = {
                 "tri": torch.from_numpy(rec).to(dev),
                 "vn": torch.from_numpy(vn).to(dev),
+                "bs": torch.from_numpy(bs).to(dev),
                 "cs": torch.from_numpy(self._cell_start.view(np.int32)).to(dev),
                 "ct": torch.from_numpy((self._cell_tri if len(self._cell_tri)
                                         else np.zeros(1, np.uint32)).view(np.int32)).to(dev),
             }
+            self._neighbourhoods(tt, dev)
             self._dev_cache[key] = tt
         return self._dev_cache[key]
+
+    def _neighbourhoods(self, tt, dev):
+        """Per grid cell, the distinct triangles of its 27-cell gather, built on the device
+        (dmsim_mesh_neighbourhoods): the walk then visits each candidate once."""
+        lib = _lib.load()
+        g = _lib.Geometry()
+        g.mesh_dims[:] = [int(x) for x in self.dims]
+        g.mesh_cell_start = tt["cs"].data_ptr()
+        g.mesh_cell_tri = tt["ct"].data_ptr()
+        n_cells = int(np.prod(self.dims))
+        start = torch.zeros(n_cells + 1, dtype=torch.int64, device=dev)
+        counts = torch.empty(n_cells + 1, dtype=torch.int32, device=dev)
+        s = _lib.stream_handle()
+        _lib.check(lib.dmsim_mesh_neighbourhoods(g, _lib.ptr(counts), None, s),
+                   "dmsim_mesh_neighbourhoods")
+        start[1:] = torch.cumsum(counts[:n_cells].to(torch.int64), 0)
+        total = int(start[-1].item())
+        if total >= 2 ** 31:
+            raise RuntimeError("mesh neighbourhood lists exceed 2^31 entries")
+        nb_start = start.to(torch.int32)
+        nb_tri = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+        _lib.check(lib.dmsim_mesh_neighbourhoods(g, _lib.ptr(nb_start), _lib.ptr(nb_tri), s),
+                   "dmsim_mesh_neighbourhoods")
+        tt["nbs"], tt["nbt"] = nb_start, nb_tri
+        self.n_neighbourhood_entries = total
 
     def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
         tt = self._tables(dev)
@@ -468,8 +503,11 @@ class Mesh(Geometry):
         g.seed_inside = 1
         g.tri = tt["tri"].data_ptr()
         g.tri_vn = tt["vn"].data_ptr()
+        g.tri_bs = tt["bs"].data_ptr()
         g.mesh_cell_start = tt["cs"].data_ptr()
         g.mesh_cell_tri = tt["ct"].data_ptr()
+        g.mesh_nb_start = tt["nbs"].data_ptr()
+        g.mesh_nb_tri = tt["nbt"].data_ptr()
         return g, (tt,)
 
     def classify_position(self, r):

@@ -92,6 +92,11 @@ def main(argv=None):
     if a.report:
         with open(a.report, "w") as f:
             json.dump(rep, f, indent=1)
+        # the held-out queries, predictions and judge signals, for error analysis
+        np.savez_compressed(a.report.rsplit(".", 1)[0] + "_held_out.npz", X=Xh, pred=pred,
+                            ref=ref, ref_se=ref_se,
+                            params=np.array([[p[k] for k in ("radius", "f", "kappa", "rho",
+                                                             "D", "TE")] for p in hp]))
     return rep
 
 

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 3
+#define DMSIM_ABI_VERSION 4
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -121,6 +121,13 @@ typedef struct dmsim_geometry {
   const float* tri_vn;           /* n_tri x 12: smooth normals at A, B, C (+3 padding)        */
   const uint32_t* mesh_cell_start; /* prod(mesh_dims) + 1 (CSR)                              */
   const uint32_t* mesh_cell_tri;   /* triangle indices, each cell in increasing order         */
+  const uint32_t* mesh_nb_start;   /* optional (NULL: the 27 cells are visited one by one):   */
+  const uint32_t* mesh_nb_tri;     /* per cell, the distinct triangles of its 27-cell gather,
+                                      from dmsim_mesh_neighbourhoods()                        */
+  const float* tri_bs;             /* optional n_tri x 4: a bounding sphere (centre, radius) of
+                                      each triangle; a candidate whose sphere misses the step's
+                                      segment is skipped before the Moller-Trumbore test.  The
+                                      radius must cover the float32 vertices (it only prunes). */
 } dmsim_geometry;
 
 /* ---- walk parameters -------------------------------------------------------------------------- */
@@ -212,6 +219,17 @@ int dmsim_walk_noalloc(const dmsim_walk_params* p, const dmsim_geometry* g,
    list of a packed geometry must have been built with reach >= every |step|. */
 int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const float* steps,
                    const float* u, float* r_out, float* dlog_unit, void* stream);
+
+/* Neighbourhood lists of a mesh grid (g->mesh_dims, mesh_cell_start, mesh_cell_tri): for each
+   cell, the triangles of its 27 neighbour cells (indices clamped to the grid) without repeats,
+   in the order the 27-cell gather of mesh.py:208-215 visits them (neighbours in x-major order,
+   each cell's triangles in increasing order, the first occurrence kept).  The walk visits each
+   candidate once instead of once per grid cell it overlaps, with the same result.  Two calls:
+   with nb_tri == NULL it writes each cell's list length to nb_start[0 .. n_cells); the caller
+   turns the lengths into offsets (exclusive prefix sum, nb_start[n_cells] = total) and calls
+   again with nb_tri of `total` entries. */
+int dmsim_mesh_neighbourhoods(const dmsim_geometry* g, uint32_t* nb_start, uint32_t* nb_tri,
+                              void* stream);
 
 /* Replay operator on saved trajectories, trajectories.py:360-641 without relaxation terms:
    phi[m,w] = gamma_dt * sum_t G[t,m,:] . traj[w,t,:]  (trajectories.py:550-552) and

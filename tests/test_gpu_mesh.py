@@ -74,3 +74,32 @@ def test_mesh_sphere_matches_analytic_sphere(cuda):
     s_mesh = d.simulate(40_000, D, wf, d.Mesh(V, F), seed=2)
     s_ana = d.simulate(200_000, D, wf, d.Sphere(5e-6), seed=2)
     np.testing.assert_allclose(s_mesh, s_ana, atol=0.02)
+
+
+@pytest.mark.parametrize("mode", ["reflect", "perm"])
+def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
+    """The per-cell neighbourhood lists (each candidate once) and the bounding-sphere pruning
+    walk exactly like the 27-cell gather that tests a triangle once per grid cell it overlaps."""
+    from dmipy_sim_gb300 import substrates as S
+    mesh, _ = S.ellipsoid_cell_mesh(n_cells=8, faces_per_cell=600, box=24e-6,
+                                    radius_range=(2e-6, 4e-6), permeable=mode == "perm")
+    g = mesh.with_walls(None, 1e-5 if mode == "perm" else None)
+    rng = np.random.default_rng(3)
+    wf, _, _, _ = S.free_waveform_set(4, 40, 0.02, rng, n_shapes=1)
+    G, _ = core._waveform_arrays(wf, g)
+    S_ = core.fused_sub_steps(g, D, wf.dt)
+    res = []
+    for use_lists in (True, False):
+        w = core.PreparedWalk(g, n_walkers=4096, diffusivity=D, G=G, dt=wf.dt, sub_steps=S_,
+                              phase_per_substep=True, seed=9, want_positions=True,
+                              want_walker_signals=True)
+        if not use_lists:
+            w.gdesc.mesh_nb_start = None
+            w.gdesc.mesh_nb_tri = None
+            w.gdesc.tri_bs = None
+        w.launch()
+        res.append(w.result())
+    assert g.n_neighbourhood_entries < len(mesh._cell_tri) * 27
+    for k in ("pos", "phi", "log_w"):
+        assert np.array_equal(res[0].extras[k].cpu().numpy(), res[1].extras[k].cpu().numpy()), k
+    assert res[0].status == res[1].status

@@ -43,7 +43,10 @@ def test_signals_within_3_standard_errors_of_reference(cuda, mc):
         # standard error of the difference: per-walker spread (measured on the GPU run, the
         # same distribution when parity holds) over both sample sizes
         se = sd * np.sqrt(1.0 / ref["n_walkers"] + 1.0 / N_GPU)
-        z = (sig - s_ref) / np.maximum(se, 1e-12)
+        # a signal with no spread across walkers (a CPMG train without gradients: every walker
+        # carries the same weight exp(-t/T2)) is compared to the FP32 rounding of that weight
+        se = np.maximum(se, 1e-6 + 1e-5 * np.abs(s_ref))
+        z = (sig - s_ref) / se
         z_all.append(z.ravel())
         report.append(f"{name}: max|z|={np.max(np.abs(z)):.2f}")
     z = np.concatenate(z_all)
