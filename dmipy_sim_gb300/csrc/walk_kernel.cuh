@@ -153,6 +153,9 @@ __host__ __device__ inline SmemLayout walk_smem_layout(int pm, int w, int M) {
 #ifndef DMSIM_BATCH_MIN_BLOCKS
 #define DMSIM_BATCH_MIN_BLOCKS 2
 #endif
+#ifndef DMSIM_SINGLE_MIN_BLOCKS
+#define DMSIM_SINGLE_MIN_BLOCKS 0
+#endif
 __host__ __device__ constexpr int batch_min_blocks(int pm, int w) {
   return (pm == 0 ? w <= 16 : w <= 4) ? DMSIM_BATCH_MIN_BLOCKS : 1;
 }
@@ -189,7 +192,7 @@ __device__ __forceinline__ int classify_mesh(float x, float y, float z, const Me
 }
 
 template <int GEOM, int WALL, int PM, int W, bool TSM, bool BATCH>
-__global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : 0) k_walk(const __grid_constant__ KArgs a0,
+__global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSIM_SINGLE_MIN_BLOCKS) k_walk(const __grid_constant__ KArgs a0,
                                                  const __grid_constant__ BatchCtl bc) {
   extern __shared__ __align__(128) uint8_t smem[];
   constexpr int ROW = walk_row(PM, W);
