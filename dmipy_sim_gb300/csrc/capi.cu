@@ -153,7 +153,8 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
   pl->lay = walk_smem_layout(pl->pm, pl->width, p->n_meas);
-  pl->smem = pl->lay.off_tab + (pl->tsm ? pl->tab_cs + pl->tab_cand : 0);
+  pl->smem = pl->lay.off_tab + (pl->tsm ? pl->tab_cs + pl->tab_cand : 0) +
+             (g->kind == DMSIM_GEOM_MESH ? kWarps * kMeshScratchBytes : 0);
 
   int dev = 0, n_sm = 0, nb = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(DMSIM_ECUDA, "cudaGetDevice failed");
@@ -339,13 +340,19 @@ __global__ void k_zero(double* p, size_t n) {
 }
 
 // ---- known-answer kernel: one sub-step of the device step functions per input triple ---------
+// The loop is uniform across the block (every lane runs every iteration, lanes past the end on
+// the last input's data without writing), so the mesh step's warp-cooperative searches see all
+// 32 lanes.
 template <int GEOM, int WALL>
 __global__ void k_step_kat(const GeoK g, const MeshK mk, int64_t n, const float* __restrict__ rin,
                            const float* __restrict__ st, const float* __restrict__ uin,
                            const uint32_t* __restrict__ cs, const float4* __restrict__ cand,
                            float* __restrict__ rout, float* __restrict__ dlog) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  extern __shared__ __align__(16) uint8_t kat_smem[];
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const bool live = base + threadIdx.x < n;
+    const int64_t i = live ? base + threadIdx.x : n - 1;
     float x = rin[3 * i], y = rin[3 * i + 1], z = rin[3 * i + 2];
     const float sx = st[3 * i], sy = st[3 * i + 1], sz = st[3 * i + 2];
     const float u = uin ? uin[i] : 0.f;
@@ -381,11 +388,13 @@ __global__ void k_step_kat(const GeoK g, const MeshK mk, int64_t n, const float*
       int cls = 1, pop = 0;
       if (mk.reject && WALL != kPermeate) cls = mesh_classify(mk, x, y, z, pop);
       uint32_t nb = 0, ne = 0;
-      dl = mesh_step<WALL>(x, y, z, ix, iy, iz, cls, pop, sx, sy, sz, u, mk, tl, nb, ne);
+      dl = mesh_step<WALL>(x, y, z, ix, iy, iz, cls, pop, sx, sy, sz, u, mk, tl, nb, ne,
+                           reinterpret_cast<MeshScratch*>(kat_smem) + (threadIdx.x >> 5));
     }
     const float Lx = GEOM == DMSIM_GEOM_MESH ? mk.box[0] : g.L;
     const float Ly = GEOM == DMSIM_GEOM_MESH ? mk.box[1] : g.L;
     const float Lz = GEOM == DMSIM_GEOM_MESH ? mk.box[2] : g.L;
+    if (!live) continue;
     rout[3 * i] = x + Lx * (float)ix;
     rout[3 * i + 1] = y + Ly * (float)iy;
     rout[3 * i + 2] = z + Lz * (float)iz;
@@ -635,7 +644,7 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
   }
   if (n == 0) return DMSIM_OK;
   const int blocks = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
-  fn<<<blocks, 256, 0, (cudaStream_t)stream>>>(make_geok(g), make_meshk(g), n, r_in, steps, u,
+  fn<<<blocks, 256, 8 * kMeshScratchBytes, (cudaStream_t)stream>>>(make_geok(g), make_meshk(g), n, r_in, steps, u,
                                                  g->cell_start,
                                                  reinterpret_cast<const float4*>(g->cand), r_out,
                                                  dlog_unit);
@@ -852,7 +861,8 @@ int batch_plan(dmsim_batch* b) {
       });
     G.n_items = 0;
     for (int m : G.members) G.n_items += b->inst[m].n_items;
-    G.smem = walk_smem_layout(1, b->inst[G.members[0]].pl.width, G.max_m).off_tab + G.max_tab;
+    G.smem = walk_smem_layout(1, b->inst[G.members[0]].pl.width, G.max_m).off_tab + G.max_tab +
+             (b->inst[G.members[0]].g.kind == DMSIM_GEOM_MESH ? kWarps * kMeshScratchBytes : 0);
     if (cudaFuncSetAttribute((const void*)G.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)G.smem) != cudaSuccess)
       return fail(DMSIM_ECUDA, "cudaFuncSetAttribute(%zu B shared) failed", G.smem);

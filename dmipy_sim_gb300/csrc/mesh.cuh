@@ -45,6 +45,16 @@ struct Tri {
   float ax, ay, az, e1x, e1y, e1z, e2x, e2y, e2z, nx, ny, nz;
 };
 
+// Per-warp shared-memory scratch of the cooperative candidate searches: each lane's list range,
+// ray (or point), the inclusive prefix of the warp's list lengths, and the best key found.
+struct MeshScratch {
+  uint32_t incl[32];
+  uint32_t ls[32];
+  float rx[32], ry[32], rz[32], dx[32], dy[32], dz[32], rem[32];
+  unsigned long long best[32];
+};
+constexpr size_t kMeshScratchBytes = sizeof(MeshScratch);
+
 __device__ __forceinline__ Tri load_tri(const MeshK& m, uint32_t k) {
   const float4 a = m.tri[4 * k], b = m.tri[4 * k + 1], c = m.tri[4 * k + 2];
   return Tri{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
@@ -290,25 +300,165 @@ __device__ __forceinline__ void mesh_fold(float& v, int& img, int a, const MeshK
 // One sub-step.  (x, y, z) is the folded position; cls / pop carry the class and gather
 // population of the current position (the leak guard's start state).  Returns -2 * sum d_perp
 // including the side multipliers (rho/D = 1).
+// ---- warp-cooperative candidate searches -----------------------------------------------------
+// Every lane of the warp calls these together (the walk keeps all 32 lanes in step).  A lane's
+// neighbourhood list can hold from none to dozens of triangles, so a lane-per-walker scan runs as
+// long as the warp's longest list while most lanes idle.  Here the warp lays the (walker,
+// candidate) pairs of all its lanes end to end and tests 32 pairs per round; each pair's result
+// goes to its walker's slot as a 64-bit key (distance bits, list position), so the minimum is the
+// nearest candidate and, among equal distances, the first in list order -- exactly what the
+// sequential scan with strict comparisons returns.
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  return v;
+}
+
+__device__ __forceinline__ int scratch_owner(const MeshScratch* w, uint32_t j) {
+  int lo = 0, hi = 31;  // first lane whose inclusive prefix exceeds j
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (w->incl[mid] > j) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ MeshHit mesh_nearest_coop(const MeshK& m, MeshScratch* w, bool need,
+                                                     float gx, float gy, float gz, float r0x,
+                                                     float r0y, float r0z, float dx, float dy,
+                                                     float dz, float rem) {
+  const int lane = threadIdx.x & 31;
+  uint32_t ls = 0, cnt = 0;
+  if (need) {
+    const int cid = (mesh_cell(gx, 0, m) * m.dims[1] + mesh_cell(gy, 1, m)) * m.dims[2] +
+                    mesh_cell(gz, 2, m);
+    ls = m.nbstart[cid];
+    cnt = m.nbstart[cid + 1] - ls;
+  }
+  const uint32_t incl = warp_incl_scan(cnt, lane);
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  MeshHit h{INFINITY, 0.f, 0.f, 0u};
+  if (total == 0) return h;
+  w->incl[lane] = incl;
+  w->ls[lane] = ls;
+  w->rx[lane] = r0x; w->ry[lane] = r0y; w->rz[lane] = r0z;
+  w->dx[lane] = dx; w->dy[lane] = dy; w->dz[lane] = dz;
+  w->rem[lane] = rem;
+  w->best[lane] = ~0ull;
+  __syncwarp();
+#pragma unroll 1
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t j = base + lane;
+    if (j < total) {
+      const int L = scratch_owner(w, j);
+      const uint32_t pos = j - (L ? w->incl[L - 1] : 0u);
+      const uint32_t k = m.nbtri[w->ls[L] + pos];
+      const float ox = w->rx[L], oy = w->ry[L], oz = w->rz[L];
+      const float ux = w->dx[L], uy = w->dy[L], uz = w->dz[L], rm = w->rem[L];
+      bool test = true;
+      if (m.bs != nullptr) {
+        const float4 b = __ldg(m.bs + k);
+        const float cx = b.x - ox, cy = b.y - oy, cz = b.z - oz;
+        const float s = fminf(fmaxf(cx * ux + cy * uy + cz * uz, 0.f), rm);
+        const float ex = cx - s * ux, ey = cy - s * uy, ez = cz - s * uz;
+        test = ex * ex + ey * ey + ez * ez <= b.w * b.w;
+      }
+      if (test) {
+        const Tri T = load_tri(m, k);
+        float u, v;
+        const float t = mt_hit(T, ox, oy, oz, ux, uy, uz, u, v);
+        if (t > m.eps && t < rm)
+          atomicMin(&w->best[L], ((unsigned long long)__float_as_uint(t) << 32) | pos);
+      }
+    }
+  }
+  __syncwarp();
+  const unsigned long long b = w->best[lane];
+  __syncwarp();
+  if (need && b != ~0ull) {
+    const uint32_t k = m.nbtri[ls + (uint32_t)(b & 0xffffffffull)];
+    const Tri T = load_tri(m, k);
+    float u, v;
+    h.t = mt_hit(T, r0x, r0y, r0z, dx, dy, dz, u, v);
+    h.u = u;
+    h.v = v;
+    h.k = k;
+  }
+  return h;
+}
+
+__device__ __forceinline__ int mesh_classify_coop(const MeshK& m, MeshScratch* w, float px,
+                                                  float py, float pz, int& populated) {
+  const int lane = threadIdx.x & 31;
+  const int cid = (mesh_cell(px, 0, m) * m.dims[1] + mesh_cell(py, 1, m)) * m.dims[2] +
+                  mesh_cell(pz, 2, m);
+  const uint32_t ls = m.nbstart[cid];
+  const uint32_t cnt = m.nbstart[cid + 1] - ls;
+  const uint32_t incl = warp_incl_scan(cnt, lane);
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  populated = cnt > 0;
+  if (total == 0) return 1;
+  w->incl[lane] = incl;
+  w->ls[lane] = ls;
+  w->rx[lane] = px; w->ry[lane] = py; w->rz[lane] = pz;
+  w->best[lane] = ~0ull;
+  __syncwarp();
+#pragma unroll 1
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t j = base + lane;
+    if (j < total) {
+      const int L = scratch_owner(w, j);
+      const uint32_t pos = j - (L ? w->incl[L - 1] : 0u);
+      const uint32_t k = m.nbtri[w->ls[L] + pos];
+      const float4 c = m.tri[4 * k + 3];
+      const float ddx = w->rx[L] - c.x, ddy = w->ry[L] - c.y, ddz = w->rz[L] - c.z;
+      const float d = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
+      atomicMin(&w->best[L], ((unsigned long long)__float_as_uint(d) << 32) | pos);
+    }
+  }
+  __syncwarp();
+  const unsigned long long b = w->best[lane];
+  __syncwarp();
+  if (cnt == 0) return 1;
+  const uint32_t kb = m.nbtri[ls + (uint32_t)(b & 0xffffffffull)];
+  const float4 c = m.tri[4 * kb + 3];
+  const float4 nn = m.tri[4 * kb + 2];
+  const float side = (px - c.x) * nn.y + (py - c.y) * nn.z + (pz - c.z) * nn.w;
+  return side < 0.f ? 0 : 1;
+}
+
 template <int WALL>
+// All 32 lanes of a warp call mesh_step together: with neighbourhood lists the candidate searches
+// are warp-cooperative (each lane's outcome is the one its own sequential search gives).
 __device__ __forceinline__ float mesh_step(float& x, float& y, float& z, int& ix, int& iy,
                                            int& iz, int& cls, int& pop, float sx, float sy,
                                            float sz, float u_rand, const MeshK& m, Tally& tl,
-                                           uint32_t& n_budget, uint32_t& n_escape) {
+                                           uint32_t& n_budget, uint32_t& n_escape,
+                                           MeshScratch* ws) {
+  const bool coop = m.nbstart != nullptr;
   const float l = sqrtf(sx * sx + sy * sy + sz * sz);
   float dx = sx / l, dy = sy / l, dz = sz / l;
   float r0x = x, r0y = y, r0z = z, rem = l;
   float dsum = 0.f;
   bool last_reflect = false;
   bool decided = false;
+  bool active = true;  // this lane is still bouncing
 #pragma unroll 1
   for (int it = 0; it < m.maxb; ++it) {
-    const MeshHit h = mesh_nearest(m, x, y, z, r0x, r0y, r0z, dx, dy, dz, rem);
+    if (coop ? !__any_sync(0xffffffffu, active) : !active) break;
+    const MeshHit h = coop ? mesh_nearest_coop(m, ws, active, x, y, z, r0x, r0y, r0z, dx, dy,
+                                               dz, rem)
+                           : mesh_nearest(m, x, y, z, r0x, r0y, r0z, dx, dy, dz, rem);
+    if (!active) continue;
     const bool hit = h.t < INFINITY;
     if constexpr (WALL != kPermeate) {
       if (!hit) {
         last_reflect = false;
-        break;
+        active = false;
+        continue;
       }
       const Tri T = load_tri(m, h.k);
       const bool outward = (dx * T.nx + dy * T.ny + dz * T.nz) > 0.f;
@@ -358,7 +508,7 @@ __device__ __forceinline__ float mesh_step(float& x, float& y, float& z, int& ix
         r0y += rem * dy;
         r0z += rem * dz;
         rem = 0.f;
-        break;
+        active = false;
       }
     }
   }
@@ -372,7 +522,8 @@ __device__ __forceinline__ float mesh_step(float& x, float& y, float& z, int& ix
   if constexpr (WALL != kPermeate) {
     if (m.reject) {
       int pop_new;
-      const int cls_new = mesh_classify(m, nxp, nyp, nzp, pop_new);
+      const int cls_new = coop ? mesh_classify_coop(m, ws, nxp, nyp, nzp, pop_new)
+                               : mesh_classify(m, nxp, nyp, nzp, pop_new);
       if (pop && pop_new && cls_new != cls) {
         ++n_escape;  // leak guard: a decidable class change without a crossing
         return 0.f;

@@ -136,7 +136,8 @@ __host__ __device__ constexpr int walk_row(int pm, int w) { return pm ? w : 3 * 
 __host__ __device__ inline size_t pad16z(size_t v) { return (v + 15) & ~(size_t)15; }
 
 // Shared-memory layout: [waveform chunk ring (2 x kTC x row)] [3 mbarriers + abort flag, 64 B]
-// [basis coefficients C (M x 3 x RT)] [warp reduction scratch (warps x M_red x 3)] [cell list].
+// [basis coefficients C (M x 3 x RT)] [warp reduction scratch (warps x M_red x 3)] [cell list
+// (packed substrates) or one MeshScratch per warp (meshes)].
 struct SmemLayout {
   size_t off_bar, off_cs, off_red, off_tab;
 };
@@ -506,7 +507,8 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
             dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
           } else if constexpr (MESH) {
             dl = mesh_step<WALL>(x, y, z, ix, iy, iz, mcls, mpop, stx, sty, stz, up, a.mk, tw,
-                                 act ? n_budget : n_idle, act ? n_escape : n_idle);
+                                 act ? n_budget : n_idle, act ? n_escape : n_idle,
+                                 reinterpret_cast<MeshScratch*>(tab) + warp);
           }
           if (a.has_weight) logw += rc * dl - dec;
           if (a.phase_sub) {
