@@ -35,7 +35,8 @@ namespace {
 
 constexpr int BM = 128;      // tile rows (tensor-memory lanes)
 constexpr int BK = 64;       // K slice per stage: 64 bf16 = 128 bytes = one swizzle row
-constexpr int kThreads = 192;
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kWaitPolls = 1u << 24;
 
 // ---- PTX helpers --------------------------------------------------------------------------------
@@ -141,7 +142,7 @@ __device__ __forceinline__ float gelu_grad(float x) {
 
 struct GemmArgs {
   int64_t M;
-  int N, K, k_per_split, epi;
+  int N, K, k_per_split, epi, splits;
   float* C;
   const float* bias;
   float* P;
@@ -160,25 +161,89 @@ struct GemmSmem {
   static constexpr uint32_t kTotal = STAGES * kStage + kBars + 1024;
 };
 
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s_addr(b)) : "memory");
+}
+
+// One tile's epilogue for one warp: tensor-memory lanes 32*q .. +31 (tile rows), accumulator
+// columns [c_lo, c_hi) of the tile.
+__device__ __forceinline__ void gemm_epilogue(const GemmArgs& g, uint32_t tacc, int q, int lane,
+                                              int64_t m0, int n0, int split, int c_lo, int c_hi) {
+  const int64_t row = m0 + q * 32 + lane;
+  const bool in = row < g.M;
+  for (int c0 = c_lo; c0 < c_hi; c0 += 32) {
+    float v[32];
+    tmem_ld32(tacc + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+    const int col0 = n0 + c0;
+    if (g.epi == DMSIM_EPI_STORE_F32) {
+      if (in) {
+        float* dst = g.C + ((size_t)split * g.M + row) * g.N + col0;
+#pragma unroll
+        for (int i = 0; i < 32; i += 4)
+          *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+      }
+      continue;
+    }
+    if (g.epi == DMSIM_EPI_BIAS_GELU) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const float p = v[i] + __ldg(g.bias + col0 + i);
+        if (in && g.P) g.P[(size_t)row * g.N + col0 + i] = p;
+        v[i] = gelu(p);
+      }
+    } else {  // DMSIM_EPI_GELU_BWD
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        v[i] = in ? v[i] * gelu_grad(g.P[(size_t)row * g.N + col0 + i]) : 0.f;
+    }
+    if (in) {
+      __nv_bfloat16* dst = g.H + (size_t)row * g.N + col0;
+#pragma unroll
+      for (int i = 0; i < 32; i += 8) {
+        uint4 pk;
+        __nv_bfloat162 h0 = __floats2bfloat162_rn(v[i], v[i + 1]);
+        __nv_bfloat162 h1 = __floats2bfloat162_rn(v[i + 2], v[i + 3]);
+        __nv_bfloat162 h2 = __floats2bfloat162_rn(v[i + 4], v[i + 5]);
+        __nv_bfloat162 h3 = __floats2bfloat162_rn(v[i + 6], v[i + 7]);
+        pk.x = *reinterpret_cast<uint32_t*>(&h0);
+        pk.y = *reinterpret_cast<uint32_t*>(&h1);
+        pk.z = *reinterpret_cast<uint32_t*>(&h2);
+        pk.w = *reinterpret_cast<uint32_t*>(&h3);
+        *reinterpret_cast<uint4*>(dst + i) = pk;
+      }
+      if (g.HT) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+          g.HT[(size_t)(col0 + i) * g.ldht + row] = __float2bfloat16_rn(v[i]);
+      }
+    }
+  }
+}
+
+// Persistent GEMM: each CTA walks the tiles blockIdx.x, +gridDim.x, ... (m fastest, then n, then
+// the K split).  Two accumulators of BN columns in tensor memory let the epilogue of one tile run
+// while the next tile's MMAs fill the other: the MMA issuer waits on acc_empty (released by the 8
+// epilogue warps after their last tcgen05.ld of that accumulator), the epilogue waits on acc_full
+// (committed after the tile's last MMA).
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(kThreads, 1)
     k_gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
            const GemmArgs g) {
   using L = GemmSmem<BN, STAGES>;
   extern __shared__ uint8_t smem_raw[];
-  // 1024-byte alignment for the swizzled stages
   uint8_t* smem = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
   uint64_t* empty = full + STAGES;
-  uint64_t* acc_bar = empty + STAGES;
-  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(acc_bar + 1);
+  uint64_t* acc_full = empty + STAGES;   // [2]
+  uint64_t* acc_empty = acc_full + 2;    // [2]
+  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(acc_empty + 2);
   volatile uint32_t* abort_flag = tmem_slot + 1;
   volatile int* consumed = reinterpret_cast<volatile int*>(tmem_slot + 2);
+  volatile int* committed = reinterpret_cast<volatile int*>(tmem_slot + 3);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t m0 = (int64_t)blockIdx.x * BM;
-  const int n0 = blockIdx.y * BN;
-  const int kb = blockIdx.z * g.k_per_split;
+  const int n_m = (int)((g.M + BM - 1) / BM), n_n = g.N / BN;
+  const int n_tiles = n_m * n_n * g.splits;
   const int n_k = g.k_per_split / BK;
 
   if (threadIdx.x == 0) {
@@ -186,15 +251,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       bar_init(&full[s], 1);
       bar_init(&empty[s], 1);
     }
-    bar_init(acc_bar, 1);
+    for (int a = 0; a < 2; ++a) {
+      bar_init(&acc_full[a], 1);
+      bar_init(&acc_empty[a], kEpiWarps);
+    }
     *abort_flag = 0;
     *consumed = 0;
+    *committed = -1;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      s_addr((const void*)tmem_slot)),
-                 "r"(BN)
+                 "r"(2 * BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -203,118 +272,100 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  int issued = 0;  // warp 0 lane 0: stages whose loads were issued
+  int issued = 0;  // warp 0 lane 0: k-steps whose loads were issued
   if (warp == 0) {
     if (lane == 0) {
-      for (int k = 0; k < n_k && !*abort_flag; ++k) {
-        const int s = k % STAGES;
-        if (!bar_wait(&empty[s], ((k / STAGES) & 1) ^ 1)) {
-          *abort_flag = 1;
-          break;
+      int qk = 0;
+      for (int tile = blockIdx.x; tile < n_tiles && !*abort_flag; tile += gridDim.x) {
+        const int mt = tile % n_m, rest = tile / n_m;
+        const int64_t m0 = (int64_t)mt * BM;
+        const int n0 = (rest % n_n) * BN, kb = (rest / n_n) * g.k_per_split;
+        for (int k = 0; k < n_k; ++k, ++qk) {
+          const int s = qk % STAGES;
+          if (!bar_wait(&empty[s], ((qk / STAGES) & 1) ^ 1)) {
+            *abort_flag = 1;
+            break;
+          }
+          uint8_t* sa = smem + s * L::kStage;
+          bar_expect(&full[s], L::kStage);
+          tma_load_2d(sa, &map_a, kb + k * BK, (int)m0, &full[s]);
+          tma_load_2d(sa + L::kA, &map_b, kb + k * BK, n0, &full[s]);
+          issued = qk + 1;
         }
-        uint8_t* sa = smem + s * L::kStage;
-        bar_expect(&full[s], L::kStage);
-        tma_load_2d(sa, &map_a, kb + k * BK, (int)m0, &full[s]);
-        tma_load_2d(sa + L::kA, &map_b, kb + k * BK, n0, &full[s]);
-        issued = k + 1;
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = instr_desc(BM, BN);
+      int qk = 0, it = 0;
       bool ok = true;
-      for (int k = 0; k < n_k && ok; ++k) {
-        const int s = k % STAGES;
-        if (!bar_wait(&full[s], (k / STAGES) & 1)) {
+      for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++it) {
+        const int acc = it & 1;
+        if (!bar_wait(&acc_empty[acc], ((it >> 1) & 1) ^ 1)) {
           *abort_flag = 1;
-          ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t a0 = s_addr(smem + s * L::kStage);
-        const uint32_t b0 = a0 + L::kA;
+        const uint32_t tacc = tmem + (uint32_t)(acc * BN);
+        for (int k = 0; k < n_k; ++k, ++qk) {
+          const int s = qk % STAGES;
+          if (!bar_wait(&full[s], (qk / STAGES) & 1)) {
+            *abort_flag = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = s_addr(smem + s * L::kStage);
+          const uint32_t b0 = a0 + L::kA;
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; ++kk)
-          mma_bf16(tmem, smem_desc(a0 + kk * 32), smem_desc(b0 + kk * 32), idesc,
-                   (k > 0 || kk > 0) ? 1u : 0u);
-        tc_commit(&empty[s]);
-        *consumed = k + 1;
+          for (int kk = 0; kk < BK / 16; ++kk)
+            mma_bf16(tacc, smem_desc(a0 + kk * 32), smem_desc(b0 + kk * 32), idesc,
+                     (k > 0 || kk > 0) ? 1u : 0u);
+          tc_commit(&empty[s]);
+          *consumed = qk + 1;
+        }
+        tc_commit(&acc_full[acc]);  // also after an abort: fires when the issued MMAs finish
+        *committed = it;
       }
-      tc_commit(acc_bar);  // also after an abort: signals when the issued MMAs are done
     }
   } else {
-    // epilogue warps 2..5: tensor-memory lanes 32 * (warp % 4) .. + 31
-    const int q = warp & 3;
-    const int64_t row = m0 + q * 32 + lane;
-    const bool ok = bar_wait(acc_bar, 0);
-    tc_fence_after();
-    if (!ok) {
-      *abort_flag = 1;
-    } else if (!*abort_flag) {
-      const bool in = row < g.M;
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        float v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-        const int col0 = n0 + c0;
-        if (g.epi == DMSIM_EPI_STORE_F32) {
-          if (in) {
-            float* dst = g.C + ((size_t)blockIdx.z * g.M + row) * g.N + col0;
-#pragma unroll
-            for (int i = 0; i < 32; i += 4)
-              *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-          }
-          continue;
-        }
-        if (g.epi == DMSIM_EPI_BIAS_GELU) {
-#pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const float p = v[i] + __ldg(g.bias + col0 + i);
-            if (in && g.P) g.P[(size_t)row * g.N + col0 + i] = p;
-            v[i] = gelu(p);
-          }
-        } else {  // DMSIM_EPI_GELU_BWD
-#pragma unroll
-          for (int i = 0; i < 32; ++i)
-            v[i] = in ? v[i] * gelu_grad(g.P[(size_t)row * g.N + col0 + i]) : 0.f;
-        }
-        if (in) {
-          __nv_bfloat16* dst = g.H + (size_t)row * g.N + col0;
-#pragma unroll
-          for (int i = 0; i < 32; i += 8) {
-            uint4 pk;
-            __nv_bfloat162 h0 = __floats2bfloat162_rn(v[i], v[i + 1]);
-            __nv_bfloat162 h1 = __floats2bfloat162_rn(v[i + 2], v[i + 3]);
-            __nv_bfloat162 h2 = __floats2bfloat162_rn(v[i + 4], v[i + 5]);
-            __nv_bfloat162 h3 = __floats2bfloat162_rn(v[i + 6], v[i + 7]);
-            pk.x = *reinterpret_cast<uint32_t*>(&h0);
-            pk.y = *reinterpret_cast<uint32_t*>(&h1);
-            pk.z = *reinterpret_cast<uint32_t*>(&h2);
-            pk.w = *reinterpret_cast<uint32_t*>(&h3);
-            *reinterpret_cast<uint4*>(dst + i) = pk;
-          }
-          if (g.HT) {
-#pragma unroll
-            for (int i = 0; i < 32; ++i)
-              g.HT[(size_t)(col0 + i) * g.ldht + row] = __float2bfloat16_rn(v[i]);
-          }
-        }
+    // epilogue warps 2..9: lane quarter warp % 4, column half (warp - 2) / 4
+    const int q = warp & 3, half = (warp - 2) >> 2;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
+      const int acc = it & 1;
+      const bool ok = bar_wait(&acc_full[acc], (it >> 1) & 1);
+      tc_fence_after();
+      if (!ok || *abort_flag) {
+        *abort_flag = 1;
+        break;
       }
+      const int mt = tile % n_m, rest = tile / n_m;
+      gemm_epilogue(g, tmem + (uint32_t)(acc * BN), q, lane, (int64_t)mt * BM,
+                    (rest % n_n) * BN, rest / n_n, half * (BN / 2), (half + 1) * (BN / 2));
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) bar_arrive(&acc_empty[acc]);
     }
   }
   tc_fence_before();
   __syncthreads();
   if (*abort_flag) {
-    // drain before leaving: the loads still in flight, then the issued MMAs (bounded waits)
+    // drain before leaving: the loads still in flight, then the last committed MMAs (bounded)
     if (threadIdx.x == 0) {
       atomicAdd(g.err, 1u);
       for (int k = *consumed; k < issued; ++k) bar_wait(&full[k % STAGES], (k / STAGES) & 1);
     }
-    if (warp == 1 && lane == 0) bar_wait(acc_bar, 0);
+    if (warp == 1 && lane == 0 && *committed >= 0) {
+      const int it = *committed;
+      bar_wait(&acc_full[it & 1], (it >> 1) & 1);
+    }
     __syncthreads();
   }
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(2 * BN)
                  : "memory");
   }
 }
@@ -501,7 +552,15 @@ int launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, const GemmArgs& a,
       return err(DMSIM_ECUDA, "gemm: cudaFuncSetAttribute failed");
     attr = true;
   }
-  dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)(N / BN), (unsigned)splits);
+  static int n_sm = 0;
+  if (n_sm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm < 1) n_sm = 1;
+  }
+  const int64_t tiles = ((M + BM - 1) / BM) * (N / BN) * splits;
+  const int grid = (int)(tiles < n_sm ? tiles : n_sm);
   k_gemm<BN, STAGES><<<grid, kThreads, L::kTotal, st>>>(ma, mb, a);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return err(DMSIM_ECUDA, cudaGetErrorString(e));
@@ -542,6 +601,7 @@ int dmsim_gemm_bf16(const dmsim_gemm* g, void* stream) {
   a.N = g->N;
   a.K = g->K;
   a.k_per_split = g->K / splits;
+  a.splits = splits;
   a.epi = g->epilogue;
   a.C = g->C;
   a.bias = g->bias;
