@@ -63,15 +63,22 @@ def in_hull(params, wf=None):
     return True
 
 
-def draw_instances(n, seed, n_meas=256, n_t=200, n_walkers=8192, n_objects=64):
+def draw_instances(n, seed, n_meas=256, n_t=200, n_walkers=8192, n_objects=64,
+                   radius_sampling="uniform"):
     """``n`` packed-cylinder instances with parameters uniform in the hull and free waveform
     sets of ``n_meas`` measurements; returns (instances, params).  Each substrate holds
     ``n_objects`` cylinders, enough that one packing's signal is close to the mean over packings
-    of the same radius and volume fraction (the 5 substrate inputs do not name the packing)."""
+    of the same radius and volume fraction (the 5 substrate inputs do not name the packing).
+    ``radius_sampling="mixture"`` draws half the radii log-uniformly instead, putting more
+    substrates at small radii, where the signal changes fastest with the parameters."""
     rng = np.random.default_rng(int(seed))
     insts, params = [], []
+    lo, hi = HULL["radius"]
     for i in range(n):
-        r = rng.uniform(*HULL["radius"])
+        if radius_sampling == "mixture" and rng.uniform() < 0.5:
+            r = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        else:
+            r = rng.uniform(lo, hi)
         f = rng.uniform(*HULL["f"])
         kappa = rng.uniform(*HULL["kappa"])
         rho = rng.uniform(*HULL["rho"])
@@ -207,10 +214,11 @@ class Surrogate:
 
 
 def build_training_set(n_instances, seed=0, n_meas=256, n_t=200, n_walkers=8192, log=None,
-                       tuning=None, form="dimensionless"):
+                       tuning=None, form="dimensionless", radius_sampling="uniform"):
     """(X, y, se, params, GPU seconds) from ``n_instances`` batched-walk instances."""
     t0 = time.time()
-    insts, params = draw_instances(n_instances, seed, n_meas, n_t, n_walkers)
+    insts, params = draw_instances(n_instances, seed, n_meas, n_t, n_walkers,
+                                   radius_sampling=radius_sampling)
     if log is not None:
         log(f"  drew {n_instances} instances in {time.time() - t0:.1f} s")
     sig, se, gpu_s = monte_carlo(insts, tuning, log=log)

@@ -1,9 +1,10 @@
 """Train the packed-cylinder surrogate from batched Monte-Carlo signals and judge it against the
 walk at high walker counts on held-out substrates.
 
-    python -m dmipy_sim_gb300.train_surrogate --instances 12000 --out surrogate.npz
+    python -m dmipy_sim_gb300.train_surrogate --instances 20000 --out surrogate.npz
 
-Steps: draw ``instances`` substrates uniformly in the hull (256 free measurements each), walk
+Steps: draw ``instances`` substrates in the hull (256 free measurements each; radii half uniform,
+half log-uniform), walk
 them with the batched kernel at ``walkers`` walkers, fit the MLP (graph-captured AdamW steps on
 the tensor cores), then draw ``held_out`` new substrates, walk them at ``judge_walkers`` and
 report the surrogate's absolute error against them, with the throughput of both methods.
@@ -21,9 +22,9 @@ from . import surrogate as SG
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--instances", type=int, default=12000)
+    ap.add_argument("--instances", type=int, default=20000)
     ap.add_argument("--meas", type=int, default=256)
-    ap.add_argument("--walkers", type=int, default=8192)
+    ap.add_argument("--walkers", type=int, default=4096)
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--held-out", type=int, default=24)
@@ -32,6 +33,7 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--form", default="dimensionless", choices=["dimensionless", "raw"])
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--radius-sampling", default="mixture", choices=["uniform", "mixture"])
     ap.add_argument("--out", default="surrogate.npz")
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
@@ -43,7 +45,8 @@ def main(argv=None):
     log(f"training set: {a.instances} instances x {a.meas} measurements, {a.walkers} walkers")
     X, y, se, params, gpu_train_mc = SG.build_training_set(a.instances, a.seed, a.meas,
                                                            n_walkers=a.walkers, log=log,
-                                                           form=a.form)
+                                                           form=a.form,
+                                                           radius_sampling=a.radius_sampling)
     log(f"  {len(y)} signals, median SE {np.median(se):.4f}, MC {gpu_train_mc:.1f} GPU s")
     # validation split: the last 5 % of instances
     n_val = max(1, a.instances // 20) * a.meas
@@ -78,6 +81,7 @@ def main(argv=None):
     sur_s = e0.elapsed_time(e1) * 1e-3
     rep = {
         "instances": a.instances, "signals": int(len(y)), "walkers": a.walkers, "form": a.form,
+        "radius_sampling": a.radius_sampling,
         "train_mc_gpu_s": gpu_train_mc, "train_s": train_s, "epochs": a.epochs,
         "final_train_mse": hist[-1][0], "val_mae_vs_training_mc": hist[-1][1],
         "held_out_instances": a.held_out, "held_out_signals": int(len(ref)),
