@@ -348,7 +348,33 @@ def _mc_configs():
         "cpmg_sph": dict(geom=("sph", 5e-6, None, None), wf=("cpmg",), n=4000, api="cpmg",
                          T2=0.06),
         "cpmg_free": dict(geom=("free",), wf=("cpmg_g",), n=4000, api="cpmg", T2=0.08),
+        # a closed icosphere mesh (4 um, 320 triangles); walkers start uniformly inside it from
+        # explicit positions (mesh_r0), since the reference seeds meshes through trimesh
+        "mesh_reflect": dict(geom=("mesh", None), wf=("pgse_mesh",), n=1600, api="simulate",
+                             r0="mesh"),
+        "mesh_perm": dict(geom=("mesh", 1e-5), wf=("pgse_mesh",), n=640, api="simulate",
+                          r0="mesh"),
     }
+
+
+def mesh_surface():
+    """The closed icosphere of the mesh fixtures (vertices, faces), from this package."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from dmipy_sim_gb300.mesh import icosphere
+    return icosphere(4e-6, 2)
+
+
+def mesh_r0(n, seed):
+    """n positions uniform inside the fixture mesh (rejection by ray-crossing parity)."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from dmipy_sim_gb300.mesh import mesh_contains
+    V, F = mesh_surface()
+    rng = np.random.default_rng(int(seed))
+    out = []
+    while sum(len(o) for o in out) < n:
+        p = rng.uniform(-4e-6, 4e-6, size=(2 * n, 3))
+        out.append(p[mesh_contains(V, F, p)])
+    return np.concatenate(out)[:n].astype(np.float32)
 
 
 def build_waveform(wfm, spec):
@@ -369,6 +395,9 @@ def build_waveform(wfm, spec):
         return wfm.cpmg(8, 12e-3, 0.0, [[1, 0, 0]], n_t_per_echo=60)
     if name == "cpmg_g":
         return wfm.cpmg(6, 10e-3, 0.02, [[1, 0, 0], [0, 0, 1]], n_t_per_echo=50)
+    if name == "pgse_mesh":
+        return wfm.set_b(wfm.pgse(0.003, 0.008, 0.2, [[1, 0, 0], [0, 0, 1], [0.6, 0.8, 0]], 60),
+                         [5e8, 1e9, 2e9])
     raise KeyError(name)
 
 
@@ -394,6 +423,9 @@ def build_geometry(geo, spec):
         sr = np.full(10, 1.5e-6)
         cen, L, _ = geo.pack_spheres(sr, target_vf=0.25, seed=3)
         return geo.PackedSpheres(sr, cen, L)
+    if kind == "mesh":
+        V, F = mesh_surface()
+        return geo.Mesh(V, F, permeability=spec[1])
     raise KeyError(kind)
 
 
@@ -403,14 +435,19 @@ def _mc_worker(args):
     import contextlib
     import io
     wf = build_waveform(m["waveforms"], cfg["wf"])
-    g = build_geometry(m["geometries"], cfg["geom"])
+    if cfg["geom"][0] == "mesh":
+        import importlib
+        g = build_geometry(importlib.import_module("dmipy_sim.mesh"), cfg["geom"])
+    else:
+        g = build_geometry(m["geometries"], cfg["geom"])
+    r0 = mesh_r0(n, seed) if cfg.get("r0") == "mesh" else None
     with contextlib.redirect_stdout(io.StringIO()):
         if cfg["api"] == "cpmg":
             s = m["core"].simulate_cpmg(n, D, wf, g, T2=cfg.get("T2"), seed=seed,
                                         require_gpu=False)
         else:
             s = m["core"].simulate(n, D, wf, g, seed=seed, T2=cfg.get("T2"), require_gpu=False,
-                                   engine=cfg.get("engine", "auto"))
+                                   engine=cfg.get("engine", "auto"), r0=r0)
     return name, n, np.asarray(s, np.float64)
 
 

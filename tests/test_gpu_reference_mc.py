@@ -6,7 +6,7 @@ import pytest
 
 import dmipy_sim_gb300 as d
 from dmipy_sim_gb300 import core
-from golden.make_golden import build_geometry, build_waveform
+from golden.make_golden import build_geometry, build_waveform, mesh_r0
 
 pytestmark = pytest.mark.gpu
 D = 2e-9
@@ -23,11 +23,13 @@ def _gpu(cfg, n, seed):
         engine = cfg.get("engine", "auto")
         gap = core._replay_gap(g, return_positions=False, return_compartments=False,
                                return_walker_signals=False, diffusivity=D)
-        rep = engine != "fused" and gap is None
+        rep = engine != "fused" and gap is None and core._replay_auto_allowed(g)
         S = core.replay_sub_steps(g, D, wf.dt) if rep else core.fused_sub_steps(g, D, wf.dt)
         ps, echo = not rep, None
+    r0 = mesh_r0(n, seed) if cfg.get("r0") == "mesh" else None
     res = core.run_walk(g, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
-                        phase_per_substep=ps, seed=seed, chi=chi, T2=cfg.get("T2"), echo_idx=echo)
+                        phase_per_substep=ps, seed=seed, chi=chi, T2=cfg.get("T2"), echo_idx=echo,
+                        r0=r0)
     sig = res.signal if cfg["api"] == "cpmg" else res.signal[0]
     sd = res.stderr * np.sqrt(n) if cfg["api"] == "cpmg" else res.stderr[0] * np.sqrt(n)
     return sig, sd
@@ -38,11 +40,12 @@ def test_signals_within_3_standard_errors_of_reference(cuda, mc):
     report = []
     for name, ref in sorted(mc.items()):
         cfg = ref["config"]
-        sig, sd = _gpu(cfg, N_GPU, seed=2024)
+        n_gpu = 50_000 if cfg.get("r0") == "mesh" else N_GPU
+        sig, sd = _gpu(cfg, n_gpu, seed=2024)
         s_ref = np.asarray(ref["signal"]).reshape(sig.shape)
         # standard error of the difference: per-walker spread (measured on the GPU run, the
         # same distribution when parity holds) over both sample sizes
-        se = sd * np.sqrt(1.0 / ref["n_walkers"] + 1.0 / N_GPU)
+        se = sd * np.sqrt(1.0 / ref["n_walkers"] + 1.0 / n_gpu)
         # a signal with no spread across walkers (a CPMG train without gradients: every walker
         # carries the same weight exp(-t/T2)) is compared to the FP32 rounding of that weight
         se = np.maximum(se, 1e-6 + 1e-5 * np.abs(s_ref))
