@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 4
+DMSIM_ABI_VERSION = 5
 TILE_WALKERS = 320
 
 GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
@@ -41,6 +41,7 @@ class Geometry(C.Structure):
         ("kappa_over_D", C.c_float), ("rho_over_D", C.c_float), ("L", C.c_float),
         ("n_objects", C.c_int32), ("grid_n", C.c_int32), ("cell_h", C.c_float),
         ("reach", C.c_float), ("n_cand", C.c_int32), ("need_min_image", C.c_int32),
+        ("max_cell_cand", C.c_int32), ("pad2", C.c_int32),
         ("cell_start", C.c_void_p), ("cand", C.c_void_p), ("cand_obj", C.c_void_p),
         ("n_tri", C.c_int32), ("mesh_dims", C.c_int32 * 3), ("periodic", C.c_int32 * 3),
         ("max_bounces", C.c_int32), ("grid_min", C.c_float * 3), ("mesh_cell", C.c_float),

@@ -33,6 +33,9 @@ namespace dmsim {
 enum { kReflect = DMSIM_WALL_REFLECT, kRelax = DMSIM_WALL_RELAX, kPermeate = DMSIM_WALL_PERMEATE };
 
 constexpr float kGrazeTol = 1e-4f;
+// Centre of the zero-radius dummy object that pads a cell's candidate slots (its squared
+// distances stay finite in FP32 and no wall test can select it).
+constexpr float kFarAway = 1e18f;
 
 struct Tally {
   uint32_t clamp = 0, graze = 0, transmit = 0;
@@ -44,6 +47,7 @@ struct GeoK {
   float L, halfL, inv_h;
   int n;   // cells per axis
   int mi;  // 1 when some cell lists two images of one object: candidates need the min-image test
+  int kmax;  // 1..4: every cell's list is scanned as kmax slots (uniform trip count); 0: as is
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -316,9 +320,13 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
   bool hit_in = false;
   const float ex = x + sx, ey = y + sy;
   float pe = 1.f, pqx = 0.f, pqy = 0.f, pR = 1.f;
-#pragma unroll 1
-  for (uint32_t k = kb; k < ke; ++k) {
-    const float4 C = cand[k];
+  // with a uniform slot count every lane runs the same trip count; a slot past the cell's list
+  // holds a zero-radius object far outside the cell, which no test can select
+  const uint32_t n_slots = g.kmax ? (uint32_t)g.kmax : ke - kb;
+#pragma unroll 2
+  for (uint32_t j = 0; j < n_slots; ++j) {
+    const uint32_t k = kb + j;
+    const float4 C = k < ke ? cand[k] : make_float4(kFarAway, kFarAway, kFarAway, 0.f);
     const float R2 = C.w * C.w;
     if constexpr (WALL != kPermeate) {
       const float fx = ex - C.x, fy = ey - C.y;
@@ -488,9 +496,11 @@ __device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, i
   bool hit_in = false;
   const float ex = x + sx, ey = y + sy, ez = z + sz;
   float pe = 1.f, pqx = 0.f, pqy = 0.f, pqz = 0.f, pR = 1.f;
-#pragma unroll 1
-  for (uint32_t k = kb; k < ke; ++k) {
-    const float4 C = cand[k];
+  const uint32_t n_slots = g.kmax ? (uint32_t)g.kmax : ke - kb;  // see packed_cyl_step
+#pragma unroll 2
+  for (uint32_t j = 0; j < n_slots; ++j) {
+    const uint32_t k = kb + j;
+    const float4 C = k < ke ? cand[k] : make_float4(kFarAway, kFarAway, kFarAway, 0.f);
     const float R2 = C.w * C.w;
     if constexpr (WALL != kPermeate) {
       const float fx = ex - C.x, fy = ey - C.y, fz = ez - C.z;

@@ -407,8 +407,10 @@ class _Packed(Geometry):
             n_cells = n ** self._dim
             cell_of = np.repeat(np.arange(n_cells), np.diff(start[:n_cells + 1].astype(np.int64)))
             need_mi = bool(np.any((cell_of[1:] == cell_of[:-1]) & (obj[1:] == obj[:-1])))
-            self._dev_cache = {key: (n, reach, t_start, t_cand, t_obj, len(obj), need_mi)}
-        n, reach, t_start, t_cand, t_obj, n_cand, need_mi = self._dev_cache[key]
+            max_cand = int(np.max(np.diff(start[:n_cells + 1].astype(np.int64)))) if n_cells else 0
+            self._dev_cache = {key: (n, reach, t_start, t_cand, t_obj, len(obj), need_mi,
+                                     max_cand)}
+        n, reach, t_start, t_cand, t_obj, n_cand, need_mi, max_cand = self._dev_cache[key]
         g = self._base_desc(self._kind, wall_mode, rho_over_D, kappa_over_D)
         g.radius = float(np.min(self._radii_np))
         g.eps_detect = self._eps_detect
@@ -420,6 +422,7 @@ class _Packed(Geometry):
         g.reach = reach
         g.n_cand = n_cand
         g.need_min_image = 1 if need_mi else 0
+        g.max_cell_cand = max_cand
         g.cell_start = t_start.data_ptr()
         g.cand = t_cand.data_ptr()
         g.cand_obj = t_obj.data_ptr()

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 4
+#define DMSIM_ABI_VERSION 5
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -91,6 +91,10 @@ typedef struct dmsim_geometry {
   int32_t n_cand;
   int32_t need_min_image; /* 1 if a cell lists two images of one object (then each candidate is
                              checked to be its object's minimum image from the walker) */
+  int32_t max_cell_cand;  /* most candidates any cell lists (0: unknown); up to 4, every walker
+                             of a warp scans that many slots, so the scan has no divergent trip
+                             count (slots past a cell's list hold an unreachable dummy) */
+  int32_t pad2;
   const uint32_t* cell_start; /* grid_n^d + 1 */
   const float* cand;          /* n_cand x 4 */
   const int32_t* cand_obj;    /* n_cand: object index of each candidate (classification) */
