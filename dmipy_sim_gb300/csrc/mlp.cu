@@ -158,7 +158,8 @@ struct GemmSmem {
   static constexpr uint32_t kB = BN * BK * 2;
   static constexpr uint32_t kStage = kA + kB;
   static constexpr uint32_t kBars = 1024;  // barriers + tensor-memory address, then 1 KB align
-  static constexpr uint32_t kTotal = STAGES * kStage + kBars + 1024;
+  static constexpr uint32_t kEpi = kEpiWarps * 32 * 33 * 4;  // per-warp 32 x 33 staging tiles
+  static constexpr uint32_t kTotal = STAGES * kStage + kBars + kEpi + 1024;
 };
 
 __device__ __forceinline__ void bar_arrive(uint64_t* b) {
@@ -166,57 +167,80 @@ __device__ __forceinline__ void bar_arrive(uint64_t* b) {
 }
 
 // One tile's epilogue for one warp: tensor-memory lanes 32*q .. +31 (tile rows), accumulator
-// columns [c_lo, c_hi) of the tile.
+// columns [c_lo, c_hi) of the tile.  A lane holds one row's 32 consecutive values per chunk, so
+// row-major stores from registers would send the 32 lanes to 32 different rows.  The warp
+// instead stages each 32 x 32 chunk in its shared-memory tile `st` (padded to 33 columns) and
+// writes it back row by row, two rows per instruction (lanes 0-15 and 16-31, two values each):
+// every store covers whole 64- or 128-byte row segments.  The transposed copy (HT) is already
+// contiguous from registers (lane = row).
 __device__ __forceinline__ void gemm_epilogue(const GemmArgs& g, uint32_t tacc, int q, int lane,
-                                              int64_t m0, int n0, int split, int c_lo, int c_hi) {
-  const int64_t row = m0 + q * 32 + lane;
+                                              int64_t m0, int n0, int split, int c_lo, int c_hi,
+                                              float* st) {
+  const int64_t row0 = m0 + q * 32;
+  const int64_t row = row0 + lane;
   const bool in = row < g.M;
+  const int half = lane >> 4, pair = lane & 15;  // write-back: row parity, column pair
   for (int c0 = c_lo; c0 < c_hi; c0 += 32) {
     float v[32];
     tmem_ld32(tacc + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
     const int col0 = n0 + c0;
     if (g.epi == DMSIM_EPI_STORE_F32) {
-      if (in) {
-        float* dst = g.C + ((size_t)split * g.M + row) * g.N + col0;
 #pragma unroll
-        for (int i = 0; i < 32; i += 4)
-          *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+      for (int i = 0; i < 32; ++i) st[lane * 33 + i] = v[i];
+      __syncwarp();
+      for (int r = half; r < 32; r += 2) {
+        if (row0 + r < g.M) {
+          float* dst = g.C + ((size_t)split * g.M + row0 + r) * g.N + col0;
+          *reinterpret_cast<float2*>(dst + 2 * pair) =
+              make_float2(st[r * 33 + 2 * pair], st[r * 33 + 2 * pair + 1]);
+        }
       }
+      __syncwarp();
       continue;
     }
     if (g.epi == DMSIM_EPI_BIAS_GELU) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const float p = v[i] + __ldg(g.bias + col0 + i);
-        if (in && g.P) g.P[(size_t)row * g.N + col0 + i] = p;
-        v[i] = gelu(p);
+      for (int i = 0; i < 32; ++i) v[i] += __ldg(g.bias + col0 + i);
+      if (g.P) {  // pre-activations for the backward pass, staged like the outputs
+#pragma unroll
+        for (int i = 0; i < 32; ++i) st[lane * 33 + i] = v[i];
+        __syncwarp();
+        for (int r = half; r < 32; r += 2) {
+          if (row0 + r < g.M)
+            *reinterpret_cast<float2*>(g.P + (size_t)(row0 + r) * g.N + col0 + 2 * pair) =
+                make_float2(st[r * 33 + 2 * pair], st[r * 33 + 2 * pair + 1]);
+        }
+        __syncwarp();
       }
-    } else {  // DMSIM_EPI_GELU_BWD
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = gelu(v[i]);
+    } else {  // DMSIM_EPI_GELU_BWD: the pre-activations arrive through the same staging
+      for (int r = half; r < 32; r += 2) {
+        float2 p = make_float2(0.f, 0.f);
+        if (row0 + r < g.M)
+          p = *reinterpret_cast<const float2*>(g.P + (size_t)(row0 + r) * g.N + col0 + 2 * pair);
+        st[r * 33 + 2 * pair] = p.x;
+        st[r * 33 + 2 * pair + 1] = p.y;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = in ? v[i] * gelu_grad(st[lane * 33 + i]) : 0.f;
+      __syncwarp();
+    }
+    if (g.HT && in) {
 #pragma unroll
       for (int i = 0; i < 32; ++i)
-        v[i] = in ? v[i] * gelu_grad(g.P[(size_t)row * g.N + col0 + i]) : 0.f;
+        g.HT[(size_t)(col0 + i) * g.ldht + row] = __float2bfloat16_rn(v[i]);
     }
-    if (in) {
-      __nv_bfloat16* dst = g.H + (size_t)row * g.N + col0;
 #pragma unroll
-      for (int i = 0; i < 32; i += 8) {
-        uint4 pk;
-        __nv_bfloat162 h0 = __floats2bfloat162_rn(v[i], v[i + 1]);
-        __nv_bfloat162 h1 = __floats2bfloat162_rn(v[i + 2], v[i + 3]);
-        __nv_bfloat162 h2 = __floats2bfloat162_rn(v[i + 4], v[i + 5]);
-        __nv_bfloat162 h3 = __floats2bfloat162_rn(v[i + 6], v[i + 7]);
-        pk.x = *reinterpret_cast<uint32_t*>(&h0);
-        pk.y = *reinterpret_cast<uint32_t*>(&h1);
-        pk.z = *reinterpret_cast<uint32_t*>(&h2);
-        pk.w = *reinterpret_cast<uint32_t*>(&h3);
-        *reinterpret_cast<uint4*>(dst + i) = pk;
-      }
-      if (g.HT) {
-#pragma unroll
-        for (int i = 0; i < 32; ++i)
-          g.HT[(size_t)(col0 + i) * g.ldht + row] = __float2bfloat16_rn(v[i]);
-      }
+    for (int i = 0; i < 32; ++i) st[lane * 33 + i] = v[i];
+    __syncwarp();
+    for (int r = half; r < 32; r += 2) {
+      if (row0 + r < g.M)
+        *reinterpret_cast<__nv_bfloat162*>(g.H + (size_t)(row0 + r) * g.N + col0 + 2 * pair) =
+            __floats2bfloat162_rn(st[r * 33 + 2 * pair], st[r * 33 + 2 * pair + 1]);
     }
+    __syncwarp();
   }
 }
 
@@ -240,6 +264,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile uint32_t* abort_flag = tmem_slot + 1;
   volatile int* consumed = reinterpret_cast<volatile int*>(tmem_slot + 2);
   volatile int* committed = reinterpret_cast<volatile int*>(tmem_slot + 3);
+  float* epi_tiles = reinterpret_cast<float*>(smem + STAGES * L::kStage + L::kBars);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_m = (int)((g.M + BM - 1) / BM), n_n = g.N / BN;
@@ -342,7 +367,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       const int mt = tile % n_m, rest = tile / n_m;
       gemm_epilogue(g, tmem + (uint32_t)(acc * BN), q, lane, (int64_t)mt * BM,
-                    (rest % n_n) * BN, rest / n_n, half * (BN / 2), (half + 1) * (BN / 2));
+                    (rest % n_n) * BN, rest / n_n, half * (BN / 2), (half + 1) * (BN / 2),
+                    epi_tiles + (warp - 2) * 32 * 33);
       tc_fence_before();
       __syncwarp();
       if (lane == 0) bar_arrive(&acc_empty[acc]);
@@ -611,8 +637,8 @@ int dmsim_gemm_bf16(const dmsim_gemm* g, void* stream) {
   a.ldht = g->ldht;
   a.err = g->err;
   cudaStream_t st = (cudaStream_t)stream;
-  return BN == 256 ? launch_gemm<256, 4>(ma, mb, a, g->M, g->N, splits, st)
-                   : launch_gemm<128, 6>(ma, mb, a, g->M, g->N, splits, st);
+  return BN == 256 ? launch_gemm<256, 3>(ma, mb, a, g->M, g->N, splits, st)
+                   : launch_gemm<128, 5>(ma, mb, a, g->M, g->N, splits, st);
 }
 
 int dmsim_mlp_pack(const float* x, int64_t rows, int32_t features, int32_t kp, const float* shift,
