@@ -480,7 +480,7 @@ GeoK make_geok(const dmsim_geometry* g) {
   gk.inv_h = packed ? (float)g->grid_n / g->L : 0.f;
   gk.n = packed ? g->grid_n : 1;
   gk.mi = packed ? (g->need_min_image != 0) : 0;
-  gk.kmax = packed && g->max_cell_cand >= 1 && g->max_cell_cand <= 4 ? g->max_cell_cand : 0;
+  gk.kmax = packed ? g->max_cell_cand : 0;
   return gk;
 }
 

@@ -47,7 +47,7 @@ struct GeoK {
   float L, halfL, inv_h;
   int n;   // cells per axis
   int mi;  // 1 when some cell lists two images of one object: candidates need the min-image test
-  int kmax;  // 1..4: every cell's list is scanned as kmax slots (uniform trip count); 0: as is
+  int kmax;  // most candidates any cell lists (0: unknown); 2 selects the two-slot scan
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -320,13 +320,7 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
   bool hit_in = false;
   const float ex = x + sx, ey = y + sy;
   float pe = 1.f, pqx = 0.f, pqy = 0.f, pR = 1.f;
-  // with a uniform slot count every lane runs the same trip count; a slot past the cell's list
-  // holds a zero-radius object far outside the cell, which no test can select
-  const uint32_t n_slots = g.kmax ? (uint32_t)g.kmax : ke - kb;
-#pragma unroll 2
-  for (uint32_t j = 0; j < n_slots; ++j) {
-    const uint32_t k = kb + j;
-    const float4 C = k < ke ? cand[k] : make_float4(kFarAway, kFarAway, kFarAway, 0.f);
+  auto visit = [&](const float4 C) {
     const float R2 = C.w * C.w;
     if constexpr (WALL != kPermeate) {
       const float fx = ex - C.x, fy = ey - C.y;
@@ -342,12 +336,12 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
       }
     }
     const float qx = x - C.x, qy = y - C.y;
-    if (g.mi && !(min_image(qx, g) && min_image(qy, g))) continue;
+    if (g.mi && !(min_image(qx, g) && min_image(qy, g))) return;
     const float dp = dx * qx + dy * qy;
     const float q2 = qx * qx + qy * qy;
     float disc = dp * dp - (q2 - R2);
     const bool ins = (WALL == kPermeate) && (q2 < R2);
-    if (!ins && dp >= 0.f) continue;  // entry root -dp - sqrt(disc) <= 0: no forward crossing
+    if (!ins && dp >= 0.f) return;  // entry root -dp - sqrt(disc) <= 0: no forward crossing
     const float sq = sqrtf(fmaxf(disc, 0.f));
     const float t = ins ? -dp + sq : -dp - sq;
     const bool valid = (disc > 0.f) && (t > g.eps) && (t < lxy) && (lxy > 0.f);
@@ -359,6 +353,17 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
       hR = C.w;
       hit_in = ins;
     }
+  };
+  if (g.kmax == 2) {
+    // every cell lists at most two candidates: two slots for every lane, no divergent trip
+    // count; the slot past a shorter list holds a zero-radius object far outside the cell,
+    // which no test can select
+#pragma unroll
+    for (uint32_t j = 0; j < 2u; ++j)
+      visit(kb + j < ke ? cand[kb + j] : make_float4(kFarAway, kFarAway, kFarAway, 0.f));
+  } else {
+#pragma unroll 1
+    for (uint32_t k = kb; k < ke; ++k) visit(cand[k]);
   }
   if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR) {
     const double qxd = (double)(x - hcx), qyd = (double)(y - hcy);
@@ -496,11 +501,9 @@ __device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, i
   bool hit_in = false;
   const float ex = x + sx, ey = y + sy, ez = z + sz;
   float pe = 1.f, pqx = 0.f, pqy = 0.f, pqz = 0.f, pR = 1.f;
-  const uint32_t n_slots = g.kmax ? (uint32_t)g.kmax : ke - kb;  // see packed_cyl_step
-#pragma unroll 2
-  for (uint32_t j = 0; j < n_slots; ++j) {
-    const uint32_t k = kb + j;
-    const float4 C = k < ke ? cand[k] : make_float4(kFarAway, kFarAway, kFarAway, 0.f);
+#pragma unroll 1
+  for (uint32_t k = kb; k < ke; ++k) {
+    const float4 C = cand[k];
     const float R2 = C.w * C.w;
     if constexpr (WALL != kPermeate) {
       const float fx = ex - C.x, fy = ey - C.y, fz = ez - C.z;

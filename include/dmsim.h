@@ -91,9 +91,9 @@ typedef struct dmsim_geometry {
   int32_t n_cand;
   int32_t need_min_image; /* 1 if a cell lists two images of one object (then each candidate is
                              checked to be its object's minimum image from the walker) */
-  int32_t max_cell_cand;  /* most candidates any cell lists (0: unknown); up to 4, every walker
-                             of a warp scans that many slots, so the scan has no divergent trip
-                             count (slots past a cell's list hold an unreachable dummy) */
+  int32_t max_cell_cand;  /* most candidates any cell lists (0: unknown).  When it is 2, every
+                             walker of a warp scans two slots (a shorter list is padded with an
+                             unreachable dummy), so the scan has no divergent trip count */
   int32_t pad2;
   const uint32_t* cell_start; /* grid_n^d + 1 */
   const float* cand;          /* n_cand x 4 */
