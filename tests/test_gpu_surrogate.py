@@ -38,8 +38,10 @@ def test_surrogate_error_on_held_out_substrates(sur, held_out):
     err = np.abs(sur.predict(X) - ref)
     # the walk's own noise at 2e5 walkers (median SE) sits inside the measured error
     assert np.median(se) < 0.003
-    assert err.mean() < 0.02, (err.mean(), np.percentile(err, 95))
-    assert np.percentile(err, 95) < 0.08
+    # the training report's judge (24 substrates at 1e6 walkers) measured MAE 0.0047; six
+    # substrates at 2e5 walkers carry more sampling noise, hence the margin
+    assert err.mean() < 0.008, (err.mean(), np.percentile(err, 95))
+    assert np.percentile(err, 95) < 0.03
 
 
 def test_surrogate_gain_over_the_walk(sur, held_out):
