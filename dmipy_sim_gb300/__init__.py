@@ -6,7 +6,8 @@ loop executed by hand-written sm_103a CUDA kernels (``libdmsim.so``, C ABI in in
 """
 from .constants import GAMMA, DEFAULT_SLEW_RATE
 from .waveforms import (Waveform, pgse, pgste, ogse, cpmg, calc_b, calc_btensor, set_b,
-                        rotate_waveform, tile_waveform)
+                        rotate_waveform, tile_waveform, trapezoidal_ogse, b_trapezoidal_ogse,
+                        btensor_invariants, ste, pte)
 from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, pack_cylinders,
                          PackedCylinders, pack_spheres, PackedSpheres, lattice_cylinders)
 from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
@@ -19,7 +20,8 @@ from .autotune import autotune
 
 __all__ = [
     "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
-    "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "Geometry", "FreeDiffusion",
+    "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "trapezoidal_ogse",
+    "b_trapezoidal_ogse", "btensor_invariants", "ste", "pte", "Geometry", "FreeDiffusion",
     "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
     "simulate", "simulate_cpmg", "simulate_trajectories", "replay", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",

@@ -1,8 +1,9 @@
 """Gradient waveforms: the ``Waveform`` object and the constructors the walk is driven by.
 
 Same fields, units and conventions as dmipy-sim's ``waveforms.py`` (Waveform 39-90, pgse 93-163,
-pgste 166-262, ogse 265-350, calc_b 490-516, calc_btensor 519-543, set_b 723-772,
-rotate_waveform 775-818, tile_waveform 821-848, cpmg 851-917): ``G`` is (n_meas, n_t, 3) float32
+pgste 166-262, ogse 265-350, trapezoidal_ogse 353-455, b_trapezoidal_ogse 458-487,
+calc_b 490-516, calc_btensor 519-543, btensor_invariants 546-595, ste 598-655, pte 658-720,
+set_b 723-772, rotate_waveform 775-818, tile_waveform 821-848, cpmg 851-917): ``G`` is (n_meas, n_t, 3) float32
 in T/m on a uniform time grid ``dt``; the second lobe of a spin echo carries the refocusing sign
 (bipolar convention), so the phase is simply gamma * sum_t G(t) . r(t) * dt.  Host-side numpy only.
 """
@@ -231,3 +232,105 @@ def tile_waveform(waveform, n_copies):
     return Waveform(G=G, dt=waveform.dt, echo_idx=waveform.echo_idx, rf_events=waveform.rf_events,
                     chi_perp=waveform.chi_perp, TM=waveform.TM,
                     stimulated_echo=waveform.stimulated_echo)
+
+
+def trapezoidal_ogse(N, delta, DELTA, G_magnitude, bvecs, n_t, rise_time=None, slew_rate=200e3):
+    """Trapezoidal N-lobe OGSE over DELTA + delta (waveforms.py:353-455): two blocks of N lobes,
+    each delta/N long with linear ramps of ``rise_time`` (default: peak G / slew_rate), the first
+    block starting at sample 0 with signs +,-,+,..., the second at round(DELTA/dt) with the signs
+    flipped.  N = 1 is a trapezoidal PGSE."""
+    bvecs = np.asarray(bvecs, dtype=np.float32)
+    n_meas = bvecs.shape[0]
+    amp = _amplitudes(G_magnitude, n_meas)
+    g_peak = float(np.max(np.abs(amp)))
+    if rise_time is None:
+        rise_time = g_peak / slew_rate if g_peak > 0 else 0.0
+    dt = (DELTA + delta) / (n_t - 1)
+    n_lobe = max(1, round(delta / (N * dt)))
+    n_rise = min(max(0, round(rise_time / dt)), n_lobe // 2)
+    starts = (0, round(DELTA / dt))
+    G = np.zeros((n_meas, n_t, 3), dtype=np.float32)
+    for m in range(n_meas):
+        for blk, b0 in enumerate(starts):
+            for k in range(N):
+                sgn = (-1) ** k if blk == 0 else -((-1) ** k)
+                peak = sgn * amp[m]                        # float32, as the lobe's flat top
+                i0, i1 = b0 + k * n_lobe, b0 + (k + 1) * n_lobe
+                if n_rise > 0:
+                    up = np.linspace(0.0, peak, n_rise, endpoint=False)
+                    down = np.linspace(peak, 0.0, n_rise, endpoint=False)
+                    G[m, i0:i0 + n_rise] = up[:, None] * bvecs[m]
+                    G[m, i0 + n_rise:i1 - n_rise] = peak * bvecs[m]
+                    G[m, i1 - n_rise:i1] = down[:, None] * bvecs[m]
+                else:
+                    G[m, i0:i1] = peak * bvecs[m]
+    mid = (n_lobe * N + starts[1]) // 2
+    rf = [{'t_s': 0.0, 'label': 'Mz→Mxy', 'flip_deg': 90},
+          {'t_s': mid * dt, 'label': 'refocus', 'flip_deg': 180}]
+    return Waveform(G=G, dt=float(dt), echo_idx=n_t - 1, rf_events=rf)
+
+
+def b_trapezoidal_ogse(N, delta, DELTA, G, rise_time):
+    """Closed-form b-value of the trapezoidal N-lobe OGSE (waveforms.py:458-487, Drobnjak et al.
+    2016 Eq. 2): the oscillating part plus, for odd N, the cross-block term of the net lobe
+    moment."""
+    x = rise_time * N / delta
+    osc = 2.0 * G ** 2 * GAMMA ** 2 * delta ** 3 / (15.0 * N ** 2) * (
+        5.0 - 7.5 * x - 1.25 * x ** 2 + 4.0 * x ** 3)
+    q_net = (1 - (-1) ** N) * (delta - N * rise_time) / (2.0 * N)
+    return float(osc + G ** 2 * GAMMA ** 2 * (DELTA - delta) * q_net ** 2)
+
+
+def btensor_invariants(B):
+    """(b, b_delta, b_eta) of B-tensors (n_meas, 3, 3) (waveforms.py:546-595): b = trace,
+    b_delta = normalised anisotropy (linear 1, spherical 0, planar -0.5) and b_eta = normalised
+    asymmetry, in the prolate/oblate convention chosen by which extreme eigenvalue lies farther
+    from b/3."""
+    lam = np.linalg.eigvalsh(np.asarray(B))[:, ::-1]         # descending
+    l1, l2, l3 = lam[:, 0], lam[:, 1], lam[:, 2]
+    b = l1 + l2 + l3
+    bs = np.where(b > 0, b, 1.0)
+    prolate = np.abs(l1 - b / 3.0) >= np.abs(l3 - b / 3.0)
+    b_delta = np.where(prolate, (l1 - (l2 + l3) / 2.0) / bs, (l3 - (l1 + l2) / 2.0) / bs)
+    b_eta = np.where(prolate, (l2 - l3) / bs, (l1 - l2) / bs)
+    return b, b_delta, b_eta
+
+
+def _bipolar_axes(axes, total, G_magnitude, n_t, slew_rate):
+    """One measurement of back-to-back bipolar lobe pairs, one pair per axis, each pair taking
+    2 / (2 len(axes)) of the n_t samples (the tensor-encoding layout of waveforms.py:598-720)."""
+    dt = total / (n_t - 1)
+    n_seg = max(1, round(n_t / (2 * len(axes))))
+    _, square = resolve_slew(slew_rate)
+    n_rise = _ramp_samples(square, abs(float(G_magnitude)), slew_rate, dt, n_seg)
+    G = np.zeros((1, n_t, 3), dtype=np.float32)
+    for i, a in enumerate(axes):
+        enc0 = 2 * i * n_seg
+        enc1 = min((2 * i + 1) * n_seg, n_t)
+        dec1 = min((2 * i + 2) * n_seg, n_t)
+        g = (G_magnitude * np.asarray(a)).astype(np.float32)
+        _lobe(G, 0, enc0, enc1 - enc0, g, n_rise)
+        _lobe(G, 0, enc1, dec1 - enc1, -g, n_rise)
+    return Waveform(G=G, dt=float(dt), echo_idx=n_t - 1,
+                    rf_events=[{'t_s': 0.0, 'label': 'Mz→Mxy', 'flip_deg': 90}])
+
+
+def ste(delta, DELTA, G_magnitude, n_t, slew_rate=DEFAULT_SLEW_RATE):
+    """Spherical tensor encoding (b_delta = 0) over DELTA + delta (waveforms.py:598-655): bipolar
+    pairs along x, y and z in turn, so every q_i(t) returns to zero before the next axis starts
+    and B = (b/3) I."""
+    return _bipolar_axes(np.eye(3, dtype=np.float32), DELTA + delta, G_magnitude, n_t, slew_rate)
+
+
+def pte(delta, DELTA, G_magnitude, plane_normal, n_t, slew_rate=DEFAULT_SLEW_RATE):
+    """Planar tensor encoding (b_delta = -0.5) over DELTA + delta (waveforms.py:658-720): bipolar
+    pairs along two orthonormal in-plane axes u, v (Gram-Schmidt from x, or y when the normal is
+    close to x, and v = n x u)."""
+    n = np.asarray(plane_normal, dtype=np.float64)
+    n = n / np.linalg.norm(n)
+    ref = np.array([1.0, 0.0, 0.0]) if abs(n[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+    u = ref - np.dot(ref, n) * n
+    u /= np.linalg.norm(u)
+    v = np.cross(n, u)
+    v /= np.linalg.norm(v)
+    return _bipolar_axes([u, v], DELTA + delta, G_magnitude, n_t, slew_rate)

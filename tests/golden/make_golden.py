@@ -307,11 +307,45 @@ def _mesh_cases(m, rng, out):
             out[key + "_dlog"], out[key + "_u"] = dl, us
 
 
+def _waveform_cases_tensor(m, out):
+    """Trapezoidal OGSE, its closed-form b, spherical/planar tensor encodings and the b-tensor
+    invariants (waveforms.py:353-720)."""
+    w = m["waveforms"]
+    t = w.trapezoidal_ogse(3, 0.02, 0.03, 0.05, [[1, 0, 0], [0, 0.6, 0.8]], 500)
+    out["wf_trap_G"] = np.asarray(t.G, np.float32)
+    out["wf_trap_dt"] = np.float64(t.dt)
+    t1 = w.trapezoidal_ogse(1, 0.01, 0.03, 0.08, [[0, 1, 0]], 301, rise_time=5e-4)
+    out["wf_trap1_G"] = np.asarray(t1.G, np.float32)
+    out["wf_trap_bformula"] = np.array([w.b_trapezoidal_ogse(n, 0.02, 0.03, 0.05, 2.5e-4)
+                                        for n in (1, 2, 3, 4)])
+    s = w.ste(0.01, 0.03, 0.05, 300)
+    out["wf_ste_G"] = np.asarray(s.G, np.float32)
+    p = w.pte(0.01, 0.03, 0.05, [0.3, 0.4, 0.866], 301)
+    out["wf_pte_G"] = np.asarray(p.G, np.float32)
+    p2 = w.pte(0.01, 0.03, 0.05, [1.0, 0.1, 0.0], 200, slew_rate=np.inf)
+    out["wf_pte2_G"] = np.asarray(p2.G, np.float32)
+    B = np.concatenate([w.calc_btensor(s), w.calc_btensor(p), w.calc_btensor(t)])
+    out["wf_inv_B"] = B
+    out["wf_inv_b"], out["wf_inv_bdelta"], out["wf_inv_beta"] = (
+        np.asarray(x) for x in w.btensor_invariants(B))
+
+
+def make_kat_extra(root):
+    """Add the tensor-encoding waveform vectors to an existing kat.npz."""
+    m = _ref(root)
+    path = HERE / "kat.npz"
+    out = dict(np.load(path))
+    _waveform_cases_tensor(m, out)
+    np.savez_compressed(path, **out)
+    print(f"kat.npz: {len(out)} arrays")
+
+
 def make_kat(root):
     m = _ref(root)
     out = {}
     rng = np.random.default_rng(2024)
     _waveform_cases(m, out)
+    _waveform_cases_tensor(m, out)
     _substep_cases(m, out)
     _pack_cases(m, out)
     _replay_cases(m, out)
@@ -489,11 +523,15 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("DMIPY_SIM_SRC", "/root/reference"))
     ap.add_argument("--kat", action="store_true")
+    ap.add_argument("--kat-extra", action="store_true",
+                    help="add the tensor-encoding waveform vectors to an existing kat.npz")
     ap.add_argument("--mc", action="store_true")
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--procs", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
     if a.kat:
         make_kat(a.ref)
+    if a.kat_extra:
+        make_kat_extra(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)

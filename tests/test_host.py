@@ -154,3 +154,26 @@ def test_no_cpu_fallback_without_gpu():
     wf = d.pgse(0.01, 0.04, 0.05, [[1, 0, 0]], 50)
     with pytest.raises(RuntimeError, match="GPU"):
         d.simulate(10, D, wf, d.FreeDiffusion())
+
+
+def test_trapezoidal_ogse_and_its_b_formula(kat):
+    w = d.trapezoidal_ogse(3, 0.02, 0.03, 0.05, [[1, 0, 0], [0, 0.6, 0.8]], 500)
+    np.testing.assert_array_equal(w.G, kat["wf_trap_G"])
+    assert w.dt == float(kat["wf_trap_dt"])
+    w1 = d.trapezoidal_ogse(1, 0.01, 0.03, 0.08, [[0, 1, 0]], 301, rise_time=5e-4)
+    np.testing.assert_array_equal(w1.G, kat["wf_trap1_G"])
+    got = [d.b_trapezoidal_ogse(n, 0.02, 0.03, 0.05, 2.5e-4) for n in (1, 2, 3, 4)]
+    np.testing.assert_allclose(got, kat["wf_trap_bformula"], rtol=1e-12)
+
+
+def test_tensor_encodings_and_invariants(kat):
+    np.testing.assert_array_equal(d.ste(0.01, 0.03, 0.05, 300).G, kat["wf_ste_G"])
+    np.testing.assert_array_equal(d.pte(0.01, 0.03, 0.05, [0.3, 0.4, 0.866], 301).G,
+                                  kat["wf_pte_G"])
+    np.testing.assert_array_equal(
+        d.pte(0.01, 0.03, 0.05, [1.0, 0.1, 0.0], 200, slew_rate=np.inf).G, kat["wf_pte2_G"])
+    b, bd, be = d.btensor_invariants(kat["wf_inv_B"])
+    np.testing.assert_allclose(b, kat["wf_inv_b"], rtol=1e-12)
+    np.testing.assert_allclose(bd, kat["wf_inv_bdelta"], atol=1e-9)
+    np.testing.assert_allclose(be, kat["wf_inv_beta"], atol=1e-9)
+    assert abs(bd[0]) < 1e-6 and abs(bd[1] + 0.5) < 1e-6 and abs(bd[2] - 1.0) < 1e-6
