@@ -44,6 +44,7 @@ static double round_half(float f) {
 #define SUF _f32
 #define SQRT sqrtf
 #define FLOOR floorf
+#define FMOD fmodf
 #define SIN sinf
 #define COS cosf
 #define MAX(a, b) fmaxf((a), (b))
@@ -53,6 +54,7 @@ static double round_half(float f) {
 #undef SUF
 #undef SQRT
 #undef FLOOR
+#undef FMOD
 #undef SIN
 #undef COS
 #undef MAX
@@ -62,6 +64,7 @@ static double round_half(float f) {
 #define SUF _f64
 #define SQRT sqrt
 #define FLOOR floor
+#define FMOD fmod
 #define SIN sin
 #define COS cos
 #define MAX(a, b) fmax((a), (b))

@@ -12,6 +12,9 @@
  *   Cylinder reflect / reflect_with_log_weight / permeate geometries.py:493-563, 565-653, 655-801
  *   PackedCylinders reflect / rwlw / permeate             geometries.py:1746-1884, 1886-2016, 2018-2183
  *   PackedSpheres reflect / rwlw / permeate               geometries.py:2445-2537, 2539-2631, 2633-2756
+ *   Mesh reflect / reflect_with_log_weight / permeate     mesh.py:637-671, 673-705, 707-743
+ *     (wrap 203-206, 27-cell gather 208-215, Moller-Trumbore 561-569, bounce 599-635,
+ *      nearest-centroid classification 227-254, leak guard 578-597)
  *   ensemble Re<w e^{i phi}>                              core.py:426-429; replay FP64 phase
  *                                                         trajectories.py:550-552, 634
  * It tests every object of a packed substrate (no cell list) with the reference's min-image
@@ -27,8 +30,27 @@
 extern "C" {
 #endif
 
-enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4 };
+enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4,
+       OR_MESH = 5 };
 enum { OR_REFLECT = 0, OR_RELAX = 1, OR_PERMEATE = 2 };
+
+/* A triangle mesh as the reference's Mesh holds it (mesh.py:311-546): every triangle including the
+   periodic ghosts, float32 values stored as double; the uniform grid's cell lists in CSR form (each
+   cell's triangles in increasing order, as the reference's buckets are filled). */
+typedef struct {
+  int32_t n_tri, n_cells;
+  int32_t dims[3], per[3];
+  double gmin[3], cs, vmin[3], box[3];
+  double eps, nudge, graze;
+  int32_t max_bounces, reject;
+  double rho_mult_intra, rho_mult_extra, kappa_mult_out, kappa_mult_in;
+  const double* tri;         /* n_tri x 9: vertices A, B, C */
+  const double* vn;          /* n_tri x 9: smooth normals at A, B, C */
+  const double* nrm;         /* n_tri x 3: unit geometric normal */
+  const double* cent;        /* n_tri x 3: centroid */
+  const int32_t* cell_start; /* n_cells + 1 */
+  const int32_t* cell_tri;
+} or_mesh;
 
 typedef struct {
   int32_t kind;
@@ -40,6 +62,7 @@ typedef struct {
   double rot[9];      /* lab -> cylinder frame (row-major), used by or_plugin only */
   int32_t rot_identity;
   int32_t pad;
+  const or_mesh* mesh;   /* OR_MESH only */
 } or_geom;
 
 typedef struct {
@@ -60,7 +83,7 @@ int or_plugin_f64(const or_geom* g, int mode, const double* r, const double* ste
                   double rho_over_D, double kappa_over_D, double u, double* r_out, double* dlog);
 
 /* A full walk in the geometry frame.  G is (n_t, n_meas, 3) float32, chi (n_t) or NULL, r0
-   (n_walkers, 3) or NULL (seeded on the Philox seeding stream).  sums (n_echo, n_meas, 3) is
+   (n_walkers, 3) or NULL (seeded on the Philox seeding stream; a mesh needs r0).  sums (n_echo, n_meas, 3) is
    overwritten with sum w cos(phi), sum w sin(phi), sum (w cos(phi))^2.  final_pos (n, 3), log_w
    (n), phi (n, n_meas) are optional.  n_threads <= 0 uses every core. */
 int or_walk_f32(const or_geom* g, const or_walk_params* p, const float* G, const float* chi,

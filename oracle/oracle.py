@@ -14,14 +14,27 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 
-FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES = range(5)
+FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH = range(6)
 REFLECT, RELAX, PERMEATE = range(3)
+
+
+class OrMesh(C.Structure):
+    _fields_ = [("n_tri", C.c_int32), ("n_cells", C.c_int32), ("dims", C.c_int32 * 3),
+                ("per", C.c_int32 * 3), ("gmin", C.c_double * 3), ("cs", C.c_double),
+                ("vmin", C.c_double * 3), ("box", C.c_double * 3), ("eps", C.c_double),
+                ("nudge", C.c_double), ("graze", C.c_double), ("max_bounces", C.c_int32),
+                ("reject", C.c_int32), ("rho_mult_intra", C.c_double),
+                ("rho_mult_extra", C.c_double), ("kappa_mult_out", C.c_double),
+                ("kappa_mult_in", C.c_double), ("tri", C.c_void_p), ("vn", C.c_void_p),
+                ("nrm", C.c_void_p), ("cent", C.c_void_p), ("cell_start", C.c_void_p),
+                ("cell_tri", C.c_void_p)]
 
 
 class OrGeom(C.Structure):
     _fields_ = [("kind", C.c_int32), ("n_objects", C.c_int32), ("radius", C.c_double),
                 ("L", C.c_double), ("rmin", C.c_double), ("objects", C.c_void_p),
-                ("rot", C.c_double * 9), ("rot_identity", C.c_int32), ("pad", C.c_int32)]
+                ("rot", C.c_double * 9), ("rot_identity", C.c_int32), ("pad", C.c_int32),
+                ("mesh", C.c_void_p)]
 
 
 class OrWalk(C.Structure):
@@ -84,6 +97,116 @@ def geom(kind, radius=0.0, L=0.0, objects=None, rot=None):
     return g
 
 
+def _vertex_normals(V, F):
+    """Area-weighted unit vertex normals (mesh.py:75-84)."""
+    tv = V[F]
+    cr = np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0])
+    vn = np.zeros((len(V), 3))
+    for c in range(3):
+        np.add.at(vn, F[:, c], cr)
+    return vn / np.maximum(np.linalg.norm(vn, axis=1, keepdims=True), 1e-30)
+
+
+def mesh_geom(vertices, faces, *, periodic=False, voxel_min=None, voxel_max=None,
+              feature_radius=None, rho_mult=(1.0, 1.0), kappa_mult=(1.0, 1.0), permeable=False,
+              cell_size=None, max_bounces=10, reject=True):
+    """Oracle mesh, built from the surface the way the reference's Mesh constructor builds its
+    tables (mesh.py:311-546): the box and feature radius, ghost copies of the triangles near each
+    periodic face, unit face normals, area-weighted vertex normals, the uniform grid over the box
+    plus one cell of margin with each triangle listed in every cell its bounding box overlaps, and
+    the float32 constants EPS = 1e-7 min(L), NUDGE = max(1e-4 step, 16 EPS), GRAZE = 1e-4.
+    ``rho_mult`` = (intra, extra) and ``kappa_mult`` = (out, in) are the side multipliers."""
+    import itertools
+    V = np.asarray(vertices, np.float64)
+    F = np.asarray(faces, np.int64)
+    per = (bool(periodic),) * 3 if isinstance(periodic, (bool, np.bool_)) else \
+        tuple(bool(p) for p in periodic)
+    vmin = np.asarray(voxel_min, np.float64) if voxel_min is not None else V.min(0)
+    vmax = np.asarray(voxel_max, np.float64) if voxel_max is not None else V.max(0)
+    L = vmax - vmin
+    radius = float(feature_radius) if feature_radius is not None else 0.5 * float(np.min(L[L > 0]))
+    step_l = radius / (25.0 if permeable else 6.0)
+    cs = float(cell_size) if cell_size is not None else 4.0 * step_l
+    tv, tn = V[F], _vertex_normals(V, F)[F]
+    lo_t, hi_t = tv.min(1), tv.max(1)
+    tris, vns = [tv], [tn]
+    for combo in itertools.product((-1, 0, 1), repeat=3):
+        if combo == (0, 0, 0) or any(c != 0 and not per[a] for a, c in enumerate(combo)):
+            continue
+        keep = np.ones(len(F), bool)
+        shift = np.zeros(3)
+        for a, c in enumerate(combo):
+            if c < 0:
+                keep &= hi_t[:, a] > vmax[a] - cs
+                shift[a] = -L[a]
+            elif c > 0:
+                keep &= lo_t[:, a] < vmin[a] + cs
+                shift[a] = L[a]
+        if keep.any():
+            tris.append(tv[keep] + shift)
+            vns.append(tn[keep])
+    tri = np.concatenate(tris)
+    vn = np.concatenate(vns)
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+    gmin = vmin - cs
+    dims = np.maximum(1, np.ceil((vmax + cs - gmin) / cs).astype(int))
+    lo = np.clip(np.floor((tri.min(1) - gmin) / cs).astype(int), 0, dims - 1)
+    hi = np.clip(np.floor((tri.max(1) - gmin) / cs).astype(int), 0, dims - 1)
+    cells = [[] for _ in range(int(np.prod(dims)))]
+    for t in range(len(tri)):
+        for ix in range(lo[t, 0], hi[t, 0] + 1):
+            for iy in range(lo[t, 1], hi[t, 1] + 1):
+                for iz in range(lo[t, 2], hi[t, 2] + 1):
+                    cells[(ix * dims[1] + iy) * dims[2] + iz].append(t)
+    start = np.zeros(len(cells) + 1, np.int32)
+    start[1:] = np.cumsum([len(c) for c in cells])
+    ctri = np.array([t for c in cells for t in c] or [0], np.int32)
+    f32 = lambda x: np.asarray(x, np.float32).astype(np.float64)   # noqa: E731
+    keep = {"tri": np.ascontiguousarray(f32(tri).reshape(-1, 9)),
+            "vn": np.ascontiguousarray(f32(vn).reshape(-1, 9)),
+            "nrm": np.ascontiguousarray(f32(nrm)), "cent": np.ascontiguousarray(f32(tri.mean(1))),
+            "start": start, "ctri": ctri}
+    m = OrMesh()
+    m.n_tri, m.n_cells = len(tri), len(cells)
+    m.dims[:] = [int(x) for x in dims]
+    m.per[:] = [int(p) for p in per]
+    m.gmin[:] = f32(gmin).tolist()
+    m.cs = float(np.float32(cs))
+    m.vmin[:] = f32(vmin).tolist()
+    m.box[:] = f32(L).tolist()
+    eps = np.float32(1e-7 * float(np.min(L)))
+    m.eps = float(eps)
+    m.nudge = float(np.float32(max(1e-4 * step_l, 16.0 * float(eps))))
+    m.graze = float(np.float32(1e-4))
+    m.max_bounces = int(max_bounces)
+    m.reject = int(bool(reject))
+    m.rho_mult_intra, m.rho_mult_extra = (float(np.float32(x)) for x in rho_mult)
+    m.kappa_mult_out, m.kappa_mult_in = (float(np.float32(x)) for x in kappa_mult)
+    m.tri, m.vn = keep["tri"].ctypes.data, keep["vn"].ctypes.data
+    m.nrm, m.cent = keep["nrm"].ctypes.data, keep["cent"].ctypes.data
+    m.cell_start, m.cell_tri = start.ctypes.data, ctri.ctypes.data
+    g = OrGeom()
+    g.kind = MESH
+    g.radius = radius
+    g.rot[:] = np.eye(3).ravel().tolist()
+    g.rot_identity = 1
+    g.mesh = C.addressof(m)
+    g._keep = (m, keep)
+    return g
+
+
+def mesh_sides(rho_intra=None, rho_extra=None, kappa_out=None, kappa_in=None):
+    """(rho_mult, kappa_mult, permeable) of per-side surface properties: each multiplier is the
+    side's value over the larger of the two (mesh.py:349-371)."""
+    ri, re_ = float(rho_intra or 0.0), float(rho_extra or 0.0)
+    ko, ki = float(kappa_out or 0.0), float(kappa_in or 0.0)
+    rn, kn = max(ri, re_), max(ko, ki)
+    rho = (ri / rn, re_ / rn) if rn > 0 else (1.0, 1.0)
+    kap = (ko / kn, ki / kn) if kn > 0 else (1.0, 1.0)
+    return rho, kap, kn > 0
+
+
 def geom_from(geometry):
     """Oracle geometry of a dmipy_sim_gb300 geometry object (walk frame)."""
     name = type(geometry).__name__
@@ -102,6 +225,15 @@ def geom_from(geometry):
         kind = PACKED_CYLINDERS if name == "PackedCylinders" else PACKED_SPHERES
         return geom(kind, L=np.float32(geometry._L_float), objects=objs,
                     rot=getattr(geometry, "_R", None))
+    if name == "Mesh":
+        return mesh_geom(geometry.vertices, geometry.faces, periodic=geometry.periodic,
+                         voxel_min=geometry.vmin, voxel_max=geometry.vmax,
+                         feature_radius=geometry.radius,
+                         rho_mult=(geometry._rho_mult_intra, geometry._rho_mult_extra),
+                         kappa_mult=(geometry._kappa_mult_out, geometry._kappa_mult_in),
+                         permeable=geometry.permeability is not None,
+                         cell_size=geometry.cell_size, max_bounces=geometry._MAX_BOUNCES,
+                         reject=geometry.reject_escape)
     raise NotImplementedError(f"no oracle geometry for {name}")
 
 

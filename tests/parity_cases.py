@@ -59,7 +59,7 @@ def plan(geom, wf, engine):
 
 
 def oracle_walk(geom, G, dt, S, phase_sub, n, seed, T2=None, echo_idx=None, fp64=False,
-                walker_offset=0, want_walkers=True):
+                walker_offset=0, want_walkers=True, r0=None):
     rho = geom.surface_relaxivity_t2
     kappa = geom.permeability
     wall = O.PERMEATE if kappa is not None else (O.RELAX if rho is not None else O.REFLECT)
@@ -67,4 +67,4 @@ def oracle_walk(geom, G, dt, S, phase_sub, n, seed, T2=None, echo_idx=None, fp64
                   phase_per_substep=phase_sub, seed=seed, wall=wall, T2=T2,
                   rho_over_D=0.0 if rho is None else rho / D,
                   kappa_over_D=0.0 if kappa is None else kappa / D, D=D, echo_idx=echo_idx,
-                  fp64=fp64, walker_offset=walker_offset, want_walkers=want_walkers)
+                  fp64=fp64, walker_offset=walker_offset, want_walkers=want_walkers, r0=r0)

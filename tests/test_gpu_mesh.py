@@ -1,7 +1,8 @@
 """Mesh substrate on the GPU: the device step (dmsim_step_kat, the walk kernel's code) against the
 reference's own Mesh.reflect / reflect_with_log_weight / permeate calls (kat.npz, closed icosphere
-and a periodic box with ghost triangles), seeding and containment, and a mesh sphere against the
-analytic sphere (the reference's tests/test_mesh_mc.py check)."""
+and a periodic box with ghost triangles), whole walks against the CPU oracle's restatement of the
+mesh walk (walker by walker on short walks, and as ensembles), seeding and containment, and a mesh
+sphere against the analytic sphere (the reference's tests/test_mesh_mc.py check)."""
 import warnings
 
 import numpy as np
@@ -9,6 +10,8 @@ import pytest
 
 import dmipy_sim_gb300 as d
 from dmipy_sim_gb300 import core
+
+from parity_cases import oracle_walk
 
 pytestmark = pytest.mark.gpu
 D = 2e-9
@@ -103,3 +106,69 @@ def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
     for k in ("pos", "phi", "log_w"):
         assert np.array_equal(res[0].extras[k].cpu().numpy(), res[1].extras[k].cpu().numpy()), k
     assert res[0].status == res[1].status
+
+
+def _inside_points(V, F, n, seed):
+    rng = np.random.default_rng(seed)
+    lo, hi = V.min(0), V.max(0)
+    pts = np.zeros((0, 3))
+    while len(pts) < n:
+        p = rng.uniform(lo, hi, size=(4 * n, 3))
+        pts = np.concatenate([pts, p[d.mesh_contains(V, F, p)]])
+    return pts[:n].astype(np.float32)
+
+
+def _oracle_mesh(mode):
+    V, F = d.icosphere(4e-6, 2)
+    kw = {}
+    if mode == "relax":
+        kw["intra"] = {"surface_relaxivity_t2": 2e-6}
+    if mode == "perm":
+        kw["permeability"] = {"intra_to_extra": 2e-5, "extra_to_intra": 1e-5}
+        kw["surface_relaxivity_t2"] = 1e-6
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        return V, F, d.Mesh(V, F, **kw)
+
+
+def _mesh_walks(mode, n, n_t, seed, want):
+    V, F, g = _oracle_mesh(mode)
+    rng = np.random.default_rng(0)
+    bv = rng.normal(size=(4, 3))
+    bv /= np.linalg.norm(bv, axis=1, keepdims=True)
+    wf = d.set_b(d.pgse(0.004, 0.012, 0.02, bv, 80), 1e9)
+    G, _ = core._waveform_arrays(wf, g)
+    S = core.fused_sub_steps(g, D, wf.dt)
+    G = G[:, :(n_t or max(1, 60 // S))]       # default: about 60 sub-steps
+    r0 = _inside_points(V, F, n, seed)
+    gpu = core.run_walk(g, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                        phase_per_substep=True, seed=seed, T2=0.07, r0=r0, want_positions=want,
+                        want_walker_signals=want)
+    ora = oracle_walk(g, G, wf.dt, S, True, n, seed=seed, T2=0.07, r0=r0, want_walkers=want)
+    return g, S, gpu, ora
+
+
+@pytest.mark.parametrize("mode", ["reflect", "relax", "perm"])
+def test_mesh_short_walk_matches_oracle_walker_by_walker(cuda, mode):
+    """Both walks read the same Philox stream from the same start positions; over a few dozen
+    sub-steps (a few hundred triangle tests each) every walker but a rounding-order few lands on
+    the same position with the same phase and log-weight.  Longer mesh walks are chaotic
+    billiards: FP32 contraction differences grow with every bounce off the smooth normals."""
+    g, S, gpu, ora = _mesh_walks(mode, 2048, None, 11, True)
+    pg = gpu.extras["pos"].cpu().numpy()
+    same = np.max(np.abs(pg - ora["pos"]), axis=1) < 1e-4 * 4e-6
+    assert same.mean() >= 0.97, f"only {same.mean():.3f} of walkers follow the oracle's walk"
+    np.testing.assert_allclose(gpu.extras["phi"].cpu().numpy()[same], ora["phi"][same],
+                               atol=1e-3, rtol=1e-4)
+    np.testing.assert_allclose(gpu.extras["log_w"].cpu().numpy()[same], ora["log_w"][same],
+                               rtol=1e-4, atol=1e-6)
+    assert gpu.status["nonfinite"] == 0
+
+
+@pytest.mark.parametrize("mode", ["reflect", "relax", "perm"])
+def test_mesh_ensemble_matches_oracle(cuda, mode):
+    """The whole echo on the same stream and start positions: signals within 4 combined SE."""
+    g, S, gpu, ora = _mesh_walks(mode, 4096, 80, 21, False)
+    se = np.sqrt(2.0) * gpu.stderr[0]
+    z = (gpu.signal[0] - ora["signal"][0]) / np.maximum(se, 1e-9)
+    assert np.max(np.abs(z)) < 4.0, z

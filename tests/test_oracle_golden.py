@@ -1,6 +1,7 @@
 """Pins the CPU oracle to the reference: every geometry plug-in call of dmipy-sim (reflect,
-reflect_with_log_weight, permeate — recorded from the reference itself in tests/golden/kat.npz)
-is reproduced by the oracle's FP32 restatement, and by its FP64 twin to FP32 rounding."""
+reflect_with_log_weight, permeate — recorded from the reference itself in tests/golden/kat.npz,
+for the cylinder, sphere, packed substrates and triangle meshes) is reproduced by the oracle's FP32
+restatement, and by its FP64 twin to FP32 rounding."""
 import numpy as np
 import pytest
 
@@ -63,6 +64,75 @@ def test_oracle_fp64_close_to_reference_plugins(kat, tag, mode):
     assert len(bad) <= max(2, len(ref) // 50), f"{len(bad)} cases beyond FP32 rounding"
     ok = np.abs(dl - dref) <= 1e-3 * np.abs(dref) + 1e-8
     assert ok.mean() > 0.97
+
+
+def _mesh_geom(kat, tag, mode):
+    """The oracle's own build of the meshes the reference recorded its calls on: a closed
+    icosphere (5 um, 320 triangles) and a periodic 10 um box whose sphere crosses a face."""
+    kw = {}
+    if tag == "mshp":
+        kw = dict(periodic=True, voxel_min=[-5e-6] * 3, voxel_max=[5e-6] * 3, feature_radius=3e-6)
+    if mode == "reflect":
+        sides = O.mesh_sides()
+    elif mode == "relax":
+        sides = O.mesh_sides(rho_intra=1e-6)
+    else:
+        sides = O.mesh_sides(rho_intra=1e-6 if tag == "msh" else None, kappa_out=1e-5,
+                             kappa_in=1e-5)
+    V = kat["mesh_V"] if tag == "msh" else kat["mesh_Vp"]
+    return O.mesh_geom(V, kat["mesh_F"], rho_mult=sides[0], kappa_mult=sides[1],
+                       permeable=sides[2], **kw)
+
+
+@pytest.mark.parametrize("tag", ["msh", "mshp"])
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("fp64", [False, True])
+def test_oracle_mesh_matches_reference_plugins(kat, tag, mode, fp64):
+    """Mesh.reflect / reflect_with_log_weight / permeate (rho/D = 500, kappa/D = 5000, the recorded
+    Bernoulli uniform): FP32 agrees to the last bit but for rounding-order cases, FP64 to FP32
+    rounding."""
+    g = _mesh_geom(kat, tag, mode)
+    wall = {"reflect": O.REFLECT, "relax": O.RELAX, "perm": O.PERMEATE}[mode]
+    key = f"pl_{tag}_{mode}"
+    rs, st, us = kat[key + "_r"], kat[key + "_step"], kat[key + "_u"]
+    ref, dref = kat[key + "_out"], kat[key + "_dlog"]
+    outs = np.zeros_like(ref)
+    dl = np.zeros(len(rs))
+    for i in range(len(rs)):
+        outs[i], dl[i] = O.plugin(g, wall, rs[i], st[i], float(np.float32(500.0)),
+                                  float(np.float32(5000.0)), float(us[i]), fp64=fp64)
+    err = np.max(np.abs(outs - ref), axis=1)
+    if not fp64:
+        assert np.mean(np.all(outs == ref, axis=1)) >= 0.95
+        assert err.max() <= 1e-7 * 5e-6 * 10      # a few ulp of the coordinates
+        np.testing.assert_allclose(dl, dref, rtol=1e-5, atol=1e-9)
+    else:
+        assert np.mean(err <= 1e-4 * 5e-6) >= 0.98
+        assert np.mean(np.abs(dl - dref) <= 1e-3 * np.abs(dref) + 1e-8) > 0.97
+
+
+def test_oracle_mesh_walk_stays_inside_a_closed_surface():
+    """A short reflecting walk of the oracle inside the closed icosphere: no walker leaves it (the
+    bounce, nudge and leak guard of the restatement keep every walker in), and the walk is
+    deterministic walker by walker."""
+    from dmipy_sim_gb300.mesh import icosphere
+    V, F = icosphere(4e-6, 2)
+    g = O.mesh_geom(V, F)
+    rng = np.random.default_rng(4)
+    d = rng.normal(size=(256, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r0 = (d * 3.2e-6 * rng.uniform(0, 1, (256, 1)) ** (1 / 3)).astype(np.float32)
+    G = np.zeros((2, 40, 3), np.float32)
+    G[0, :20, 0], G[0, 20:, 0] = 0.05, -0.05
+    G[1, :20, 2], G[1, 20:, 2] = 0.05, -0.05
+    kw = dict(n_walkers=256, G=G, dt=1e-4, sub_steps=4, phase_per_substep=True, seed=3, r0=r0,
+              want_walkers=True, n_threads=2)
+    a = O.walk(g, **kw)
+    b = O.walk(g, **kw)
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["phi"], b["phi"])
+    rad = np.linalg.norm(a["pos"].astype(np.float64), axis=1)
+    assert rad.max() < 4e-6 and np.all(np.isfinite(a["phi"]))
+    assert np.max(np.abs(a["pos"] - r0)) > 1e-7           # the walkers moved
 
 
 def _philox_py(seed, walker, stream, j):
