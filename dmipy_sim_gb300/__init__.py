@@ -13,18 +13,25 @@ from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, pack_cylinde
 from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
                    fused_sub_steps)
-from .trajectories import replay
+from . import trajectories
 from .mesh import Mesh, load_ply, icosphere, random_ellipsoid_cells, mesh_contains
 from .batched import Instance, Tuning, PreparedBatch, simulate_batch
 from .autotune import autotune
+# as in the reference, the trajectory replay is trajectories.replay and the name ``replay`` is
+# the replay-pack module
+from . import compression, bank, replay
+from .replay import ReplayPack, read_rpk, write_rpk, compile_scheme, replay_signal
+from .bank import build_replay_pack, build_to_floor
 
 __all__ = [
     "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
     "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "trapezoidal_ogse",
     "b_trapezoidal_ogse", "btensor_invariants", "ste", "pte", "Geometry", "FreeDiffusion",
     "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
-    "simulate", "simulate_cpmg", "simulate_trajectories", "replay", "run_walk", "WalkResult",
+    "simulate", "simulate_cpmg", "simulate_trajectories", "trajectories", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
     "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
-    "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune",
+    "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune", "compression", "bank", "replay",
+    "ReplayPack", "read_rpk", "write_rpk", "compile_scheme", "replay_signal", "build_replay_pack",
+    "build_to_floor",
 ]

@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 5
+DMSIM_ABI_VERSION = 6
 TILE_WALKERS = 320
 
 GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
@@ -29,7 +29,7 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_replay", "dmsim_batch_create", "dmsim_batch_bind", "dmsim_batch_launch",
             "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_pack",
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
-            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods")
+            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes")
 
 EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
@@ -154,6 +154,8 @@ def load():
     lib.dmsim_mesh_neighbourhoods.argtypes = [C.POINTER(Geometry), vp, vp, vp]
     lib.dmsim_adam_advance.restype = C.c_int
     lib.dmsim_adam_advance.argtypes = [vp, vp]
+    lib.dmsim_project_modes.restype = C.c_int
+    lib.dmsim_project_modes.argtypes = [vp, i32, i64, i32, i32, vp, i32, vp, vp, vp, vp]
     if lib.dmsim_version() != DMSIM_ABI_VERSION:
         raise RuntimeError(f"libdmsim ABI {lib.dmsim_version()} != {DMSIM_ABI_VERSION}")
     _lib = lib

@@ -563,11 +563,19 @@ def simulate_trajectories(n_walkers, diffusivity, geometry, T_max, dt_save, seed
     Returns ``(trajectories (n, n_t, 3) float16, dt_actual, sub_steps, dt_sim)`` and, with
     ``save_relaxation_data``, also ``dlog_boundary_unit (n, n_t) float16`` and ``comp_traj``
     (float16 occupancy of compartment 1 for a permeable Cylinder/Sphere, int8 zeros otherwise).
+
+    ``compress=K`` returns a compressed master instead (core.py:1370-1407, 1503-1517): the first
+    K orthonormal DCT-II bands of every walker's float32 path (``pos_modes`` (n, K, 3)) and, with
+    ``save_relaxation_data``, the boundary channel as its cumulative endpoint and detrended bands
+    (``blt_endpoint`` (n,), ``blt_modes`` (n, K)) plus the raw ``comp_traj``.  The projection
+    runs on the GPU per walker batch; the raw trajectory never leaves the device.
     """
     if kappa_MT and kappa_MT > 0:
         raise NotImplementedError("magnetisation-transfer binding walks are not supported")
     if compress is not None:
-        raise NotImplementedError("compressed (DCT) trajectory export is not supported")
+        return _simulate_trajectories_compressed(
+            n_walkers, diffusivity, geometry, T_max, dt_save, seed, walker_batch_size,
+            save_relaxation_data, require_gpu, r0, int(compress))
     _check_gpu(require_gpu)
     n_t = int(round(T_max / dt_save)) + 1
     dt_actual = T_max / (n_t - 1)
@@ -593,3 +601,57 @@ def simulate_trajectories(n_walkers, diffusivity, geometry, T_max, dt_save, seed
     else:
         comp = np.zeros((n_walkers, n_t), dtype=np.int8)
     return t, dt_actual, S, dt_sim, dlog, comp
+
+
+def _simulate_trajectories_compressed(n_walkers, diffusivity, geometry, T_max, dt_save, seed,
+                                      walker_batch_size, save_relaxation_data, require_gpu, r0,
+                                      K):
+    """simulate_trajectories(compress=K): walk each walker batch with a float32 trajectory
+    export, project it onto the DCT-II bands on the device (dmsim_project_modes), keep only the
+    bands.  Walkers are keyed by their global index, so the batches partition one walk."""
+    from . import compression as _cx
+    if K < 1:
+        raise ValueError(f"compress must be a positive mode count, got {K}")
+    _check_gpu(require_gpu)
+    n_t = int(round(T_max / dt_save)) + 1
+    dt_actual = T_max / (n_t - 1)
+    S = replay_sub_steps(geometry, diffusivity, dt_actual)
+    dev = _lib.device()
+    Kc = min(K, n_t)
+    batch = max(1, int(walker_batch_size or n_walkers))
+    perm2 = (getattr(geometry, 'permeability', None) is not None
+             and type(geometry).__name__ in ("Cylinder", "Sphere"))
+    want_dlog = save_relaxation_data and hasattr(geometry, "_desc")
+    r0f = None if r0 is None else _to_frame(geometry, r0)
+    G = np.zeros((1, n_t, 3), dtype=np.float32)
+    pos_modes = np.empty((n_walkers, Kc, 3), np.float32)
+    blt_end = np.zeros(n_walkers, np.float32) if save_relaxation_data else None
+    blt_modes = np.zeros((n_walkers, Kc), np.float32) if save_relaxation_data else None
+    comp = None
+    if save_relaxation_data:
+        comp = np.zeros((n_walkers, n_t), np.float16 if perm2 else np.int8)
+    for b0 in range(0, n_walkers, batch):
+        nb = min(batch, n_walkers - b0)
+        traj = torch.empty((nb, n_t, 3), dtype=torch.float32, device=dev)
+        res = run_walk(geometry, n_walkers=nb, diffusivity=diffusivity, G=G, dt=dt_actual,
+                       sub_steps=S, phase_per_substep=False, seed=seed, walker_offset=b0,
+                       r0=None if r0f is None else r0f[b0:b0 + nb], traj=traj, traj_f16=False,
+                       want_dlog=want_dlog, want_comp_occ=save_relaxation_data and perm2)
+        modes = _cx.project_modes(traj, Kc).cpu().numpy()
+        pos_modes[b0:b0 + nb] = _to_lab(geometry, modes.reshape(-1, 3)).reshape(nb, Kc, 3)
+        del traj
+        if save_relaxation_data:
+            if want_dlog:
+                e, m = _cx.project_modes(res.extras["dlog"], Kc, cumulative=True)
+                blt_end[b0:b0 + nb] = e.cpu().numpy()
+                blt_modes[b0:b0 + nb] = m.cpu().numpy()
+            if perm2:
+                comp[b0:b0 + nb] = res.extras["comp_occ"].cpu().numpy().astype(np.float16)
+    master = {"compressed": True, "method": "temporal_dct", "K": int(Kc), "n_t": int(n_t),
+              "dt_traj": dt_actual, "sub_steps": S, "dt_sim": dt_actual / S,
+              "pos_modes": pos_modes}
+    if save_relaxation_data:
+        master["blt_endpoint"] = blt_end
+        master["blt_modes"] = blt_modes
+        master["comp_traj"] = comp
+    return master

@@ -27,6 +27,9 @@ WalkFn walk_batch_fn_sph(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_pcyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_psph(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_mesh(int wall, int pm, int width, bool tsm);
+cudaError_t launch_project_modes(const void* x, bool f16, int64_t n_walkers, int n_t, int n_ch,
+                                 const float* basis, int K, const float* ramp, float* endpoint,
+                                 float* out, cudaStream_t st);
 }  // namespace dmsim
 
 using namespace dmsim;
@@ -698,6 +701,21 @@ int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t 
   k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, grid, 1, n_meas, n_meas, sums);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(DMSIM_ECUDA, "replay launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
+}
+
+int dmsim_project_modes(const void* x, int32_t x_f16, int64_t n_walkers, int32_t n_t, int32_t n_ch,
+                        const float* basis, int32_t K, const float* ramp, float* endpoint,
+                        float* out, void* stream) {
+  if (!x || !basis || !out || n_walkers < 1 || n_t < 1 || K < 1)
+    return fail(DMSIM_EINVAL, "project_modes: bad arguments");
+  if (n_ch != 1 && n_ch != 3) return fail(DMSIM_EINVAL, "project_modes: n_ch must be 1 or 3");
+  if (ramp && (n_ch != 1 || !endpoint))
+    return fail(DMSIM_EINVAL, "project_modes: the cumulative form needs n_ch == 1 and endpoint");
+  const cudaError_t err = launch_project_modes(x, x_f16 != 0, n_walkers, n_t, n_ch, basis, K, ramp,
+                                               endpoint, out, (cudaStream_t)stream);
+  if (err != cudaSuccess)
+    return fail(DMSIM_ECUDA, "project_modes launch failed: %s", cudaGetErrorString(err));
   return DMSIM_OK;
 }
 

@@ -18,7 +18,7 @@ def _resample(G, chi_perp, n_t_traj, dt_traj, dt_wf):
     if abs(dt_wf - dt_traj) / max(abs(dt_traj), 1e-30) > 1e-9:
         t_wf = np.arange(n_t_wf, dtype=np.float64) * dt_wf
         t_tr = np.arange(n_t_traj, dtype=np.float64) * dt_traj
-        Gt = np.zeros((n_meas, n_t_traj, 3), dtype=np.float32)
+        Gt = np.zeros((n_meas, n_t_traj, 3), dtype=G.dtype)
         for m in range(n_meas):
             for a in range(3):
                 Gt[m, :, a] = np.interp(t_tr, t_wf, G[m, :, a], left=0.0, right=0.0)
@@ -27,7 +27,7 @@ def _resample(G, chi_perp, n_t_traj, dt_traj, dt_wf):
     elif n_t_wf > n_t_traj:
         Gt = G[:, :n_t_traj, :]
     else:
-        Gt = np.zeros((n_meas, n_t_traj, 3), dtype=np.float32)
+        Gt = np.zeros((n_meas, n_t_traj, 3), dtype=G.dtype)
         Gt[:, :n_t_wf, :] = G
     t_wf = np.arange(n_t_wf, dtype=np.float64) * dt_wf
     t_tr = np.arange(n_t_traj, dtype=np.float64) * dt_traj
@@ -55,8 +55,15 @@ def replay(trajectory, dt_traj, G, dt_wf, *, chi_perp=None, dlog_boundary_unit=N
     (n_meas,) float64, or ``(phi (n_meas, n), log_w_total, signals)`` with
     ``return_walker_signals``.
     """
+    if isinstance(trajectory, dict) and trajectory.get("compressed"):
+        return _replay_compressed(trajectory, G, dt_wf, chi_perp=chi_perp, T2=T2, T1=T1,
+                                  surface_relaxivity=surface_relaxivity, D=D,
+                                  stimulated_echo=stimulated_echo, comp_traj=comp_traj,
+                                  T2_per_comp=T2_per_comp, T1_per_comp=T1_per_comp,
+                                  return_walker_signals=return_walker_signals,
+                                  susceptibility=susceptibility)
     if isinstance(trajectory, dict):
-        raise NotImplementedError("compressed (DCT mode-space) trajectories are not supported")
+        raise ValueError("a trajectory dict must be a compressed master (compressed=True)")
     if susceptibility is not None:
         raise NotImplementedError("susceptibility off-resonance replay is not supported")
     lib = _lib.load()
@@ -129,4 +136,85 @@ def replay(trajectory, dt_traj, G, dt_wf, *, chi_perp=None, dlog_boundary_unit=N
     if return_walker_signals:
         lw_tot = lw_scalar[:, None] + (np.zeros((1, 1)) if lw_walker is None else lw_walker)
         return phi.cpu().numpy().T.astype(np.float64), lw_tot, signals
+    return signals
+
+
+def _replay_compressed(master, G, dt_wf, *, chi_perp, T2, T1, surface_relaxivity, D,
+                       stimulated_echo, comp_traj, T2_per_comp, T1_per_comp,
+                       return_walker_signals, susceptibility):
+    """Replay of a compressed master (simulate_trajectories(compress=K); trajectories.py:258-357).
+
+    The phase is taken in mode space -- the stored (n, K, 3) DCT-II bands contracted with the
+    first K bands of DCT(G) on the trajectory grid, one ``dmsim_replay`` pass on the GPU -- and the
+    trajectory is never reconstructed.  Surface relaxivity reads the stored cumulative endpoint
+    (no gate) or the decoded per-save channel (gated); per-compartment T2/T1 read ``comp_traj``."""
+    from scipy.fft import dct
+    from . import compression as _cx
+    if susceptibility is not None:
+        raise NotImplementedError(
+            "susceptibility replay needs the raw trajectory: the off-resonance phase is not "
+            "linear in position and does not commute with the DCT")
+    K, n_t, dt_traj = int(master["K"]), int(master["n_t"]), float(master["dt_traj"])
+    C = np.ascontiguousarray(master["pos_modes"], np.float32)
+    n_w = C.shape[0]
+    G = np.asarray(G, np.float64)
+    n_meas, n_t_wf, _ = G.shape
+    chi = np.ones(n_t_wf) if chi_perp is None else np.asarray(chi_perp, np.float64)
+    Gt, chi_r = _resample(G, chi, n_t, dt_traj, float(dt_wf))
+    if chi_perp is None:
+        chi_r = np.ones((1, n_t))
+    Ghat = dct(Gt, type=2, norm="ortho", axis=1)[:, :K, :]
+
+    lw_scalar = np.zeros(n_meas)
+    lw_walker = None
+
+    def add(x):
+        nonlocal lw_walker
+        lw_walker = x if lw_walker is None else lw_walker + x
+
+    def inv_at(inv, comp):
+        comp = np.asarray(comp)
+        if np.issubdtype(comp.dtype, np.floating):
+            return inv[0] + comp.astype(np.float64) * (inv[1] - inv[0])
+        return inv[comp]
+    if T2_per_comp is not None:
+        comp = comp_traj if comp_traj is not None else master.get("comp_traj")
+        if comp is None:
+            raise ValueError("comp_traj required when T2_per_comp is provided.")
+        add(-dt_traj * (chi_r @ inv_at(1.0 / np.asarray(T2_per_comp, np.float64), comp).T))
+    elif T2 is not None:
+        lw_scalar -= (dt_traj / T2) * chi_r.sum(1)
+    if T1_per_comp is not None:
+        comp = comp_traj if comp_traj is not None else master.get("comp_traj")
+        if comp is None:
+            raise ValueError("comp_traj required when T1_per_comp is provided.")
+        add(-dt_traj * ((1.0 - chi_r) @ inv_at(1.0 / np.asarray(T1_per_comp, np.float64),
+                                                 comp).T))
+    elif T1 is not None:
+        lw_scalar -= (dt_traj / T1) * (n_t - chi_r.sum(1))
+    if surface_relaxivity is not None:
+        if D is None:
+            raise ValueError("D must be provided when surface_relaxivity is not None.")
+        if "blt_endpoint" not in master:
+            raise ValueError("compressed master lacks the boundary channel "
+                             "(re-run simulate_trajectories with save_relaxation_data=True).")
+        if chi_perp is None:
+            add((surface_relaxivity / D) * np.asarray(master["blt_endpoint"], np.float64)[None, :])
+        else:
+            blt = _cx.decode_boundary_dct(
+                {"blt_dct_coeffs": master["blt_modes"], "blt_endpoint": master["blt_endpoint"]},
+                {"n_t": n_t, "K": K}).astype(np.float64)
+            add((surface_relaxivity / D) * (chi_r @ blt.T))
+    if lw_walker is not None and lw_walker.shape[0] != 1:
+        raise NotImplementedError("per-measurement chi with walker-dependent relaxation weights "
+                                  "is not supported by the GPU replay")
+    sums, phi = _cx._replay_sums(C, Ghat, GAMMA * dt_traj,
+                                 log_w=None if lw_walker is None else lw_walker[0],
+                                 want_phi=return_walker_signals)
+    signals = np.exp(lw_scalar) * sums[:, 0] / n_w
+    if stimulated_echo:
+        signals = signals * 0.5
+    if return_walker_signals:
+        lw_tot = lw_scalar[:, None] + (np.zeros((1, 1)) if lw_walker is None else lw_walker)
+        return phi.T, lw_tot, signals
     return signals

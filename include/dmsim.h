@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 5
+#define DMSIM_ABI_VERSION 6
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -246,6 +246,17 @@ int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t 
                  const float* G, int32_t n_meas, float gamma_dt, const float* log_w,
                  double* sums, float* phi_out, void* workspace, size_t workspace_bytes,
                  void* stream);
+
+/* Temporal-mode projection, the compressed trajectory export of simulate_trajectories(compress=K)
+   (core.py:1370-1407) and the temporal_dct / boundary_dct codecs of compression.py:55-62, 224-249:
+   out[w,k,c] = sum_t basis[k,t] * x[w,t,c] with x (n_walkers, n_t, n_ch) float16 (x_f16 = 1) or
+   float32, n_ch 1 or 3, basis (K, n_t) float32, out (n_walkers, K, n_ch) float32.  With ramp
+   (n_t floats; n_ch must be 1) the series is replaced by its detrended running sum
+   B_t - B_{n_t-1} ramp_t before the projection and B_{n_t-1} is written to endpoint[w].
+   Kahan-compensated FP32 sums; no workspace. */
+int dmsim_project_modes(const void* x, int32_t x_f16, int64_t n_walkers, int32_t n_t, int32_t n_ch,
+                        const float* basis, int32_t K, const float* ramp, float* endpoint,
+                        float* out, void* stream);
 
 /* ---- batched walks ---------------------------------------------------------------------------
    Many independent walks (instances: geometry, waveform, rho, kappa, n_walkers, n_t, seed each

@@ -330,6 +330,115 @@ def _waveform_cases_tensor(m, out):
         np.asarray(x) for x in w.btensor_invariants(B))
 
 
+def make_replay_kat(root):
+    """Known answers of the reference's compression.py / replay.py codecs and mode-space replay
+    and of trajectories.replay on a compressed master, on a seeded synthetic walk
+    (replay_kat.npz)."""
+    import importlib
+    m = _ref(root)
+    cx = importlib.import_module("dmipy_sim.compression")
+    rp = importlib.import_module("dmipy_sim.replay")
+    wfm, tr = m["waveforms"], m["trajectories"]
+    rng = np.random.default_rng(11)
+    n_w, n_t, dt = 200, 100, 2.5e-4
+    X = np.cumsum(rng.normal(scale=0.25e-6, size=(n_w, n_t, 3)), axis=1)
+    out = {"traj": X, "dt": np.float64(dt)}
+    a, mm, nb = cx.encode_temporal_dct(X, 16)
+    for k, v in a.items():
+        out[f"tdct_{k}"] = v
+    out["tdct_decoded"] = cx.decode(a, mm).astype(np.float32)
+    a, mm, nb = cx.encode_lowrank(X, 8)
+    out["lowrank_decoded"] = cx.decode(a, mm).astype(np.float32)
+    # boundary local time: spiky, mostly zero, <= 0
+    dlog = -np.abs(rng.normal(scale=1e-7, size=(n_w, n_t))) * (rng.uniform(size=(n_w, n_t)) < 0.1)
+    out["blt_raw"] = dlog
+    a, mm = cx.encode_boundary_dct(dlog, K=8)
+    out["blt_dct_coeffs"], out["blt_endpoint"] = a["blt_dct_coeffs"], a["blt_endpoint"]
+    out["blt_dct_decoded"] = cx.decode_boundary_dct(a, mm)
+    a, mm = cx.encode_boundary_local_time(dlog)
+    out["blt_sparse_mode"] = np.array(mm["mode"] == "sparse")
+    for k, v in a.items():
+        out[f"bltq_{k}"] = v
+    out["bltq_decoded"] = cx.decode_boundary_local_time(a, mm)
+    dense = -np.abs(rng.normal(scale=1e-7, size=(40, n_t)))
+    a, mm = cx.encode_boundary_local_time(dense)
+    out["bltd_raw"] = dense
+    out["bltd_q"], out["bltd_decoded"] = a["blt_dense_q"], cx.decode_boundary_local_time(a, mm)
+    comp = (rng.uniform(size=(n_w, 1)) < 0.4).astype(np.int32) * np.ones((1, n_t), np.int32)
+    comp[:50, 60:] = 2
+    a, mm = cx.encode_compartment(comp)
+    for k, v in a.items():
+        out[f"comp_{k}"] = v
+    fr = np.clip(np.cumsum(rng.normal(scale=0.05, size=(30, n_t)), axis=1) * 0.3 + 0.5, 0, 1)
+    a, mm = cx.encode_compartment(fr)
+    out["compf_decoded"] = cx.decode_compartment(a, mm)
+    a, mm = cx.encode_bound_fraction(fr)
+    out["bfrac_decoded"] = cx.decode_bound_fraction(a, mm)
+    out["comp_frac"] = fr
+    out["comp_int"] = comp
+    out["relax_lw"] = cx.relaxation_logweight(comp.clip(0, 1), [0.06, 0.08], [0.9, 1.2], dt,
+                                              chi=(np.arange(n_t) < 80).astype(float))
+    out["relax_lw_frac"] = cx.relaxation_logweight(fr, [0.06, 0.08], [0.9, 1.2], dt)
+    out["surf_lw"] = cx.surface_logweight(dlog, 500.0, chi=(np.arange(n_t) % 3 == 0).astype(float))
+    # acquisition battery, mode-space replay and fidelity
+    env = cx.default_envelope()
+    G, meta = cx.acquisition_battery(n_t, dt, env)
+    out["battery_G"] = G
+    out["battery_b"] = np.array([q["b"] for q in meta])
+    out["battery_Gpeak"] = np.array([q["Gpeak"] for q in meta])
+    out["battery_fam"] = np.array([q["fam"] for q in meta])
+    a16, m16, _ = cx.encode_temporal_dct(X, 16)
+    out["ms_phi"] = cx.mode_space_phi(a16, m16, G[:12], dt)
+    lw = -np.abs(rng.normal(scale=0.05, size=n_w))
+    w = rng.uniform(0.5, 1.5, n_w)
+    out["ms_logw"], out["ms_w"] = lw, w
+    out["ms_signal"] = cx.mode_space_signal(a16, m16, G[:12], dt, logw=lw, weights=w)
+    a8, m8, _ = cx.encode_temporal_dct(X, 8)
+    fid = cx.measure_fidelity(X, dt, cx.decode(a8, m8), env)
+    out["fid_err_max"], out["fid_floor_max"] = fid["err_max"], fid["floor_max"]
+    out["fid_fams"] = np.array(sorted(fid["per_family"]))
+    out["fid_fam_err"] = np.array([fid["per_family"][f]["err_max"] for f in out["fid_fams"]])
+    out["fid_fam_floor"] = np.array([fid["per_family"][f]["floor_max"]
+                                     for f in out["fid_fams"]])
+    Kbest, fbest = cx.auto_select_modes(X, X, dt, env=env, K_grid=(4, 8, 16, 32))
+    out["auto_K"] = np.array(Kbest)
+    # compiled-scheme forward of a pack with spin weights and boundary bands
+    W = rp.compile_scheme(G[:12], dt, 16)
+    out["scheme_W"] = W
+    blt_pack = rng.normal(scale=1e-8, size=(n_w, 6))
+    pack = dict(a16, spin_weights=w.astype(np.float32), blt_dct=blt_pack)
+    out["pack_blt_dct"] = blt_pack
+    out["rs_plain"] = rp.replay_signal(dict(a16), W)
+    out["rs_complex"] = rp.replay_signal(pack, W, complex_signal=True)
+    out["rs_surface"] = rp.replay_signal(rp.ReplayPack(pack, {"n_t": n_t}), W, rho_over_D=500.0)
+    chi_hat = rng.normal(size=4)
+    out["rs_chi_hat"] = chi_hat
+    out["rs_gated"] = rp.replay_signal(rp.ReplayPack(pack, {"n_t": n_t}), W, rho_over_D=500.0,
+                                       chi_hat=chi_hat)
+    # trajectories.replay on a compressed master (mode space, no reconstruction)
+    C = cx.read_position_coeffs(a16, dtype=np.float32)
+    ab, _ = cx.encode_boundary_dct(dlog, K=16)
+    master = {"compressed": True, "method": "temporal_dct", "K": 16, "n_t": n_t, "dt_traj": dt,
+              "pos_modes": C, "blt_endpoint": ab["blt_endpoint"],
+              "blt_modes": ab["blt_dct_coeffs"], "comp_traj": comp.clip(0, 1)}
+    out["master_blt_modes"], out["master_blt_endpoint"] = ab["blt_dct_coeffs"], ab["blt_endpoint"]
+    w1 = wfm.set_b(wfm.pgse(0.006, 0.015, 0.1, [[1, 0, 0], [0, 0.6, 0.8]], 61), [1e9, 2e9])
+    out["rc_G"], out["rc_dt"] = np.asarray(w1.G), np.float64(w1.dt)
+    out["rc_plain"] = np.asarray(tr.replay(master, None, np.asarray(w1.G), w1.dt))
+    out["rc_relax"] = np.asarray(tr.replay(master, None, np.asarray(w1.G), w1.dt, T2=0.07,
+                                           T1=0.9, surface_relaxivity=1e-5, D=2e-9))
+    w2 = wfm.pgste(0.005, 0.012, 0.02, [[1, 0, 0]], 101)
+    out["rc2_G"], out["rc2_dt"] = np.asarray(w2.G), np.float64(w2.dt)
+    out["rc2_chi"] = np.asarray(w2.chi_perp, np.float64)
+    out["rc_gated"] = np.asarray(tr.replay(master, None, np.asarray(w2.G), w2.dt,
+                                           chi_perp=w2.chi_perp, T2_per_comp=[0.05, 0.08],
+                                           T1_per_comp=[0.8, 1.1], surface_relaxivity=2e-5, D=2e-9,
+                                           stimulated_echo=True))
+    path = HERE / "replay_kat.npz"
+    np.savez_compressed(path, **out)
+    print(f"replay_kat.npz: {len(out)} arrays")
+
+
 def make_kat_extra(root):
     """Add the tensor-encoding waveform vectors to an existing kat.npz."""
     m = _ref(root)
@@ -525,6 +634,8 @@ if __name__ == "__main__":
     ap.add_argument("--kat", action="store_true")
     ap.add_argument("--kat-extra", action="store_true",
                     help="add the tensor-encoding waveform vectors to an existing kat.npz")
+    ap.add_argument("--replay-kat", action="store_true",
+                    help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--procs", type=int, default=os.cpu_count() or 4)
@@ -533,5 +644,7 @@ if __name__ == "__main__":
         make_kat(a.ref)
     if a.kat_extra:
         make_kat_extra(a.ref)
+    if a.replay_kat:
+        make_replay_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)
