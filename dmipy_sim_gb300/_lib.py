@@ -16,7 +16,8 @@ LIB_PATH = _PKG / "libdmsim.so"
 DMSIM_ABI_VERSION = 6
 TILE_WALKERS = 320
 
-GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH = range(6)
+(GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
+ GEOM_MYELIN) = range(7)
 WALL_REFLECT, WALL_RELAX, WALL_PERMEATE = range(3)
 
 STATUS_NAMES = ("nonfinite", "clamped", "init_fail", "bounce_budget", "escape_reject",
@@ -53,6 +54,10 @@ class Geometry(C.Structure):
         ("tri", C.c_void_p), ("tri_vn", C.c_void_p), ("mesh_cell_start", C.c_void_p),
         ("mesh_cell_tri", C.c_void_p), ("mesh_nb_start", C.c_void_p), ("mesh_nb_tri", C.c_void_p),
         ("tri_bs", C.c_void_p),
+        ("myelin_r_out", C.c_float), ("myelin_step", C.c_float * 3),
+        ("myelin_kin_over_D", C.c_float * 3), ("myelin_kout_over_D", C.c_float * 3),
+        ("myelin_t2dec", C.c_float * 3), ("myelin_logw0", C.c_float * 3),
+        ("myelin_seed_n", C.c_int64 * 2),
     ]
 
 

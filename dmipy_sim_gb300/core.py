@@ -116,7 +116,10 @@ def replay_sub_steps(geometry, diffusivity, dt):
 
 
 def fused_sub_steps(geometry, diffusivity, dt):
-    """The fused engine's sub-step count for this geometry (physics.py:276-415 branch order)."""
+    """The fused engine's sub-step count for this geometry (physics.py:276-415 branch order); a
+    myelinated cylinder takes one step per sample (physics.py:420-680)."""
+    if getattr(geometry, '_is_myelinated', False):
+        return 1
     if getattr(geometry, 'permeability', None) is not None:
         return permeable_sub_steps(geometry, diffusivity, dt)
     if getattr(geometry, 'surface_relaxivity_t2', None) is not None:
@@ -242,7 +245,7 @@ class PreparedWalk:
                  seed, chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
                  want_positions=False, want_walker_signals=False, want_compartments=False,
                  traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False,
-                 use_basis=True, allocate_workspace=True):
+                 use_basis=True, allocate_workspace=True, total_walkers=None):
         self.lib = _lib.load()
         dev = self.dev = _lib.device()
         G = np.asarray(G, dtype=np.float32)
@@ -250,17 +253,30 @@ class PreparedWalk:
         dt = float(dt)
         S = int(sub_steps)
         dt_sub = dt / S
-        D = float(diffusivity)
-        step_l = np.float32(np.sqrt(6.0 * D * dt_sub))
         gamma_dt = np.float32(GAMMA * (dt_sub if phase_per_substep else dt))
-        rho = getattr(geometry, 'surface_relaxivity_t2', None)
-        kappa = getattr(geometry, 'permeability', None)
-        rho_over_D = np.float32(rho / D) if rho is not None else np.float32(0.0)
-        kappa_over_D = np.float32(kappa / D) if kappa is not None else np.float32(0.0)
-        want_w = (rho is not None) or (kappa is not None) or (T2 is not None) or (T1 is not None)
-        wall = geometry._wall_mode(rho is not None or want_dlog)
-        self.gdesc, self._keep = geometry._desc(float(step_l), wall, rho_over_D, kappa_over_D,
-                                                dev)
+        self.myelin = bool(getattr(geometry, '_is_myelinated', False))
+        if self.myelin:
+            # unit directions scaled per compartment on the device; T2 per compartment only (the
+            # reference's myelin step ignores simulate's T2, physics.py:420-505)
+            if S != 1:
+                raise ValueError("a myelinated cylinder takes one step per waveform sample")
+            step_l = np.float32(1.0)
+            T2 = None
+            want_w = geometry._has_weight() or T1 is not None
+            self.gdesc = geometry._myelin_desc(dt, int(total_walkers or
+                                                       (n_walkers + walker_offset)))
+            self._keep = ()
+        else:
+            D = float(diffusivity)
+            step_l = np.float32(np.sqrt(6.0 * D * dt_sub))
+            rho = getattr(geometry, 'surface_relaxivity_t2', None)
+            kappa = getattr(geometry, 'permeability', None)
+            rho_over_D = np.float32(rho / D) if rho is not None else np.float32(0.0)
+            kappa_over_D = np.float32(kappa / D) if kappa is not None else np.float32(0.0)
+            want_w = (rho is not None) or (kappa is not None) or (T2 is not None) or (T1 is not None)
+            wall = geometry._wall_mode(rho is not None or want_dlog)
+            self.gdesc, self._keep = geometry._desc(float(step_l), wall, rho_over_D, kappa_over_D,
+                                                    dev)
         echo = np.asarray([n_t - 1] if echo_idx is None else echo_idx, dtype=np.int32).ravel()
         self._echo_c = (ctypes.c_int32 * len(echo))(*echo.tolist())
         self.G_dev = torch.from_numpy(np.ascontiguousarray(G.transpose(1, 0, 2))).to(dev)
@@ -436,10 +452,11 @@ def simulate(n_walkers, diffusivity=None, waveform=None, geometry=None, seed=123
         raise ValueError(f"engine must be 'auto', 'replay', or 'fused'; got {engine!r}")
     if hasattr(waveform, 'waveform'):
         waveform = waveform.waveform
-    if diffusivity is None:
+    myelin = bool(getattr(geometry, '_is_myelinated', False))
+    if diffusivity is None and not myelin:
         raise NotImplementedError(
-            "simulate() without an explicit diffusivity (myelin geometries carrying their own D) "
-            "is not supported by this engine")
+            "simulate() without an explicit diffusivity is only defined for geometries carrying "
+            "their own D (MyelinatedCylinder)")
     if return_compartments == 'full':
         raise NotImplementedError("return_compartments='full' is not supported by this engine")
 
@@ -477,6 +494,11 @@ def simulate(n_walkers, diffusivity=None, waveform=None, geometry=None, seed=123
                    want_walker_signals=bool(return_walker_signals),
                    want_compartments=return_compartments is not False, traj=traj, traj_f16=False)
     signals = res.signal[0].astype(np.float32)
+    if myelin:
+        # the walkers' log-weights start at log(spin weight): normalise by the weight sum
+        # instead of the walker count (core.py:426-427)
+        sw = geometry.spin_weight_sum(n_walkers, r0)
+        signals = (signals.astype(np.float64) * n_walkers / sw).astype(np.float32)
     if getattr(waveform, 'stimulated_echo', False):
         signals = signals * np.float32(0.5)
     out = [signals]
@@ -525,6 +547,9 @@ def simulate_cpmg(n_walkers, diffusivity, waveform, geometry, *, T2=None, seed=1
     """Multi-echo CPMG signal (n_echoes, n_meas) from one walk (core.py:861-969): the ensemble is
     reduced only at the echo samples instead of materialising the (n, n_t, n_meas) trace."""
     _check_gpu(require_gpu)
+    if getattr(geometry, '_is_myelinated', False):
+        raise NotImplementedError("MyelinatedCylinder is walked by simulate() only (the reference's "
+                                  "CPMG path has no myelin step rule)")
     if hasattr(waveform, 'waveform'):
         waveform = waveform.waveform
     echo = getattr(waveform, 'echo_indices', None)
@@ -572,6 +597,9 @@ def simulate_trajectories(n_walkers, diffusivity, geometry, T_max, dt_save, seed
     """
     if kappa_MT and kappa_MT > 0:
         raise NotImplementedError("magnetisation-transfer binding walks are not supported")
+    if getattr(geometry, '_is_myelinated', False):
+        raise NotImplementedError("MyelinatedCylinder is walked by simulate() only (its own step "
+                                  "rule has no trajectory producer)")
     if compress is not None:
         return _simulate_trajectories_compressed(
             n_walkers, diffusivity, geometry, T_max, dt_save, seed, walker_batch_size,

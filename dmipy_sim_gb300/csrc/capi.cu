@@ -21,6 +21,7 @@ WalkFn walk_fn_sph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_pcyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_psph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_mesh(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_myelin(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_sph(int wall, int pm, int width, bool tsm);
@@ -92,8 +93,20 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
       return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
   }
   const bool packed = g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  if (g->kind < 0 || g->kind > DMSIM_GEOM_MESH)
+  if (g->kind < 0 || g->kind > DMSIM_GEOM_MYELIN)
     return fail(DMSIM_EINVAL, "unsupported geometry kind %d", g->kind);
+  if (g->kind == DMSIM_GEOM_MYELIN) {
+    if (!(g->radius > 0.f) || !(g->myelin_r_out > g->radius))
+      return fail(DMSIM_EINVAL, "myelinated cylinder needs 0 < inner radius < outer radius");
+    if (g->wall_mode == DMSIM_WALL_RELAX)
+      return fail(DMSIM_EINVAL, "myelinated cylinder walls reflect or permeate");
+    if (g->rho_over_D != 1.f)
+      return fail(DMSIM_EINVAL, "myelinated cylinder: rho_over_D must be 1 (T2 per compartment)");
+    for (int c = 0; c < 3; ++c)
+      if (!(g->myelin_step[c] >= 0.f)) return fail(DMSIM_EINVAL, "negative myelin step length");
+    if (p->step_length != 1.f)
+      return fail(DMSIM_EINVAL, "myelinated cylinder walks unit directions (step_length = 1)");
+  }
   if (g->kind == DMSIM_GEOM_MESH) {
     if (!g->tri || !g->tri_vn || !g->mesh_cell_start || !g->mesh_cell_tri)
       return fail(DMSIM_EINVAL, "mesh geometry needs its triangle and grid tables");
@@ -153,6 +166,9 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
       pl->fn = walk_fn_psph(g->wall_mode, pl->pm, pl->width, pl->tsm);
       break;
     case DMSIM_GEOM_MESH: pl->fn = walk_fn_mesh(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_MYELIN:
+      pl->fn = walk_fn_myelin(g->wall_mode, pl->pm, pl->width, false);
+      break;
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
   pl->lay = walk_smem_layout(pl->pm, pl->width, p->n_meas);
@@ -467,6 +483,25 @@ __global__ void k_mesh_nb(const uint32_t* __restrict__ cs, const uint32_t* __res
   }
 }
 
+MyelinK make_myelk(const dmsim_geometry* g) {
+  MyelinK m;
+  memset(&m, 0, sizeof(m));
+  if (g->kind != DMSIM_GEOM_MYELIN) return m;
+  m.r_in = g->radius;
+  m.r_out = g->myelin_r_out;
+  m.nudge = g->nudge;
+  for (int c = 0; c < 3; ++c) {
+    m.sl[c] = g->myelin_step[c];
+    m.kin[c] = g->myelin_kin_over_D[c];
+    m.kout[c] = g->myelin_kout_over_D[c];
+    m.t2dec[c] = g->myelin_t2dec[c];
+    m.lw0[c] = g->myelin_logw0[c];
+  }
+  m.n0 = g->myelin_seed_n[0];
+  m.n1 = g->myelin_seed_n[1];
+  return m;
+}
+
 GeoK make_geok(const dmsim_geometry* g) {
   GeoK gk;
   memset(&gk, 0, sizeof(gk));
@@ -532,6 +567,7 @@ void fill_kargs(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim
   a->rho = g->rho_over_D;
   a->g = make_geok(g);
   a->mk = make_meshk(g);
+  a->my = make_myelk(g);
   a->tab_cs_bytes = (uint32_t)pl.tab_cs;
   a->tab_cand_bytes = (uint32_t)pl.tab_cand;
   a->cs = g->cell_start;
@@ -839,7 +875,8 @@ int batch_plan(dmsim_batch* b) {
     if (rc != DMSIM_OK) return rc;
     rc = check_outputs(&I.p, &I.g, &I.o);
     if (rc != DMSIM_OK) return rc;
-    I.batched = I.pl.pm == 1;
+    // a myelinated cylinder has no batched kernel: its instances run as plain walks
+    I.batched = I.pl.pm == 1 && I.g.kind != DMSIM_GEOM_MYELIN;
     if (!I.batched) {
       I.off_ws = off;
       off = align256(off + I.pl.total);

@@ -1,19 +1,21 @@
 """Writes the walk-kernel instantiation tables (walk_<kind>.cu, walk_batch_<kind>.cu).
 
 Each geometry gets one translation unit of single-instance variants (wall mode x phase form x
-cell list in shared memory) and one of batched variants (basis phase form only), so that the
-parallel build compiles them side by side.  Run after changing the variant set.
+cell list in shared memory) and, except the myelinated cylinder (whose batch instances run as
+plain walks), one of batched variants (basis phase form only), so that the parallel build compiles
+them side by side.  Run after changing the variant set.
 """
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-KINDS = [  # (file stem, enum, wall modes, has a cell list)
-    ("free", "DMSIM_GEOM_FREE", [0], False),
-    ("cyl", "DMSIM_GEOM_CYLINDER", [0, 1, 2], False),
-    ("sph", "DMSIM_GEOM_SPHERE", [0, 1, 2], False),
-    ("pcyl", "DMSIM_GEOM_PACKED_CYLINDERS", [0, 1, 2], True),
-    ("psph", "DMSIM_GEOM_PACKED_SPHERES", [0, 1, 2], True),
-    ("mesh", "DMSIM_GEOM_MESH", [0, 1, 2], False),
+KINDS = [  # (file stem, enum, wall modes, has a cell list, has batched variants)
+    ("free", "DMSIM_GEOM_FREE", [0], False, True),
+    ("cyl", "DMSIM_GEOM_CYLINDER", [0, 1, 2], False, True),
+    ("sph", "DMSIM_GEOM_SPHERE", [0, 1, 2], False, True),
+    ("pcyl", "DMSIM_GEOM_PACKED_CYLINDERS", [0, 1, 2], True, True),
+    ("psph", "DMSIM_GEOM_PACKED_SPHERES", [0, 1, 2], True, True),
+    ("mesh", "DMSIM_GEOM_MESH", [0, 1, 2], False, True),
+    ("myelin", "DMSIM_GEOM_MYELIN", [0, 2], False, False),
 ]
 VARIANTS = [(0, 16), (0, 32), (0, 64), (1, 2), (1, 4), (1, 8)]  # (phase form, width)
 
@@ -40,9 +42,10 @@ def _table(stem, enum, walls, packed, batch):
 
 
 def main():
-    for stem, enum, walls, packed in KINDS:
+    for stem, enum, walls, packed, batched in KINDS:
         (HERE / f"walk_{stem}.cu").write_text(_table(stem, enum, walls, packed, False))
-        (HERE / f"walk_batch_{stem}.cu").write_text(_table(stem, enum, walls, packed, True))
+        if batched:
+            (HERE / f"walk_batch_{stem}.cu").write_text(_table(stem, enum, walls, packed, True))
 
 
 if __name__ == "__main__":

@@ -50,6 +50,79 @@ struct GeoK {
   int kmax;  // most candidates any cell lists (0: unknown); 2 selects the two-slot scan
 };
 
+// Myelinated cylinder: two concentric walls (axis z) around three compartments.
+struct MyelinK {
+  float r_in, r_out, nudge;
+  float sl[3];     // step length of each compartment
+  float kin[3];    // kappa_inner / max(D_c, 1e-30) of the compartment left
+  float kout[3];   // kappa_outer / max(D_c, 1e-30)
+  float t2dec[3];  // dt / T2_c
+  float lw0[3];    // log water proton density of each compartment
+  long long n0, n1;  // seeding ranges of the global walker index (intra, myelin, extra)
+};
+
+// One step of make_myelin_step_fn (physics.py:506-677): the walker moves by its compartment's
+// step along the unit direction (ux, uy, uz); a crossing of the inner (intra <-> myelin) or outer
+// (myelin <-> extra) wall -- decided on the end point's radius, at most one per step -- transmits
+// with the Powles probability min(1, 2 kappa/D_left |r - R|) on its own uniform (u1 inner, u2
+// outer), else the end point is mirrored across the wall; then the walker is clamped onto its
+// compartment's side of each wall (1e-4 R_in inside).  Returns the per-compartment T2 decrement
+// (-dt/T2 of the new compartment), which the kernel gates by the coherence flag.
+template <int WALL>
+__device__ __forceinline__ float myelin_step(float& x, float& y, float& z, int& comp, float ux,
+                                             float uy, float uz, float u1, float u2,
+                                             const MyelinK& m, Tally& tl) {
+  const float sl = comp == 0 ? m.sl[0] : (comp == 1 ? m.sl[1] : m.sl[2]);
+  float nx = x + ux * sl, ny = y + uy * sl;
+  const float nz = z + uz * sl;
+  const float rn = sqrtf(nx * nx + ny * ny);
+  const bool cio = comp == 0 && rn >= m.r_in, cii = comp == 1 && rn < m.r_in;
+  const bool coo = comp == 1 && rn >= m.r_out, coi = comp == 2 && rn < m.r_out;
+  const bool ci = cio || cii, co = coo || coi;
+  bool ti = false, to = false;
+  if constexpr (WALL == kPermeate) {
+    const float kin = comp == 0 ? m.kin[0] : (comp == 1 ? m.kin[1] : m.kin[2]);
+    const float kout = comp == 0 ? m.kout[0] : (comp == 1 ? m.kout[1] : m.kout[2]);
+    const float p_in = fminf(1.f, 2.f * kin * fabsf(rn - m.r_in));
+    const float p_out = fminf(1.f, 2.f * kout * fabsf(rn - m.r_out));
+    ti = ci && (u1 < p_in);
+    to = co && (u2 < p_out);
+  }
+  int nc = comp;
+  if (ci && !ti) {  // mirror across the inner wall
+    const float s = (2.f * m.r_in - rn) / fmaxf(rn, 1e-20f);
+    nx *= s;
+    ny *= s;
+  }
+  if (ti) nc = cio ? 1 : 0;
+  if (co && !to) {  // mirror across the outer wall
+    const float r2 = sqrtf(nx * nx + ny * ny);
+    const float s = (2.f * m.r_out - r2) / fmaxf(r2, 1e-20f);
+    nx *= s;
+    ny *= s;
+  }
+  if (to) nc = coo ? 2 : 1;
+  // safety clamps onto the compartment's side of each wall (physics.py:633-664)
+  float rc = sqrtf(nx * nx + ny * ny);
+  auto put = [&](float target) {
+    const float s = target / fmaxf(rc, 1e-20f);
+    nx *= s;
+    ny *= s;
+    rc = sqrtf(nx * nx + ny * ny);
+    ++tl.clamp;
+  };
+  if (nc == 0 && rc >= m.r_in) put(m.r_in - m.nudge);
+  if (nc == 1 && rc < m.r_in) put(m.r_in + m.nudge);
+  if (nc == 1 && rc >= m.r_out) put(m.r_out - m.nudge);
+  if (nc == 2 && rc < m.r_out) put(m.r_out + m.nudge);
+  if (ti || to) ++tl.transmit;
+  x = nx;
+  y = ny;
+  z = nz;
+  comp = nc;
+  return -(nc == 0 ? m.t2dec[0] : (nc == 1 ? m.t2dec[1] : m.t2dec[2]));
+}
+
 // ------------------------------------------------------------------------------------------------
 // Single cylinder, axis z, centred at the origin.
 // ------------------------------------------------------------------------------------------------

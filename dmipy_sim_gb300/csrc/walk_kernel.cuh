@@ -46,6 +46,7 @@ struct KArgs {
   float step_l, gamma_dt, t2dec, t1dec, rho;
   GeoK g;
   MeshK mk;  // GEOM_MESH only
+  MyelinK my;  // GEOM_MYELIN only
   uint32_t tab_cs_bytes, tab_cand_bytes;  // shared-memory staging sizes (multiples of 16 B)
   const float* Cp;                        // basis mode: (M, 3, RT) coefficients
   const uint32_t* cs;
@@ -211,6 +212,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
   constexpr bool PACKED = GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool MESH = GEOM == DMSIM_GEOM_MESH;
+  constexpr bool MYEL = GEOM == DMSIM_GEOM_MYELIN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   // single-instance launches walk a static share of tiles; batched ones pull work items
@@ -332,6 +334,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
     float x = 0.f, y = 0.f, z = 0.f;
     int ix = 0, iy = 0, iz = 0;
     int mcls = 1, mpop = 0;  // mesh: class and gather population of the current position
+    int mcomp = 0;           // myelinated cylinder: the walker's compartment
     if (a.r0 != nullptr) {
       if (act) {
         x = a.r0[3 * w];
@@ -348,6 +351,10 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
           z -= g.L * iz;
         }
       }
+      if constexpr (MYEL) {  // compartment of a given start position (geometries.py:1018-1029)
+        const float q = x * x + y * y;
+        mcomp = q < a.my.r_in * a.my.r_in ? 0 : (q < a.my.r_out * a.my.r_out ? 1 : 2);
+      }
       if constexpr (MESH) {
         const MeshK& m = a.mk;
         if (m.per[0]) { ix = (int)floorf((x - m.vmin[0]) / m.box[0]); x -= m.box[0] * ix; }
@@ -356,13 +363,31 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
       }
     } else if constexpr (GEOM != DMSIM_GEOM_FREE) {
       // Uniform seeding by rejection, as the reference's host samplers (geometries.py:186-195,
-      // 477-491, 1717-1744, 2421-2443), on the seeding stream.
+      // 477-491, 1717-1744, 2421-2443), on the seeding stream.  A myelinated cylinder takes its
+      // compartment from the walker's index range (volume-proportional counts, intra first,
+      // geometries.py:928-1006) and a uniform point of that disc or annulus (extra: out to
+      // 2 R_out).
+      if constexpr (MYEL) {
+        const long long gi = (long long)gw;
+        mcomp = gi < a.my.n0 ? 0 : (gi < a.my.n1 ? 1 : 2);
+      }
+      const float s_lo = MYEL ? (mcomp == 0 ? 0.f : (mcomp == 1 ? a.my.r_in : a.my.r_out)) : 0.f;
+      const float s_hi = MYEL ? (mcomp == 0 ? a.my.r_in : (mcomp == 1 ? a.my.r_out
+                                                                       : 2.f * a.my.r_out))
+                              : 0.f;
       bool ok = false;
 #pragma unroll 1
       for (uint32_t j = 0; j < 256u && !ok; ++j) {
         const u32x4 r = draw(a.seed, gw, 1u, j);
         const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z), u3 = u01(r.w);
-        if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
+        if constexpr (MYEL) {
+          for (int h = 0; h < 2 && !ok; ++h) {
+            const float px = s_hi * (2.f * (h ? u2 : u0) - 1.f);
+            const float py = s_hi * (2.f * (h ? u3 : u1) - 1.f);
+            const float q = px * px + py * py;
+            if (q >= s_lo * s_lo && q < s_hi * s_hi) { x = px; y = py; ok = true; }
+          }
+        } else if constexpr (GEOM == DMSIM_GEOM_CYLINDER) {
           float px = g.R * (2.f * u0 - 1.f), py = g.R * (2.f * u1 - 1.f);
           if (px * px + py * py < g.R2) {
             x = px; y = py; ok = true;
@@ -420,15 +445,19 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
       if (a.mk.reject && WALL != kPermeate) mcls = mesh_classify(a.mk, x, y, z, mpop);
     }
     if (act && a.comp0 != nullptr && a.pass == 0)
-      a.comp0[w] = MESH ? classify_mesh(x, y, z, a.mk)
-                        : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+      a.comp0[w] = MYEL ? mcomp
+                        : (MESH ? classify_mesh(x, y, z, a.mk)
+                                : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
 
     // phase accumulators: direct form phi[m] (+ Kahan), basis form Q[j][k] (+ Kahan)
     constexpr int NACC = PM ? 3 * W : W;
     float acc[NACC], kc[NACC];
 #pragma unroll
     for (int i = 0; i < NACC; ++i) acc[i] = kc[i] = 0.f;
-    float logw = 0.f;
+    // a myelinated cylinder's walkers start with the log of their compartment's spin weight
+    const float logw0 = MYEL ? (mcomp == 0 ? a.my.lw0[0] : (mcomp == 1 ? a.my.lw0[1] : a.my.lw0[2]))
+                             : 0.f;
+    float logw = logw0;
     uint32_t s = 0;   // global sub-step counter of this walker
     u32x4 rr{0, 0, 0, 0};
     int e = 0;        // next echo ordinal
@@ -467,12 +496,13 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
         float Rx = 0.f, Ry = 0.f, Rz = 0.f, dls = 0.f, occ = 0.f;
 #pragma unroll 1
         for (int sub = 0; sub < a.S; ++sub, ++s) {
-          float ua, ub, up = 0.f;
+          float ua, ub, up = 0.f, up2 = 0.f;
           if constexpr (WALL == kPermeate) {
             rr = draw(a.seed, gw, 0u, s);
             ua = u01(rr.x);
             ub = u01(rr.y);
             up = u01(rr.z);
+            if constexpr (MYEL) up2 = u01(rr.w);
           } else {
             if ((s & 1u) == 0u) {
               rr = draw(a.seed, gw, 0u, s >> 1);
@@ -505,6 +535,8 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
             dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
+          } else if constexpr (MYEL) {
+            dl = myelin_step<WALL>(x, y, z, mcomp, stx, sty, stz, up, up2, a.my, tw);
           } else if constexpr (MESH) {
             dl = mesh_step<WALL>(x, y, z, ix, iy, iz, mcls, mpop, stx, sty, stz, up, a.mk, tw,
                                  act ? n_budget : n_idle, act ? n_escape : n_idle,
@@ -518,8 +550,9 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
           }
           if (a.dlog_unit) dls += dl;
           if (a.comp_occ)
-            occ += (float)(MESH ? classify_mesh(x, y, z, a.mk)
-                                : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
+            occ += (float)(MYEL ? mcomp
+                                : (MESH ? classify_mesh(x, y, z, a.mk)
+                                        : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj)));
         }
         const float ux = x + Lx * (float)ix, uy = y + Ly * (float)iy, uz = z + Lz * (float)iz;
         if (!a.phase_sub) {
@@ -644,10 +677,11 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
           a.final_pos[3 * w + 1] = uy;
           a.final_pos[3 * w + 2] = uz;
         }
-        if (a.log_w) a.log_w[w] = logw;
+        if (a.log_w) a.log_w[w] = logw - logw0;  // the walk's own log-weight, without spin weight
         if (a.comp_end)
-          a.comp_end[w] = MESH ? classify_mesh(x, y, z, a.mk)
-                               : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj);
+          a.comp_end[w] = MYEL ? mcomp
+                               : (MESH ? classify_mesh(x, y, z, a.mk)
+                                       : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
       }
       if (a.phi_out) {
         if constexpr (PM == 0) {

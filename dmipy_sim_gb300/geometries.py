@@ -15,8 +15,9 @@ import torch
 
 from . import _lib
 
-__all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "pack_cylinders", "PackedCylinders",
-           "pack_spheres", "PackedSpheres", "lattice_cylinders"]
+__all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "MyelinatedCylinder",
+           "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres",
+           "lattice_cylinders"]
 
 
 def _rotation_to_z(v):
@@ -172,6 +173,156 @@ class Cylinder(Geometry):
         g.eps_detect = np.float32(1e-7 * self.radius)
         g.nudge = np.float32(1e-4 * self.radius)
         return g, ()
+
+
+# water per unit myelin volume, the default proton density of the myelin compartment
+# (substrate/biophysical_constants.py: myelin_water_proton_density)
+MYELIN_WATER_PROTON_DENSITY = 0.40
+
+
+class MyelinatedCylinder(Geometry):
+    """Three-compartment myelinated cylinder along ``orientation`` (geometries.py:847-1134): intra-
+    axonal (r < inner_radius), myelin sheath (inner_radius <= r < outer_radius) and extra-axonal
+    space, each with its own isotropic diffusivity, optional T2, and water proton density
+    (``water_fractions``, the signal weight of a walker by its starting compartment); the two walls
+    have independent permeabilities.  Walked by its own step rule (physics.py:420-680): one step
+    per waveform sample of the compartment's length, mirror reflection at a wall unless a Powles
+    draw lets the walker through, then a clamp onto its compartment's side.
+    """
+
+    _is_myelinated = True
+
+    def __init__(self, inner_radius, outer_radius, orientation, D_intra, D_extra, D_myelin=0.0,
+                 kappa_inner=None, kappa_outer=None, T2_intra=None, T2_myelin=None,
+                 T2_extra=None, water_fractions=None):
+        if outer_radius <= inner_radius:
+            raise ValueError("outer_radius must be > inner_radius")
+        self.inner_radius = float(inner_radius)
+        self.outer_radius = float(outer_radius)
+        self.radius = self.inner_radius
+        self.D_intra, self.D_myelin, self.D_extra = float(D_intra), float(D_myelin), float(D_extra)
+        self.kappa_inner = _opt_float(kappa_inner)
+        self.kappa_outer = _opt_float(kappa_outer)
+        self.T2_intra = _opt_float(T2_intra)
+        self.T2_myelin = _opt_float(T2_myelin)
+        self.T2_extra = _opt_float(T2_extra)
+        if water_fractions is None:
+            water_fractions = (1.0, MYELIN_WATER_PROTON_DENSITY, 1.0)
+        self.water_fractions = tuple(float(w) for w in water_fractions)
+        o = np.asarray(orientation, dtype=np.float64)
+        self.orientation = (o / np.linalg.norm(o)).astype(np.float32)
+        R = _rotation_to_z(self.orientation)
+        self._R = R.astype(np.float32)
+        self._R_inv = R.T.astype(np.float32)
+        self._is_identity_rotation = bool(np.allclose(R, np.eye(3)))
+        self._init_compartments = None
+
+    def _frame(self):
+        return None if self._is_identity_rotation else self._R.astype(np.float64)
+
+    def _wall_mode(self, with_weight_channel=False):
+        permeable = self.kappa_inner is not None or self.kappa_outer is not None
+        return _lib.WALL_PERMEATE if permeable else _lib.WALL_REFLECT
+
+    # ---- compartments -------------------------------------------------------------------------
+    def _areas(self):
+        ri, ro = self.inner_radius, self.outer_radius
+        return np.pi * ri ** 2, np.pi * (ro ** 2 - ri ** 2), np.pi * ((2 * ro) ** 2 - ro ** 2)
+
+    def seed_counts(self, n_walkers):
+        """Walkers seeded per compartment, proportional to the compartment areas with the
+        extra-axonal space taken out to 2 outer_radius (geometries.py:935-952)."""
+        a = self._areas()
+        tot = sum(a)
+        n0 = int(round(n_walkers * a[0] / tot))
+        n1 = int(round(n_walkers * a[1] / tot))
+        return n0, n1, n_walkers - n0 - n1
+
+    def classify_position(self, r):
+        """0 intra-axonal, 1 myelin, 2 extra-axonal by the squared distance from the axis
+        (geometries.py:1018-1029)."""
+        r = np.asarray(r, dtype=np.float32)
+        rc = r if self._is_identity_rotation else r @ self._R.T
+        q = np.sum(rc[..., :2] ** 2, axis=-1)
+        ri2, ro2 = np.float32(self.inner_radius) ** 2, np.float32(self.outer_radius) ** 2
+        return np.where(q < ri2, 0, np.where(q < ro2, 1, 2)).astype(np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        """Host sampler: the compartment counts of :meth:`seed_counts`, uniform in the disc and the
+        annuli (geometries.py:928-1006); sets ``_init_compartments``."""
+        rng = _host_rng(key)
+        counts = self.seed_counts(n_walkers)
+        bounds = ((0.0, self.inner_radius), (self.inner_radius, self.outer_radius),
+                  (self.outer_radius, 2.0 * self.outer_radius))
+        pos, comp = [], []
+        for c, (n, (lo, hi)) in enumerate(zip(counts, bounds)):
+            got = np.zeros((0, 2))
+            while len(got) < n:
+                xy = rng.uniform(-hi, hi, (n * 3 + 8, 2))
+                rr = np.linalg.norm(xy, axis=1)
+                got = np.concatenate([got, xy[(rr >= lo) & (rr < hi)]])
+            pos.append(got[:n])
+            comp.append(np.full(n, c, np.int32))
+        xy = np.concatenate(pos).astype(np.float32)
+        rc = np.concatenate([xy, np.zeros((n_walkers, 1), np.float32)], axis=1)
+        self._init_compartments = np.concatenate(comp)
+        return (rc @ self._R).astype(np.float32)
+
+    def spin_weight_sum(self, n_walkers, r0=None):
+        """Sum over the walkers of their compartment's water proton density: the normaliser of
+        the signal sum (core.py:426-427)."""
+        wf = np.asarray(self.water_fractions, np.float64)
+        if r0 is not None:
+            return float(np.sum(wf[self.classify_position(r0)]))
+        return float(np.dot(self.seed_counts(n_walkers), wf))
+
+    def volume(self, compartment, L=1.0):
+        a = dict(zip(("intra", "myelin", "extra"), self._areas()))
+        if compartment not in a:
+            raise ValueError(f"compartment must be 'intra', 'myelin', or 'extra'; got {compartment!r}")
+        return a[compartment] * float(L)
+
+    def surface_area(self, compartment, L=1.0):
+        ri, ro = self.inner_radius, self.outer_radius
+        a = {"intra": ri, "myelin": ri + ro, "extra": ro}
+        if compartment not in a:
+            raise ValueError(f"compartment must be 'intra', 'myelin', or 'extra'; got {compartment!r}")
+        return 2.0 * np.pi * a[compartment] * float(L)
+
+    def volume_fraction(self, compartment):
+        return self.volume(compartment) / (np.pi * (2.0 * self.outer_radius) ** 2)
+
+    # ---- device descriptor --------------------------------------------------------------------
+    def _myelin_desc(self, dt, n_total):
+        """Descriptor of a walk with time step ``dt`` over ``n_total`` walkers (global indices):
+        per-compartment step lengths sqrt(6 D dt), kappa/D of the compartment left, dt/T2, log
+        spin weights and the seeding ranges, in the reference's float32 arithmetic
+        (physics.py:451-503)."""
+        g = self._base_desc(_lib.GEOM_MYELIN, self._wall_mode(), 1.0, 0.0)
+        g.radius = self.inner_radius
+        g.myelin_r_out = self.outer_radius
+        g.eps_detect = np.float32(1e-7 * self.inner_radius)
+        g.nudge = np.float32(1e-4 * self.inner_radius)
+        dt32 = np.float32(dt)
+        D = np.array([self.D_intra, self.D_myelin, self.D_extra], np.float32)
+        g.myelin_step[:] = [float(np.sqrt(np.float32(6.0) * d * dt32)) for d in D]
+        Dl = np.maximum(D, np.float32(1e-30))
+        ki = np.float32(self.kappa_inner or 0.0)
+        ko = np.float32(self.kappa_outer or 0.0)
+        g.myelin_kin_over_D[:] = [float(ki / d) for d in Dl]
+        g.myelin_kout_over_D[:] = [float(ko / d) for d in Dl]
+        T2 = (self.T2_intra, self.T2_myelin, self.T2_extra)
+        if any(t is not None for t in T2):
+            g.myelin_t2dec[:] = [float(dt32 / np.float32(t if t is not None else 1e6)) for t in T2]
+        with np.errstate(divide="ignore"):
+            g.myelin_logw0[:] = [float(np.log(np.float32(w))) for w in self.water_fractions]
+        n0, n1, _ = self.seed_counts(n_total)
+        g.myelin_seed_n[:] = [n0, n0 + n1]
+        return g
+
+    def _has_weight(self):
+        return (any(t is not None for t in (self.T2_intra, self.T2_myelin, self.T2_extra))
+                or any(w != 1.0 for w in self.water_fractions))
 
 
 # ------------------------------------------------------------------------------------------------

@@ -60,7 +60,8 @@ enum dmsim_geom_kind {
   DMSIM_GEOM_SPHERE = 2,           /* geometries.py:143-424, centred at the origin             */
   DMSIM_GEOM_PACKED_CYLINDERS = 3, /* geometries.py:1604-2242, periodic square cell, axis z    */
   DMSIM_GEOM_PACKED_SPHERES = 4,   /* geometries.py:2343-2786, periodic cubic cell             */
-  DMSIM_GEOM_MESH = 5              /* mesh.py:257-907                                          */
+  DMSIM_GEOM_MESH = 5,             /* mesh.py:257-907                                          */
+  DMSIM_GEOM_MYELIN = 6            /* geometries.py:847-1134 + physics.py:420-680, axis frame z */
 };
 
 enum dmsim_wall_mode {
@@ -132,6 +133,22 @@ typedef struct dmsim_geometry {
                                       each triangle; a candidate whose sphere misses the step's
                                       segment is skipped before the Moller-Trumbore test.  The
                                       radius must cover the float32 vertices (it only prunes). */
+
+  /* myelinated cylinder (DMSIM_GEOM_MYELIN): compartments 0 intra-axonal (r < radius), 1 myelin
+     (radius <= r < myelin_r_out), 2 extra-axonal, r the distance from the frame z axis.  Each
+     walker carries its compartment; a step is the unit direction times its compartment's
+     step length, mirrored at a boundary it crosses unless a Powles draw lets it through (wall
+     mode PERMEATE; REFLECT when neither boundary is permeable).  rho_over_D must be 1: the
+     kernel adds -myelin_t2dec[c] (times the coherence flag) to the log-weight each step. */
+  float myelin_r_out;
+  float myelin_step[3];        /* sqrt(6 D_c dt) per compartment (m)                           */
+  float myelin_kin_over_D[3];  /* kappa_inner / max(D_c, 1e-30), c = the compartment left        */
+  float myelin_kout_over_D[3]; /* kappa_outer / max(D_c, 1e-30)                                  */
+  float myelin_t2dec[3];       /* dt / T2_c (0 without per-compartment T2)                       */
+  float myelin_logw0[3];       /* log of each compartment's water proton density (spin weight)   */
+  int64_t myelin_seed_n[2];    /* seeding without r0: global walkers [0, n0) intra, [n0, n1)
+                                  myelin, [n1, ...) extra, uniform in the disc / annuli up to
+                                  2 myelin_r_out (geometries.py:928-1006)                        */
 } dmsim_geometry;
 
 /* ---- walk parameters -------------------------------------------------------------------------- */

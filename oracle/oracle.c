@@ -45,6 +45,7 @@ static double round_half(float f) {
 #define SQRT sqrtf
 #define FLOOR floorf
 #define FMOD fmodf
+#define FABS fabsf
 #define SIN sinf
 #define COS cosf
 #define MAX(a, b) fmaxf((a), (b))
@@ -55,6 +56,7 @@ static double round_half(float f) {
 #undef SQRT
 #undef FLOOR
 #undef FMOD
+#undef FABS
 #undef SIN
 #undef COS
 #undef MAX
@@ -65,6 +67,7 @@ static double round_half(float f) {
 #define SQRT sqrt
 #define FLOOR floor
 #define FMOD fmod
+#define FABS fabs
 #define SIN sin
 #define COS cos
 #define MAX(a, b) fmax((a), (b))

@@ -13,6 +13,7 @@
  *   PackedCylinders reflect / rwlw / permeate             geometries.py:1746-1884, 1886-2016, 2018-2183
  *   PackedSpheres reflect / rwlw / permeate               geometries.py:2445-2537, 2539-2631, 2633-2756
  *   Mesh reflect / reflect_with_log_weight / permeate     mesh.py:637-671, 673-705, 707-743
+ *   MyelinatedCylinder step (own walk rule)               physics.py:506-677
  *     (wrap 203-206, 27-cell gather 208-215, Moller-Trumbore 561-569, bounce 599-635,
  *      nearest-centroid classification 227-254, leak guard 578-597)
  *   ensemble Re<w e^{i phi}>                              core.py:426-429; replay FP64 phase
@@ -31,7 +32,7 @@ extern "C" {
 #endif
 
 enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4,
-       OR_MESH = 5 };
+       OR_MESH = 5, OR_MYELIN = 6 };
 enum { OR_REFLECT = 0, OR_RELAX = 1, OR_PERMEATE = 2 };
 
 /* A triangle mesh as the reference's Mesh holds it (mesh.py:311-546): every triangle including the
@@ -52,6 +53,15 @@ typedef struct {
   const int32_t* cell_tri;
 } or_mesh;
 
+/* A myelinated cylinder (geometries.py:847-1134) as make_myelin_step_fn sees it (physics.py:451-
+   503): inner / outer radius, nudge 1e-4 R_in, and per compartment (intra, myelin, extra) the step
+   length sqrt(6 D dt), kappa_inner / max(D, 1e-30), kappa_outer / max(D, 1e-30), dt / T2 (0
+   without T2) and the log of the water proton density (float32 values stored as double). */
+typedef struct {
+  double r_in, r_out, nudge;
+  double step[3], kin[3], kout[3], t2dec[3], logw0[3];
+} or_myelin;
+
 typedef struct {
   int32_t kind;
   int32_t n_objects;
@@ -63,6 +73,7 @@ typedef struct {
   int32_t rot_identity;
   int32_t pad;
   const or_mesh* mesh;   /* OR_MESH only */
+  const or_myelin* myelin; /* OR_MYELIN only */
 } or_geom;
 
 typedef struct {
@@ -81,6 +92,16 @@ int or_plugin_f32(const or_geom* g, int mode, const double* r, const double* ste
                   double rho_over_D, double kappa_over_D, double u, double* r_out, double* dlog);
 int or_plugin_f64(const or_geom* g, int mode, const double* r, const double* step,
                   double rho_over_D, double kappa_over_D, double u, double* r_out, double* dlog);
+
+/* One step of the myelinated cylinder's own walk rule (physics.py:528-677) in its frame: start r in
+   compartment comp, unit direction `unit`, Powles uniforms u1 (inner) / u2 (outer) when permeate.
+   Writes the end point, the new compartment and dt/T2 of the new compartment. */
+int or_myelin_plugin_f32(const or_geom* g, const double* r, const double* unit, int comp,
+                         int permeate, double u1, double u2, double* r_out, int* comp_out,
+                         double* t2dec);
+int or_myelin_plugin_f64(const or_geom* g, const double* r, const double* unit, int comp,
+                         int permeate, double u1, double u2, double* r_out, int* comp_out,
+                         double* t2dec);
 
 /* A full walk in the geometry frame.  G is (n_t, n_meas, 3) float32, chi (n_t) or NULL, r0
    (n_walkers, 3) or NULL (seeded on the Philox seeding stream; a mesh needs r0).  sums (n_echo, n_meas, 3) is

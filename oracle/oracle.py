@@ -14,7 +14,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 
-FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH = range(6)
+FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH, MYELIN = range(7)
 REFLECT, RELAX, PERMEATE = range(3)
 
 
@@ -30,11 +30,17 @@ class OrMesh(C.Structure):
                 ("cell_tri", C.c_void_p)]
 
 
+class OrMyelin(C.Structure):
+    _fields_ = [("r_in", C.c_double), ("r_out", C.c_double), ("nudge", C.c_double),
+                ("step", C.c_double * 3), ("kin", C.c_double * 3), ("kout", C.c_double * 3),
+                ("t2dec", C.c_double * 3), ("logw0", C.c_double * 3)]
+
+
 class OrGeom(C.Structure):
     _fields_ = [("kind", C.c_int32), ("n_objects", C.c_int32), ("radius", C.c_double),
                 ("L", C.c_double), ("rmin", C.c_double), ("objects", C.c_void_p),
                 ("rot", C.c_double * 9), ("rot_identity", C.c_int32), ("pad", C.c_int32),
-                ("mesh", C.c_void_p)]
+                ("mesh", C.c_void_p), ("myelin", C.c_void_p)]
 
 
 class OrWalk(C.Structure):
@@ -74,6 +80,12 @@ def load():
                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         lib.or_philox.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
                                   C.POINTER(C.c_uint32)]
+        for suf in ("_f32", "_f64"):
+            f = getattr(lib, "or_myelin_plugin" + suf)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(OrGeom), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                          C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double),
+                          C.POINTER(C.c_int), C.POINTER(C.c_double)]
         _lib = lib
     return _lib
 
@@ -207,7 +219,36 @@ def mesh_sides(rho_intra=None, rho_extra=None, kappa_out=None, kappa_in=None):
     return rho, kap, kn > 0
 
 
-def geom_from(geometry):
+def myelin_geom(inner_radius, outer_radius, D, dt, kappa_inner=None, kappa_outer=None,
+                T2=(None, None, None), water_fractions=(1.0, 0.4, 1.0)):
+    """Oracle myelinated cylinder for a walk with time step ``dt``: the float32 constants of
+    make_myelin_step_fn (physics.py:451-503) -- step sqrt(6 D_c dt), kappa / max(D_c, 1e-30) of
+    the compartment left, dt / T2_c (T2 1e6 s where unset, 0 without any), nudge 1e-4 R_in -- and
+    the log water proton densities.  ``D`` = (D_intra, D_myelin, D_extra)."""
+    f = np.float32
+    m = OrMyelin()
+    m.r_in, m.r_out = float(f(inner_radius)), float(f(outer_radius))
+    m.nudge = float(f(1e-4 * inner_radius))
+    dt32 = f(dt)
+    Df = [f(x) for x in D]
+    m.step[:] = [float(np.sqrt(f(6.0) * d * dt32)) for d in Df]
+    ki, ko = f(kappa_inner or 0.0), f(kappa_outer or 0.0)
+    m.kin[:] = [float(ki / max(d, f(1e-30))) for d in Df]
+    m.kout[:] = [float(ko / max(d, f(1e-30))) for d in Df]
+    if any(t is not None for t in T2):
+        m.t2dec[:] = [float(dt32 / f(t if t is not None else 1e6)) for t in T2]
+    m.logw0[:] = [float(np.log(w)) if w > 0 else -np.inf for w in water_fractions]
+    g = OrGeom()
+    g.kind = MYELIN
+    g.radius = float(inner_radius)
+    g.rot[:] = np.eye(3).ravel().tolist()
+    g.rot_identity = 1
+    g.myelin = C.addressof(m)
+    g._keep = (m,)
+    return g
+
+
+def geom_from(geometry, dt=None):
     """Oracle geometry of a dmipy_sim_gb300 geometry object (walk frame)."""
     name = type(geometry).__name__
     if name == "FreeDiffusion":
@@ -225,6 +266,14 @@ def geom_from(geometry):
         kind = PACKED_CYLINDERS if name == "PackedCylinders" else PACKED_SPHERES
         return geom(kind, L=np.float32(geometry._L_float), objects=objs,
                     rot=getattr(geometry, "_R", None))
+    if name == "MyelinatedCylinder":
+        if dt is None:
+            raise ValueError("the oracle's myelinated cylinder needs the walk's time step")
+        return myelin_geom(geometry.inner_radius, geometry.outer_radius,
+                           (geometry.D_intra, geometry.D_myelin, geometry.D_extra), dt,
+                           geometry.kappa_inner, geometry.kappa_outer,
+                           (geometry.T2_intra, geometry.T2_myelin, geometry.T2_extra),
+                           geometry.water_fractions)
     if name == "Mesh":
         return mesh_geom(geometry.vertices, geometry.faces, periodic=geometry.periodic,
                          voxel_min=geometry.vmin, voxel_max=geometry.vmax,
@@ -252,11 +301,29 @@ def plugin(g, mode, r, step, rho_over_D=0.0, kappa_over_D=0.0, u=0.0, fp64=False
     return np.array(ro[:]), dl.value
 
 
+def myelin_plugin(g, r, unit, comp, u1=0.0, u2=0.0, permeate=False, fp64=False):
+    """One step of the myelinated cylinder's walk rule; returns (r_new (3,), comp_new, dt/T2)."""
+    lib = load()
+    f = lib.or_myelin_plugin_f64 if fp64 else lib.or_myelin_plugin_f32
+    ri = (C.c_double * 3)(*map(float, r))
+    ui = (C.c_double * 3)(*map(float, unit))
+    ro = (C.c_double * 3)()
+    co = C.c_int()
+    t2 = C.c_double()
+    if f(C.byref(g), ri, ui, int(comp), int(bool(permeate)), float(u1), float(u2), ro,
+         C.byref(co), C.byref(t2)) != 0:
+        raise RuntimeError("oracle myelin step failed")
+    return np.array(ro[:]), co.value, t2.value
+
+
 def walk(g, *, n_walkers, G, dt, sub_steps, phase_per_substep, seed, wall=REFLECT, chi=None,
          T2=None, T1=None, rho_over_D=0.0, kappa_over_D=0.0, D=2e-9, echo_idx=None, r0=None,
-         walker_offset=0, fp64=False, f16_positions=False, want_walkers=False, n_threads=0):
+         walker_offset=0, fp64=False, f16_positions=False, want_walkers=False, n_threads=0,
+         has_weight=None, step_length=None):
     """Restated reference walk.  ``G`` is (M, n_t, 3) in the walk frame.  Returns a dict with
-    ``sums`` (n_echo, M, 3) and, with ``want_walkers``, ``pos``, ``log_w``, ``phi``."""
+    ``sums`` (n_echo, M, 3) and, with ``want_walkers``, ``pos``, ``log_w``, ``phi``.
+    ``has_weight`` / ``step_length`` override the defaults (the myelinated cylinder walks unit
+    directions scaled per compartment and weights by its own T2 and spin weights)."""
     from dmipy_sim_gb300.constants import GAMMA
     lib = load()
     G = np.asarray(G, dtype=np.float32)
@@ -272,13 +339,14 @@ def walk(g, *, n_walkers, G, dt, sub_steps, phase_per_substep, seed, wall=REFLEC
     p.n_t, p.n_meas, p.sub_steps = n_t, M, S
     p.phase_per_substep = int(bool(phase_per_substep))
     p.has_weight = int(T2 is not None or T1 is not None or rho_over_D != 0.0
-                       or wall == PERMEATE)
+                       or wall == PERMEATE) if has_weight is None else int(bool(has_weight))
     p.wall = int(wall)
     p.n_echo = len(echo)
     p.f16_positions = int(bool(f16_positions))
     echo_c = (C.c_int32 * len(echo))(*echo.tolist())
     p.echo_idx = echo_c
-    step_l = np.float32(np.sqrt(6.0 * D * dt_sub))
+    step_l = np.float32(np.sqrt(6.0 * D * dt_sub)) if step_length is None else \
+        np.float32(step_length)
     p.step_length = float(step_l)
     p.gamma_dt = float(np.float32(GAMMA * (dt_sub if phase_per_substep else float(dt))))
     p.t2_decay = float(np.float32(dt_sub / T2)) if T2 is not None else 0.0
@@ -300,7 +368,15 @@ def walk(g, *, n_walkers, G, dt, sub_steps, phase_per_substep, seed, wall=REFLEC
            None if r0_a is None else r0_a.ctypes.data, sums.ctypes.data, *ptrs, int(n_threads))
     if rc != 0:
         raise RuntimeError("oracle walk failed")
-    out["signal"] = sums[..., 0] / max(n_walkers, 1)
+    norm = max(n_walkers, 1)
+    if g.kind == MYELIN:
+        # the ensemble is normalised by the sum of the spin weights (core.py:426-427)
+        m = OrMyelin.from_address(g.myelin)
+        q = np.sum(np.asarray(r0, np.float32)[:, :2] ** 2, axis=1)
+        comp = np.where(q < np.float32(m.r_in) ** 2, 0,
+                        np.where(q < np.float32(m.r_out) ** 2, 1, 2))
+        norm = float(np.sum(np.exp(np.asarray(m.logw0[:]))[comp]))
+    out["signal"] = sums[..., 0] / norm
     return out
 
 

@@ -115,8 +115,32 @@ def jit(f=None, **kw):
     return f
 
 
+class _AtArray(np.ndarray):
+    """An ndarray with JAX's functional update ``x.at[idx].set(v)`` (returns a modified copy)."""
+
+    @property
+    def at(self):
+        base = self
+
+        class _Index:
+            def __getitem__(self, idx):
+                class _Set:
+                    def set(self, v):
+                        out = np.array(base, copy=True).view(_AtArray)
+                        out[idx] = v
+                        return out
+                return _Set()
+        return _Index()
+
+
+def _array(*a, **k):
+    return np.array(*a, **k).view(_AtArray)
+
+
 class _NumpyModule(types.ModuleType):
     def __getattr__(self, name):
+        if name == "array":
+            return _array
         return getattr(np, name)
 
 

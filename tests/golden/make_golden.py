@@ -330,6 +330,72 @@ def _waveform_cases_tensor(m, out):
         np.asarray(x) for x in w.btensor_invariants(B))
 
 
+def _myelin_cases(m, rng, out):
+    """make_myelin_step_fn (physics.py:420-680) of the reference, one step per case, with the
+    direction and the two Powles uniforms the step drew recorded: a sheath thin enough that most
+    cases cross a wall, every compartment, permeable and impermeable walls."""
+    geo, phys = m["geometries"], m["physics"]
+    rnd = sys.modules["jax.random"]
+    drawn = {}
+    real_normal, real_uniform = rnd.normal, rnd.uniform
+
+    def normal(key, shape=(), dtype=np.float32):
+        v = real_normal(key, shape, dtype)
+        drawn["noise"] = np.asarray(v, np.float32)
+        return v
+
+    def uniform(key, shape=(), dtype=np.float32, minval=0.0, maxval=1.0):
+        v = real_uniform(key, shape, dtype, minval, maxval)
+        drawn.setdefault("u", []).append(np.float32(v))
+        return v
+    rnd.normal, rnd.uniform = normal, uniform
+    try:
+        n = 256
+        dt = 1e-4
+        # permeabilities high enough that about half the crossings transmit
+        for tag, kw in (("perm", dict(kappa_inner=2e-3, kappa_outer=1e-3)), ("refl", {})):
+            g = geo.MyelinatedCylinder(2e-6, 2.6e-6, (0, 0, 1), D_intra=2e-9, D_extra=2.5e-9,
+                                       D_myelin=0.8e-9, T2_intra=0.08, T2_myelin=0.012,
+                                       T2_extra=0.07, water_fractions=(1.0, 0.4, 1.0), **kw)
+            step = phys.make_myelin_step_fn(g, dt, T1=0.9)
+            ang = rng.uniform(0, 2 * np.pi, n)
+            rad = rng.uniform(0.0, 3.4e-6, n)
+            r = np.stack([rad * np.cos(ang), rad * np.sin(ang),
+                          rng.uniform(-1e-6, 1e-6, n)], 1).astype(np.float32)
+            comp = np.where(rad < 2e-6, 0, np.where(rad < 2.6e-6, 1, 2)).astype(np.int32)
+            chi = (rng.uniform(size=n) < 0.7).astype(np.float32)
+            ro, co, dl, units, us = [], [], [], [], []
+            for i in range(n):
+                drawn.clear()
+                key = rnd.PRNGKey(1000 + i)
+                carry = (r[i], np.zeros(1, np.float32), np.float32(0.0), np.int32(comp[i]), key)
+                new, _ = step(carry, (np.zeros((1, 3), np.float32), np.float32(chi[i])))
+                nz = drawn["noise"]
+                units.append(nz / np.linalg.norm(nz))
+                us.append(drawn["u"][:2])
+                ro.append(np.asarray(new[0], np.float64))
+                co.append(int(new[3]))
+                dl.append(float(new[2]))
+            key = f"my_{tag}"
+            out[key + "_r"], out[key + "_comp"], out[key + "_chi"] = r, comp, chi
+            out[key + "_unit"] = np.asarray(units, np.float32)
+            out[key + "_u"] = np.asarray(us, np.float32)
+            out[key + "_out"], out[key + "_comp_out"] = np.asarray(ro), np.asarray(co, np.int32)
+            out[key + "_dlog"] = np.asarray(dl)
+    finally:
+        rnd.normal, rnd.uniform = real_normal, real_uniform
+
+
+def make_myelin_kat(root):
+    """Add the myelinated-cylinder step known answers to kat.npz."""
+    m = _ref(root)
+    path = HERE / "kat.npz"
+    out = dict(np.load(path))
+    _myelin_cases(m, np.random.default_rng(17), out)
+    np.savez_compressed(path, **out)
+    print(f"kat.npz: {len(out)} arrays")
+
+
 def make_replay_kat(root):
     """Known answers of the reference's compression.py / replay.py codecs and mode-space replay
     and of trajectories.replay on a compressed master, on a seeded synthetic walk
@@ -497,6 +563,11 @@ def _mc_configs():
                              r0="mesh"),
         "mesh_perm": dict(geom=("mesh", 1e-5), wf=("pgse_mesh",), n=640, api="simulate",
                           r0="mesh"),
+        # the myelinated cylinder's own step rule, one step per sample, diffusivity None
+        "myelin_refl": dict(geom=("myelin", None, None, 0.0), wf=("pgse_my",), n=8000,
+                            api="simulate", D=None),
+        "myelin_perm": dict(geom=("myelin", 5e-5, 3e-5, 0.5e-9), wf=("pgse_my",), n=8000,
+                            api="simulate", D=None),
     }
 
 
@@ -538,6 +609,9 @@ def build_waveform(wfm, spec):
         return wfm.cpmg(8, 12e-3, 0.0, [[1, 0, 0]], n_t_per_echo=60)
     if name == "cpmg_g":
         return wfm.cpmg(6, 10e-3, 0.02, [[1, 0, 0], [0, 0, 1]], n_t_per_echo=50)
+    if name == "pgse_my":
+        return wfm.set_b(wfm.pgse(0.006, 0.02, 0.1, [[1, 0, 0], [0, 0, 1], [0.6, 0.8, 0]], 120),
+                         [5e8, 1e9, 2e9])
     if name == "pgse_mesh":
         return wfm.set_b(wfm.pgse(0.003, 0.008, 0.2, [[1, 0, 0], [0, 0, 1], [0.6, 0.8, 0]], 60),
                          [5e8, 1e9, 2e9])
@@ -569,6 +643,12 @@ def build_geometry(geo, spec):
     if kind == "mesh":
         V, F = mesh_surface()
         return geo.Mesh(V, F, permeability=spec[1])
+    if kind == "myelin":
+        # an axon of 2 um in a 0.8 um sheath, T2 per compartment, myelin water density 0.4
+        return geo.MyelinatedCylinder(2e-6, 2.8e-6, (0.2, 0.3, 1.0), D_intra=2e-9, D_extra=2.2e-9,
+                                      D_myelin=spec[3], kappa_inner=spec[1], kappa_outer=spec[2],
+                                      T2_intra=0.07, T2_myelin=0.015, T2_extra=0.06,
+                                      water_fractions=(1.0, 0.4, 1.0))
     raise KeyError(kind)
 
 
@@ -589,8 +669,8 @@ def _mc_worker(args):
             s = m["core"].simulate_cpmg(n, D, wf, g, T2=cfg.get("T2"), seed=seed,
                                         require_gpu=False)
         else:
-            s = m["core"].simulate(n, D, wf, g, seed=seed, T2=cfg.get("T2"), require_gpu=False,
-                                   engine=cfg.get("engine", "auto"), r0=r0)
+            s = m["core"].simulate(n, cfg.get("D", D), wf, g, seed=seed, T2=cfg.get("T2"),
+                                   require_gpu=False, engine=cfg.get("engine", "auto"), r0=r0)
     return name, n, np.asarray(s, np.float64)
 
 
@@ -634,6 +714,8 @@ if __name__ == "__main__":
     ap.add_argument("--kat", action="store_true")
     ap.add_argument("--kat-extra", action="store_true",
                     help="add the tensor-encoding waveform vectors to an existing kat.npz")
+    ap.add_argument("--myelin-kat", action="store_true",
+                    help="add the myelinated-cylinder step vectors to an existing kat.npz")
     ap.add_argument("--replay-kat", action="store_true",
                     help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
@@ -646,5 +728,7 @@ if __name__ == "__main__":
         make_kat_extra(a.ref)
     if a.replay_kat:
         make_replay_kat(a.ref)
+    if a.myelin_kat:
+        make_myelin_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)

@@ -1,0 +1,128 @@
+"""Myelinated cylinder on the GPU: walks against the CPU oracle's restatement of
+make_myelin_step_fn (walker by walker on short walks, and as ensembles, on the same Philox stream),
+the seeding by compartment, impermeable walls and a stuck myelin pool, the b = 0 signal as the
+T2-weighted spin density, and the simulate() surface (normalisation, outputs, routing)."""
+import numpy as np
+import pytest
+
+import dmipy_sim_gb300 as d
+from dmipy_sim_gb300 import core
+from parity_cases import oracle_walk
+
+pytestmark = pytest.mark.gpu
+
+
+def _geom(perm, D_myelin=0.6e-9, orientation=(0, 0, 1)):
+    kw = dict(kappa_inner=5e-5, kappa_outer=3e-5) if perm else {}
+    return d.MyelinatedCylinder(2e-6, 2.8e-6, orientation, D_intra=2e-9, D_extra=2.2e-9,
+                                D_myelin=D_myelin, T2_intra=0.07, T2_myelin=0.015,
+                                T2_extra=0.06, water_fractions=(1.0, 0.4, 1.0), **kw)
+
+
+def _waveform(n_t=120):
+    return d.set_b(d.pgse(0.006, 0.02, 0.1, [[1, 0, 0], [0, 0, 1], [0.6, 0.8, 0]], n_t),
+                   [5e8, 1e9, 2e9])
+
+
+def _walks(g, n, n_t, seed, want, T1=None):
+    wf = _waveform()
+    G, chi = core._waveform_arrays(wf, g)
+    G = G[:, :n_t]
+    r0 = g.init_positions(n, 11)
+    gpu = core.run_walk(g, n_walkers=n, diffusivity=None, G=G, dt=wf.dt, sub_steps=1,
+                        phase_per_substep=True, seed=seed, T1=T1, r0=r0, want_positions=want,
+                        want_walker_signals=want, want_compartments=want)
+    ora = oracle_walk(g, G, wf.dt, 1, True, n, seed=seed, r0=r0, want_walkers=want, T1=T1)
+    return r0, gpu, ora
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_myelin_short_walk_matches_oracle_walker_by_walker(cuda, perm):
+    g = _geom(perm)
+    r0, gpu, ora = _walks(g, 4096, 40, 7, True, T1=0.9)
+    pg = gpu.extras["pos"].cpu().numpy()
+    same = np.max(np.abs(pg - ora["pos"]), axis=1) < 1e-4 * 2e-6
+    assert same.mean() >= 0.97, f"only {same.mean():.3f} of walkers follow the oracle's walk"
+    comp_o = g.classify_position(ora["pos"])
+    np.testing.assert_array_equal(gpu.extras["comp_end"].cpu().numpy()[same], comp_o[same])
+    np.testing.assert_allclose(gpu.extras["phi"].cpu().numpy()[same], ora["phi"][same],
+                               atol=1e-3, rtol=1e-4)
+    np.testing.assert_allclose(gpu.extras["log_w"].cpu().numpy()[same], ora["log_w"][same],
+                               rtol=1e-5, atol=1e-6)
+    if perm:
+        assert gpu.status["transmit"] > 0
+    else:
+        np.testing.assert_array_equal(gpu.extras["comp_end"].cpu().numpy(),
+                                      gpu.extras["comp0"].cpu().numpy())
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_myelin_ensemble_matches_oracle(cuda, perm):
+    g = _geom(perm)
+    n = 16384
+    r0, gpu, ora = _walks(g, n, 120, 21, False)
+    norm = n / g.spin_weight_sum(n, r0)
+    sig = gpu.signal[0] * norm
+    se = np.sqrt(2.0) * gpu.stderr[0] * norm
+    z = (sig - ora["signal"][0]) / np.maximum(se, 1e-9)
+    assert np.max(np.abs(z)) < 4.0, z
+
+
+def test_myelin_seeding_walls_and_stuck_pool(cuda):
+    """Seeding by index range gives the volume-proportional counts, each walker in its disc or
+    annulus; impermeable walls keep every walker in its compartment; a myelin pool with D = 0 does
+    not move."""
+    g = _geom(False, D_myelin=0.0)
+    wf = _waveform()
+    n = 20_000
+    G, _ = core._waveform_arrays(wf, g)
+    res = core.run_walk(g, n_walkers=n, diffusivity=None, G=G, dt=wf.dt, sub_steps=1,
+                        phase_per_substep=True, seed=3, want_positions=True,
+                        want_compartments=True)
+    c0 = res.extras["comp0"].cpu().numpy()
+    np.testing.assert_array_equal(np.bincount(c0, minlength=3), g.seed_counts(n))
+    np.testing.assert_array_equal(res.extras["comp_end"].cpu().numpy(), c0)
+    pos = res.extras["pos"].cpu().numpy()
+    np.testing.assert_array_equal(g.classify_position(pos), c0)
+    assert res.status["init_fail"] == 0 and res.status["nonfinite"] == 0
+    r0 = g.init_positions(4096, 5)
+    res = core.run_walk(g, n_walkers=4096, diffusivity=None, G=G, dt=wf.dt, sub_steps=1,
+                        phase_per_substep=True, seed=3, r0=r0, want_positions=True)
+    pos = res.extras["pos"].cpu().numpy()
+    stuck = g.classify_position(r0) == 1
+    np.testing.assert_array_equal(pos[stuck], r0[stuck])
+    assert np.all(np.linalg.norm(pos[~stuck] - r0[~stuck], axis=1) > 0)
+
+
+def test_myelin_b0_signal_is_the_T2_weighted_spin_density(cuda):
+    g = _geom(False, orientation=(0.3, 0.1, 1.0))
+    wf = d.set_b(d.pgse(0.006, 0.02, 0.1, [[1, 0, 0]], 120), 0.0)
+    n = 30_000
+    s = d.simulate(n, None, wf, g, seed=4)
+    n_t = wf.G.shape[1]
+    cnt = np.asarray(g.seed_counts(n), float)
+    wfr = np.asarray(g.water_fractions)
+    T2 = np.array([g.T2_intra, g.T2_myelin, g.T2_extra])
+    expect = np.sum(cnt * wfr * np.exp(-n_t * wf.dt / T2)) / np.sum(cnt * wfr)
+    np.testing.assert_allclose(s, expect, rtol=2e-5)
+
+
+def test_myelin_simulate_surface(cuda):
+    g = _geom(True, orientation=(0.2, 0.3, 1.0))
+    wf = _waveform()
+    n = 8192
+    s, c0, c1, lw, phi = d.simulate(n, None, wf, g, seed=9, return_compartments="final",
+                                    return_walker_signals=True)
+    assert s.shape == (3,) and c0.shape == c1.shape == (n,) and phi.shape == (n, 3)
+    sw = np.asarray(g.water_fractions)[c0]
+    np.testing.assert_allclose(s, (sw[:, None] * np.exp(lw)[:, None] * np.cos(phi)).sum(0) /
+                               sw.sum(), rtol=1e-4, atol=1e-6)
+    assert np.any(c0 != c1)                                 # permeable walls exchange
+    s2 = d.simulate(n, None, wf, g, seed=9, walker_batch_size=3000)
+    assert s2.shape == (3,) and np.all(np.abs(s2 - s) < 0.06)
+    with pytest.raises(NotImplementedError):
+        d.simulate(n, None, wf, g, engine="replay")
+    with pytest.raises(NotImplementedError):
+        d.simulate_trajectories(n, None, g, 0.02, 1e-4)
+    with pytest.raises(NotImplementedError):
+        d.simulate_cpmg(n, None, d.cpmg(4, 5e-3, 0.02, [[1, 0, 0]]), g)

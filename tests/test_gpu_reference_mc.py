@@ -16,6 +16,13 @@ N_GPU = 200_000
 def _gpu(cfg, n, seed):
     wf = build_waveform(d, cfg["wf"])
     g = build_geometry(d, tuple(cfg["geom"]))
+    if getattr(g, "_is_myelinated", False):
+        # through simulate(): the myelin step rule and the spin-weight normalisation
+        s, c0, _, lw, phi = d.simulate(n, None, wf, g, seed=seed, return_compartments="final",
+                                       return_walker_signals=True)
+        sw = np.asarray(g.water_fractions)[c0]
+        x = sw[:, None] * np.exp(lw)[:, None] * np.cos(phi) / sw.mean()
+        return s, x.std(axis=0)
     G, chi = core._waveform_arrays(wf, g)
     if cfg["api"] == "cpmg":
         S, ps, echo = core.fused_sub_steps(g, D, wf.dt), True, wf.echo_indices

@@ -135,6 +135,38 @@ def test_oracle_mesh_walk_stays_inside_a_closed_surface():
     assert np.max(np.abs(a["pos"] - r0)) > 1e-7           # the walkers moved
 
 
+@pytest.mark.parametrize("tag", ["perm", "refl"])
+@pytest.mark.parametrize("fp64", [False, True])
+def test_oracle_myelin_step_matches_reference(kat, tag, fp64):
+    """make_myelin_step_fn (physics.py:420-680), one step per case with the direction and Powles
+    uniforms the reference drew: FP32 restatement bit for bit (end point, compartment, weight),
+    FP64 twin to FP32 rounding."""
+    kw = (2e-3, 1e-3) if tag == "perm" else (None, None)
+    g = O.myelin_geom(2e-6, 2.6e-6, (2e-9, 0.8e-9, 2.5e-9), 1e-4, kw[0], kw[1],
+                      (0.08, 0.012, 0.07), (1.0, 0.4, 1.0))
+    k = f"my_{tag}"
+    r, comp, unit, u = kat[k + "_r"], kat[k + "_comp"], kat[k + "_unit"], kat[k + "_u"]
+    ref, cref, dref, chi = kat[k + "_out"], kat[k + "_comp_out"], kat[k + "_dlog"], kat[k + "_chi"]
+    out = np.zeros_like(ref)
+    co = np.zeros(len(r), int)
+    dl = np.zeros(len(r))
+    t1 = np.float32(1e-4) * np.float32(1 / 0.9)
+    for i in range(len(r)):
+        out[i], co[i], t2 = O.myelin_plugin(g, r[i], unit[i], comp[i], u[i][0], u[i][1],
+                                            permeate=tag == "perm", fp64=fp64)
+        dl[i] = np.float32(-(np.float32(t2) * chi[i])) - t1 * (1 - chi[i])
+    if tag == "perm":
+        assert np.sum(comp != cref) > 20        # the cases exercise transmission
+    if fp64:
+        assert np.mean(co == cref) > 0.99
+        ok = co == cref
+        assert np.max(np.abs(out[ok] - ref[ok])) < 1e-12
+    else:
+        np.testing.assert_array_equal(out, ref)
+        np.testing.assert_array_equal(co, cref)
+        np.testing.assert_array_equal(dl, dref)
+
+
 def _philox_py(seed, walker, stream, j):
     """Philox4x32-10 round function written out from the published description (Salmon et al.,
     SC'11), independent of the C and CUDA implementations."""
