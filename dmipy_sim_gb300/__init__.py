@@ -8,7 +8,8 @@ from .constants import GAMMA, DEFAULT_SLEW_RATE
 from .waveforms import (Waveform, pgse, pgste, ogse, cpmg, calc_b, calc_btensor, set_b,
                         rotate_waveform, tile_waveform, trapezoidal_ogse, b_trapezoidal_ogse,
                         btensor_invariants, ste, pte)
-from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, MyelinatedCylinder, pack_cylinders,
+from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, MyelinatedCylinder,
+                         PackedMyelinatedCylinders, pack_myelinated_cylinders, pack_cylinders,
                          PackedCylinders, pack_spheres, PackedSpheres, lattice_cylinders)
 from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
@@ -27,7 +28,8 @@ __all__ = [
     "GAMMA", "DEFAULT_SLEW_RATE", "Waveform", "pgse", "pgste", "ogse", "cpmg", "calc_b",
     "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "trapezoidal_ogse",
     "b_trapezoidal_ogse", "btensor_invariants", "ste", "pte", "Geometry", "FreeDiffusion",
-    "Cylinder", "Sphere", "MyelinatedCylinder", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
+    "Cylinder", "Sphere", "MyelinatedCylinder", "PackedMyelinatedCylinders",
+    "pack_myelinated_cylinders", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
     "simulate", "simulate_cpmg", "simulate_trajectories", "trajectories", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
     "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",

@@ -120,6 +120,8 @@ def fused_sub_steps(geometry, diffusivity, dt):
     myelinated cylinder takes one step per sample (physics.py:420-680)."""
     if getattr(geometry, '_is_myelinated', False):
         return 1
+    if getattr(geometry, '_is_packed_myelinated', False):
+        return geometry.sub_steps(dt)
     if getattr(geometry, 'permeability', None) is not None:
         return permeable_sub_steps(geometry, diffusivity, dt)
     if getattr(geometry, 'surface_relaxivity_t2', None) is not None:
@@ -255,7 +257,16 @@ class PreparedWalk:
         dt_sub = dt / S
         gamma_dt = np.float32(GAMMA * (dt_sub if phase_per_substep else dt))
         self.myelin = bool(getattr(geometry, '_is_myelinated', False))
-        if self.myelin:
+        self.pmyelin = bool(getattr(geometry, '_is_packed_myelinated', False))
+        if self.pmyelin:
+            # unit directions scaled per compartment and axon on the device; the per-step
+            # log-weight (T2 per compartment, surface relaxivity) comes from the geometry
+            step_l = np.float32(1.0)
+            T2 = None
+            want_w = geometry._has_weight() or T1 is not None
+            self.gdesc, self._keep = geometry._pmyelin_desc(
+                dt_sub, int(total_walkers or (n_walkers + walker_offset)), dev)
+        elif self.myelin:
             # unit directions scaled per compartment on the device; T2 per compartment only (the
             # reference's myelin step ignores simulate's T2, physics.py:420-505)
             if S != 1:
@@ -453,7 +464,12 @@ def simulate(n_walkers, diffusivity=None, waveform=None, geometry=None, seed=123
     if hasattr(waveform, 'waveform'):
         waveform = waveform.waveform
     myelin = bool(getattr(geometry, '_is_myelinated', False))
-    if diffusivity is None and not myelin:
+    pmyelin = bool(getattr(geometry, '_is_packed_myelinated', False))
+    if pmyelin and r0 is not None:
+        raise NotImplementedError(
+            "simulate(r0=...) is unsupported for PackedMyelinatedCylinders; it initialises walkers "
+            "(and their compartments) from `seed`")
+    if diffusivity is None and not (myelin or pmyelin):
         raise NotImplementedError(
             "simulate() without an explicit diffusivity is only defined for geometries carrying "
             "their own D (MyelinatedCylinder)")
@@ -494,10 +510,11 @@ def simulate(n_walkers, diffusivity=None, waveform=None, geometry=None, seed=123
                    want_walker_signals=bool(return_walker_signals),
                    want_compartments=return_compartments is not False, traj=traj, traj_f16=False)
     signals = res.signal[0].astype(np.float32)
-    if myelin:
+    if myelin or pmyelin:
         # the walkers' log-weights start at log(spin weight): normalise by the weight sum
         # instead of the walker count (core.py:426-427)
-        sw = geometry.spin_weight_sum(n_walkers, r0)
+        sw = (geometry.spin_weight_sum(n_walkers, r0) if myelin
+              else geometry.spin_weight_sum(n_walkers))
         signals = (signals.astype(np.float64) * n_walkers / sw).astype(np.float32)
     if getattr(waveform, 'stimulated_echo', False):
         signals = signals * np.float32(0.5)
@@ -547,9 +564,10 @@ def simulate_cpmg(n_walkers, diffusivity, waveform, geometry, *, T2=None, seed=1
     """Multi-echo CPMG signal (n_echoes, n_meas) from one walk (core.py:861-969): the ensemble is
     reduced only at the echo samples instead of materialising the (n, n_t, n_meas) trace."""
     _check_gpu(require_gpu)
-    if getattr(geometry, '_is_myelinated', False):
-        raise NotImplementedError("MyelinatedCylinder is walked by simulate() only (the reference's "
-                                  "CPMG path has no myelin step rule)")
+    if getattr(geometry, '_is_myelinated', False) or getattr(geometry, '_is_packed_myelinated',
+                                                            False):
+        raise NotImplementedError("myelinated cylinders are walked by simulate() only (the "
+                                  "reference's CPMG path has no myelin step rule)")
     if hasattr(waveform, 'waveform'):
         waveform = waveform.waveform
     echo = getattr(waveform, 'echo_indices', None)
@@ -597,9 +615,10 @@ def simulate_trajectories(n_walkers, diffusivity, geometry, T_max, dt_save, seed
     """
     if kappa_MT and kappa_MT > 0:
         raise NotImplementedError("magnetisation-transfer binding walks are not supported")
-    if getattr(geometry, '_is_myelinated', False):
-        raise NotImplementedError("MyelinatedCylinder is walked by simulate() only (its own step "
-                                  "rule has no trajectory producer)")
+    if getattr(geometry, '_is_myelinated', False) or getattr(geometry, '_is_packed_myelinated',
+                                                            False):
+        raise NotImplementedError("myelinated cylinders are walked by simulate() only (the packed "
+                                  "producer's magnetisation-transfer walk is not built here)")
     if compress is not None:
         return _simulate_trajectories_compressed(
             n_walkers, diffusivity, geometry, T_max, dt_save, seed, walker_batch_size,

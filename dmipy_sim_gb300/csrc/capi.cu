@@ -22,6 +22,7 @@ WalkFn walk_fn_pcyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_psph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_mesh(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_myelin(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_pmyelin(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_sph(int wall, int pm, int width, bool tsm);
@@ -93,8 +94,18 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
       return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
   }
   const bool packed = g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  if (g->kind < 0 || g->kind > DMSIM_GEOM_MYELIN)
+  if (g->kind < 0 || g->kind > DMSIM_GEOM_PMYELIN)
     return fail(DMSIM_EINVAL, "unsupported geometry kind %d", g->kind);
+  if (g->kind == DMSIM_GEOM_PMYELIN) {
+    if (g->pmy_n < 1 || g->pmy_nmax < g->pmy_n || !g->pmy_cyl || !g->pmy_seed || !(g->L > 0.f))
+      return fail(DMSIM_EINVAL, "packed myelinated cylinders need their axon and seeding tables");
+    if (((uintptr_t)g->pmy_cyl & 15) || ((uintptr_t)g->pmy_seed & 7))
+      return fail(DMSIM_EINVAL, "packed myelin tables must be 16-byte aligned");
+    if (g->wall_mode == DMSIM_WALL_RELAX)
+      return fail(DMSIM_EINVAL, "packed myelin walls reflect or permeate");
+    if (g->rho_over_D != 1.f || p->step_length != 1.f)
+      return fail(DMSIM_EINVAL, "packed myelin walks unit directions with rho_over_D = 1");
+  }
   if (g->kind == DMSIM_GEOM_MYELIN) {
     if (!(g->radius > 0.f) || !(g->myelin_r_out > g->radius))
       return fail(DMSIM_EINVAL, "myelinated cylinder needs 0 < inner radius < outer radius");
@@ -168,6 +179,9 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
     case DMSIM_GEOM_MESH: pl->fn = walk_fn_mesh(g->wall_mode, pl->pm, pl->width, false); break;
     case DMSIM_GEOM_MYELIN:
       pl->fn = walk_fn_myelin(g->wall_mode, pl->pm, pl->width, false);
+      break;
+    case DMSIM_GEOM_PMYELIN:
+      pl->fn = walk_fn_pmyelin(g->wall_mode, pl->pm, pl->width, false);
       break;
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
@@ -502,6 +516,22 @@ MyelinK make_myelk(const dmsim_geometry* g) {
   return m;
 }
 
+PMyelinK make_pmyk(const dmsim_geometry* g) {
+  PMyelinK m;
+  memset(&m, 0, sizeof(m));
+  if (g->kind != DMSIM_GEOM_PMYELIN) return m;
+  m.cyl = reinterpret_cast<const float4*>(g->pmy_cyl);
+  m.seed = reinterpret_cast<const long long*>(g->pmy_seed);
+  m.n = g->pmy_n;
+  m.nmax = g->pmy_nmax;
+  m.L = g->L;
+  m.nudge = g->nudge;
+  m.rho = g->pmy_rho_over_D;
+  m.lwm = g->pmy_logw_myelin;
+  for (int c = 0; c < 3; ++c) m.t2dec[c] = g->pmy_t2dec[c];
+  return m;
+}
+
 GeoK make_geok(const dmsim_geometry* g) {
   GeoK gk;
   memset(&gk, 0, sizeof(gk));
@@ -513,7 +543,7 @@ GeoK make_geok(const dmsim_geometry* g) {
   gk.eps = g->eps_detect;
   gk.nudge = g->nudge;
   gk.kod = g->kappa_over_D;
-  gk.L = packed ? g->L : 0.f;
+  gk.L = (packed || g->kind == DMSIM_GEOM_PMYELIN) ? g->L : 0.f;
   gk.halfL = packed ? 0.5f * g->L : 0.f;
   gk.inv_h = packed ? (float)g->grid_n / g->L : 0.f;
   gk.n = packed ? g->grid_n : 1;
@@ -568,6 +598,7 @@ void fill_kargs(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim
   a->g = make_geok(g);
   a->mk = make_meshk(g);
   a->my = make_myelk(g);
+  a->pm = make_pmyk(g);
   a->tab_cs_bytes = (uint32_t)pl.tab_cs;
   a->tab_cand_bytes = (uint32_t)pl.tab_cand;
   a->cs = g->cell_start;
@@ -876,7 +907,7 @@ int batch_plan(dmsim_batch* b) {
     rc = check_outputs(&I.p, &I.g, &I.o);
     if (rc != DMSIM_OK) return rc;
     // a myelinated cylinder has no batched kernel: its instances run as plain walks
-    I.batched = I.pl.pm == 1 && I.g.kind != DMSIM_GEOM_MYELIN;
+    I.batched = I.pl.pm == 1 && I.g.kind != DMSIM_GEOM_MYELIN && I.g.kind != DMSIM_GEOM_PMYELIN;
     if (!I.batched) {
       I.off_ws = off;
       off = align256(off + I.pl.total);

@@ -1,7 +1,7 @@
 """Writes the walk-kernel instantiation tables (walk_<kind>.cu, walk_batch_<kind>.cu).
 
 Each geometry gets one translation unit of single-instance variants (wall mode x phase form x
-cell list in shared memory) and, except the myelinated cylinder (whose batch instances run as
+cell list in shared memory) and, except the myelinated cylinders (whose batch instances run as
 plain walks), one of batched variants (basis phase form only), so that the parallel build compiles
 them side by side.  Run after changing the variant set.
 """
@@ -16,6 +16,7 @@ KINDS = [  # (file stem, enum, wall modes, has a cell list, has batched variants
     ("psph", "DMSIM_GEOM_PACKED_SPHERES", [0, 1, 2], True, True),
     ("mesh", "DMSIM_GEOM_MESH", [0, 1, 2], False, True),
     ("myelin", "DMSIM_GEOM_MYELIN", [0, 2], False, False),
+    ("pmyelin", "DMSIM_GEOM_PMYELIN", [0, 2], False, False),
 ]
 VARIANTS = [(0, 16), (0, 32), (0, 64), (1, 2), (1, 4), (1, 8)]  # (phase form, width)
 

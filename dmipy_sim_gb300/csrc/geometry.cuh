@@ -123,6 +123,128 @@ __device__ __forceinline__ float myelin_step(float& x, float& y, float& z, int& 
   return -(nc == 0 ? m.t2dec[0] : (nc == 1 ? m.t2dec[1] : m.t2dec[2]));
 }
 
+// Packed myelinated cylinders: N axons in a periodic square cell.
+struct PMyelinK {
+  const float4* cyl;  // 4 float4 per axon: (cx, cy, R_in, R_out), (sl_i, sl_m, sl_e, kin_i),
+                      // (kin_m, kin_e, kout_i, kout_m), (kout_e, -, -, -)
+  const long long* seed;  // 2n + 1 range ends of the seeding
+  int n, nmax;
+  float L, nudge, rho, lwm;
+  float t2dec[3];
+};
+
+__device__ __forceinline__ float pm_mi(float q, float L) { return q - L * floorf(q / L + 0.5f); }
+
+// One sub-step of make_packed_myelin_traj_step_fn + the fused weight (physics.py:742-930,
+// 1034-1056).  (x, y) is the in-cell position (wrapped into [-L/2, L/2) where the reference
+// wraps it), z free; comp the encoded compartment.  The walker's axon k (axon 0 for an
+// extra-axonal walker, as in the reference) supplies the walls it can cross and the step length;
+// an extra-axonal walker that ends inside any sheath is mirrored out of the deepest one.  Returns
+// the step's log-weight without the coherence gate's T1 part: (rho/D * unit boundary log-weight
+// - dt/T2 of the new compartment); the kernel multiplies it by chi.
+template <int WALL>
+__device__ __forceinline__ float pmyelin_step(float& x, float& y, float& z, int& comp, float ux,
+                                              float uy, float uz, float u1, float u2,
+                                              const PMyelinK& m, Tally& tl) {
+  const bool ext = comp == 0, intra = comp >= 1 && comp <= m.nmax, myel = comp > m.nmax;
+  int k = intra ? comp - 1 : (myel ? comp - m.nmax - 1 : 0);
+  k = max(k, 0);
+  const float4 A = m.cyl[4 * k], B = m.cyl[4 * k + 1], C4 = m.cyl[4 * k + 2],
+               D4 = m.cyl[4 * k + 3];
+  const float cx = A.x, cy = A.y, rin = A.z, rout = A.w;
+  const float sl = intra ? B.x : (myel ? B.y : B.z);
+  const float stx = ux * sl, sty = uy * sl, stz = uz * sl;
+  float qx = pm_mi(x + stx - cx, m.L), qy = pm_mi(y + sty - cy, m.L);
+  const float rn = sqrtf(qx * qx + qy * qy);
+  const bool cio = intra && rn >= rin, cii = myel && rn < rin;
+  const bool coo = myel && rn >= rout, coi = ext && rn < rout;
+  const bool ci = cio || cii, co = coo || coi;
+  const float dpi = fabsf(rn - rin), dpo = fabsf(rn - rout);
+  bool ti = false, to = false;
+  if constexpr (WALL == kPermeate) {
+    const float kin = intra ? B.w : (myel ? C4.x : C4.y);
+    const float kout = intra ? C4.z : (myel ? C4.w : D4.x);
+    ti = ci && (u1 < fminf(1.f, 2.f * kin * dpi));
+    to = co && (u2 < fminf(1.f, 2.f * kout * dpo));
+  }
+  int nc = comp;
+  float dlog = 0.f;
+  if (ci && !ti) {  // mirror across the inner wall
+    const float s = (2.f * rin - rn) / fmaxf(rn, 1e-20f);
+    qx *= s;
+    qy *= s;
+    dlog += -2.f * dpi;
+  }
+  if (ti) nc = cio ? m.nmax + k + 1 : k + 1;
+  if (co && !to) {  // mirror across the outer wall
+    const float r2 = sqrtf(qx * qx + qy * qy);
+    const float s = (2.f * rout - r2) / fmaxf(r2, 1e-20f);
+    qx *= s;
+    qy *= s;
+    dlog += -2.f * dpo;
+  }
+  if (to) nc = coo ? 0 : m.nmax + k + 1;
+  float nx = pm_mi(qx + cx, m.L), ny = pm_mi(qy + cy, m.L);
+  if (ext) {
+    // an extra-axonal end point inside any sheath: mirror out of the one it penetrates deepest
+    // (relative to R_out^2; first of equals), recording its outer-wall contact
+    float pmin = 1.f;
+    int kc = 0;
+#pragma unroll 1
+    for (int j = 0; j < m.n; ++j) {
+      const float4 Cj = m.cyl[4 * j];
+      const float fx = pm_mi(nx - Cj.x, m.L), fy = pm_mi(ny - Cj.y, m.L);
+      const float d2 = fx * fx + fy * fy, R2 = Cj.w * Cj.w;
+      const float pen = (Cj.w > 0.f && d2 < R2) ? d2 / (R2 + 1e-30f) : 1.f;
+      if (pen < pmin) {
+        pmin = pen;
+        kc = j;
+      }
+    }
+    if (pmin < 1.f) {
+      const float4 Cc = m.cyl[4 * kc];
+      const float qcx = pm_mi(nx - Cc.x, m.L), qcy = pm_mi(ny - Cc.y, m.L);
+      const float dcl = sqrtf(qcx * qcx + qcy * qcy);
+      const float s = (2.f * Cc.w - dcl) / fmaxf(dcl, m.nudge);
+      nx = (nx - qcx) + qcx * s;
+      ny = (ny - qcy) + qcy * s;
+      dlog += -2.f * fmaxf(Cc.w - dcl, 0.f);
+      ++tl.clamp;
+    }
+  } else if (nc == comp) {
+    // clamps of a walker that stayed in its axon's intra space or sheath
+    auto put = [&](float target) {
+      const float ex = pm_mi(nx - cx, m.L), ey = pm_mi(ny - cy, m.L);
+      const float d = sqrtf(ex * ex + ey * ey);
+      const float s = target / fmaxf(d, 1e-20f);
+      nx = cx + ex * s;
+      ny = cy + ey * s;
+      ++tl.clamp;
+    };
+    auto dist = [&]() {
+      const float ex = pm_mi(nx - cx, m.L), ey = pm_mi(ny - cy, m.L);
+      return sqrtf(ex * ex + ey * ey);
+    };
+    if (intra && dist() >= rin) put(rin - m.nudge);
+    if (myel && dist() < rin) put(rin + m.nudge);
+    if (myel && dist() >= rout) put(rout - m.nudge);
+  }
+  // reclassification of an intra / myelin walker against its own axon
+  if (!ext) {
+    const float ex = pm_mi(nx - cx, m.L), ey = pm_mi(ny - cy, m.L);
+    const float d2 = ex * ex + ey * ey;
+    if (d2 < rin * rin) nc = k + 1;
+    else if (d2 < rout * rout) nc = m.nmax + k + 1;
+  }
+  if (ti || to) ++tl.transmit;
+  x = nx;
+  y = ny;
+  z = z + stz;
+  comp = nc;
+  const float t2 = nc == 0 ? m.t2dec[2] : (nc > m.nmax ? m.t2dec[1] : m.t2dec[0]);
+  return m.rho * dlog - t2;
+}
+
 // ------------------------------------------------------------------------------------------------
 // Single cylinder, axis z, centred at the origin.
 // ------------------------------------------------------------------------------------------------

@@ -47,6 +47,7 @@ struct KArgs {
   GeoK g;
   MeshK mk;  // GEOM_MESH only
   MyelinK my;  // GEOM_MYELIN only
+  PMyelinK pm;  // GEOM_PMYELIN only
   uint32_t tab_cs_bytes, tab_cand_bytes;  // shared-memory staging sizes (multiples of 16 B)
   const float* Cp;                        // basis mode: (M, 3, RT) coefficients
   const uint32_t* cs;
@@ -213,6 +214,9 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
   constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
   constexpr bool MESH = GEOM == DMSIM_GEOM_MESH;
   constexpr bool MYEL = GEOM == DMSIM_GEOM_MYELIN;
+  constexpr bool PMYEL = GEOM == DMSIM_GEOM_PMYELIN;
+  // compartment ids reported by a packed myelin walk: 0 intra, 1 myelin, 2 extra (core.py:548-550)
+  auto to3 = [&](int c, int nmax) { return c == 0 ? 2 : (c > nmax ? 1 : 0); };
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   // single-instance launches walk a static share of tiles; batched ones pull work items
@@ -355,6 +359,18 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
         const float q = x * x + y * y;
         mcomp = q < a.my.r_in * a.my.r_in ? 0 : (q < a.my.r_out * a.my.r_out ? 1 : 2);
       }
+      if constexpr (PMYEL) {  // intra of the first axon holding it, else myelin, else extra
+        const PMyelinK& m = a.pm;
+        int ci = -1, cm = -1;
+        for (int j = m.n - 1; j >= 0; --j) {
+          const float4 Cj = m.cyl[4 * j];
+          const float fx = pm_mi(x - Cj.x, m.L), fy = pm_mi(y - Cj.y, m.L);
+          const float d2 = fx * fx + fy * fy;
+          if (d2 < Cj.z * Cj.z) ci = j;
+          if (d2 < Cj.w * Cj.w) cm = j;
+        }
+        mcomp = ci >= 0 ? ci + 1 : (cm >= 0 ? m.nmax + cm + 1 : 0);
+      }
       if constexpr (MESH) {
         const MeshK& m = a.mk;
         if (m.per[0]) { ix = (int)floorf((x - m.vmin[0]) / m.box[0]); x -= m.box[0] * ix; }
@@ -371,6 +387,20 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
         const long long gi = (long long)gw;
         mcomp = gi < a.my.n0 ? 0 : (gi < a.my.n1 ? 1 : 2);
       }
+      // packed myelin: the seeding segment of this walker (intra of axon 0..n-1, then myelin of
+      // axon 0..n-1, then extra-axonal; geometries.py:3127-3208), its axon and compartment
+      int pm_seg = 0;
+      if constexpr (PMYEL) {
+        const long long gi = (long long)gw;
+        int lo = 0, hi = 2 * a.pm.n;  // first segment whose end exceeds gi
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (a.pm.seed[mid] > gi) hi = mid; else lo = mid + 1;
+        }
+        pm_seg = lo;
+        mcomp = pm_seg < a.pm.n ? pm_seg + 1
+                                : (pm_seg < 2 * a.pm.n ? a.pm.nmax + (pm_seg - a.pm.n) + 1 : 0);
+      }
       const float s_lo = MYEL ? (mcomp == 0 ? 0.f : (mcomp == 1 ? a.my.r_in : a.my.r_out)) : 0.f;
       const float s_hi = MYEL ? (mcomp == 0 ? a.my.r_in : (mcomp == 1 ? a.my.r_out
                                                                        : 2.f * a.my.r_out))
@@ -380,7 +410,29 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
       for (uint32_t j = 0; j < 256u && !ok; ++j) {
         const u32x4 r = draw(a.seed, gw, 1u, j);
         const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z), u3 = u01(r.w);
-        if constexpr (MYEL) {
+        if constexpr (PMYEL) {
+          const PMyelinK& m = a.pm;
+          for (int h = 0; h < 2 && !ok; ++h) {
+            const float v0 = h ? u2 : u0, v1 = h ? u3 : u1;
+            if (pm_seg < 2 * m.n) {  // inner disc or sheath of one axon, around its centre
+              const float4 Cj = m.cyl[4 * (pm_seg % m.n)];
+              const float lo = pm_seg < m.n ? 0.f : Cj.z, hi = pm_seg < m.n ? Cj.z : Cj.w;
+              const float px = hi * (2.f * v0 - 1.f), py = hi * (2.f * v1 - 1.f);
+              const float q = px * px + py * py;
+              if (q >= lo * lo && q < hi * hi) { x = Cj.x + px; y = Cj.y + py; ok = true; }
+            } else {  // extra-axonal: uniform in the cell outside every sheath
+              const float px = m.L * (v0 - 0.5f), py = m.L * (v1 - 0.5f);
+              bool out = true;
+              for (int j = 0; j < m.n && out; ++j) {
+                const float4 Cj = m.cyl[4 * j];
+                const float fx = px - Cj.x - m.L * rintf((px - Cj.x) / m.L);
+                const float fy = py - Cj.y - m.L * rintf((py - Cj.y) / m.L);
+                if (!(fx * fx + fy * fy > Cj.w * Cj.w)) out = false;
+              }
+              if (out) { x = px; y = py; ok = true; }
+            }
+          }
+        } else if constexpr (MYEL) {
           for (int h = 0; h < 2 && !ok; ++h) {
             const float px = s_hi * (2.f * (h ? u2 : u0) - 1.f);
             const float py = s_hi * (2.f * (h ? u3 : u1) - 1.f);
@@ -445,7 +497,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
       if (a.mk.reject && WALL != kPermeate) mcls = mesh_classify(a.mk, x, y, z, mpop);
     }
     if (act && a.comp0 != nullptr && a.pass == 0)
-      a.comp0[w] = MYEL ? mcomp
+      a.comp0[w] = PMYEL ? to3(mcomp, a.pm.nmax) : MYEL ? mcomp
                         : (MESH ? classify_mesh(x, y, z, a.mk)
                                 : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
 
@@ -455,8 +507,9 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
 #pragma unroll
     for (int i = 0; i < NACC; ++i) acc[i] = kc[i] = 0.f;
     // a myelinated cylinder's walkers start with the log of their compartment's spin weight
-    const float logw0 = MYEL ? (mcomp == 0 ? a.my.lw0[0] : (mcomp == 1 ? a.my.lw0[1] : a.my.lw0[2]))
-                             : 0.f;
+    const float logw0 =
+        MYEL ? (mcomp == 0 ? a.my.lw0[0] : (mcomp == 1 ? a.my.lw0[1] : a.my.lw0[2]))
+             : (PMYEL ? (mcomp > a.pm.nmax ? a.pm.lwm : 0.f) : 0.f);
     float logw = logw0;
     uint32_t s = 0;   // global sub-step counter of this walker
     u32x4 rr{0, 0, 0, 0};
@@ -537,6 +590,13 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
             dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
           } else if constexpr (MYEL) {
             dl = myelin_step<WALL>(x, y, z, mcomp, stx, sty, stz, up, up2, a.my, tw);
+          } else if constexpr (PMYEL) {
+            // the phase reads the unwrapped position: the image counters take up the minimum-
+            // image displacement of the in-cell step (physics.py:1038-1042)
+            const float xo = x, yo = y;
+            dl = pmyelin_step<WALL>(x, y, z, mcomp, stx, sty, stz, up, up2, a.pm, tw);
+            ix -= (int)rintf((x - xo) / a.pm.L);
+            iy -= (int)rintf((y - yo) / a.pm.L);
           } else if constexpr (MESH) {
             dl = mesh_step<WALL>(x, y, z, ix, iy, iz, mcls, mpop, stx, sty, stz, up, a.mk, tw,
                                  act ? n_budget : n_idle, act ? n_escape : n_idle,
@@ -550,7 +610,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
           }
           if (a.dlog_unit) dls += dl;
           if (a.comp_occ)
-            occ += (float)(MYEL ? mcomp
+            occ += (float)(PMYEL ? to3(mcomp, a.pm.nmax) : MYEL ? mcomp
                                 : (MESH ? classify_mesh(x, y, z, a.mk)
                                         : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj)));
         }
@@ -672,14 +732,14 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
     if (act) {
       if (!(isfinite(ux) && isfinite(uy) && isfinite(uz))) ++n_nonfinite;
       if (a.pass == 0) {
-        if (a.final_pos) {
-          a.final_pos[3 * w] = ux;
-          a.final_pos[3 * w + 1] = uy;
+        if (a.final_pos) {  // a packed myelin walk reports the in-cell position (core.py:560-566)
+          a.final_pos[3 * w] = PMYEL ? x : ux;
+          a.final_pos[3 * w + 1] = PMYEL ? y : uy;
           a.final_pos[3 * w + 2] = uz;
         }
         if (a.log_w) a.log_w[w] = logw - logw0;  // the walk's own log-weight, without spin weight
         if (a.comp_end)
-          a.comp_end[w] = MYEL ? mcomp
+          a.comp_end[w] = PMYEL ? to3(mcomp, a.pm.nmax) : MYEL ? mcomp
                                : (MESH ? classify_mesh(x, y, z, a.mk)
                                        : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
       }

@@ -16,6 +16,7 @@ import torch
 from . import _lib
 
 __all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "MyelinatedCylinder",
+           "PackedMyelinatedCylinders", "pack_myelinated_cylinders",
            "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres",
            "lattice_cylinders"]
 
@@ -323,6 +324,291 @@ class MyelinatedCylinder(Geometry):
     def _has_weight(self):
         return (any(t is not None for t in (self.T2_intra, self.T2_myelin, self.T2_extra))
                 or any(w != 1.0 for w in self.water_fractions))
+
+
+def pack_myelinated_cylinders(inner_radii, g_ratios, target_packing, cell_size=None, seed=0,
+                              max_attempts=100_000):
+    """RSA of myelinated cylinders (outer radius = inner / g-ratio) in a periodic square cell,
+    largest first, outer walls not overlapping -- the same draws as geometries.py:2787-2857, so a
+    seed gives the same packing.  Returns (inner_radii, g_ratios, centers (N, 2))."""
+    inner_radii = np.asarray(inner_radii, dtype=np.float64).ravel()
+    N = len(inner_radii)
+    g = np.broadcast_to(np.asarray(g_ratios, dtype=np.float64).ravel(), (N,)).copy()
+    outer = inner_radii / g
+    if cell_size is None:
+        if target_packing is None:
+            raise ValueError("Provide either cell_size or target_packing.")
+        cell_size = float(np.sqrt(np.pi * np.sum(outer ** 2) / target_packing))
+    L = float(cell_size)
+    rng = np.random.default_rng(int(seed))
+    order = np.argsort(outer)[::-1]
+    out_s = outer[order]
+    cs = np.zeros((N, 2))
+    for i, r in enumerate(out_s):
+        for _ in range(max_attempts):
+            c = rng.uniform(-L / 2.0, L / 2.0, 2)
+            dq = c - cs[:i]
+            dq -= L * np.round(dq / L)
+            if i == 0 or not np.any(np.linalg.norm(dq, axis=1) < r + out_s[:i]):
+                cs[i] = c
+                break
+        else:
+            raise RuntimeError(f"RSA failed after {max_attempts} attempts placing cylinder {i}.")
+    centers = np.empty_like(cs)
+    centers[order] = cs
+    return inner_radii, g, centers
+
+
+class PackedMyelinatedCylinders(Geometry):
+    """Myelinated axons in a periodic square cell (geometries.py:2860-3218), three compartments:
+    extra-axonal (id 0), intra-axonal of axon k (id 1 + k), myelin of axon k (id N_max + 1 + k).
+    Per-axon diffusivities and wall permeabilities, per-compartment T2 (axon 0's values, as the
+    reference's step reads them), surface relaxivity at the myelin walls.  Walked by its own step
+    rule (physics.py:682-1062): a step of the walker's compartment along a unit direction,
+    mirror reflection or Powles transmission at its axon's walls, an extra-axonal walker pushed out
+    of whichever sheath it entered, clamps, reclassification; the phase reads the periodic-
+    unwrapped position and myelin water carries the myelin proton density as its spin weight.
+    """
+
+    _is_packed_myelinated = True
+
+    def __init__(self, inner_radii, g_ratios, centers, cell_size, N_max=128,
+                 orientation=(0.0, 0.0, 1.0), D_intra=2e-9, D_myelin=0.0, D_extra=2e-9,
+                 T2_intra=None, T2_myelin=None, T2_extra=None, kappa_inner=0.0, kappa_outer=0.0,
+                 rho_inner=0.0, rho_outer=0.0):
+        inner = np.asarray(inner_radii, dtype=np.float64).ravel()
+        N = len(inner)
+        g = np.broadcast_to(np.asarray(g_ratios, dtype=np.float64).ravel(), (N,)).copy()
+        centers = np.asarray(centers, dtype=np.float64)
+        if centers.shape != (N, 2):
+            raise ValueError(f"centers shape {centers.shape} must be ({N}, 2)")
+        if N_max < N:
+            raise ValueError(f"N_max={N_max} < N_actual={N}")
+        self.N_actual, self.N_max = N, int(N_max)
+        self._cell_size = self._L_float = float(cell_size)
+        self._myelin_proton_density = MYELIN_WATER_PROTON_DENSITY
+
+        def bc(x, name, opt=False):
+            if x is None:
+                if opt:
+                    return None
+                x = 0.0
+            x = np.asarray(x, dtype=np.float64).ravel()
+            if x.size == 1:
+                return np.full(N, float(x[0]))
+            if x.size != N:
+                raise ValueError(f"{name} must be scalar or length {N}, got {x.size}")
+            return x.copy()
+
+        def pad(a, fill=0.0):
+            out = np.full(self.N_max, fill, dtype=np.float64)
+            out[:N] = a
+            return out
+        self._inner_radii_np = pad(inner)
+        self._outer_radii_np = pad(inner / g)
+        cen = np.zeros((self.N_max, 2))
+        cen[:N] = centers
+        self._centers_np = cen
+        self._D = {k: pad(bc(v, k)) for k, v in (("intra", D_intra), ("myelin", D_myelin),
+                                                  ("extra", D_extra))}
+        T2 = {k: bc(v, k, opt=True) for k, v in (("intra", T2_intra), ("myelin", T2_myelin),
+                                                  ("extra", T2_extra))}
+        self._has_t2 = any(v is not None for v in T2.values())
+        self._T2 = {k: (pad(v) if v is not None else np.full(self.N_max, 1e6))
+                    for k, v in T2.items()}
+        self._kappa_inner = pad(bc(kappa_inner, "kappa_inner"))
+        self._kappa_outer = pad(bc(kappa_outer, "kappa_outer"))
+        self._rho_inner = pad(bc(rho_inner, "rho_inner"))
+        self._rho_outer = pad(bc(rho_outer, "rho_outer"))
+        o = np.asarray(orientation, dtype=np.float64)
+        self.orientation = (o / np.linalg.norm(o)).astype(np.float32)
+        R = _rotation_to_z(self.orientation)
+        self._R = R.astype(np.float32)
+        self._R_inv = R.T.astype(np.float32)
+        self._is_identity_rotation = bool(np.allclose(R, np.eye(3)))
+        nz = self._inner_radii_np[self._inner_radii_np > 0]
+        ref_r = float(np.min(nz)) if len(nz) else 1e-6
+        self._eps = np.float32(1e-7 * ref_r)
+        self._nudge = np.float32(1e-4 * ref_r)
+        self.min_gap = self._compute_min_gap()
+        self._init_compartments = None
+        self._dev_cache = {}
+
+    def _frame(self):
+        return None if self._is_identity_rotation else self._R.astype(np.float64)
+
+    def _wall_mode(self, with_weight_channel=False):
+        permeable = np.any(self._kappa_inner > 0) or np.any(self._kappa_outer > 0)
+        return _lib.WALL_PERMEATE if permeable else _lib.WALL_REFLECT
+
+    def _compute_min_gap(self):
+        N, L = self.N_actual, self._L_float
+        c, o = self._centers_np[:N], self._outer_radii_np[:N]
+        gap = float("inf")
+        for i in range(N):
+            dq = c[i] - c[i + 1:]
+            dq -= L * np.round(dq / L)
+            if len(dq):
+                gap = min(gap, float(np.min(np.linalg.norm(dq, axis=1) - o[i] - o[i + 1:])))
+            gap = min(gap, L - 2.0 * o[i])
+        return gap
+
+    def volume_fraction(self, compartment):
+        L, N = self._L_float, self.N_actual
+        i, o = self._inner_radii_np[:N], self._outer_radii_np[:N]
+        if compartment == "intra":
+            return float(np.pi * np.sum(i ** 2) / L ** 2)
+        if compartment == "myelin":
+            return float(np.pi * np.sum(o ** 2 - i ** 2) / L ** 2)
+        if compartment == "extra":
+            return float((L ** 2 - np.pi * np.sum(o ** 2)) / L ** 2)
+        raise ValueError(f"compartment must be 'intra', 'myelin', or 'extra'; got {compartment!r}")
+
+    # ---- seeding ------------------------------------------------------------------------------
+    def seed_counts(self, n_walkers):
+        """(n_intra (N,), n_myelin (N,), n_extra): area-proportional counts, extra-axonal space
+        taking the remainder, intra counts trimmed in order when rounding overshoots
+        (geometries.py:3100-3125)."""
+        L, N = self._L_float, self.N_actual
+        i, o = self._inner_radii_np[:N], self._outer_radii_np[:N]
+        a_in, a_my = np.pi * i ** 2, np.pi * (o ** 2 - i ** 2)
+        a_ex = L * L - np.pi * np.sum(o ** 2)
+        tot = a_ex + np.sum(a_in) + np.sum(a_my)
+        n_in = np.array([int(round(n_walkers * a / tot)) for a in a_in], dtype=np.int64)
+        n_my = np.array([int(round(n_walkers * a / tot)) for a in a_my], dtype=np.int64)
+        n_ex = n_walkers - int(n_in.sum()) - int(n_my.sum())
+        if n_ex < 0:
+            excess = -n_ex
+            for k in range(N):
+                trim = min(excess, int(n_in[k]))
+                n_in[k] -= trim
+                excess -= trim
+                if excess == 0:
+                    break
+            n_ex = 0
+        return n_in, n_my, n_ex
+
+    def to3(self, comp):
+        """Encoded compartment ids -> 0 intra, 1 myelin, 2 extra (core.py:548-550)."""
+        comp = np.asarray(comp)
+        return np.where(comp == 0, 2, np.where(comp > self.N_max, 1, 0)).astype(np.int32)
+
+    def classify_position(self, r):
+        """Encoded compartment of positions (lab frame) by their min-image distance to each axon:
+        intra of the axon whose inner disc holds it, else myelin of the axon whose sheath holds
+        it, else extra-axonal (0)."""
+        r = np.atleast_2d(np.asarray(r, dtype=np.float32))
+        rc = r if self._is_identity_rotation else r @ self._R.T
+        L, N = np.float32(self._L_float), self.N_actual
+        out = np.zeros(len(rc), np.int32)
+        for k in range(N - 1, -1, -1):
+            q = rc[:, :2] - self._centers_np[k].astype(np.float32)
+            q = q - L * np.floor(q / L + np.float32(0.5))
+            d2 = np.sum(q * q, axis=1)
+            ri, ro = np.float32(self._inner_radii_np[k]), np.float32(self._outer_radii_np[k])
+            out = np.where(d2 < ro * ro, self.N_max + 1 + k, out)
+        for k in range(N - 1, -1, -1):
+            q = rc[:, :2] - self._centers_np[k].astype(np.float32)
+            q = q - L * np.floor(q / L + np.float32(0.5))
+            d2 = np.sum(q * q, axis=1)
+            ri = np.float32(self._inner_radii_np[k])
+            out = np.where(d2 < ri * ri, 1 + k, out)
+        return out
+
+    def init_positions(self, n_walkers, key=None):
+        """Host sampler of the reference (geometries.py:3084-3214): the counts of
+        :meth:`seed_counts`, uniform in each inner disc, sheath and in the extra-axonal space;
+        sets ``_init_compartments`` (encoded ids)."""
+        rng = _host_rng(key)
+        L, N = self._L_float, self.N_actual
+        n_in, n_my, n_ex = self.seed_counts(n_walkers)
+        pos, comp = [], []
+        for kind, counts in ((0, n_in), (1, n_my)):
+            for k in range(N):
+                nk = int(counts[k])
+                if nk == 0:
+                    continue
+                ri, ro = self._inner_radii_np[k], self._outer_radii_np[k]
+                lo, hi = (0.0, ri) if kind == 0 else (ri, ro)
+                got = np.zeros((0, 2))
+                while len(got) < nk:
+                    xy = rng.uniform(-hi, hi, (max(nk * 4, 64), 2))
+                    d = np.linalg.norm(xy, axis=1)
+                    got = np.concatenate([got, xy[(d >= lo) & (d < hi)]])
+                pos.append(got[:nk] + self._centers_np[k])
+                comp.append(np.full(nk, (1 + k) if kind == 0 else (self.N_max + 1 + k), np.int32))
+        if n_ex > 0:
+            got = np.zeros((0, 2))
+            while len(got) < n_ex:
+                xy = rng.uniform(-L / 2.0, L / 2.0, (max(n_ex * 4, 1024), 2))
+                ok = np.ones(len(xy), bool)
+                for k in range(N):
+                    d = xy - self._centers_np[k]
+                    d -= L * np.round(d / L)
+                    ok &= np.sum(d ** 2, axis=1) > self._outer_radii_np[k] ** 2
+                got = np.concatenate([got, xy[ok]])
+            pos.append(got[:n_ex])
+            comp.append(np.zeros(n_ex, np.int32))
+        xy = np.concatenate(pos).astype(np.float32)
+        rc = np.concatenate([xy, np.zeros((n_walkers, 1), np.float32)], axis=1)
+        self._init_compartments = np.concatenate(comp)
+        return (rc @ self._R).astype(np.float32)
+
+    def spin_weight_sum(self, n_walkers):
+        """Walkers seeded in a sheath weigh the myelin proton density, the others 1."""
+        n_in, n_my, n_ex = self.seed_counts(n_walkers)
+        return float(n_in.sum() + n_ex) + float(n_my.sum()) * self._myelin_proton_density
+
+    # ---- the walk -----------------------------------------------------------------------------
+    def _rho_D(self):
+        f = np.float32
+        rho = max(float(np.max(self._rho_inner.astype(f))), float(np.max(self._rho_outer.astype(f))))
+        D_ref = float(max(np.max(self._D["intra"].astype(f)), np.max(self._D["extra"].astype(f))))
+        return rho, D_ref
+
+    def sub_steps(self, dt):
+        """One walk step per sample; with surface relaxivity, sub-steps to the extra-axonal pore
+        scale (physics.py:1009-1022)."""
+        from .core import surface_sub_steps
+        rho, D_ref = self._rho_D()
+        return surface_sub_steps(self, D_ref, dt) if rho > 0.0 else 1
+
+    def _pmyelin_desc(self, dt_sub, n_total, dev):
+        """Descriptor and device tables of a walk with sub-step ``dt_sub`` (physics.py:705-740,
+        995-1025), in the reference's float32 arithmetic."""
+        f = np.float32
+        N = self.N_actual
+        dt32 = f(dt_sub)
+        tab = np.zeros((max(N, 1), 16), np.float32)
+        tab[:N, 0:2] = self._centers_np[:N].astype(f)
+        tab[:N, 2] = self._inner_radii_np[:N].astype(f)
+        tab[:N, 3] = self._outer_radii_np[:N].astype(f)
+        for j, c in enumerate(("intra", "myelin", "extra")):
+            Dc = self._D[c][:N].astype(f)
+            tab[:N, 4 + j] = np.sqrt(f(6.0) * Dc * dt32)
+            Dl = np.maximum(Dc, f(1e-30))
+            tab[:N, 7 + j] = self._kappa_inner[:N].astype(f) / Dl
+            tab[:N, 10 + j] = self._kappa_outer[:N].astype(f) / Dl
+        n_in, n_my, n_ex = self.seed_counts(n_total)
+        ends = np.cumsum(np.concatenate([n_in, n_my, [n_ex]])).astype(np.int64)
+        t_tab = torch.from_numpy(tab).to(dev)
+        t_seed = torch.from_numpy(ends).to(dev)
+        g = self._base_desc(_lib.GEOM_PMYELIN, self._wall_mode(), 1.0, 0.0)
+        g.radius = float(np.min(self._inner_radii_np[:N]))
+        g.L = self._L_float
+        g.eps_detect = self._eps
+        g.nudge = self._nudge
+        g.pmy_n, g.pmy_nmax = N, self.N_max
+        g.pmy_cyl, g.pmy_seed = t_tab.data_ptr(), t_seed.data_ptr()
+        if self._has_t2:
+            g.pmy_t2dec[:] = [float(dt32 / f(self._T2[c][0])) for c in ("intra", "myelin", "extra")]
+        rho, D_ref = self._rho_D()
+        g.pmy_rho_over_D = float(f(rho / D_ref)) if rho > 0.0 else 0.0
+        g.pmy_logw_myelin = float(np.log(f(self._myelin_proton_density)))
+        return g, (t_tab, t_seed)
+
+    def _has_weight(self):
+        return self._has_t2 or self._rho_D()[0] > 0.0 or self._myelin_proton_density != 1.0
 
 
 # ------------------------------------------------------------------------------------------------

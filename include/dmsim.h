@@ -61,7 +61,8 @@ enum dmsim_geom_kind {
   DMSIM_GEOM_PACKED_CYLINDERS = 3, /* geometries.py:1604-2242, periodic square cell, axis z    */
   DMSIM_GEOM_PACKED_SPHERES = 4,   /* geometries.py:2343-2786, periodic cubic cell             */
   DMSIM_GEOM_MESH = 5,             /* mesh.py:257-907                                          */
-  DMSIM_GEOM_MYELIN = 6            /* geometries.py:847-1134 + physics.py:420-680, axis frame z */
+  DMSIM_GEOM_MYELIN = 6,           /* geometries.py:847-1134 + physics.py:420-680, axis frame z */
+  DMSIM_GEOM_PMYELIN = 7           /* geometries.py:2860-3218 + physics.py:682-1062, periodic   */
 };
 
 enum dmsim_wall_mode {
@@ -149,6 +150,23 @@ typedef struct dmsim_geometry {
   int64_t myelin_seed_n[2];    /* seeding without r0: global walkers [0, n0) intra, [n0, n1)
                                   myelin, [n1, ...) extra, uniform in the disc / annuli up to
                                   2 myelin_r_out (geometries.py:928-1006)                        */
+
+  /* packed myelinated cylinders (DMSIM_GEOM_PMYELIN): pmy_n axons in the periodic square cell of
+     side L (cell [-L/2, L/2)^2, axis along frame z).  Compartment ids as the reference's: 0
+     extra-axonal, 1 + k intra-axonal of axon k, pmy_nmax + 1 + k myelin of axon k.  pmy_cyl holds
+     16 floats per axon: cx, cy, R_in, R_out, the step sqrt(6 D dt_sub) of its intra / myelin /
+     extra water, kappa_inner / max(D, 1e-30) and kappa_outer / max(D, 1e-30) for each of the
+     three, and 3 unused.  nudge is 1e-4 of the smallest R_in; rho_over_D must be 1 (the step
+     returns the whole per-step log-weight). */
+  int32_t pmy_n;
+  int32_t pmy_nmax;
+  const float* pmy_cyl;        /* pmy_n x 16 */
+  const int64_t* pmy_seed;     /* 2 pmy_n + 1 range ends of the global walker index seeded
+                                  intra of axon 0..n-1, then myelin of axon 0..n-1, then extra  */
+  float pmy_t2dec[3];          /* dt_sub / T2 (intra, myelin, extra), 0 without T2             */
+  float pmy_rho_over_D;        /* surface relaxivity rho / D_ref (0: none)                     */
+  float pmy_logw_myelin;       /* log of the myelin water proton density (spin weight)          */
+  float pmy_pad;
 } dmsim_geometry;
 
 /* ---- walk parameters -------------------------------------------------------------------------- */

@@ -46,6 +46,7 @@ static double round_half(float f) {
 #define FLOOR floorf
 #define FMOD fmodf
 #define FABS fabsf
+#define NEARBYINT nearbyintf
 #define SIN sinf
 #define COS cosf
 #define MAX(a, b) fmaxf((a), (b))
@@ -57,6 +58,7 @@ static double round_half(float f) {
 #undef FLOOR
 #undef FMOD
 #undef FABS
+#undef NEARBYINT
 #undef SIN
 #undef COS
 #undef MAX
@@ -68,6 +70,7 @@ static double round_half(float f) {
 #define FLOOR floor
 #define FMOD fmod
 #define FABS fabs
+#define NEARBYINT nearbyint
 #define SIN sin
 #define COS cos
 #define MAX(a, b) fmax((a), (b))

@@ -14,6 +14,7 @@
  *   PackedSpheres reflect / rwlw / permeate               geometries.py:2445-2537, 2539-2631, 2633-2756
  *   Mesh reflect / reflect_with_log_weight / permeate     mesh.py:637-671, 673-705, 707-743
  *   MyelinatedCylinder step (own walk rule)               physics.py:506-677
+ *   PackedMyelinatedCylinders step + fused weights         physics.py:742-930, 1034-1056
  *     (wrap 203-206, 27-cell gather 208-215, Moller-Trumbore 561-569, bounce 599-635,
  *      nearest-centroid classification 227-254, leak guard 578-597)
  *   ensemble Re<w e^{i phi}>                              core.py:426-429; replay FP64 phase
@@ -32,7 +33,7 @@ extern "C" {
 #endif
 
 enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4,
-       OR_MESH = 5, OR_MYELIN = 6 };
+       OR_MESH = 5, OR_MYELIN = 6, OR_PMYELIN = 7 };
 enum { OR_REFLECT = 0, OR_RELAX = 1, OR_PERMEATE = 2 };
 
 /* A triangle mesh as the reference's Mesh holds it (mesh.py:311-546): every triangle including the
@@ -62,6 +63,19 @@ typedef struct {
   double step[3], kin[3], kout[3], t2dec[3], logw0[3];
 } or_myelin;
 
+/* Packed myelinated cylinders (geometries.py:2860-3218) as make_packed_myelin_traj_step_fn and
+   make_packed_myelin_step_fn see them (physics.py:705-740, 995-1025): n axons in the periodic
+   cell of side L, compartment ids 0 extra / 1 + k intra / nmax + 1 + k myelin; per axon 16
+   numbers: cx, cy, R_in, R_out, the intra / myelin / extra steps sqrt(6 D dt_sub), and
+   kappa_inner / max(D, 1e-30), kappa_outer / max(D, 1e-30) for intra, myelin, extra water
+   (float32 values stored as double). */
+typedef struct {
+  int32_t n, nmax;
+  double L, nudge, rho_over_D, logw_myelin;
+  double t2dec[3];   /* dt_sub / T2 of intra, myelin, extra (axon 0's values), 0 without T2 */
+  const double* cyl; /* n x 16 */
+} or_pmyelin;
+
 typedef struct {
   int32_t kind;
   int32_t n_objects;
@@ -74,6 +88,7 @@ typedef struct {
   int32_t pad;
   const or_mesh* mesh;   /* OR_MESH only */
   const or_myelin* myelin; /* OR_MYELIN only */
+  const or_pmyelin* pmyelin; /* OR_PMYELIN only */
 } or_geom;
 
 typedef struct {
@@ -102,6 +117,16 @@ int or_myelin_plugin_f32(const or_geom* g, const double* r, const double* unit, 
 int or_myelin_plugin_f64(const or_geom* g, const double* r, const double* unit, int comp,
                          int permeate, double u1, double u2, double* r_out, int* comp_out,
                          double* t2dec);
+
+/* One sub-step of the packed myelin walk rule (physics.py:742-930) in the cylinder frame:
+   in-cell start r, encoded compartment comp, unit direction, Powles uniforms u1 / u2 (permeate).
+   Writes the in-cell end point, the new compartment and the unit boundary log-weight. */
+int or_pmyelin_plugin_f32(const or_geom* g, const double* r, const double* unit, int comp,
+                          int permeate, double u1, double u2, double* r_out, int* comp_out,
+                          double* dlog);
+int or_pmyelin_plugin_f64(const or_geom* g, const double* r, const double* unit, int comp,
+                          int permeate, double u1, double u2, double* r_out, int* comp_out,
+                          double* dlog);
 
 /* A full walk in the geometry frame.  G is (n_t, n_meas, 3) float32, chi (n_t) or NULL, r0
    (n_walkers, 3) or NULL (seeded on the Philox seeding stream; a mesh needs r0).  sums (n_echo, n_meas, 3) is

@@ -14,7 +14,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 
-FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH, MYELIN = range(7)
+FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH, MYELIN, PMYELIN = range(8)
 REFLECT, RELAX, PERMEATE = range(3)
 
 
@@ -36,11 +36,17 @@ class OrMyelin(C.Structure):
                 ("t2dec", C.c_double * 3), ("logw0", C.c_double * 3)]
 
 
+class OrPMyelin(C.Structure):
+    _fields_ = [("n", C.c_int32), ("nmax", C.c_int32), ("L", C.c_double), ("nudge", C.c_double),
+                ("rho_over_D", C.c_double), ("logw_myelin", C.c_double),
+                ("t2dec", C.c_double * 3), ("cyl", C.c_void_p)]
+
+
 class OrGeom(C.Structure):
     _fields_ = [("kind", C.c_int32), ("n_objects", C.c_int32), ("radius", C.c_double),
                 ("L", C.c_double), ("rmin", C.c_double), ("objects", C.c_void_p),
                 ("rot", C.c_double * 9), ("rot_identity", C.c_int32), ("pad", C.c_int32),
-                ("mesh", C.c_void_p), ("myelin", C.c_void_p)]
+                ("mesh", C.c_void_p), ("myelin", C.c_void_p), ("pmyelin", C.c_void_p)]
 
 
 class OrWalk(C.Structure):
@@ -80,6 +86,12 @@ def load():
                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         lib.or_philox.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
                                   C.POINTER(C.c_uint32)]
+        for suf in ("_f32", "_f64"):
+            f = getattr(lib, "or_pmyelin_plugin" + suf)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(OrGeom), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                          C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double),
+                          C.POINTER(C.c_int), C.POINTER(C.c_double)]
         for suf in ("_f32", "_f64"):
             f = getattr(lib, "or_myelin_plugin" + suf)
             f.restype = C.c_int
@@ -248,6 +260,69 @@ def myelin_geom(inner_radius, outer_radius, D, dt, kappa_inner=None, kappa_outer
     return g
 
 
+def pmyelin_geom(inner_radii, outer_radii, centers, L, dt_sub, D, kappa_inner, kappa_outer,
+                 N_max=128, T2=None, rho=(None, None), myelin_proton_density=0.4):
+    """Oracle packed myelinated cylinders for sub-step ``dt_sub``: the float32 per-axon tables of
+    make_packed_myelin_traj_step_fn (physics.py:705-740) -- steps sqrt(6 D dt_sub) of intra /
+    myelin / extra water, kappa / max(D, 1e-30) for each -- T2 of axon 0 (physics.py:995-1001),
+    rho / D_ref with D_ref the largest intra or extra D (1009-1018), nudge 1e-4 of the smallest
+    inner radius.  ``D`` = (D_intra, D_myelin, D_extra), each scalar or per axon; ``T2`` a
+    (T2_intra, T2_myelin, T2_extra) triple of scalars or None."""
+    f = np.float32
+    ri = np.asarray(inner_radii, np.float64)
+    ro = np.asarray(outer_radii, np.float64)
+    n = len(ri)
+    Ds = [np.broadcast_to(np.asarray(x, np.float64), (n,)).astype(f) for x in D]
+    def per_axon(x):
+        return np.broadcast_to(np.asarray(0.0 if x is None else x, np.float64), (n,)).astype(f)
+    ki, ko = per_axon(kappa_inner), per_axon(kappa_outer)
+    dt32 = f(dt_sub)
+    tab = np.zeros((n, 16))
+    tab[:, 0:2] = np.asarray(centers, np.float64).astype(f)
+    tab[:, 2], tab[:, 3] = ri.astype(f), ro.astype(f)
+    for j, Dc in enumerate(Ds):
+        tab[:, 4 + j] = np.sqrt(f(6.0) * Dc * dt32)
+        Dl = np.maximum(Dc, f(1e-30))
+        tab[:, 7 + j] = ki / Dl
+        tab[:, 10 + j] = ko / Dl
+    m = OrPMyelin()
+    m.n, m.nmax = n, int(N_max)
+    m.L = float(f(L))
+    m.nudge = float(f(1e-4 * float(np.min(ri[ri > 0]))))
+    if T2 is not None and any(t is not None for t in T2):
+        m.t2dec[:] = [float(dt32 / f(t if t is not None else 1e6)) for t in T2]
+    r_i, r_o = (float(np.max(per_axon(x))) for x in rho)
+    rr = max(r_i, r_o)
+    D_ref = float(max(np.max(Ds[0]), np.max(Ds[2])))
+    m.rho_over_D = float(f(rr / D_ref)) if rr > 0 else 0.0
+    m.logw_myelin = float(np.log(f(myelin_proton_density)))
+    tab = np.ascontiguousarray(tab)
+    m.cyl = tab.ctypes.data
+    g = OrGeom()
+    g.kind = PMYELIN
+    g.radius = float(np.min(ri))
+    g.rot[:] = np.eye(3).ravel().tolist()
+    g.rot_identity = 1
+    g.pmyelin = C.addressof(m)
+    g._keep = (m, tab)
+    return g
+
+
+def pmyelin_plugin(g, r, unit, comp, u1=0.0, u2=0.0, permeate=False, fp64=False):
+    """One sub-step of the packed myelin walk rule; returns (r_new (3,), comp_new, unit dlog)."""
+    lib = load()
+    f = lib.or_pmyelin_plugin_f64 if fp64 else lib.or_pmyelin_plugin_f32
+    ri = (C.c_double * 3)(*map(float, r))
+    ui = (C.c_double * 3)(*map(float, unit))
+    ro = (C.c_double * 3)()
+    co = C.c_int()
+    dl = C.c_double()
+    if f(C.byref(g), ri, ui, int(comp), int(bool(permeate)), float(u1), float(u2), ro,
+         C.byref(co), C.byref(dl)) != 0:
+        raise RuntimeError("oracle packed myelin step failed")
+    return np.array(ro[:]), co.value, dl.value
+
+
 def geom_from(geometry, dt=None):
     """Oracle geometry of a dmipy_sim_gb300 geometry object (walk frame)."""
     name = type(geometry).__name__
@@ -266,6 +341,19 @@ def geom_from(geometry, dt=None):
         kind = PACKED_CYLINDERS if name == "PackedCylinders" else PACKED_SPHERES
         return geom(kind, L=np.float32(geometry._L_float), objects=objs,
                     rot=getattr(geometry, "_R", None))
+    if name == "PackedMyelinatedCylinders":
+        if dt is None:
+            raise ValueError("the oracle's packed myelin needs the walk's sub-step")
+        n = geometry.N_actual
+        T2 = tuple(geometry._T2[c][0] for c in ("intra", "myelin", "extra")) \
+            if geometry._has_t2 else None
+        return pmyelin_geom(geometry._inner_radii_np[:n], geometry._outer_radii_np[:n],
+                            geometry._centers_np[:n], geometry._L_float, dt,
+                            tuple(geometry._D[c][:n] for c in ("intra", "myelin", "extra")),
+                            geometry._kappa_inner[:n], geometry._kappa_outer[:n],
+                            N_max=geometry.N_max, T2=T2,
+                            rho=(geometry._rho_inner[:n], geometry._rho_outer[:n]),
+                            myelin_proton_density=geometry._myelin_proton_density)
     if name == "MyelinatedCylinder":
         if dt is None:
             raise ValueError("the oracle's myelinated cylinder needs the walk's time step")
@@ -369,6 +457,21 @@ def walk(g, *, n_walkers, G, dt, sub_steps, phase_per_substep, seed, wall=REFLEC
     if rc != 0:
         raise RuntimeError("oracle walk failed")
     norm = max(n_walkers, 1)
+    if g.kind == PMYELIN:
+        m = OrPMyelin.from_address(g.pmyelin)
+        tab = g._keep[1]
+        rr = np.asarray(r0, np.float32)
+        L = np.float32(m.L)
+        ci = np.full(len(rr), -1)
+        cm = np.full(len(rr), -1)
+        for j in range(m.n - 1, -1, -1):
+            q = rr[:, :2] - tab[j, :2].astype(np.float32)
+            q = q - L * np.floor(q / L + np.float32(0.5))
+            d2 = np.sum(q * q, axis=1)
+            ci = np.where(d2 < np.float32(tab[j, 2]) ** 2, j, ci)
+            cm = np.where(d2 < np.float32(tab[j, 3]) ** 2, j, cm)
+        myel = (ci < 0) & (cm >= 0)
+        norm = float(np.sum(np.where(myel, np.exp(m.logw_myelin), 1.0)))
     if g.kind == MYELIN:
         # the ensemble is normalised by the sum of the spin weights (core.py:426-427)
         m = OrMyelin.from_address(g.myelin)

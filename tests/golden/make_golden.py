@@ -386,12 +386,84 @@ def _myelin_cases(m, rng, out):
         rnd.normal, rnd.uniform = real_normal, real_uniform
 
 
+def pmyelin_substrate(geo, perm):
+    """Five myelinated axons packed in a periodic cell (the same packing for the reference and
+    this package: pack_myelinated_cylinders draws the same numbers)."""
+    ri = np.array([1.0e-6, 1.3e-6, 0.8e-6, 1.1e-6, 0.9e-6])
+    ri, g, c = geo.pack_myelinated_cylinders(ri, 0.7, 0.5, seed=4)
+    L = float(np.sqrt(np.pi * np.sum((ri / g) ** 2) / 0.5))
+    kw = dict(kappa_inner=2e-3, kappa_outer=1e-3) if perm else {}
+    return geo.PackedMyelinatedCylinders(ri, g, c, L, N_max=8, D_intra=2e-9, D_myelin=0.5e-9,
+                                         D_extra=2.5e-9, T2_intra=0.07, T2_myelin=0.015,
+                                         T2_extra=0.06, **kw)
+
+
+def _pmyelin_cases(m, rng, out):
+    """make_packed_myelin_traj_step_fn (physics.py:682-976) of the reference, one sub-step per
+    case with the direction and Powles uniforms it drew: walkers of every compartment anywhere in
+    the cell (walls across the cell edge, extra-axonal walkers entering a sheath)."""
+    geo, phys = m["geometries"], m["physics"]
+    rnd = sys.modules["jax.random"]
+    drawn = {}
+    real_normal, real_uniform = rnd.normal, rnd.uniform
+
+    def normal(key, shape=(), dtype=np.float32):
+        v = real_normal(key, shape, dtype)
+        drawn["noise"] = np.asarray(v, np.float32)
+        return v
+
+    def uniform(key, shape=(), dtype=np.float32, minval=0.0, maxval=1.0):
+        v = real_uniform(key, shape, dtype, minval, maxval)
+        drawn.setdefault("u", []).append(np.float32(v))
+        return v
+    rnd.normal, rnd.uniform = normal, uniform
+    try:
+        n = 384
+        for tag, perm in (("perm", True), ("refl", False)):
+            g = pmyelin_substrate(geo, perm)
+            step = phys.make_packed_myelin_traj_step_fn(g, 1e-4)
+            L = g._L_float
+            r = np.concatenate([rng.uniform(-L / 2, L / 2, (n, 2)),
+                                rng.uniform(-1e-6, 1e-6, (n, 1))], 1).astype(np.float32)
+            comp = np.zeros(n, np.int32)
+            for k in range(g.N_actual - 1, -1, -1):
+                q = r[:, :2] - g._centers_np[k].astype(np.float32)
+                q = q - np.float32(L) * np.floor(q / np.float32(L) + np.float32(0.5))
+                d2 = np.sum(q * q, 1)
+                comp = np.where(d2 < np.float32(g._outer_radii_np[k]) ** 2, g.N_max + 1 + k, comp)
+            for k in range(g.N_actual - 1, -1, -1):
+                q = r[:, :2] - g._centers_np[k].astype(np.float32)
+                q = q - np.float32(L) * np.floor(q / np.float32(L) + np.float32(0.5))
+                d2 = np.sum(q * q, 1)
+                comp = np.where(d2 < np.float32(g._inner_radii_np[k]) ** 2, 1 + k, comp)
+            ro, co, dl, units, us = [], [], [], [], []
+            for i in range(n):
+                drawn.clear()
+                new, _ = step((r[i], rnd.PRNGKey(5000 + i), np.float32(0.0), np.int32(comp[i])),
+                              None)
+                nz = drawn["noise"]
+                units.append(nz / np.linalg.norm(nz))
+                us.append(drawn["u"][:2])
+                ro.append(np.asarray(new[0], np.float64))
+                dl.append(float(new[2]))
+                co.append(int(new[3]))
+            key = f"pmy_{tag}"
+            out[key + "_r"], out[key + "_comp"] = r, comp
+            out[key + "_unit"] = np.asarray(units, np.float32)
+            out[key + "_u"] = np.asarray(us, np.float32)
+            out[key + "_out"], out[key + "_comp_out"] = np.asarray(ro), np.asarray(co, np.int32)
+            out[key + "_dlog"] = np.asarray(dl)
+    finally:
+        rnd.normal, rnd.uniform = real_normal, real_uniform
+
+
 def make_myelin_kat(root):
     """Add the myelinated-cylinder step known answers to kat.npz."""
     m = _ref(root)
     path = HERE / "kat.npz"
-    out = dict(np.load(path))
+    out = {k: v for k, v in np.load(path).items() if not k.startswith(("my_", "pmy_"))}
     _myelin_cases(m, np.random.default_rng(17), out)
+    _pmyelin_cases(m, np.random.default_rng(23), out)
     np.savez_compressed(path, **out)
     print(f"kat.npz: {len(out)} arrays")
 
@@ -568,6 +640,10 @@ def _mc_configs():
                             api="simulate", D=None),
         "myelin_perm": dict(geom=("myelin", 5e-5, 3e-5, 0.5e-9), wf=("pgse_my",), n=8000,
                             api="simulate", D=None),
+        "pmyelin_refl": dict(geom=("pmyelin", False), wf=("pgse_my",), n=8000, api="simulate",
+                             D=None),
+        "pmyelin_perm": dict(geom=("pmyelin", True), wf=("pgse_my",), n=8000, api="simulate",
+                             D=None),
     }
 
 
@@ -643,6 +719,8 @@ def build_geometry(geo, spec):
     if kind == "mesh":
         V, F = mesh_surface()
         return geo.Mesh(V, F, permeability=spec[1])
+    if kind == "pmyelin":
+        return pmyelin_substrate(geo, spec[1])
     if kind == "myelin":
         # an axon of 2 um in a 0.8 um sheath, T2 per compartment, myelin water density 0.4
         return geo.MyelinatedCylinder(2e-6, 2.8e-6, (0.2, 0.3, 1.0), D_intra=2e-9, D_extra=2.2e-9,

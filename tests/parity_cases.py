@@ -60,6 +60,14 @@ def plan(geom, wf, engine):
 
 def oracle_walk(geom, G, dt, S, phase_sub, n, seed, T2=None, echo_idx=None, fp64=False,
                 walker_offset=0, want_walkers=True, r0=None, T1=None):
+    if getattr(geom, "_is_packed_myelinated", False):
+        wall = O.PERMEATE if (np.any(geom._kappa_inner > 0) or np.any(geom._kappa_outer > 0)) \
+            else O.REFLECT
+        return O.walk(O.geom_from(geom, dt / S), n_walkers=n, G=G, dt=dt, sub_steps=S,
+                      phase_per_substep=phase_sub, seed=seed, wall=wall, T1=T1,
+                      has_weight=geom._has_weight() or T1 is not None, step_length=1.0,
+                      echo_idx=echo_idx, fp64=fp64, walker_offset=walker_offset,
+                      want_walkers=want_walkers, r0=r0)
     if getattr(geom, "_is_myelinated", False):
         # unit steps, per-compartment T2 in the geometry, simulate's T2 unused
         wall = O.PERMEATE if (geom.kappa_inner is not None or geom.kappa_outer is not None) \

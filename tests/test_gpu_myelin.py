@@ -126,3 +126,80 @@ def test_myelin_simulate_surface(cuda):
         d.simulate_trajectories(n, None, g, 0.02, 1e-4)
     with pytest.raises(NotImplementedError):
         d.simulate_cpmg(n, None, d.cpmg(4, 5e-3, 0.02, [[1, 0, 0]]), g)
+
+
+# ---- packed myelinated cylinders ----------------------------------------------------------------
+def _packed(perm, rho=0.0):
+    from golden.make_golden import pmyelin_substrate
+    g = pmyelin_substrate(d, perm)
+    if rho:
+        g._rho_outer[:g.N_actual] = rho
+    return g
+
+
+def _pwalks(g, n, n_t, seed, want, T1=None):
+    wf = _waveform()
+    G, _ = core._waveform_arrays(wf, g)
+    G = G[:, :n_t]
+    S = g.sub_steps(wf.dt)
+    r0 = g.init_positions(n, 13)
+    gpu = core.run_walk(g, n_walkers=n, diffusivity=None, G=G, dt=wf.dt, sub_steps=S,
+                        phase_per_substep=True, seed=seed, T1=T1, r0=r0, want_positions=want,
+                        want_walker_signals=want, want_compartments=want)
+    ora = oracle_walk(g, G, wf.dt, S, True, n, seed=seed, r0=r0, want_walkers=want, T1=T1)
+    return r0, gpu, ora
+
+
+@pytest.mark.parametrize("perm", [False, True])
+def test_packed_myelin_short_walk_matches_oracle_walker_by_walker(cuda, perm):
+    g = _packed(perm)
+    r0, gpu, ora = _pwalks(g, 4096, 30, 7, True, T1=0.9)
+    pg = gpu.extras["pos"].cpu().numpy()
+    same = np.max(np.abs(pg - ora["pos"]), axis=1) < 1e-4 * 1e-6
+    assert same.mean() >= 0.97, f"only {same.mean():.3f} of walkers follow the oracle's walk"
+    np.testing.assert_array_equal(gpu.extras["comp_end"].cpu().numpy()[same],
+                                  g.to3(g.classify_position(ora["pos"]))[same])
+    np.testing.assert_allclose(gpu.extras["phi"].cpu().numpy()[same], ora["phi"][same],
+                               atol=1e-3, rtol=1e-4)
+    np.testing.assert_allclose(gpu.extras["log_w"].cpu().numpy()[same], ora["log_w"][same],
+                               rtol=1e-5, atol=1e-6)
+    if perm:
+        assert gpu.status["transmit"] > 0
+
+
+@pytest.mark.parametrize("perm,rho", [(False, 0.0), (True, 0.0), (False, 2e-5)])
+def test_packed_myelin_ensemble_matches_oracle(cuda, perm, rho):
+    """Whole echoes on the same stream, incl. surface relaxivity (sub-steps to the pore)."""
+    g = _packed(perm, rho)
+    n = 8192 if rho else 16384
+    r0, gpu, ora = _pwalks(g, n, 40 if rho else 120, 21, False)
+    myel = g.to3(g.classify_position(r0)) == 1
+    norm = n / float(np.sum(np.where(myel, g._myelin_proton_density, 1.0)))
+    sig = gpu.signal[0] * norm
+    se = np.sqrt(2.0) * gpu.stderr[0] * norm
+    z = (sig - ora["signal"][0]) / np.maximum(se, 1e-9)
+    assert np.max(np.abs(z)) < 4.0, z
+
+
+def test_packed_myelin_seeding_walls_and_b0_signal(cuda):
+    """Seeding by index range gives the reference's per-axon counts; impermeable walls keep the
+    compartments; at b = 0 the signal is the T2-weighted spin density."""
+    g = _packed(False)
+    wf = d.set_b(d.pgse(0.006, 0.02, 0.1, [[1, 0, 0]], 120), 0.0)
+    n = 20_000
+    s, pos, c0, c1 = d.simulate(n, None, wf, g, seed=3, return_positions=True,
+                                return_compartments="final")
+    n_in, n_my, n_ex = g.seed_counts(n)
+    np.testing.assert_array_equal(np.bincount(c0, minlength=3), [n_in.sum(), n_my.sum(), n_ex])
+    np.testing.assert_array_equal(c1, c0)
+    assert np.mean(g.to3(g.classify_position(pos)) == c1) > 0.999
+    L = g._L_float
+    assert np.all(np.abs(pos[:, :2]) <= 0.5 * L + 2 * float(np.max(g._outer_radii_np)))
+    n_t = wf.G.shape[1]
+    T2 = np.array([g._T2[c][0] for c in ("intra", "myelin", "extra")])
+    cnt = np.array([n_in.sum(), n_my.sum(), n_ex], float)
+    wts = np.array([1.0, g._myelin_proton_density, 1.0])
+    expect = np.sum(cnt * wts * np.exp(-n_t * wf.dt / T2)) / np.sum(cnt * wts)
+    np.testing.assert_allclose(s, expect, rtol=2e-5)
+    with pytest.raises(NotImplementedError):
+        d.simulate(n, None, wf, g, r0=np.zeros((n, 3)))

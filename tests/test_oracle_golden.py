@@ -167,6 +167,38 @@ def test_oracle_myelin_step_matches_reference(kat, tag, fp64):
         np.testing.assert_array_equal(dl, dref)
 
 
+@pytest.mark.parametrize("tag", ["perm", "refl"])
+@pytest.mark.parametrize("fp64", [False, True])
+def test_oracle_packed_myelin_step_matches_reference(kat, tag, fp64):
+    """make_packed_myelin_traj_step_fn (physics.py:682-976), one sub-step per case with the
+    direction and uniforms the reference drew, on five axons packed by this package's
+    pack_myelinated_cylinders (the reference's packer gave the same cell): FP32 bit for bit
+    (in-cell end point, compartment, boundary log-weight), FP64 to FP32 rounding."""
+    import dmipy_sim_gb300 as d
+    from golden.make_golden import pmyelin_substrate
+    g = O.geom_from(pmyelin_substrate(d, tag == "perm"), 1e-4)
+    k = f"pmy_{tag}"
+    r, comp, unit, u = kat[k + "_r"], kat[k + "_comp"], kat[k + "_unit"], kat[k + "_u"]
+    ref, cref, dref = kat[k + "_out"], kat[k + "_comp_out"], kat[k + "_dlog"]
+    out = np.zeros_like(ref)
+    co = np.zeros(len(r), int)
+    dl = np.zeros(len(r))
+    for i in range(len(r)):
+        out[i], co[i], dl[i] = O.pmyelin_plugin(g, r[i], unit[i], comp[i], u[i][0], u[i][1],
+                                                permeate=tag == "perm", fp64=fp64)
+    if tag == "perm":
+        assert np.sum(comp != cref) > 40            # transmissions are exercised
+    assert np.sum(comp == 0) > 100 and np.sum(dref != 0) > 50
+    if fp64:
+        ok = co == cref
+        assert ok.mean() > 0.98
+        assert np.mean(np.max(np.abs(out[ok] - ref[ok]), axis=1) < 1e-12) > 0.98
+    else:
+        np.testing.assert_array_equal(out, ref)
+        np.testing.assert_array_equal(co, cref)
+        np.testing.assert_array_equal(dl, dref)
+
+
 def _philox_py(seed, walker, stream, j):
     """Philox4x32-10 round function written out from the published description (Salmon et al.,
     SC'11), independent of the C and CUDA implementations."""
