@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
             ua = u01(rr.x);
             ub = u01(rr.y);
             up = u01(rr.z);
-            if constexpr (MYEL) up2 = u01(rr.w);
+            if constexpr (MYEL || PMYEL) up2 = u01(rr.w);  // the outer wall's own uniform
           } else {
             if ((s & 1u) == 0u) {
               rr = draw(a.seed, gw, 0u, s >> 1);

@@ -131,13 +131,14 @@ int or_pmyelin_plugin_f64(const or_geom* g, const double* r, const double* unit,
 /* A full walk in the geometry frame.  G is (n_t, n_meas, 3) float32, chi (n_t) or NULL, r0
    (n_walkers, 3) or NULL (seeded on the Philox seeding stream; a mesh needs r0).  sums (n_echo, n_meas, 3) is
    overwritten with sum w cos(phi), sum w sin(phi), sum (w cos(phi))^2.  final_pos (n, 3), log_w
-   (n), phi (n, n_meas) are optional.  n_threads <= 0 uses every core. */
+   (n), phi (n, n_meas) are optional.  n_threads <= 0 uses every core.  comp_end (n) is optional:
+   the walker's final compartment for the myelinated geometries (0 intra, 1 myelin, 2 extra). */
 int or_walk_f32(const or_geom* g, const or_walk_params* p, const float* G, const float* chi,
                 const float* r0, double* sums, float* final_pos, float* log_w, float* phi,
-                int n_threads);
+                int n_threads, int32_t* comp_end);
 int or_walk_f64(const or_geom* g, const or_walk_params* p, const float* G, const float* chi,
                 const float* r0, double* sums, float* final_pos, float* log_w, float* phi,
-                int n_threads);
+                int n_threads, int32_t* comp_end);
 
 /* Philox4x32-10 draw (for cross-checking the stream contract). */
 void or_philox(uint64_t seed, uint64_t walker, uint32_t stream, uint32_t j, uint32_t out[4]);

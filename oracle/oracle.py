@@ -83,7 +83,7 @@ def load():
             f = getattr(lib, "or_walk" + suf)
             f.restype = C.c_int
             f.argtypes = [C.POINTER(OrGeom), C.POINTER(OrWalk), C.c_void_p, C.c_void_p, C.c_void_p,
-                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         lib.or_philox.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
                                   C.POINTER(C.c_uint32)]
         for suf in ("_f32", "_f64"):
@@ -446,14 +446,18 @@ def walk(g, *, n_walkers, G, dt, sub_steps, phase_per_substep, seed, wall=REFLEC
     sums = np.zeros((len(echo), M, 3), dtype=np.float64)
     out = {"sums": sums}
     ptrs = [None, None, None]
+    comp_ptr = None
     if want_walkers:
         out["pos"] = np.zeros((n_walkers, 3), np.float32)
         out["log_w"] = np.zeros(n_walkers, np.float32)
         out["phi"] = np.zeros((n_walkers, M), np.float32)
+        out["comp"] = np.zeros(n_walkers, np.int32)
         ptrs = [out["pos"].ctypes.data, out["log_w"].ctypes.data, out["phi"].ctypes.data]
+        comp_ptr = out["comp"].ctypes.data
     f = lib.or_walk_f64 if fp64 else lib.or_walk_f32
     rc = f(C.byref(g), C.byref(p), Gt.ctypes.data, None if chi_a is None else chi_a.ctypes.data,
-           None if r0_a is None else r0_a.ctypes.data, sums.ctypes.data, *ptrs, int(n_threads))
+           None if r0_a is None else r0_a.ctypes.data, sums.ctypes.data, *ptrs, int(n_threads),
+           comp_ptr)
     if rc != 0:
         raise RuntimeError("oracle walk failed")
     norm = max(n_walkers, 1)
