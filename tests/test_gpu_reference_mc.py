@@ -16,11 +16,12 @@ N_GPU = 200_000
 def _gpu(cfg, n, seed):
     wf = build_waveform(d, cfg["wf"])
     g = build_geometry(d, tuple(cfg["geom"]))
-    if getattr(g, "_is_myelinated", False):
-        # through simulate(): the myelin step rule and the spin-weight normalisation
+    if getattr(g, "_is_myelinated", False) or getattr(g, "_is_packed_myelinated", False):
+        # through simulate(): the myelin step rules and the spin-weight normalisation
         s, c0, _, lw, phi = d.simulate(n, None, wf, g, seed=seed, return_compartments="final",
                                        return_walker_signals=True)
-        sw = np.asarray(g.water_fractions)[c0]
+        sw = (np.asarray(g.water_fractions)[c0] if hasattr(g, "water_fractions")
+              else np.where(c0 == 1, g._myelin_proton_density, 1.0))
         x = sw[:, None] * np.exp(lw)[:, None] * np.cos(phi) / sw.mean()
         return s, x.std(axis=0)
     G, chi = core._waveform_arrays(wf, g)
