@@ -23,6 +23,12 @@ WalkFn walk_fn_psph(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_mesh(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_myelin(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_pmyelin(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_box1d(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_slab(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_shell(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_box1d(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_slab(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_shell(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_sph(int wall, int pm, int width, bool tsm);
@@ -94,8 +100,14 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
       return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
   }
   const bool packed = g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  if (g->kind < 0 || g->kind > DMSIM_GEOM_PMYELIN)
+  if (g->kind < 0 || g->kind > DMSIM_GEOM_SHELL)
     return fail(DMSIM_EINVAL, "unsupported geometry kind %d", g->kind);
+  if ((g->kind == DMSIM_GEOM_BOX1D || g->kind == DMSIM_GEOM_SLAB) && !(g->L > 0.f))
+    return fail(DMSIM_EINVAL, "slab geometry needs its length L > 0");
+  if (g->kind == DMSIM_GEOM_BOX1D && g->wall_mode == DMSIM_WALL_PERMEATE)
+    return fail(DMSIM_EINVAL, "Box1D walls are not permeable");
+  if (g->kind == DMSIM_GEOM_SHELL && !(g->radius > 0.f && g->shell_r_out > g->radius))
+    return fail(DMSIM_EINVAL, "shell needs 0 < R_in < R_out");
   if (g->kind == DMSIM_GEOM_PMYELIN) {
     if (g->pmy_n < 1 || g->pmy_nmax < g->pmy_n || !g->pmy_cyl || !g->pmy_seed || !(g->L > 0.f))
       return fail(DMSIM_EINVAL, "packed myelinated cylinders need their axon and seeding tables");
@@ -183,6 +195,9 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
     case DMSIM_GEOM_PMYELIN:
       pl->fn = walk_fn_pmyelin(g->wall_mode, pl->pm, pl->width, false);
       break;
+    case DMSIM_GEOM_BOX1D: pl->fn = walk_fn_box1d(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_SLAB: pl->fn = walk_fn_slab(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_SHELL: pl->fn = walk_fn_shell(g->wall_mode, pl->pm, pl->width, false); break;
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
   pl->lay = walk_smem_layout(pl->pm, pl->width, p->n_meas);
@@ -414,6 +429,12 @@ __global__ void k_step_kat(const GeoK g, const MeshK mk, int64_t n, const float*
       z += sz;
     } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
       dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, sx, sy, sz, u, g, cs, cand, tl);
+    } else if constexpr (GEOM == DMSIM_GEOM_BOX1D) {
+      dl = box1d_step<WALL == 2 ? 0 : WALL>(x, y, z, sx, sy, sz, g);
+    } else if constexpr (GEOM == DMSIM_GEOM_SLAB) {
+      dl = slab_step<WALL>(x, y, z, sx, sy, sz, u, g, tl);
+    } else if constexpr (GEOM == DMSIM_GEOM_SHELL) {
+      dl = shell_step<WALL>(x, y, z, sx, sy, sz, u, g, tl);
     } else {
       if (mk.per[0]) { ix = (int)floorf((x - mk.vmin[0]) / mk.box[0]); x -= mk.box[0] * ix; }
       if (mk.per[1]) { iy = (int)floorf((y - mk.vmin[1]) / mk.box[1]); y -= mk.box[1] * iy; }
@@ -549,6 +570,9 @@ GeoK make_geok(const dmsim_geometry* g) {
   gk.n = packed ? g->grid_n : 1;
   gk.mi = packed ? (g->need_min_image != 0) : 0;
   gk.kmax = packed ? g->max_cell_cand : 0;
+  if (g->kind == DMSIM_GEOM_BOX1D || g->kind == DMSIM_GEOM_SLAB) gk.L = g->L;
+  gk.r_out = g->shell_r_out;
+  gk.cyl = g->shell_cyl ? 1 : 0;
   return gk;
 }
 
@@ -711,6 +735,9 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
     case DMSIM_GEOM_PACKED_CYLINDERS: fn = kat_fn<DMSIM_GEOM_PACKED_CYLINDERS>(g->wall_mode); break;
     case DMSIM_GEOM_PACKED_SPHERES: fn = kat_fn<DMSIM_GEOM_PACKED_SPHERES>(g->wall_mode); break;
     case DMSIM_GEOM_MESH: fn = kat_fn<DMSIM_GEOM_MESH>(g->wall_mode); break;
+    case DMSIM_GEOM_BOX1D: fn = kat_fn<DMSIM_GEOM_BOX1D>(g->wall_mode); break;
+    case DMSIM_GEOM_SLAB: fn = kat_fn<DMSIM_GEOM_SLAB>(g->wall_mode); break;
+    case DMSIM_GEOM_SHELL: fn = kat_fn<DMSIM_GEOM_SHELL>(g->wall_mode); break;
     default: return fail(DMSIM_EINVAL, "step_kat: unsupported geometry kind %d", g->kind);
   }
   if (n == 0) return DMSIM_OK;
@@ -847,6 +874,9 @@ WalkFn batch_fn(const dmsim_geometry* g, int width, bool tsm) {
     case DMSIM_GEOM_PACKED_CYLINDERS: return walk_batch_fn_pcyl(g->wall_mode, 1, width, tsm);
     case DMSIM_GEOM_PACKED_SPHERES: return walk_batch_fn_psph(g->wall_mode, 1, width, tsm);
     case DMSIM_GEOM_MESH: return walk_batch_fn_mesh(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_BOX1D: return walk_batch_fn_box1d(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_SLAB: return walk_batch_fn_slab(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_SHELL: return walk_batch_fn_shell(g->wall_mode, 1, width, false);
   }
   return nullptr;
 }

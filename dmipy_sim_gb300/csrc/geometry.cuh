@@ -48,6 +48,8 @@ struct GeoK {
   int n;   // cells per axis
   int mi;  // 1 when some cell lists two images of one object: candidates need the min-image test
   int kmax;  // most candidates any cell lists (0: unknown); 2 selects the two-slot scan
+  float r_out;  // shell: the reflecting outer wall
+  int cyl;      // shell: radii from the z axis (1) or the origin (0)
 };
 
 // Myelinated cylinder: two concentric walls (axis z) around three compartments.
@@ -243,6 +245,127 @@ __device__ __forceinline__ float pmyelin_step(float& x, float& y, float& z, int&
   comp = nc;
   const float t2 = nc == 0 ? m.t2dec[2] : (nc > m.nmax ? m.t2dec[1] : m.t2dec[0]);
   return m.rho * dlog - t2;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Validation slabs and shell (geometries.py:48-140, 3221-3431).
+// ------------------------------------------------------------------------------------------------
+// x mirrored into [0, L]: the floored modulo 2L, then the upper half folded back.
+__device__ __forceinline__ float fold_slab(float x, float L) {
+  const float L2 = 2.f * L;
+  float xf = fmodf(x, L2);
+  if (xf < 0.f) xf += L2;
+  return xf > L ? L2 - xf : xf;
+}
+
+// Box1D.reflect / reflect_with_log_weight (geometries.py:90-140): walls at x = 0 and L.
+template <int WALL>
+__device__ __forceinline__ float box1d_step(float& x, float& y, float& z, float sx, float sy,
+                                            float sz, const GeoK& g) {
+  const float xr = x + sx;
+  float dl = 0.f;
+  if constexpr (WALL == kRelax) {
+    const float dp = fmaxf(xr - g.L, 0.f) + fmaxf(-xr, 0.f);
+    dl = dp > 0.f ? -2.f * dp : 0.f;
+  }
+  x = fold_slab(xr, g.L);
+  y += sy;
+  z += sz;
+  return dl;
+}
+
+// PermeableSlab1D (geometries.py:3268-3300): membrane at x = L/2 (g.R), outer walls folded.
+template <int WALL>
+__device__ __forceinline__ float slab_step(float& x, float& y, float& z, float sx, float sy,
+                                           float sz, float u, const GeoK& g, Tally& tl) {
+  const float xm = g.R, xn = x + sx;
+  const bool crossed = (x - xm) * (xn - xm) < 0.f;
+  const float dp = crossed ? fabsf(xn - xm) : 0.f;
+  bool refl = crossed;
+  if constexpr (WALL == kPermeate) {
+    const bool transmit = crossed && (u < fminf(1.f, 2.f * g.kod * dp));
+    refl = crossed && !transmit;
+    if (transmit) ++tl.transmit;
+  }
+  x = fold_slab(refl ? 2.f * xm - xn : xn, g.L);
+  y += sy;
+  z += sz;
+  if constexpr (WALL == kRelax) return -2.f * dp;
+  return refl ? -2.f * dp : 0.f;
+}
+
+// PermeableShell._permeate_impl (geometries.py:3366-3425): the first crossing of the permeable
+// membrane R_in (g.R) or the reflecting wall R_out along the step, radii measured from the origin
+// (sphere) or the z axis (cylinder); a membrane hit transmits with p = min(1, 2 kappa/D d_perp),
+// d_perp = remaining * |d . n|; a reflection nudges the hit point onto its own side and flies
+// the rest along the mirrored direction; a walker past R_out is mirrored back.
+template <int WALL>
+__device__ __forceinline__ float shell_step(float& x, float& y, float& z, float sx, float sy,
+                                            float sz, float u, const GeoK& g, Tally& tl) {
+  const float r_out = g.r_out;
+  const int cyl = g.cyl;
+  const float Rin = g.R, EPS = g.eps, BIG = 1e30f;
+  const float sl = sqrtf(sx * sx + sy * sy + sz * sz);
+  const float inv = 1.f / fmaxf(sl, EPS);
+  const float dx = sx * inv, dy = sy * inv, dz = sz * inv;
+  const float cz = cyl ? 0.f : 1.f;  // radial subspace: drop z for a cylindrical shell
+  const float b = dx * x + dy * y + cz * dz * z;
+  const float r2 = x * x + y * y + cz * z * z;
+  const float dd2 = fmaxf(dx * dx + dy * dy + cz * dz * dz, EPS);
+  auto first_t = [&](float Rk) {
+    const float c = r2 - Rk * Rk;
+    const float disc = b * b - dd2 * c;
+    const float s = sqrtf(fmaxf(disc, 0.f));
+    float t1 = (-b - s) / dd2, t2 = (-b + s) / dd2;
+    t1 = (disc > 0.f && t1 > EPS && t1 < sl) ? t1 : BIG;
+    t2 = (disc > 0.f && t2 > EPS && t2 < sl) ? t2 : BIG;
+    return fminf(t1, t2);
+  };
+  const float t_in = first_t(Rin), t_out = first_t(r_out);
+  const bool hit_in = t_in < t_out;
+  const float t = fminf(t_in, t_out);
+  const bool any = t < 1e29f;
+  float dl = 0.f;
+  if (any) {
+    const float hx = x + t * dx, hy = y + t * dy, hz = z + t * dz;
+    const float nrm = sqrtf(hx * hx + hy * hy + cz * hz * hz);
+    const float ni = 1.f / fmaxf(nrm, EPS);
+    const float nx = hx * ni, ny = hy * ni, nz = cz * hz * ni;
+    const float rem = sl - t;
+    const float dn = dx * nx + dy * ny + dz * nz;
+    const float dperp = rem * fabsf(dn);
+    bool transmit = false;
+    if constexpr (WALL == kPermeate) transmit = hit_in && (u < fminf(1.f, 2.f * g.kod * dperp));
+    if (transmit) {
+      ++tl.transmit;
+      x += sx;
+      y += sy;
+      z += sz;
+    } else {
+      const float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny, rz = dz - 2.f * dn * nz;
+      const float Rk = hit_in ? Rin : r_out;
+      const float side = sqrtf(r2) < Rk ? -1.f : 1.f;
+      const float f = fmaxf(rem - g.nudge, 0.f);
+      x = hx + side * g.nudge * nx + rx * f;
+      y = hy + side * g.nudge * ny + ry * f;
+      z = hz + side * g.nudge * nz + rz * f;
+      if (hit_in) dl = -2.f * dperp;
+    }
+  } else {
+    x += sx;
+    y += sy;
+    z += sz;
+  }
+  const float ro = sqrtf(x * x + y * y + cz * z * z);
+  const float over = ro - r_out;
+  if (over > 0.f) {  // never outside the reflecting wall
+    const float s = 2.f * over / fmaxf(ro, EPS);
+    x -= s * x;
+    y -= s * y;
+    z -= s * cz * z;
+    ++tl.clamp;
+  }
+  return dl;
 }
 
 // ------------------------------------------------------------------------------------------------

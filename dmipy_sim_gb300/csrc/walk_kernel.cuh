@@ -171,6 +171,10 @@ __device__ __forceinline__ int classify(float x, float y, float z, const GeoK& g
     return (x * x + y * y < g.R2) ? 0 : 1;  // geometries.py:803-813
   } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
     return (x * x + y * y + z * z < g.R2) ? 0 : 1;  // geometries.py:161-165
+  } else if constexpr (GEOM == DMSIM_GEOM_SLAB) {
+    return x < g.R ? 0 : 1;  // geometries.py:3262-3263
+  } else if constexpr (GEOM == DMSIM_GEOM_SHELL) {
+    return sqrtf(x * x + y * y + (g.cyl ? 0.f : z * z)) < g.R ? 0 : 1;  // geometries.py:3362-3364
   } else if constexpr (GEOM == DMSIM_GEOM_PACKED_CYLINDERS || GEOM == DMSIM_GEOM_PACKED_SPHERES) {
     // 0 = extra, k+1 = inside object k; the largest id wins (geometries.py:2185-2214)
     constexpr bool P3 = GEOM == DMSIM_GEOM_PACKED_SPHERES;
@@ -410,7 +414,24 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
       for (uint32_t j = 0; j < 256u && !ok; ++j) {
         const u32x4 r = draw(a.seed, gw, 1u, j);
         const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z), u3 = u01(r.w);
-        if constexpr (PMYEL) {
+        if constexpr (GEOM == DMSIM_GEOM_BOX1D || GEOM == DMSIM_GEOM_SLAB) {
+          // x uniform over the slab (Box1D) or its first half (the permeable slab starts every
+          // walker in compartment A), y = z = 0 (geometries.py:84-88, 3257-3261)
+          x = (GEOM == DMSIM_GEOM_BOX1D ? g.L : g.R) * u0;
+          ok = true;
+        } else if constexpr (GEOM == DMSIM_GEOM_SHELL) {
+          // uniform in compartment A (r < R_in); a cylindrical shell also spreads z over
+          // [0, R_in) (geometries.py:3343-3358)
+          const float px = g.R * (2.f * u0 - 1.f), py = g.R * (2.f * u1 - 1.f);
+          const float pz = g.R * (2.f * u2 - 1.f);
+          const float q = px * px + py * py + (g.cyl ? 0.f : pz * pz);
+          if (q < g.R2) {
+            x = px;
+            y = py;
+            z = g.cyl ? g.R * u3 : pz;
+            ok = true;
+          }
+        } else if constexpr (PMYEL) {
           const PMyelinK& m = a.pm;
           for (int h = 0; h < 2 && !ok; ++h) {
             const float v0 = h ? u2 : u0, v1 = h ? u3 : u1;
@@ -588,6 +609,12 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
             dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
+          } else if constexpr (GEOM == DMSIM_GEOM_BOX1D) {
+            dl = box1d_step<WALL == kPermeate ? kReflect : WALL>(x, y, z, stx, sty, stz, g);
+          } else if constexpr (GEOM == DMSIM_GEOM_SLAB) {
+            dl = slab_step<WALL>(x, y, z, stx, sty, stz, up, g, tw);
+          } else if constexpr (GEOM == DMSIM_GEOM_SHELL) {
+            dl = shell_step<WALL>(x, y, z, stx, sty, stz, up, g, tw);
           } else if constexpr (MYEL) {
             dl = myelin_step<WALL>(x, y, z, mcomp, stx, sty, stz, up, up2, a.my, tw);
           } else if constexpr (PMYEL) {

@@ -16,7 +16,8 @@ import torch
 from . import _lib
 
 __all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "MyelinatedCylinder",
-           "PackedMyelinatedCylinders", "pack_myelinated_cylinders",
+           "PackedMyelinatedCylinders", "pack_myelinated_cylinders", "Box1D", "PermeableSlab1D",
+           "PermeableShell",
            "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres",
            "lattice_cylinders"]
 
@@ -173,6 +174,132 @@ class Cylinder(Geometry):
         g.radius = self.radius
         g.eps_detect = np.float32(1e-7 * self.radius)
         g.nudge = np.float32(1e-4 * self.radius)
+        return g, ()
+
+
+class Box1D(Geometry):
+    """1-D reflecting slab, walls at x = 0 and x = length, free along y and z
+    (geometries.py:48-140); surface relaxivity weights each wall overshoot."""
+
+    def __init__(self, length, surface_relaxivity_t2=None):
+        self.length = float(length)
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+
+    def volume(self):
+        return self.length
+
+    def surface_area(self):
+        return 2.0
+
+    def classify_position(self, r):
+        return np.zeros(np.shape(r)[:-1], dtype=np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        x = _host_rng(key).uniform(0.0, self.length, n_walkers)
+        return np.stack([x, np.zeros(n_walkers), np.zeros(n_walkers)], 1).astype(np.float32)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        g = self._base_desc(_lib.GEOM_BOX1D, wall_mode, rho_over_D, 0.0)
+        g.L = np.float32(self.length)
+        return g, ()
+
+
+class PermeableSlab1D(Geometry):
+    """Closed two-compartment slab: a permeable membrane at x = length/2 between reflecting
+    walls at 0 and length (geometries.py:3221-3300); every walker starts in compartment A
+    (x < length/2), so f_A(t) = 1/2 + 1/2 exp(-4 kappa t / length)."""
+
+    def __init__(self, length, permeability, surface_relaxivity_t2=None):
+        self.length = float(length)
+        self.permeability = float(permeability)
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+        self.radius = float(length) / 2.0
+
+    def volume(self):
+        return self.length / 2.0
+
+    def surface_area(self):
+        return 1.0
+
+    def classify_position(self, r):
+        r = np.asarray(r, dtype=np.float32)
+        return np.where(r[..., 0] < np.float32(self.length / 2.0), 0, 1).astype(np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        x = _host_rng(key).uniform(0.0, self.length / 2.0, n_walkers)
+        return np.stack([x, np.zeros(n_walkers), np.zeros(n_walkers)], 1).astype(np.float32)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        g = self._base_desc(_lib.GEOM_SLAB, wall_mode, rho_over_D, kappa_over_D)
+        g.L = np.float32(self.length)
+        g.radius = np.float32(self.length / 2.0)
+        return g, ()
+
+
+class PermeableShell(Geometry):
+    """Closed radial two-compartment shell: a permeable membrane at r = r_inner inside a
+    reflecting wall at r = r_outer (geometries.py:3303-3431); ``kind='sphere'`` measures r from the
+    origin, ``'cylinder'`` from the axis along ``orientation`` (walked in the axis frame)."""
+
+    def __init__(self, r_inner, r_outer, permeability, kind="sphere", orientation=(0.0, 0.0, 1.0),
+                 surface_relaxivity_t2=None):
+        if kind not in ("sphere", "cylinder"):
+            raise ValueError("kind must be 'sphere' or 'cylinder'")
+        self.r_inner, self.r_outer = float(r_inner), float(r_outer)
+        self.permeability = float(permeability)
+        self.kind = kind
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+        self.radius = float(r_inner)
+        o = np.asarray(orientation, dtype=np.float64)
+        self._o = o / np.linalg.norm(o)
+        R = _rotation_to_z(self._o)
+        self._R = R.astype(np.float32)
+        self._is_identity_rotation = kind == "sphere" or bool(np.allclose(R, np.eye(3)))
+
+    def _frame(self):
+        return None if self._is_identity_rotation else self._R.astype(np.float64)
+
+    def _radial(self, r):
+        r = np.asarray(r, dtype=np.float64)
+        if self.kind == "sphere":
+            return r
+        return r - (r @ self._o)[..., None] * self._o
+
+    def volume(self):
+        if self.kind == "sphere":
+            return (4.0 / 3.0) * np.pi * self.r_inner ** 3
+        return np.pi * self.r_inner ** 2
+
+    def surface_area(self):
+        if self.kind == "sphere":
+            return 4.0 * np.pi * self.r_inner ** 2
+        return 2.0 * np.pi * self.r_inner
+
+    def classify_position(self, r):
+        rad = np.linalg.norm(self._radial(r), axis=-1)
+        return np.where(rad < self.r_inner, 0, 1).astype(np.int32)
+
+    def init_positions(self, n_walkers, key=None):
+        """Uniform in compartment A; a cylindrical shell spreads the axial coordinate over
+        [0, r_inner) (geometries.py:3343-3358)."""
+        rng = _host_rng(key)
+        v = rng.normal(size=(n_walkers, 3))
+        if self.kind == "cylinder":
+            v -= (v @ self._o)[:, None] * self._o
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        dim = 3.0 if self.kind == "sphere" else 2.0
+        pos = v * (rng.uniform(size=n_walkers) ** (1.0 / dim) * self.r_inner)[:, None]
+        if self.kind == "cylinder":
+            pos += (rng.uniform(size=n_walkers) * self.r_inner)[:, None] * self._o
+        return pos.astype(np.float32)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        g = self._base_desc(_lib.GEOM_SHELL, wall_mode, rho_over_D, kappa_over_D)
+        g.radius = self.r_inner
+        g.shell_r_out = self.r_outer
+        g.shell_cyl = 1 if self.kind == "cylinder" else 0
+        g.eps_detect = np.float32(1e-7 * self.r_inner)
+        g.nudge = np.float32(1e-4 * self.r_inner)
         return g, ()
 
 

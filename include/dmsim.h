@@ -62,7 +62,10 @@ enum dmsim_geom_kind {
   DMSIM_GEOM_PACKED_SPHERES = 4,   /* geometries.py:2343-2786, periodic cubic cell             */
   DMSIM_GEOM_MESH = 5,             /* mesh.py:257-907                                          */
   DMSIM_GEOM_MYELIN = 6,           /* geometries.py:847-1134 + physics.py:420-680, axis frame z */
-  DMSIM_GEOM_PMYELIN = 7           /* geometries.py:2860-3218 + physics.py:682-1062, periodic   */
+  DMSIM_GEOM_PMYELIN = 7,          /* geometries.py:2860-3218 + physics.py:682-1062, periodic   */
+  DMSIM_GEOM_BOX1D = 8,            /* geometries.py:48-140, walls at x = 0 and x = L           */
+  DMSIM_GEOM_SLAB = 9,             /* geometries.py:3221-3300, membrane at x = L/2 in [0, L]   */
+  DMSIM_GEOM_SHELL = 10            /* geometries.py:3303-3431, membrane R_in, wall R_out       */
 };
 
 enum dmsim_wall_mode {
@@ -167,6 +170,12 @@ typedef struct dmsim_geometry {
   float pmy_rho_over_D;        /* surface relaxivity rho / D_ref (0: none)                     */
   float pmy_logw_myelin;       /* log of the myelin water proton density (spin weight)          */
   float pmy_pad;
+
+  /* the validation slabs and shell: Box1D and PermeableSlab1D use L (slab length); the shell
+     uses radius (R_in, the permeable membrane), shell_r_out (the reflecting outer wall) and
+     shell_cyl (1: radii measured from the frame z axis, 0: from the origin) */
+  float shell_r_out;
+  int32_t shell_cyl;
 } dmsim_geometry;
 
 /* ---- walk parameters -------------------------------------------------------------------------- */

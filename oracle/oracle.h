@@ -15,6 +15,9 @@
  *   Mesh reflect / reflect_with_log_weight / permeate     mesh.py:637-671, 673-705, 707-743
  *   MyelinatedCylinder step (own walk rule)               physics.py:506-677
  *   PackedMyelinatedCylinders step + fused weights         physics.py:742-930, 1034-1056
+ *   Box1D reflect / reflect_with_log_weight               geometries.py:90-140
+ *   PermeableSlab1D reflect / rwlw / permeate             geometries.py:3270-3300
+ *   PermeableShell permeate / reflect                     geometries.py:3366-3431
  *     (wrap 203-206, 27-cell gather 208-215, Moller-Trumbore 561-569, bounce 599-635,
  *      nearest-centroid classification 227-254, leak guard 578-597)
  *   ensemble Re<w e^{i phi}>                              core.py:426-429; replay FP64 phase
@@ -33,7 +36,7 @@ extern "C" {
 #endif
 
 enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4,
-       OR_MESH = 5, OR_MYELIN = 6, OR_PMYELIN = 7 };
+       OR_MESH = 5, OR_MYELIN = 6, OR_PMYELIN = 7, OR_BOX1D = 8, OR_SLAB = 9, OR_SHELL = 10 };
 enum { OR_REFLECT = 0, OR_RELAX = 1, OR_PERMEATE = 2 };
 
 /* A triangle mesh as the reference's Mesh holds it (mesh.py:311-546): every triangle including the
@@ -89,6 +92,9 @@ typedef struct {
   const or_mesh* mesh;   /* OR_MESH only */
   const or_myelin* myelin; /* OR_MYELIN only */
   const or_pmyelin* pmyelin; /* OR_PMYELIN only */
+  double r_out;   /* OR_SHELL: the reflecting outer wall (radius = the permeable membrane) */
+  int32_t cyl;    /* OR_SHELL: radii from the frame z axis (1) or the origin (0) */
+  int32_t pad2;
 } or_geom;
 
 typedef struct {

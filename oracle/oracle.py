@@ -14,7 +14,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 
-FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH, MYELIN, PMYELIN = range(8)
+(FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH, MYELIN, PMYELIN, BOX1D, SLAB,
+ SHELL) = range(11)
 REFLECT, RELAX, PERMEATE = range(3)
 
 
@@ -46,7 +47,8 @@ class OrGeom(C.Structure):
     _fields_ = [("kind", C.c_int32), ("n_objects", C.c_int32), ("radius", C.c_double),
                 ("L", C.c_double), ("rmin", C.c_double), ("objects", C.c_void_p),
                 ("rot", C.c_double * 9), ("rot_identity", C.c_int32), ("pad", C.c_int32),
-                ("mesh", C.c_void_p), ("myelin", C.c_void_p), ("pmyelin", C.c_void_p)]
+                ("mesh", C.c_void_p), ("myelin", C.c_void_p), ("pmyelin", C.c_void_p),
+                ("r_out", C.c_double), ("cyl", C.c_int32), ("pad2", C.c_int32)]
 
 
 class OrWalk(C.Structure):
@@ -323,6 +325,22 @@ def pmyelin_plugin(g, r, unit, comp, u1=0.0, u2=0.0, permeate=False, fp64=False)
     return np.array(ro[:]), co.value, dl.value
 
 
+def slab_geom(kind, length):
+    """Oracle Box1D (``kind`` BOX1D) or permeable slab (SLAB, membrane at length/2)."""
+    g = geom(kind, L=float(np.float32(length)))
+    g.radius = float(np.float32(length / 2.0))
+    return g
+
+
+def shell_geom(r_inner, r_outer, cylinder=False):
+    """Oracle permeable shell (membrane r_inner, reflecting wall r_outer), in the frame whose z
+    axis is the cylinder's."""
+    g = geom(SHELL, radius=float(np.float32(r_inner)))
+    g.r_out = float(np.float32(r_outer))
+    g.cyl = int(bool(cylinder))
+    return g
+
+
 def geom_from(geometry, dt=None):
     """Oracle geometry of a dmipy_sim_gb300 geometry object (walk frame)."""
     name = type(geometry).__name__
@@ -341,6 +359,12 @@ def geom_from(geometry, dt=None):
         kind = PACKED_CYLINDERS if name == "PackedCylinders" else PACKED_SPHERES
         return geom(kind, L=np.float32(geometry._L_float), objects=objs,
                     rot=getattr(geometry, "_R", None))
+    if name == "Box1D":
+        return slab_geom(BOX1D, geometry.length)
+    if name == "PermeableSlab1D":
+        return slab_geom(SLAB, geometry.length)
+    if name == "PermeableShell":
+        return shell_geom(geometry.r_inner, geometry.r_outer, geometry.kind == "cylinder")
     if name == "PackedMyelinatedCylinders":
         if dt is None:
             raise ValueError("the oracle's packed myelin needs the walk's sub-step")

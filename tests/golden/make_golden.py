@@ -457,13 +457,64 @@ def _pmyelin_cases(m, rng, out):
         rnd.normal, rnd.uniform = real_normal, real_uniform
 
 
+def _validation_geom_cases(m, rng, out):
+    """Box1D, PermeableSlab1D and PermeableShell (sphere and cylinder) plug-in calls of the
+    reference (geometries.py:48-140, 3221-3431): reflect, reflect_with_log_weight where defined,
+    permeate with recorded uniforms."""
+    geo = m["geometries"]
+    n = 256
+    L = 6e-6
+    rho, kappa = 500.0, 5000.0
+
+    def run(tag, g, mode, rs, st, us):
+        ro = np.zeros((n, 3))
+        dl = np.zeros(n)
+        for i in range(n):
+            if mode == "reflect":
+                o, dd = g.reflect(rs[i], st[i]), 0.0
+            elif mode == "relax":
+                o, dd = g.reflect_with_log_weight(rs[i], st[i], np.float32(rho))
+            else:
+                o, dd = g.permeate(rs[i], st[i], np.float32(kappa), np.float32(rho),
+                                   jaxstub.Injected(us[i]))
+            ro[i] = np.asarray(o, np.float64)
+            dl[i] = float(dd)
+        key = f"pl_{tag}_{mode}"
+        out[key + "_r"], out[key + "_step"], out[key + "_u"] = rs, st, us
+        out[key + "_out"], out[key + "_dlog"] = ro, dl
+
+    us = rng.uniform(0, 1, n).astype(np.float32)
+    # slabs: x spread over the slab and a little beyond each wall's reach, steps up to 0.4 L
+    rs = np.stack([rng.uniform(0, L, n), rng.normal(0, 1e-6, n), rng.normal(0, 1e-6, n)],
+                  1).astype(np.float32)
+    st = (_unit(rng, n) * rng.uniform(0.02, 0.4, (n, 1)) * L).astype(np.float32)
+    box = geo.Box1D(L)
+    run("box", box, "reflect", rs, st, us)
+    run("box", box, "relax", rs, st, us)
+    slab = geo.PermeableSlab1D(L, permeability=1e-5)
+    for mode in ("reflect", "relax", "perm"):
+        run("slab", slab, mode, rs, st, us)
+    for kind, tag in (("sphere", "shs"), ("cylinder", "shc")):
+        sh = geo.PermeableShell(2e-6, 4e-6, permeability=1e-5, kind=kind)
+        d = _unit(rng, n)
+        rad = rng.uniform(0.2, 1.0, n) * 4e-6
+        rs = (d * rad[:, None]).astype(np.float32)
+        if kind == "cylinder":
+            rs[:, 2] = rng.uniform(-3e-6, 3e-6, n)
+        st = (_unit(rng, n) * rng.uniform(0.05, 0.6, (n, 1)) * 2e-6).astype(np.float32)
+        run(tag, sh, "reflect", rs, st, us)
+        run(tag, sh, "perm", rs, st, us)
+
+
 def make_myelin_kat(root):
     """Add the myelinated-cylinder step known answers to kat.npz."""
     m = _ref(root)
     path = HERE / "kat.npz"
-    out = {k: v for k, v in np.load(path).items() if not k.startswith(("my_", "pmy_"))}
+    out = {k: v for k, v in np.load(path).items()
+           if not k.startswith(("my_", "pmy_", "pl_box_", "pl_slab_", "pl_shs_", "pl_shc_"))}
     _myelin_cases(m, np.random.default_rng(17), out)
     _pmyelin_cases(m, np.random.default_rng(23), out)
+    _validation_geom_cases(m, np.random.default_rng(29), out)
     np.savez_compressed(path, **out)
     print(f"kat.npz: {len(out)} arrays")
 

@@ -199,6 +199,42 @@ def test_oracle_packed_myelin_step_matches_reference(kat, tag, fp64):
         np.testing.assert_array_equal(dl, dref)
 
 
+VALIDATION_CASES = [("box", "reflect"), ("box", "relax"), ("slab", "reflect"), ("slab", "relax"),
+                    ("slab", "perm"), ("shs", "reflect"), ("shs", "perm"), ("shc", "reflect"),
+                    ("shc", "perm")]
+
+
+def _validation_geom(tag):
+    L = 6e-6
+    if tag == "box":
+        return O.slab_geom(O.BOX1D, L)
+    if tag == "slab":
+        return O.slab_geom(O.SLAB, L)
+    return O.shell_geom(2e-6, 4e-6, cylinder=tag == "shc")
+
+
+@pytest.mark.parametrize("tag,mode", VALIDATION_CASES)
+def test_oracle_validation_geometries_match_reference(kat, tag, mode):
+    """Box1D, PermeableSlab1D, PermeableShell (sphere, cylinder) plug-in calls of the reference:
+    end points to the last bit or one ulp, log-weights of the weighted modes to FP32 rounding."""
+    g = _validation_geom(tag)
+    wall = {"reflect": O.REFLECT, "relax": O.RELAX, "perm": O.PERMEATE}[mode]
+    k = f"pl_{tag}_{mode}"
+    r, st, u, ref, dref = kat[k + "_r"], kat[k + "_step"], kat[k + "_u"], kat[k + "_out"], \
+        kat[k + "_dlog"]
+    out = np.zeros_like(ref)
+    dl = np.zeros(len(r))
+    for i in range(len(r)):
+        out[i], dl[i] = O.plugin(g, wall, r[i], st[i], float(np.float32(500.0)),
+                                 float(np.float32(5000.0)), float(u[i]))
+    scale = np.maximum(np.max(np.abs(ref), axis=1), 1e-6)
+    assert np.all(np.max(np.abs(out - ref), axis=1) <= 2e-7 * scale)
+    assert np.mean(np.all(out == ref, axis=1)) > 0.9
+    if mode != "reflect":
+        assert np.mean(dref != 0) > 0.05
+        np.testing.assert_allclose(dl, dref, rtol=1e-5, atol=1e-9)
+
+
 def _philox_py(seed, walker, stream, j):
     """Philox4x32-10 round function written out from the published description (Salmon et al.,
     SC'11), independent of the C and CUDA implementations."""
