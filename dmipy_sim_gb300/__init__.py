@@ -10,7 +10,7 @@ from .waveforms import (Waveform, pgse, pgste, ogse, cpmg, calc_b, calc_btensor,
                         btensor_invariants, ste, pte)
 from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, MyelinatedCylinder,
                          PackedMyelinatedCylinders, pack_myelinated_cylinders, Box1D,
-                         PermeableSlab1D, PermeableShell, pack_cylinders,
+                         PermeableSlab1D, PermeableShell, Ellipsoid, pack_cylinders,
                          PackedCylinders, pack_spheres, PackedSpheres, lattice_cylinders)
 from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
@@ -30,7 +30,8 @@ __all__ = [
     "calc_btensor", "set_b", "rotate_waveform", "tile_waveform", "trapezoidal_ogse",
     "b_trapezoidal_ogse", "btensor_invariants", "ste", "pte", "Geometry", "FreeDiffusion",
     "Cylinder", "Sphere", "MyelinatedCylinder", "PackedMyelinatedCylinders",
-    "pack_myelinated_cylinders", "Box1D", "PermeableSlab1D", "PermeableShell", "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
+    "pack_myelinated_cylinders", "Box1D", "PermeableSlab1D", "PermeableShell", "Ellipsoid",
+    "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
     "simulate", "simulate_cpmg", "simulate_trajectories", "trajectories", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
     "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",

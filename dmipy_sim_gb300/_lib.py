@@ -17,7 +17,7 @@ DMSIM_ABI_VERSION = 6
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
- GEOM_MYELIN, GEOM_PMYELIN, GEOM_BOX1D, GEOM_SLAB, GEOM_SHELL) = range(11)
+ GEOM_MYELIN, GEOM_PMYELIN, GEOM_BOX1D, GEOM_SLAB, GEOM_SHELL, GEOM_ELLIPSOID) = range(12)
 WALL_REFLECT, WALL_RELAX, WALL_PERMEATE = range(3)
 
 STATUS_NAMES = ("nonfinite", "clamped", "init_fail", "bounce_budget", "escape_reject",
@@ -62,6 +62,7 @@ class Geometry(C.Structure):
         ("pmy_seed", C.c_void_p), ("pmy_t2dec", C.c_float * 3), ("pmy_rho_over_D", C.c_float),
         ("pmy_logw_myelin", C.c_float), ("pmy_pad", C.c_float),
         ("shell_r_out", C.c_float), ("shell_cyl", C.c_int32),
+        ("ell_inv2", C.c_float * 3), ("ell_pad", C.c_float),
     ]
 
 

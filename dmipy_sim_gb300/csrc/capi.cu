@@ -29,6 +29,8 @@ WalkFn walk_fn_shell(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_box1d(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_slab(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_shell(int wall, int pm, int width, bool tsm);
+WalkFn walk_fn_ellipsoid(int wall, int pm, int width, bool tsm);
+WalkFn walk_batch_fn_ellipsoid(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_sph(int wall, int pm, int width, bool tsm);
@@ -100,8 +102,11 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
       return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
   }
   const bool packed = g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
-  if (g->kind < 0 || g->kind > DMSIM_GEOM_SHELL)
+  if (g->kind < 0 || g->kind > DMSIM_GEOM_ELLIPSOID)
     return fail(DMSIM_EINVAL, "unsupported geometry kind %d", g->kind);
+  if (g->kind == DMSIM_GEOM_ELLIPSOID &&
+      !(g->radius > 0.f && g->ell_inv2[0] > 0.f && g->ell_inv2[1] > 0.f && g->ell_inv2[2] > 0.f))
+    return fail(DMSIM_EINVAL, "ellipsoid needs positive semi-axes");
   if ((g->kind == DMSIM_GEOM_BOX1D || g->kind == DMSIM_GEOM_SLAB) && !(g->L > 0.f))
     return fail(DMSIM_EINVAL, "slab geometry needs its length L > 0");
   if (g->kind == DMSIM_GEOM_BOX1D && g->wall_mode == DMSIM_WALL_PERMEATE)
@@ -198,6 +203,9 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
     case DMSIM_GEOM_BOX1D: pl->fn = walk_fn_box1d(g->wall_mode, pl->pm, pl->width, false); break;
     case DMSIM_GEOM_SLAB: pl->fn = walk_fn_slab(g->wall_mode, pl->pm, pl->width, false); break;
     case DMSIM_GEOM_SHELL: pl->fn = walk_fn_shell(g->wall_mode, pl->pm, pl->width, false); break;
+    case DMSIM_GEOM_ELLIPSOID:
+      pl->fn = walk_fn_ellipsoid(g->wall_mode, pl->pm, pl->width, false);
+      break;
   }
   if (!pl->fn) return fail(DMSIM_EINVAL, "no kernel for this geometry/wall combination");
   pl->lay = walk_smem_layout(pl->pm, pl->width, p->n_meas);
@@ -429,6 +437,8 @@ __global__ void k_step_kat(const GeoK g, const MeshK mk, int64_t n, const float*
       z += sz;
     } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
       dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, sx, sy, sz, u, g, cs, cand, tl);
+    } else if constexpr (GEOM == DMSIM_GEOM_ELLIPSOID) {
+      dl = ellipsoid_step<WALL>(x, y, z, sx, sy, sz, u, g, tl);
     } else if constexpr (GEOM == DMSIM_GEOM_BOX1D) {
       dl = box1d_step<WALL == 2 ? 0 : WALL>(x, y, z, sx, sy, sz, g);
     } else if constexpr (GEOM == DMSIM_GEOM_SLAB) {
@@ -573,6 +583,7 @@ GeoK make_geok(const dmsim_geometry* g) {
   if (g->kind == DMSIM_GEOM_BOX1D || g->kind == DMSIM_GEOM_SLAB) gk.L = g->L;
   gk.r_out = g->shell_r_out;
   gk.cyl = g->shell_cyl ? 1 : 0;
+  for (int a = 0; a < 3; ++a) gk.e2[a] = g->ell_inv2[a];
   return gk;
 }
 
@@ -738,6 +749,7 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
     case DMSIM_GEOM_BOX1D: fn = kat_fn<DMSIM_GEOM_BOX1D>(g->wall_mode); break;
     case DMSIM_GEOM_SLAB: fn = kat_fn<DMSIM_GEOM_SLAB>(g->wall_mode); break;
     case DMSIM_GEOM_SHELL: fn = kat_fn<DMSIM_GEOM_SHELL>(g->wall_mode); break;
+    case DMSIM_GEOM_ELLIPSOID: fn = kat_fn<DMSIM_GEOM_ELLIPSOID>(g->wall_mode); break;
     default: return fail(DMSIM_EINVAL, "step_kat: unsupported geometry kind %d", g->kind);
   }
   if (n == 0) return DMSIM_OK;
@@ -877,6 +889,7 @@ WalkFn batch_fn(const dmsim_geometry* g, int width, bool tsm) {
     case DMSIM_GEOM_BOX1D: return walk_batch_fn_box1d(g->wall_mode, 1, width, false);
     case DMSIM_GEOM_SLAB: return walk_batch_fn_slab(g->wall_mode, 1, width, false);
     case DMSIM_GEOM_SHELL: return walk_batch_fn_shell(g->wall_mode, 1, width, false);
+    case DMSIM_GEOM_ELLIPSOID: return walk_batch_fn_ellipsoid(g->wall_mode, 1, width, false);
   }
   return nullptr;
 }

@@ -20,6 +20,7 @@ KINDS = [  # (file stem, enum, wall modes, has a cell list, has batched variants
     ("box1d", "DMSIM_GEOM_BOX1D", [0, 1], False, True),
     ("slab", "DMSIM_GEOM_SLAB", [0, 1, 2], False, True),
     ("shell", "DMSIM_GEOM_SHELL", [0, 2], False, True),
+    ("ellipsoid", "DMSIM_GEOM_ELLIPSOID", [0, 1, 2], False, True),
 ]
 VARIANTS = [(0, 16), (0, 32), (0, 64), (1, 2), (1, 4), (1, 8)]  # (phase form, width)
 

@@ -50,6 +50,7 @@ struct GeoK {
   int kmax;  // most candidates any cell lists (0: unknown); 2 selects the two-slot scan
   float r_out;  // shell: the reflecting outer wall
   int cyl;      // shell: radii from the z axis (1) or the origin (0)
+  float e2[3];  // ellipsoid: 1 / semi-axis^2
 };
 
 // Myelinated cylinder: two concentric walls (axis z) around three compartments.
@@ -366,6 +367,102 @@ __device__ __forceinline__ float shell_step(float& x, float& y, float& z, float 
     ++tl.clamp;
   }
   return dl;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Axis-aligned ellipsoid at the origin (geometries.py:1137-1427): reflect /
+// reflect_with_log_weight with up to 10 specular bounces on the quadratic
+// A t^2 + 2 B t + C = 0 (A = d.D.d, B = r.D.d, C = r.D.r - 1, D = diag(1/a^2, 1/b^2, 1/c^2)), the
+// outward normal along D r, the nudge inwards, and the clamp to the scaled surface; permeate with
+// one Powles decision on the inside or outside root.  g.R = the smallest semi-axis.
+// ------------------------------------------------------------------------------------------------
+template <int WALL>
+__device__ __forceinline__ float ellipsoid_step(float& x, float& y, float& z, float sx, float sy,
+                                                float sz, float u, const GeoK& g, Tally& tl) {
+  const float ea = g.e2[0], eb = g.e2[1], ec = g.e2[2];
+  const float l = sqrtf(sx * sx + sy * sy + sz * sz);
+  float dx = sx / l, dy = sy / l, dz = sz / l;
+  if constexpr (WALL != kPermeate) {
+    float rx = x, ry = y, rz = z, rem = l, dsum = 0.f;
+#pragma unroll 1
+    for (int it = 0; it < 10; ++it) {
+      const float A = dx * ea * dx + dy * eb * dy + dz * ec * dz;
+      const float B = rx * ea * dx + ry * eb * dy + rz * ec * dz;
+      const float C = (rx * ea * rx + ry * eb * ry + rz * ec * rz) - 1.f;
+      const float disc = fmaxf(B * B - A * C, 0.f);
+      const float d = (-B + sqrtf(disc)) / A;
+      if (!(d > g.eps && d < rem)) break;
+      const float hx = rx + d * dx, hy = ry + d * dy, hz = rz + d * dz;
+      float nx = hx * ea, ny = hy * eb, nz = hz * ec;
+      const float nn = sqrtf(nx * nx + ny * ny + nz * nz);
+      nx /= nn;
+      ny /= nn;
+      nz /= nn;
+      const float dn = dx * nx + dy * ny + dz * nz;
+      float qx = dx - 2.f * dn * nx, qy = dy - 2.f * dn * ny, qz = dz - 2.f * dn * nz;
+      const float qn = sqrtf(qx * qx + qy * qy + qz * qz);
+      if constexpr (WALL == kRelax) dsum += (rem - d) * dn;
+      rx = hx - g.nudge * nx;
+      ry = hy - g.nudge * ny;
+      rz = hz - g.nudge * nz;
+      dx = qx / qn;
+      dy = qy / qn;
+      dz = qz / qn;
+      rem = rem - d - g.nudge;
+    }
+    const float f = fmaxf(rem, 0.f);
+    x = rx + dx * f;
+    y = ry + dy * f;
+    z = rz + dz * f;
+    const float q = sqrtf(x * x * ea + y * y * eb + z * z * ec);
+    if (q >= 1.f) {
+      const float s = (1.f - g.nudge / g.R) / q;
+      x *= s;
+      y *= s;
+      z *= s;
+      ++tl.clamp;
+    }
+    return -2.f * dsum;
+  } else {
+    const float A = dx * ea * dx + dy * eb * dy + dz * ec * dz;
+    const float B = x * ea * dx + y * eb * dy + z * ec * dz;
+    const float C = (x * ea * x + y * eb * y + z * ec * z) - 1.f;
+    const float draw_ = B * B - A * C;
+    const float sq = sqrtf(fmaxf(draw_, 0.f));
+    const bool inside = C < 0.f;
+    const float t = inside ? (-B + sq) / A : (-B - sq) / A;
+    const bool hit = (draw_ > 0.f) && (t > g.eps) && (t < l) && (l > 0.f);
+    if (!hit) {
+      x += sx;
+      y += sy;
+      z += sz;
+      return 0.f;
+    }
+    const float hx = x + t * dx, hy = y + t * dy, hz = z + t * dz;
+    float nx = hx * ea, ny = hy * eb, nz = hz * ec;
+    const float nn = sqrtf(nx * nx + ny * ny + nz * nz);
+    nx /= nn;
+    ny /= nn;
+    nz /= nn;
+    const float rem = l - t;
+    const float dn = dx * nx + dy * ny + dz * nz;
+    const float dperp = rem * fabsf(dn);
+    if (u < fminf(1.f, 2.f * g.kod * dperp)) {
+      ++tl.transmit;
+      x += sx;
+      y += sy;
+      z += sz;
+      return 0.f;
+    }
+    float qx = dx - 2.f * dn * nx, qy = dy - 2.f * dn * ny, qz = dz - 2.f * dn * nz;
+    const float qn = sqrtf(qx * qx + qy * qy + qz * qz);
+    const float sg = inside ? -1.f : 1.f;
+    const float f = fmaxf(rem - g.nudge, 0.f);
+    x = hx + g.nudge * sg * nx + qx / qn * f;
+    y = hy + g.nudge * sg * ny + qy / qn * f;
+    z = hz + g.nudge * sg * nz + qz / qn * f;
+    return -2.f * dperp;
+  }
 }
 
 // ------------------------------------------------------------------------------------------------

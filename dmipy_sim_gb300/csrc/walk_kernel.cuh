@@ -171,6 +171,8 @@ __device__ __forceinline__ int classify(float x, float y, float z, const GeoK& g
     return (x * x + y * y < g.R2) ? 0 : 1;  // geometries.py:803-813
   } else if constexpr (GEOM == DMSIM_GEOM_SPHERE) {
     return (x * x + y * y + z * z < g.R2) ? 0 : 1;  // geometries.py:161-165
+  } else if constexpr (GEOM == DMSIM_GEOM_ELLIPSOID) {  // geometries.py:1396-1403
+    return (x * g.e2[0] * x + y * g.e2[1] * y + z * g.e2[2] * z) < 1.f ? 0 : 1;
   } else if constexpr (GEOM == DMSIM_GEOM_SLAB) {
     return x < g.R ? 0 : 1;  // geometries.py:3262-3263
   } else if constexpr (GEOM == DMSIM_GEOM_SHELL) {
@@ -414,7 +416,16 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
       for (uint32_t j = 0; j < 256u && !ok; ++j) {
         const u32x4 r = draw(a.seed, gw, 1u, j);
         const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z), u3 = u01(r.w);
-        if constexpr (GEOM == DMSIM_GEOM_BOX1D || GEOM == DMSIM_GEOM_SLAB) {
+        if constexpr (GEOM == DMSIM_GEOM_ELLIPSOID) {
+          // uniform in the unit ball, scaled by the semi-axes (geometries.py:1167-1182)
+          const float px = 2.f * u0 - 1.f, py = 2.f * u1 - 1.f, pz = 2.f * u2 - 1.f;
+          if (px * px + py * py + pz * pz < 1.f) {
+            x = px * rsqrtf(g.e2[0]);
+            y = py * rsqrtf(g.e2[1]);
+            z = pz * rsqrtf(g.e2[2]);
+            ok = true;
+          }
+        } else if constexpr (GEOM == DMSIM_GEOM_BOX1D || GEOM == DMSIM_GEOM_SLAB) {
           // x uniform over the slab (Box1D) or its first half (the permeable slab starts every
           // walker in compartment A), y = z = 0 (geometries.py:84-88, 3257-3261)
           x = (GEOM == DMSIM_GEOM_BOX1D ? g.L : g.R) * u0;
@@ -609,6 +620,8 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
             z += stz;
           } else if constexpr (GEOM == DMSIM_GEOM_PACKED_SPHERES) {
             dl = packed_sph_step<WALL>(x, y, z, ix, iy, iz, stx, sty, stz, up, g, cs, cand, tw);
+          } else if constexpr (GEOM == DMSIM_GEOM_ELLIPSOID) {
+            dl = ellipsoid_step<WALL>(x, y, z, stx, sty, stz, up, g, tw);
           } else if constexpr (GEOM == DMSIM_GEOM_BOX1D) {
             dl = box1d_step<WALL == kPermeate ? kReflect : WALL>(x, y, z, stx, sty, stz, g);
           } else if constexpr (GEOM == DMSIM_GEOM_SLAB) {

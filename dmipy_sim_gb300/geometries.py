@@ -17,7 +17,7 @@ from . import _lib
 
 __all__ = ["Geometry", "FreeDiffusion", "Cylinder", "Sphere", "MyelinatedCylinder",
            "PackedMyelinatedCylinders", "pack_myelinated_cylinders", "Box1D", "PermeableSlab1D",
-           "PermeableShell",
+           "PermeableShell", "Ellipsoid",
            "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres",
            "lattice_cylinders"]
 
@@ -174,6 +174,54 @@ class Cylinder(Geometry):
         g.radius = self.radius
         g.eps_detect = np.float32(1e-7 * self.radius)
         g.nudge = np.float32(1e-4 * self.radius)
+        return g, ()
+
+
+class Ellipsoid(Geometry):
+    """Reflecting (optionally relaxing / permeable) axis-aligned ellipsoid with semi-axes
+    (a, b, c) along (x, y, z) at the origin (geometries.py:1137-1427); a = b = c = R is the
+    sphere."""
+
+    def __init__(self, semiaxes, surface_relaxivity_t2=None, permeability=None):
+        self.semiaxes = np.asarray(semiaxes, dtype=np.float64)
+        self.surface_relaxivity_t2 = _opt_float(surface_relaxivity_t2)
+        self.permeability = _opt_float(permeability)
+
+    def _inv2(self):
+        s = self.semiaxes.astype(np.float32)
+        return np.float32(1.0) / (s * s)
+
+    def init_positions(self, n_walkers, key=None):
+        """Uniform in the unit ball scaled by the semi-axes (geometries.py:1167-1182)."""
+        rng = _host_rng(key)
+        out = []
+        while sum(len(a) for a in out) < n_walkers:
+            p = rng.uniform(-1.0, 1.0, (n_walkers * 4, 3))
+            out.append(p[np.linalg.norm(p, axis=1) < 1.0])
+        return (np.concatenate(out)[:n_walkers] * self.semiaxes).astype(np.float32)
+
+    def classify_position(self, r):
+        r = np.asarray(r, dtype=np.float32)
+        return np.where(np.sum(r * self._inv2() * r, axis=-1) < np.float32(1.0), 0,
+                        1).astype(np.int32)
+
+    def volume(self):
+        a, b, c = self.semiaxes
+        return (4.0 / 3.0) * np.pi * a * b * c
+
+    def surface_area(self):
+        """Thomsen's approximation (p = 1.6075, relative error < 1.061 %)."""
+        p = 1.6075
+        a, b, c = self.semiaxes ** p
+        return 4.0 * np.pi * ((a * b + a * c + b * c) / 3.0) ** (1.0 / p)
+
+    def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
+        g = self._base_desc(_lib.GEOM_ELLIPSOID, wall_mode, rho_over_D, kappa_over_D)
+        m = float(np.min(self.semiaxes))
+        g.radius = m
+        g.eps_detect = np.float32(1e-7 * m)
+        g.nudge = np.float32(1e-4 * m)
+        g.ell_inv2[:] = [float(v) for v in self._inv2()]
         return g, ()
 
 

@@ -65,7 +65,8 @@ enum dmsim_geom_kind {
   DMSIM_GEOM_PMYELIN = 7,          /* geometries.py:2860-3218 + physics.py:682-1062, periodic   */
   DMSIM_GEOM_BOX1D = 8,            /* geometries.py:48-140, walls at x = 0 and x = L           */
   DMSIM_GEOM_SLAB = 9,             /* geometries.py:3221-3300, membrane at x = L/2 in [0, L]   */
-  DMSIM_GEOM_SHELL = 10            /* geometries.py:3303-3431, membrane R_in, wall R_out       */
+  DMSIM_GEOM_SHELL = 10,           /* geometries.py:3303-3431, membrane R_in, wall R_out       */
+  DMSIM_GEOM_ELLIPSOID = 11        /* geometries.py:1137-1427, axis-aligned at the origin      */
 };
 
 enum dmsim_wall_mode {
@@ -176,6 +177,11 @@ typedef struct dmsim_geometry {
      shell_cyl (1: radii measured from the frame z axis, 0: from the origin) */
   float shell_r_out;
   int32_t shell_cyl;
+
+  /* ellipsoid (DMSIM_GEOM_ELLIPSOID): 1 / a^2, 1 / b^2, 1 / c^2 of the semi-axes along x, y, z;
+     radius = the smallest semi-axis (eps_detect = 1e-7, nudge = 1e-4 of it) */
+  float ell_inv2[3];
+  float ell_pad;
 } dmsim_geometry;
 
 /* ---- walk parameters -------------------------------------------------------------------------- */

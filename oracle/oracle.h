@@ -18,6 +18,7 @@
  *   Box1D reflect / reflect_with_log_weight               geometries.py:90-140
  *   PermeableSlab1D reflect / rwlw / permeate             geometries.py:3270-3300
  *   PermeableShell permeate / reflect                     geometries.py:3366-3431
+ *   Ellipsoid reflect / rwlw / permeate                   geometries.py:1184-1392
  *     (wrap 203-206, 27-cell gather 208-215, Moller-Trumbore 561-569, bounce 599-635,
  *      nearest-centroid classification 227-254, leak guard 578-597)
  *   ensemble Re<w e^{i phi}>                              core.py:426-429; replay FP64 phase
@@ -36,7 +37,8 @@ extern "C" {
 #endif
 
 enum { OR_FREE = 0, OR_CYLINDER = 1, OR_SPHERE = 2, OR_PACKED_CYLINDERS = 3, OR_PACKED_SPHERES = 4,
-       OR_MESH = 5, OR_MYELIN = 6, OR_PMYELIN = 7, OR_BOX1D = 8, OR_SLAB = 9, OR_SHELL = 10 };
+       OR_MESH = 5, OR_MYELIN = 6, OR_PMYELIN = 7, OR_BOX1D = 8, OR_SLAB = 9, OR_SHELL = 10,
+       OR_ELLIPSOID = 11 };
 enum { OR_REFLECT = 0, OR_RELAX = 1, OR_PERMEATE = 2 };
 
 /* A triangle mesh as the reference's Mesh holds it (mesh.py:311-546): every triangle including the
@@ -95,6 +97,7 @@ typedef struct {
   double r_out;   /* OR_SHELL: the reflecting outer wall (radius = the permeable membrane) */
   int32_t cyl;    /* OR_SHELL: radii from the frame z axis (1) or the origin (0) */
   int32_t pad2;
+  double semi[3]; /* OR_ELLIPSOID: semi-axes along x, y, z */
 } or_geom;
 
 typedef struct {

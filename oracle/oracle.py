@@ -15,7 +15,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 
 (FREE, CYLINDER, SPHERE, PACKED_CYLINDERS, PACKED_SPHERES, MESH, MYELIN, PMYELIN, BOX1D, SLAB,
- SHELL) = range(11)
+ SHELL, ELLIPSOID) = range(12)
 REFLECT, RELAX, PERMEATE = range(3)
 
 
@@ -48,7 +48,8 @@ class OrGeom(C.Structure):
                 ("L", C.c_double), ("rmin", C.c_double), ("objects", C.c_void_p),
                 ("rot", C.c_double * 9), ("rot_identity", C.c_int32), ("pad", C.c_int32),
                 ("mesh", C.c_void_p), ("myelin", C.c_void_p), ("pmyelin", C.c_void_p),
-                ("r_out", C.c_double), ("cyl", C.c_int32), ("pad2", C.c_int32)]
+                ("r_out", C.c_double), ("cyl", C.c_int32), ("pad2", C.c_int32),
+                ("semi", C.c_double * 3)]
 
 
 class OrWalk(C.Structure):
@@ -341,6 +342,13 @@ def shell_geom(r_inner, r_outer, cylinder=False):
     return g
 
 
+def ellipsoid_geom(semiaxes):
+    """Oracle axis-aligned ellipsoid with semi-axes (a, b, c) along x, y, z."""
+    g = geom(ELLIPSOID)
+    g.semi[:] = [float(x) for x in semiaxes]
+    return g
+
+
 def geom_from(geometry, dt=None):
     """Oracle geometry of a dmipy_sim_gb300 geometry object (walk frame)."""
     name = type(geometry).__name__
@@ -359,6 +367,8 @@ def geom_from(geometry, dt=None):
         kind = PACKED_CYLINDERS if name == "PackedCylinders" else PACKED_SPHERES
         return geom(kind, L=np.float32(geometry._L_float), objects=objs,
                     rot=getattr(geometry, "_R", None))
+    if name == "Ellipsoid":
+        return ellipsoid_geom(geometry.semiaxes)
     if name == "Box1D":
         return slab_geom(BOX1D, geometry.length)
     if name == "PermeableSlab1D":

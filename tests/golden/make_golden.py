@@ -494,6 +494,13 @@ def _validation_geom_cases(m, rng, out):
     slab = geo.PermeableSlab1D(L, permeability=1e-5)
     for mode in ("reflect", "relax", "perm"):
         run("slab", slab, mode, rs, st, us)
+    ell = geo.Ellipsoid([2e-6, 3e-6, 4.5e-6])
+    d = _unit(rng, n)
+    rs = (d * rng.uniform(0.3, 1.15, (n, 1)) * np.array([2e-6, 3e-6, 4.5e-6])).astype(np.float32)
+    st = (_unit(rng, n) * rng.uniform(0.05, 0.5, (n, 1)) * 2e-6).astype(np.float32)
+    run("ell", ell, "reflect", rs, st, us)
+    run("ell", ell, "relax", rs, st, us)
+    run("ell", geo.Ellipsoid([2e-6, 3e-6, 4.5e-6], permeability=1e-5), "perm", rs, st, us)
     for kind, tag in (("sphere", "shs"), ("cylinder", "shc")):
         sh = geo.PermeableShell(2e-6, 4e-6, permeability=1e-5, kind=kind)
         d = _unit(rng, n)
@@ -511,7 +518,8 @@ def make_myelin_kat(root):
     m = _ref(root)
     path = HERE / "kat.npz"
     out = {k: v for k, v in np.load(path).items()
-           if not k.startswith(("my_", "pmy_", "pl_box_", "pl_slab_", "pl_shs_", "pl_shc_"))}
+           if not k.startswith(("my_", "pmy_", "pl_box_", "pl_slab_", "pl_shs_", "pl_shc_",
+                                "pl_ell_"))}
     _myelin_cases(m, np.random.default_rng(17), out)
     _pmyelin_cases(m, np.random.default_rng(23), out)
     _validation_geom_cases(m, np.random.default_rng(29), out)

@@ -1,4 +1,5 @@
-"""The validation slabs and shell on the GPU (Box1D, PermeableSlab1D, PermeableShell): the device
+"""The validation slabs and shell and the ellipsoid on the GPU (Box1D, PermeableSlab1D,
+PermeableShell, Ellipsoid): the device
 steps against the reference's own plug-in calls (kat.npz), walks against the CPU oracle, and the
 closed-form limits these geometries exist for (two-compartment exchange across a planar membrane,
 Brownstein-Tarr relaxation between two walls)."""
@@ -14,10 +15,12 @@ D = 2e-9
 L = 6e-6
 CASES = [("box", "reflect"), ("box", "relax"), ("slab", "reflect"), ("slab", "relax"),
          ("slab", "perm"), ("shs", "reflect"), ("shs", "perm"), ("shc", "reflect"),
-         ("shc", "perm")]
+         ("shc", "perm"), ("ell", "reflect"), ("ell", "relax"), ("ell", "perm")]
 
 
-def _geom(tag, rho=None):
+def _geom(tag, rho=None, kappa=None):
+    if tag == "ell":
+        return d.Ellipsoid([2e-6, 3e-6, 4.5e-6], surface_relaxivity_t2=rho, permeability=kappa)
     if tag == "box":
         return d.Box1D(L, surface_relaxivity_t2=rho)
     if tag == "slab":
@@ -51,7 +54,7 @@ def _plan(g, wf):
     return core.fused_sub_steps(g, D, wf.dt), True
 
 
-@pytest.mark.parametrize("tag", ["box", "slab", "shs", "shc"])
+@pytest.mark.parametrize("tag", ["box", "slab", "shs", "shc", "ell"])
 def test_walks_match_oracle(cuda, tag):
     """Walker by walker over ~100 sub-steps and whole echoes on the same stream, with surface
     relaxivity on (the weighted walls) and T2."""
@@ -110,3 +113,15 @@ def test_two_wall_surface_relaxation_fast_limit(cuda):
     s = d.simulate(50_000, D, wf, g, seed=2)
     t = (wf.G.shape[1]) * wf.dt
     np.testing.assert_allclose(s, np.exp(-rho * 2.0 / Lb * t), atol=3e-3)
+
+
+def test_round_ellipsoid_is_the_sphere(cuda):
+    """a = b = c = R walks the sphere: the two step rules agree on the ensemble signal."""
+    R = 4e-6
+    rng = np.random.default_rng(2)
+    bv = rng.normal(size=(4, 3))
+    bv /= np.linalg.norm(bv, axis=1, keepdims=True)
+    wf = d.set_b(d.pgse(0.006, 0.02, 0.05, bv, 80), 1.5e9)
+    s_e = d.simulate(200_000, D, wf, d.Ellipsoid([R, R, R]), seed=3)
+    s_s = d.simulate(200_000, D, wf, d.Sphere(R), seed=3)
+    np.testing.assert_allclose(s_e, s_s, atol=6e-3)
