@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 6
+DMSIM_ABI_VERSION = 7
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
@@ -30,7 +30,8 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_replay", "dmsim_batch_create", "dmsim_batch_bind", "dmsim_batch_launch",
             "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_pack",
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
-            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes")
+            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes",
+            "dmsim_bloch_workspace_bytes", "dmsim_bloch")
 
 EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
@@ -87,6 +88,13 @@ class WalkOutputs(C.Structure):
     ]
 
 
+class BlochParams(C.Structure):
+    _fields_ = [
+        ("rf_flip", C.c_void_p), ("rf_axis", C.c_void_p), ("carrier", C.c_void_p),
+        ("crush", C.c_void_p), ("m0", C.c_float), ("t1_sample", C.c_float),
+    ]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [
         ("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("order", C.c_int32),
@@ -122,6 +130,12 @@ def load():
     lib.dmsim_walk.restype = C.c_int
     lib.dmsim_walk.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry), C.POINTER(WalkOutputs),
                                C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.dmsim_bloch_workspace_bytes.restype = C.c_size_t
+    lib.dmsim_bloch_workspace_bytes.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry)]
+    lib.dmsim_bloch.restype = C.c_int
+    lib.dmsim_bloch.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
+                                C.POINTER(BlochParams), C.POINTER(WalkOutputs), C.c_void_p,
+                                C.c_size_t, C.c_void_p]
     lib.dmsim_walk_noalloc.restype = C.c_int
     lib.dmsim_walk_noalloc.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
                                        C.POINTER(WalkOutputs), C.c_void_p]

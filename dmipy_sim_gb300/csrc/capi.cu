@@ -75,7 +75,7 @@ constexpr int kMaxBasisMeas = 512;
 
 struct Plan {
   WalkFn fn = nullptr;
-  int pm = 0;      // 0 direct, 1 basis
+  int pm = 0;      // 0 direct, 1 basis, 2 vector Bloch (direct waveform)
   int width = 0;   // MT (direct) or RT (basis)
   int mt = 0;      // measurements per pass (direct) or 1 (basis: a single pass of all M)
   int row = 0;     // floats per staged waveform sample
@@ -87,8 +87,14 @@ struct Plan {
 };
 
 int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
-              size_t tab_budget = kTabSmemBudget) {
+              size_t tab_budget = kTabSmemBudget, bool bloch = false) {
   if (!p || !g) return fail(DMSIM_EINVAL, "null params or geometry");
+  if (bloch) {
+    if (g->kind == DMSIM_GEOM_MYELIN || g->kind == DMSIM_GEOM_PMYELIN)
+      return fail(DMSIM_EINVAL, "the Bloch walk does not take myelinated geometries");
+    if (p->chi || p->t1_decay != 0.f || p->basis_rank != 0)
+      return fail(DMSIM_EINVAL, "the Bloch walk takes no chi, t1_decay or waveform basis");
+  }
   if (p->n_walkers < 0) return fail(DMSIM_EINVAL, "n_walkers < 0");
   if (p->n_t < 1 || p->n_meas < 1 || p->sub_steps < 1)
     return fail(DMSIM_EINVAL, "n_t, n_meas and sub_steps must be >= 1");
@@ -159,7 +165,13 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
   }
   if (p->basis_rank < 0 || p->basis_rank > kMaxBasisRank)
     return fail(DMSIM_EINVAL, "basis_rank must be in [0, %d]", kMaxBasisRank);
-  if (p->basis_rank > 0) {
+  if (bloch) {
+    if (p->G == nullptr) return fail(DMSIM_EINVAL, "G is null");
+    pl->pm = 2;
+    pl->width = pl->mt = p->n_meas <= 4 ? 4 : 16;
+    pl->n_pass = (p->n_meas + pl->mt - 1) / pl->mt;
+    pl->row = 3 * pl->mt;
+  } else if (p->basis_rank > 0) {
     if (!p->basis_V || !p->basis_C) return fail(DMSIM_EINVAL, "basis_V / basis_C is null");
     if (p->n_meas > kMaxBasisMeas)
       return fail(DMSIM_ETOOBIG, "the basis form handles at most %d measurements", kMaxBasisMeas);
@@ -229,14 +241,14 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
   if (grid < 1) grid = 1;
   pl->grid = (int)grid;
 
-  const int Mp = pl->pm ? p->n_meas : pl->n_pass * pl->mt;
+  const int Mp = pl->pm == 1 ? p->n_meas : pl->n_pass * pl->mt;
   size_t off = 0;
   pl->off_gp = off;
   off = align256(off + (size_t)pl->n_pass * pl->n_chunks * kTC * pl->row * 4);
   pl->off_act = off;
   off = align256(off + (size_t)pl->n_pass * p->n_t);
   pl->off_cp = off;
-  off = align256(off + (pl->pm ? (size_t)p->n_meas * 3 * pl->width * 4 : 0));
+  off = align256(off + (pl->pm == 1 ? (size_t)p->n_meas * 3 * pl->width * 4 : 0));
   pl->off_part = off;
   off = align256(off + (size_t)pl->grid * p->n_echo * Mp * 3 * 8);
   pl->total = off;
@@ -623,7 +635,7 @@ void fill_kargs(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim
   a->phase_sub = p->phase_per_substep ? 1 : 0;
   a->has_weight = p->has_weight ? 1 : 0;
   a->n_echo = p->n_echo;
-  a->Mp = pl.pm ? p->n_meas : pl.n_pass * pl.mt;
+  a->Mp = pl.pm == 1 ? p->n_meas : pl.n_pass * pl.mt;
   a->M = p->n_meas;
   a->step_l = p->step_length;
   a->gamma_dt = p->gamma_dt;
@@ -656,7 +668,8 @@ void fill_kargs(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim
 
 // One walk on its own launches: waveform re-layout, one walk launch per pass, reduction.
 int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_walk_outputs* o,
-                  const Plan& pl, uint8_t* ws, cudaStream_t st) {
+                  const Plan& pl, uint8_t* ws, cudaStream_t st,
+                  const dmsim_bloch_params* bl = nullptr) {
   int rc = check_outputs(p, g, o);
   if (rc != DMSIM_OK) return rc;
   if (p->n_walkers == 0) {
@@ -668,7 +681,7 @@ int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dms
   double* part = reinterpret_cast<double*>(ws + pl.off_part);
   float* Cp = reinterpret_cast<float*>(ws + pl.off_cp);
   const int t_pad = pl.n_chunks * kTC;
-  if (pl.pm)
+  if (pl.pm == 1)
     k_prep_basis<<<64, 256, 0, st>>>(p->basis_V, p->basis_C, p->n_t, p->n_meas, p->basis_rank,
                                      pl.width, t_pad, Gp, act, Cp);
   else
@@ -677,6 +690,14 @@ int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dms
   fill_kargs(p, g, o, pl, &a);
   a.Cp = Cp;
   a.part = part;
+  if (bl) {
+    a.rf_flip = bl->rf_flip;
+    a.rf_axis = bl->rf_axis;
+    a.carrier = bl->carrier;
+    a.crush = bl->crush;
+    a.m0 = bl->m0;
+    a.t1_sample = bl->t1_sample;
+  }
   BatchCtl none;
   memset(&none, 0, sizeof(none));
   for (int pass = 0; pass < pl.n_pass; ++pass) {
@@ -723,6 +744,30 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
     return fail(DMSIM_EWORKSPACE, "workspace %zu B < required %zu B", workspace_bytes, pl.total);
   if (((uintptr_t)workspace & 255) != 0) return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
   return launch_single(p, g, o, pl, static_cast<uint8_t*>(workspace), (cudaStream_t)stream);
+}
+
+size_t dmsim_bloch_workspace_bytes(const dmsim_walk_params* p, const dmsim_geometry* g) {
+  Plan pl;
+  if (make_plan(p, g, &pl, kTabSmemBudget, true) != DMSIM_OK) return 0;
+  return pl.total;
+}
+
+int dmsim_bloch(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_bloch_params* b,
+                const dmsim_walk_outputs* o, void* workspace, size_t workspace_bytes,
+                void* stream) {
+  if (!b || !b->rf_flip || !b->rf_axis)
+    return fail(DMSIM_EINVAL, "Bloch parameters need the per-sample flip and axis");
+  if (!(b->t1_sample >= 0.f)) return fail(DMSIM_EINVAL, "t1_sample must be >= 0");
+  if (o && o->phi) return fail(DMSIM_EINVAL, "the Bloch walk has no per-walker phase output");
+  Plan pl;
+  int rc = make_plan(p, g, &pl, kTabSmemBudget, true);
+  if (rc != DMSIM_OK) return rc;
+  rc = check_outputs(p, g, o);
+  if (rc != DMSIM_OK) return rc;
+  if (!workspace || workspace_bytes < pl.total)
+    return fail(DMSIM_EWORKSPACE, "workspace %zu B < required %zu B", workspace_bytes, pl.total);
+  if (((uintptr_t)workspace & 255) != 0) return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
+  return launch_single(p, g, o, pl, static_cast<uint8_t*>(workspace), (cudaStream_t)stream, b);
 }
 
 int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const float* steps,

@@ -1,7 +1,7 @@
 """Writes the walk-kernel instantiation tables (walk_<kind>.cu, walk_batch_<kind>.cu).
 
 Each geometry gets one translation unit of single-instance variants (wall mode x phase form x
-cell list in shared memory) and, except the myelinated cylinders (whose batch instances run as
+cell list in shared memory; the vector-Bloch form for every geometry but the myelinated ones) and, except the myelinated cylinders (whose batch instances run as
 plain walks), one of batched variants (basis phase form only), so that the parallel build compiles
 them side by side.  Run after changing the variant set.
 """
@@ -23,19 +23,24 @@ KINDS = [  # (file stem, enum, wall modes, has a cell list, has batched variants
     ("ellipsoid", "DMSIM_GEOM_ELLIPSOID", [0, 1, 2], False, True),
 ]
 VARIANTS = [(0, 16), (0, 32), (0, 64), (1, 2), (1, 4), (1, 8)]  # (phase form, width)
+BLOCH_VARIANTS = [(2, 4), (2, 16)]  # vector Bloch: measurements per pass
+NO_BLOCH = {"myelin", "pmyelin"}
 
 
 def _table(stem, enum, walls, packed, batch):
     tsms = [False, True] if packed else [False]
     fn = f"walk_{'batch_' if batch else ''}fn_{stem}"
-    what = "batched variants (basis phase form)" if batch else "wall mode x phase form (direct MT / basis RT) x cell list in shared memory"
+    what = ("batched variants (basis phase form)" if batch else
+            "wall mode x phase form (direct MT / basis RT / vector Bloch) x cell list in shared "
+            "memory")
     lines = [f"// Instantiations of the walk kernel for {enum}: {what}.",
              "// Written by gen_instances.py.",
              '#include "walk_kernel.cuh"', "", "namespace dmsim {", "",
              f"WalkFn {fn}(int wall, int pm, int width, bool tsm) {{"]
     b = "true" if batch else "false"
+    variants = VARIANTS + ([] if batch or stem in NO_BLOCH else BLOCH_VARIANTS)
     for wall in walls:
-        for pm, width in VARIANTS:
+        for pm, width in variants:
             if batch and pm == 0:
                 continue
             for tsm in tsms:

@@ -1,4 +1,4 @@
-// Instantiations of the walk kernel for DMSIM_GEOM_FREE: wall mode x phase form (direct MT / basis RT) x cell list in shared memory.
+// Instantiations of the walk kernel for DMSIM_GEOM_FREE: wall mode x phase form (direct MT / basis RT / vector Bloch) x cell list in shared memory.
 // Written by gen_instances.py.
 #include "walk_kernel.cuh"
 
@@ -11,6 +11,8 @@ WalkFn walk_fn_free(int wall, int pm, int width, bool tsm) {
   if (wall == 0 && pm == 1 && width == 2 && tsm == false) return k_walk<DMSIM_GEOM_FREE, 0, 1, 2, false, false>;
   if (wall == 0 && pm == 1 && width == 4 && tsm == false) return k_walk<DMSIM_GEOM_FREE, 0, 1, 4, false, false>;
   if (wall == 0 && pm == 1 && width == 8 && tsm == false) return k_walk<DMSIM_GEOM_FREE, 0, 1, 8, false, false>;
+  if (wall == 0 && pm == 2 && width == 4 && tsm == false) return k_walk<DMSIM_GEOM_FREE, 0, 2, 4, false, false>;
+  if (wall == 0 && pm == 2 && width == 16 && tsm == false) return k_walk<DMSIM_GEOM_FREE, 0, 2, 16, false, false>;
   return nullptr;
 }
 

@@ -18,8 +18,15 @@
 //         G[t, m, k] = sum_j C[m, k, j] V[t, j], the kernel accumulates only
 //         Q[j, k] += gamma_dt * V[t, j] R_k(t) (3 RT registers, 3 RT FMAs per sample) and forms
 //         phi_m = sum_jk C[m, k, j] Q[j, k] at the echo samples;
-//   * at every echo sample the block reduces w*cos(phi), w*sin(phi) and (w*cos(phi))^2 with warp
-//     shuffles and adds them, in FP64 and in a fixed order, into the block's own partial slice.
+//       vector Bloch (PM = 2, bloch.py:44-57, 109-131, 180-198): each walker carries the
+//         magnetisation M_m = (Mx, My, Mz) of every measurement through RF rotations, free
+//         precession and relaxation.  Between RF events precession, T2 and the wall weight act on
+//         Mxy alone and commute, so the kernel keeps M_m as of the last RF event plus the phase
+//         (gradient, Kahan; carriers), log-weight and T1 time accrued since, and forms M_m only
+//         at an RF sample (before the rotation) and at an echo;
+//   * at every echo sample the block reduces w*cos(phi), w*sin(phi) and (w*cos(phi))^2 (Bloch:
+//     Mx, My, Mz) with warp shuffles and adds them, in FP64 and in a fixed order, into the
+//     block's own partial slice.
 // Blocks loop over walker tiles (grid = SMs x resident blocks), so the partial buffer is
 // independent of n_walkers.
 #pragma once
@@ -68,6 +75,14 @@ struct KArgs {
   int traj_f16;
   float* dlog_unit;
   float* comp_occ;
+  // vector-Bloch form: per-sample RF flip and B1 axis (rad; flip 0 = no pulse), extra precession
+  // per sample (rad: off-resonance + pulse carrier), crusher rate per sample (rad per unit of the
+  // walker's crusher coordinate), equilibrium M0 and dt/T1 per sample
+  const float* rf_flip;
+  const float* rf_axis;
+  const float* carrier;
+  const float* crush;
+  float m0, t1_sample;
   int echo[kMaxEcho];
 };
 
@@ -132,8 +147,9 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-// Floats per sample of the staged waveform: 3 per measurement (direct) or 1 per shape (basis).
-__host__ __device__ constexpr int walk_row(int pm, int w) { return pm ? w : 3 * w; }
+// Floats per sample of the staged waveform: 3 per measurement (direct, Bloch) or 1 per shape
+// (basis).
+__host__ __device__ constexpr int walk_row(int pm, int w) { return pm == 1 ? w : 3 * w; }
 
 __host__ __device__ inline size_t pad16z(size_t v) { return (v + 15) & ~(size_t)15; }
 
@@ -147,8 +163,8 @@ __host__ __device__ inline SmemLayout walk_smem_layout(int pm, int w, int M) {
   SmemLayout L;
   L.off_bar = (size_t)2 * kTC * walk_row(pm, w) * 4;
   L.off_cs = L.off_bar + 64;
-  L.off_red = L.off_cs + (pm ? pad16z((size_t)M * 3 * w * 4) : 0);
-  L.off_tab = L.off_red + pad16z((size_t)kWarps * (pm ? M : w) * 3 * 4);
+  L.off_red = L.off_cs + (pm == 1 ? pad16z((size_t)M * 3 * w * 4) : 0);
+  L.off_tab = L.off_red + pad16z((size_t)kWarps * (pm == 1 ? M : w) * 3 * 4);
   return L;
 }
 
@@ -206,7 +222,8 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
   extern __shared__ __align__(128) uint8_t smem[];
   constexpr int ROW = walk_row(PM, W);
   constexpr int GCH = kTC * ROW;  // floats per waveform chunk
-  constexpr int MT = PM ? 1 : W;  // measurements held per thread in the direct form
+  constexpr int MT = PM == 1 ? 1 : W;  // measurements held per thread (direct, Bloch)
+  constexpr bool BLOCH = PM == 2;
   float* Gs = reinterpret_cast<float*>(smem);
   const SmemLayout lay = walk_smem_layout(PM, W, BATCH ? bc.max_m : a0.M);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.off_bar);
@@ -241,7 +258,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
   if constexpr (!BATCH) {
     // zero this block's partial slice for this pass
     for (int e = 0; e < a0.n_echo; ++e)
-      for (int j = tid; j < (PM ? a0.M : W) * 3; j += kBlock)
+      for (int j = tid; j < (PM == 1 ? a0.M : W) * 3; j += kBlock)
         a0.part[((size_t)(blockIdx.x * a0.n_echo + e) * a0.Mp + a0.pass * MT) * 3 + j] = 0.0;
   }
   __syncthreads();
@@ -291,7 +308,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
     // per-axis period used to unfold positions (packed: the cell side; mesh: the periodic box)
     const float Lx = MESH ? a.mk.box[0] : g.L, Ly = MESH ? a.mk.box[1] : g.L,
                 Lz = MESH ? a.mk.box[2] : g.L;
-    const int MR = PM ? a.M : W;  // measurements reduced per emission
+    const int MR = PM == 1 ? a.M : W;  // measurements reduced per emission
     const uint32_t* cs = a.cs;
     const float4* cand = a.cand;
     if constexpr (PACKED && TSM) {
@@ -534,15 +551,30 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
                                 : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
 
     // phase accumulators: direct form phi[m] (+ Kahan), basis form Q[j][k] (+ Kahan)
-    constexpr int NACC = PM ? 3 * W : W;
+    constexpr int NACC = PM == 1 ? 3 * W : W;
     float acc[NACC], kc[NACC];
 #pragma unroll
     for (int i = 0; i < NACC; ++i) acc[i] = kc[i] = 0.f;
+    // Bloch form: M as of the last RF event, the carrier phase (Kahan) and the T1 samples since,
+    // the log-weight at that event and the walker's crusher coordinate (its own Philox stream)
+    constexpr int NB = BLOCH ? W : 1;
+    float bx[NB], by[NB], bz[NB];
+    float psi = 0.f, psik = 0.f, lw_rf = 0.f, uc = 0.f;
+    int k1 = 0;
+    if constexpr (BLOCH) {
+#pragma unroll
+      for (int m = 0; m < W; ++m) {
+        bx[m] = by[m] = 0.f;
+        bz[m] = a.m0;
+      }
+      if (a.crush) uc = u01(draw(a.seed, gw, 2u, 0u).x);
+    }
     // a myelinated cylinder's walkers start with the log of their compartment's spin weight
     const float logw0 =
         MYEL ? (mcomp == 0 ? a.my.lw0[0] : (mcomp == 1 ? a.my.lw0[1] : a.my.lw0[2]))
              : (PMYEL ? (mcomp > a.pm.nmax ? a.pm.lwm : 0.f) : 0.f);
     float logw = logw0;
+    lw_rf = logw0;
     uint32_t s = 0;   // global sub-step counter of this walker
     u32x4 rr{0, 0, 0, 0};
     int e = 0;        // next echo ordinal
@@ -578,6 +610,7 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
         const float chi = a.chi ? __ldg(a.chi + t) : 1.f;
         const float rc = a.rho * chi;
         const float dec = a.t2dec * chi + a.t1dec * (1.f - chi);
+        const float logw_t0 = logw;  // Bloch: the weight through sample t - 1
         float Rx = 0.f, Ry = 0.f, Rz = 0.f, dls = 0.f, occ = 0.f;
 #pragma unroll 1
         for (int sub = 0; sub < a.S; ++sub, ++s) {
@@ -660,11 +693,40 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
           Ry = uy;
           Rz = uz;
         }
+        // ---- Bloch: an RF pulse at this sample rotates M, formed through sample t - 1, about the
+        // in-plane axis (cos ax, sin ax, 0) before this sample's precession (bloch.py:44-57,
+        // 125).  The flip is the same for every walker: a block-uniform branch.
+        if constexpr (BLOCH) {
+          const float flip = __ldg(a.rf_flip + t);
+          if (flip != 0.f) {
+            float ux, uy, sf, cf;
+            sincosf(__ldg(a.rf_axis + t), &uy, &ux);
+            sincosf(flip, &sf, &cf);
+            const float omc = 1.f - cf;
+            const float amp = a.has_weight ? expf(logw_t0 - lw_rf) : 1.f;
+            const float e1 = expf(-(float)k1 * a.t1_sample);
+#pragma unroll
+            for (int m = 0; m < W; ++m) {
+              float sn, cs_;
+              sincosf(acc[m] + psi, &sn, &cs_);
+              const float mx = amp * (cs_ * bx[m] - sn * by[m]);
+              const float my = amp * (sn * bx[m] + cs_ * by[m]);
+              const float mz = a.m0 + (bz[m] - a.m0) * e1;
+              bx[m] = (cf + ux * ux * omc) * mx + (ux * uy * omc) * my + (uy * sf) * mz;
+              by[m] = (ux * uy * omc) * mx + (cf + uy * uy * omc) * my - (ux * sf) * mz;
+              bz[m] = -(uy * sf) * mx + (ux * sf) * my + cf * mz;
+              acc[m] = kc[m] = 0.f;
+            }
+            psi = psik = 0.f;
+            lw_rf = logw_t0;
+            k1 = 0;
+          }
+        }
         // ---- phase, Kahan-compensated ------------------------------------------------------
         if (__ldg(a.active + t)) {
           const float px = a.gamma_dt * Rx, py = a.gamma_dt * Ry, pz = a.gamma_dt * Rz;
           const float* gt = Gc + (t - ch * kTC) * ROW;
-          if constexpr (PM == 0) {
+          if constexpr (PM != 1) {
             // direct: phi_m += g_m(t) . R
             const float4* g4 = reinterpret_cast<const float4*>(gt);
             float d = 0.f;
@@ -701,6 +763,16 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
               }
             }
           }
+        }
+        if constexpr (BLOCH) {
+          // carriers of this sample: off-resonance + pulse carrier + crusher (bloch.py:126)
+          const float dpsi = (a.carrier ? __ldg(a.carrier + t) : 0.f) +
+                             (a.crush ? __ldg(a.crush + t) * uc : 0.f);
+          const float yk = dpsi - psik;
+          const float tk = psi + yk;
+          psik = (tk - psi) - yk;
+          psi = tk;
+          ++k1;
         }
         if (act) {
           if (a.traj != nullptr && a.pass == 0) {
@@ -739,6 +811,23 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
           if constexpr (PM == 0) {
 #pragma unroll
             for (int m = 0; m < W; ++m) emit(m, acc[m]);
+          } else if constexpr (BLOCH) {
+            // walker's (Mx, My, Mz) at this sample (bloch.py:127-131)
+            const float amp = act ? (a.has_weight ? expf(logw - lw_rf) : 1.f) : 0.f;
+            const float e1 = expf(-(float)k1 * a.t1_sample);
+#pragma unroll
+            for (int m = 0; m < W; ++m) {
+              float sn, cs_;
+              sincosf(acc[m] + psi, &sn, &cs_);
+              const float c1 = warp_sum(amp * (cs_ * bx[m] - sn * by[m]));
+              const float c2 = warp_sum(amp * (sn * bx[m] + cs_ * by[m]));
+              const float c3 = warp_sum(act ? a.m0 + (bz[m] - a.m0) * e1 : 0.f);
+              if (lane == 0) {
+                red[(warp * MR + m) * 3] = c1;
+                red[(warp * MR + m) * 3 + 1] = c2;
+                red[(warp * MR + m) * 3 + 2] = c3;
+              }
+            }
           } else {
 #pragma unroll 1
             for (int m = 0; m < MR; ++m) {
@@ -783,12 +872,12 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
                                : (MESH ? classify_mesh(x, y, z, a.mk)
                                        : classify<GEOM>(x, y, z, g, cs, cand, a.cand_obj));
       }
-      if (a.phi_out) {
+      if (a.phi_out && !BLOCH) {
         if constexpr (PM == 0) {
 #pragma unroll
           for (int m = 0; m < W; ++m)
             if (a.pass * W + m < a.M) a.phi_out[(size_t)w * a.M + a.pass * W + m] = acc[m];
-        } else {
+        } else if constexpr (PM == 1) {
           for (int m = 0; m < a.M; ++m) {
             const float* c = Cs + (size_t)m * 3 * W;
             float ph = 0.f;

@@ -1,4 +1,4 @@
-// Instantiations of the walk kernel for DMSIM_GEOM_PMYELIN: wall mode x phase form (direct MT / basis RT) x cell list in shared memory.
+// Instantiations of the walk kernel for DMSIM_GEOM_PMYELIN: wall mode x phase form (direct MT / basis RT / vector Bloch) x cell list in shared memory.
 // Written by gen_instances.py.
 #include "walk_kernel.cuh"
 

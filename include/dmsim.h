@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 6
+#define DMSIM_ABI_VERSION 7
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -296,6 +296,35 @@ int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t 
                  const float* G, int32_t n_meas, float gamma_dt, const float* log_w,
                  double* sums, float* phi_out, void* workspace, size_t workspace_bytes,
                  void* stream);
+
+/* ---- vector Bloch ------------------------------------------------------------------------------
+   The forward vector-Bloch walk of bloch.py:212-340 (simulate_bloch without magnetisation
+   transfer or susceptibility): every walker carries M_m = (Mx, My, Mz) for each measurement m,
+   starting from (0, 0, m0), and each waveform sample t applies, after the move of the walk
+   (the same walk, stream and sub-steps as dmsim_walk for the same parameters):
+     an RF rotation by rf_flip[t] about (cos rf_axis[t], sin rf_axis[t], 0)    (bloch.py:44-57),
+     free precession of Mxy by phi_t + carrier[t] + crush[t] * u_w, with phi_t the gradient
+       phase of the sample as in dmsim_walk (gamma_dt, phase_per_substep) and u_w the walker's
+       crusher coordinate, uniform in [0, 1) from Philox stream 2 (bloch.py:126),
+     Mxy *= exp(log-weight of the sample) (t2_decay per sub-step, rho_over_D x the boundary
+       log-weight), Mz -> m0 + (Mz - m0) exp(-t1_sample)                      (bloch.py:129-131).
+   p->chi must be NULL, p->t1_decay 0 and p->basis_rank 0; myelinated geometries are refused.
+   o->sums (n_echo, n_meas, 3) receives sum_w Mx, sum_w My, sum_w Mz at each echo sample (after
+   that sample's update); o->phi must be NULL; the other per-walker outputs are as dmsim_walk's. */
+typedef struct dmsim_bloch_params {
+  const float* rf_flip;  /* DEVICE (n_t): flip of the sample (rad), 0 = no pulse                 */
+  const float* rf_axis;  /* DEVICE (n_t): B1 phase of the sample (rad; 0 = x, pi/2 = y)          */
+  const float* carrier;  /* DEVICE (n_t) extra precession (rad: off-resonance, pulse carrier) or
+                            NULL                                                                  */
+  const float* crush;    /* DEVICE (n_t) crusher rate (rad per unit coordinate) or NULL          */
+  float m0;              /* equilibrium longitudinal magnetisation                                */
+  float t1_sample;       /* dt/T1 per waveform sample, 0 if none                                  */
+} dmsim_bloch_params;
+
+size_t dmsim_bloch_workspace_bytes(const dmsim_walk_params* p, const dmsim_geometry* g);
+int dmsim_bloch(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_bloch_params* b,
+                const dmsim_walk_outputs* o, void* workspace, size_t workspace_bytes,
+                void* stream);
 
 /* Temporal-mode projection, the compressed trajectory export of simulate_trajectories(compress=K)
    (core.py:1370-1407) and the temporal_dct / boundary_dct codecs of compression.py:55-62, 224-249:

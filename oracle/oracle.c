@@ -49,6 +49,7 @@ static double round_half(float f) {
 #define NEARBYINT nearbyintf
 #define SIN sinf
 #define COS cosf
+#define EXP expf
 #define MAX(a, b) fmaxf((a), (b))
 #define MIN(a, b) fminf((a), (b))
 #include "oracle_impl.inc"
@@ -61,6 +62,7 @@ static double round_half(float f) {
 #undef NEARBYINT
 #undef SIN
 #undef COS
+#undef EXP
 #undef MAX
 #undef MIN
 
@@ -73,6 +75,7 @@ static double round_half(float f) {
 #define NEARBYINT nearbyint
 #define SIN sin
 #define COS cos
+#define EXP exp
 #define MAX(a, b) fmax((a), (b))
 #define MIN(a, b) fmin((a), (b))
 #include "oracle_impl.inc"

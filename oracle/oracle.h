@@ -149,6 +149,26 @@ int or_walk_f64(const or_geom* g, const or_walk_params* p, const float* G, const
                 const float* r0, double* sums, float* final_pos, float* log_w, float* phi,
                 int n_threads, int32_t* comp_end);
 
+/* Vector-Bloch walk (bloch.py:109-131, 180-198 with the RF rotation of bloch.py:44-57): the walk
+   of or_walk (same draws, sub-steps and steps; p->chi, t1_decay and t2_decay unused) with each
+   walker's magnetisation of every measurement updated at every sample in the reference's order:
+   RF rotation, precession by the sample's gradient phase plus carrier[t] + crush[t] * u_w,
+   Mxy *= e2 * exp(-2 rho_over_D sum d_perp), Mz -> m0 + (Mz - m0) e1.  u_w is the walker's
+   crusher coordinate (Philox stream 2, counter 0, first word).  The per-sample arrays are host
+   arrays of n_t floats; carrier and crush may be NULL.  sums (n_echo, M, 3) receives sum Mx,
+   sum My, sum Mz at each echo sample. */
+typedef struct {
+  const float* rf_flip;
+  const float* rf_axis;
+  const float* carrier;
+  const float* crush;
+  double m0, e2, e1;
+} or_bloch_params;
+int or_bloch_f32(const or_geom* g, const or_walk_params* p, const or_bloch_params* b,
+                 const float* G, const float* r0, double* sums, int n_threads);
+int or_bloch_f64(const or_geom* g, const or_walk_params* p, const or_bloch_params* b,
+                 const float* G, const float* r0, double* sums, int n_threads);
+
 /* Philox4x32-10 draw (for cross-checking the stream contract). */
 void or_philox(uint64_t seed, uint64_t walker, uint32_t stream, uint32_t j, uint32_t out[4]);
 

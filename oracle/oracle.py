@@ -62,6 +62,12 @@ class OrWalk(C.Structure):
                 ("rho_over_D", C.c_double), ("kappa_over_D", C.c_double)]
 
 
+class OrBloch(C.Structure):
+    _fields_ = [("rf_flip", C.c_void_p), ("rf_axis", C.c_void_p), ("carrier", C.c_void_p),
+                ("crush", C.c_void_p), ("m0", C.c_double), ("e2", C.c_double),
+                ("e1", C.c_double)]
+
+
 _lib = None
 
 
@@ -89,6 +95,11 @@ def load():
                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         lib.or_philox.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
                                   C.POINTER(C.c_uint32)]
+        for suf in ("_f32", "_f64"):
+            f = getattr(lib, "or_bloch" + suf)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(OrGeom), C.POINTER(OrWalk), C.POINTER(OrBloch), C.c_void_p,
+                          C.c_void_p, C.c_void_p, C.c_int]
         for suf in ("_f32", "_f64"):
             f = getattr(lib, "or_pmyelin_plugin" + suf)
             f.restype = C.c_int
@@ -519,6 +530,48 @@ def walk(g, *, n_walkers, G, dt, sub_steps, phase_per_substep, seed, wall=REFLEC
         norm = float(np.sum(np.exp(np.asarray(m.logw0[:]))[comp]))
     out["signal"] = sums[..., 0] / norm
     return out
+
+
+def bloch(g, *, n_walkers, G, dt, sub_steps, seed, rf_flip, rf_axis, carrier=None, crush=None,
+          wall=REFLECT, T2=None, T1=None, M0=1.0, rho_over_D=0.0, kappa_over_D=0.0, D=2e-9,
+          echo_idx=None, r0=None, fp64=False, n_threads=0):
+    """Restated vector-Bloch walk (bloch.py:109-131, 180-198).  ``G`` (M, n_t, 3) in the walk
+    frame; per-sample ``rf_flip`` / ``rf_axis`` / ``carrier`` / ``crush`` in rad.  Returns the
+    sums (n_echo, M, 3) of Mx, My, Mz over the walkers."""
+    from dmipy_sim_gb300.constants import GAMMA
+    lib = load()
+    G = np.asarray(G, dtype=np.float32)
+    M, n_t, _ = G.shape
+    Gt = np.ascontiguousarray(G.transpose(1, 0, 2))
+    S = int(sub_steps)
+    dt = float(dt)
+    echo = np.asarray([n_t - 1] if echo_idx is None else echo_idx, dtype=np.int32)
+    p = OrWalk()
+    p.n_walkers, p.seed = int(n_walkers), int(seed)
+    p.n_t, p.n_meas, p.sub_steps, p.phase_per_substep = n_t, M, S, 1
+    p.wall, p.n_echo = int(wall), len(echo)
+    echo_c = (C.c_int32 * len(echo))(*echo.tolist())
+    p.echo_idx = echo_c
+    p.step_length = float(np.float32(np.sqrt(6.0 * D * dt / S)))
+    p.gamma_dt = float(np.float32(GAMMA * dt / S))
+    p.rho_over_D = float(np.float32(rho_over_D))
+    p.kappa_over_D = float(np.float32(kappa_over_D))
+    arrs = [None if a is None else np.ascontiguousarray(a, np.float32)
+            for a in (rf_flip, rf_axis, carrier, crush)]
+    b = OrBloch()
+    b.rf_flip, b.rf_axis, b.carrier, b.crush = [None if a is None else a.ctypes.data
+                                                for a in arrs]
+    b.m0 = float(M0)
+    b.e2 = float(np.float32(np.exp(-dt / T2))) if T2 is not None else 1.0
+    b.e1 = float(np.float32(np.exp(-dt / T1))) if T1 is not None else 1.0
+    r0_a = None if r0 is None else np.ascontiguousarray(r0, dtype=np.float32)
+    sums = np.zeros((len(echo), M, 3), dtype=np.float64)
+    f = lib.or_bloch_f64 if fp64 else lib.or_bloch_f32
+    rc = f(C.byref(g), C.byref(p), C.byref(b), Gt.ctypes.data,
+           None if r0_a is None else r0_a.ctypes.data, sums.ctypes.data, int(n_threads))
+    if rc != 0:
+        raise RuntimeError("oracle Bloch walk failed")
+    return sums
 
 
 def philox(seed, walker, stream, j):

@@ -53,6 +53,12 @@ def split(key, num=2):
     return KeyArray(Key(s) for s in key.ss.spawn(int(num)))
 
 
+def fold_in(key, data):
+    """A key derived from ``key`` and an integer, distinct from its split children."""
+    return Key(np.random.SeedSequence(key.ss.entropy,
+                                      spawn_key=tuple(key.ss.spawn_key) + (int(data) + (1 << 40),)))
+
+
 def normal(key, shape=(), dtype=np.float32):
     return _rng(key).standard_normal(shape).astype(np.float32)
 
@@ -137,10 +143,16 @@ def _array(*a, **k):
     return np.array(*a, **k).view(_AtArray)
 
 
+def _zeros(*a, **k):
+    return np.zeros(*a, **k).view(_AtArray)
+
+
 class _NumpyModule(types.ModuleType):
     def __getattr__(self, name):
         if name == "array":
             return _array
+        if name == "zeros":
+            return _zeros
         return getattr(np, name)
 
 
@@ -150,7 +162,7 @@ def install():
     jnp = _NumpyModule("jax.numpy")
     jnp.linalg = np.linalg
     rnd = types.ModuleType("jax.random")
-    for f in (PRNGKey, split, normal, uniform, randint):
+    for f in (PRNGKey, split, fold_in, normal, uniform, randint):
         setattr(rnd, f.__name__, f)
     lax = types.ModuleType("jax.lax")
     lax.scan = scan

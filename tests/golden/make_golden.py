@@ -841,6 +841,100 @@ def make_mc(root, procs, only=None):
     print(f"mc.json: {sorted(out)}")
 
 
+def _bloch_worker(args):
+    root, name, seed, n = args
+    m = _ref(root)
+    import importlib
+    sys.path.insert(0, str(HERE.parent))
+    import bloch_cases as bc
+    ps = importlib.import_module("dmipy_sim.pulse_sequence")
+    case = bc.CASES[name]
+    seq = bc.sequence(ps, case["seq"])
+    g = bc.geometry(m["geometries"], case["geom"])
+    out = ps.run_bloch_sequence(seq, n, bc.D, g, seed=seed, require_gpu=False, **case["kw"])
+    return name, n, bc.flatten(out, case["kw"].get("return_mz", False))
+
+
+def make_mc_bloch(root, procs, only=None):
+    """mc_bloch.json: dmipy-sim's own simulate_bloch on the scenarios of bloch_cases.py, mean and
+    standard error over independent chunks (Re S, Im S, and Mz where returned)."""
+    sys.path.insert(0, str(HERE.parent))
+    import bloch_cases as bc
+    jobs = []
+    for name, case in bc.CASES.items():
+        if only and name not in only:
+            continue
+        per = max(1, case["n"] // procs)
+        for k in range(procs):
+            jobs.append((root, name, 3000 + 29 * k, per))
+    t0 = time.time()
+    res = {}
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for name, n, s in pool.imap_unordered(_bloch_worker, jobs):
+            res.setdefault(name, []).append((n, s))
+            print(f"  {name}: chunk of {n} done ({time.time() - t0:.0f}s)", flush=True)
+    path = HERE / "mc_bloch.json"
+    out = json.loads(path.read_text()) if path.exists() else {}
+    for name, chunks in res.items():
+        arr = np.stack([s for _, s in chunks])
+        ns = np.array([n for n, _ in chunks], float)
+        mean = np.tensordot(ns, arr, axes=1) / ns.sum()
+        se = np.sqrt(np.sum(ns[:, None] * (arr - mean[None]) ** 2, axis=0) / ns.sum()
+                     / (len(ns) - 1))
+        out[name] = dict(n_walkers=int(ns.sum()), chunks=len(ns), value=mean.tolist(),
+                         stderr=se.tolist())
+    path.write_text(json.dumps(out, indent=1))
+    print(f"mc_bloch.json: {sorted(out)}")
+
+
+def make_bloch_kat(root):
+    """bloch_kat.npz: dmipy-sim's own RF rasterisation, crusher schedule and sequence builders
+    (bloch.py:60-89, 208-225; pulse_sequence.py:47-213) on fixed inputs."""
+    m = _ref(root)
+    import importlib
+    b = importlib.import_module("dmipy_sim.bloch")
+    ps = importlib.import_module("dmipy_sim.pulse_sequence")
+    out = {}
+    events = [
+        [{'t_s': 0.0, 'flip_deg': 90.0, 'axis_deg': 90.0}],
+        [{'t_s': 0.0, 'flip_deg': 90.0}, {'t_s': 2.05e-3, 'flip_deg': 180.0, 'axis_deg': 0.0,
+                                           'duration_s': 1e-3, 'offset_hz': 120.0}],
+        [{'t_s': 1e-3, 'flip_deg': 45.0, 'axis_deg': 30.0, 'duration_s': 2.4e-3,
+          'offset_hz': -80.0}, {'t_s': 9.99e-3, 'flip_deg': 33.0, 'duration_s': 5e-4}],
+    ]
+    for i, ev in enumerate(events):
+        fl, ax, ca = b._build_rf_schedule(ev, 1e-4, 100)
+        out[f"rf{i}_flip"], out[f"rf{i}_axis"], out[f"rf{i}_carrier"] = fl, ax, ca
+    for i, cr in enumerate([None, {'windows_s': [(1e-3, 3e-3)], 'n_cycles': 8.0},
+                            {'windows_s': [(-1e-3, 2e-3), (8e-3, 20e-3)]}]):
+        rate, has = b._build_crusher(cr, 1e-4, 100)
+        out[f"crush{i}_rate"], out[f"crush{i}_has"] = rate, np.array(has)
+    seqs = {
+        "gre": ps.gradient_echo(5e-3, 1e-4, n_meas=2),
+        "se": ps.spin_echo(6e-3, 1e-4, exc_axis_deg=45.0),
+        "fexi": ps.fexi(2e-3, 5e-3, 1e-4, g_filter=0.2, g_detect=[0.0, 0.1, 0.2], Delta=4e-3,
+                        direction=(1.0, 1.0, 0.0), crush_cycles=16.0),
+        "fexi2": ps.fexi(2e-3, 3e-3, 2e-4, g_filter=0.1, g_detect=0.05),
+        "mt": ps.prepend_mt_prep(ps.spin_echo(6e-3, 1e-4),
+                                 {'offset_hz': 2000.0, 'duration_s': 3e-3, 'b1_hz': 100.0}),
+        "mt2": ps.prepend_mt_prep(
+            ps.BlochSequence(G=np.zeros((1, 30, 3)), dt=1e-4, rf_events=[
+                {'t_s': 0.0, 'flip_deg': 90.0}], echo_steps=[10, 29]),
+            {'offset_hz': -500.0, 'duration_s': 1e-3, 'flip_deg': 400.0, 'spoiler_s': 0.0}),
+    }
+    for k, q in seqs.items():
+        out[f"seq_{k}_G"] = np.asarray(q.G)
+        out[f"seq_{k}_dt"] = np.float64(q.dt)
+        out[f"seq_{k}_rf"] = np.array(json.dumps(q.rf_events))
+        out[f"seq_{k}_echo"] = np.array(json.dumps(q.echo_steps))
+        out[f"seq_{k}_crusher"] = np.array(json.dumps(q.crusher))
+        out[f"seq_{k}_meta"] = np.array(json.dumps([q.complex_signal, q.family]))
+        if hasattr(q, "b_detect"):
+            out[f"seq_{k}_b_detect"] = np.asarray(q.b_detect)
+    np.savez_compressed(HERE / "bloch_kat.npz", **out)
+    print(f"bloch_kat.npz: {len(out)} arrays")
+
+
 def _jsonable(cfg):
     return {k: (list(v) if isinstance(v, tuple) else v) for k, v in cfg.items()}
 
@@ -856,6 +950,10 @@ if __name__ == "__main__":
     ap.add_argument("--replay-kat", action="store_true",
                     help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
+    ap.add_argument("--mc-bloch", action="store_true",
+                    help="write mc_bloch.json (the reference's simulate_bloch on bloch_cases.py)")
+    ap.add_argument("--bloch-kat", action="store_true",
+                    help="write bloch_kat.npz (RF schedule, crusher, sequence builders)")
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--procs", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
@@ -869,3 +967,7 @@ if __name__ == "__main__":
         make_myelin_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)
+    if a.mc_bloch:
+        make_mc_bloch(a.ref, a.procs, a.only)
+    if a.bloch_kat:
+        make_bloch_kat(a.ref)
