@@ -234,7 +234,10 @@ def profile_case(a):
     mesh      the permeable walk through the 200-cell ellipsoid mesh (~500k triangles),
               8192 walkers x 64 samples;
     mlp       the surrogate's forward pass on 262,144 queries (4 tensor-core GEMMs + head);
-    batched   a 32-instance slice of the batched study at 4096 walkers per instance."""
+    batched   a 32-instance slice of the batched study at 4096 walkers per instance;
+    bloch     the vector-Bloch walk of a diffusion-weighted spin echo (2 measurements, 201
+              samples) in a 4 um cylinder with surface relaxivity, 1,048,576 walkers; also
+              times the scalar walk of the same gradient, geometry and walk."""
     import dataclasses
     import torch
     import dmipy_sim_gb300 as d
@@ -242,6 +245,33 @@ def profile_case(a):
     from dmipy_sim_gb300 import substrates as S
     dev = torch.device("cuda", 0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    extra = {}
+    if a.profile_case == "bloch":
+        from dmipy_sim_gb300 import bloch as B
+        n_w = 1 << 20
+        seq = d.spin_echo(20e-3, 1e-4, n_meas=2)
+        seq.G[0, 20:60, 0] = seq.G[0, 110:150, 0] = 0.1
+        seq.G[1, 20:60, 2] = seq.G[1, 110:150, 2] = 0.1
+        cyl = d.Cylinder(4e-6, (0, 0, 1))
+        bw, _u, _i = B._prepare(n_w, D, seq, cyl, seq.rf_events, T2=0.08, T1=1.0, M0=1.0,
+                                off_resonance_hz=20.0, seed=7, echo_steps=None, return_mz=True,
+                                crusher=None, surface_relaxivity=2e-5)
+        sw = core.PreparedWalk(d.Cylinder(4e-6, (0, 0, 1), surface_relaxivity_t2=2e-5),
+                               n_walkers=n_w, diffusivity=D, G=seq.G, dt=seq.dt, sub_steps=1,
+                               phase_per_substep=True, seed=7, T2=0.08)
+        for _ in range(2):
+            sw.launch()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        s0.record()
+        for _ in range(max(1, a.steps)):
+            sw.launch()
+        s1.record()
+        torch.cuda.synchronize(dev)
+        ms = s0.elapsed_time(s1) / max(1, a.steps)
+        extra = {"walker_steps_per_launch": n_w * seq.n_t,
+                 "scalar_walk_ms": ms,
+                 "scalar_walker_steps_per_s": n_w * seq.n_t / (ms * 1e-3)}
     for _ in range(max(1, a.warmup) + a.steps):
         if _ == max(1, a.warmup):
             torch.cuda.synchronize(dev)
@@ -263,6 +293,8 @@ def profile_case(a):
                 net = MLP(69, 256, 4, seed=0)
                 x = torch.randn(262_144, 69, device=dev)
             net.predict(x)
+        elif a.profile_case == "bloch":
+            bw.launch()
         else:
             if _ == 0:
                 from dmipy_sim_gb300.batched import PreparedBatch
@@ -272,8 +304,11 @@ def profile_case(a):
             b.launch()
     e1.record()
     torch.cuda.synchronize(dev)
-    print(json.dumps({"profile_case": a.profile_case, "ok": True,
-                      "ms_per_step": e0.elapsed_time(e1) / max(1, a.steps)}))
+    ms = e0.elapsed_time(e1) / max(1, a.steps)
+    if a.profile_case == "bloch":
+        extra["bloch_walker_steps_per_s"] = extra["walker_steps_per_launch"] / (ms * 1e-3)
+    print(json.dumps(dict({"profile_case": a.profile_case, "ok": True, "ms_per_step": ms},
+                          **extra)))
 
 
 def gpu_arm(a):
@@ -454,7 +489,7 @@ def main():
                     help="walkers per instance of the batched study (20000: <= 0.005 error)")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per GPU (smaller only for profiling captures)")
-    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched"], default=None,
+    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched", "bloch"], default=None,
                     help="run one small kernel case for a profiler capture and exit")
     a = ap.parse_args()
     if a.profile_case:

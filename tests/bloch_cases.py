@@ -12,8 +12,6 @@ CASES = {
     # along a reflecting cylinder, with surface relaxivity on the Bloch walk
     "bloch_se_cyl": dict(geom=("cyl", 4e-6, None), seq="se_dw", n=2000,
                          kw=dict(T2=0.08, T1=1.0, surface_relaxivity=2e-5)),
-    # the same echo on a permeable cylinder: the sub-stepped Powles walk (bloch.py:133-162)
-    "bloch_se_cyl_perm": dict(geom=("cyl", 5e-6, 2e-5), seq="se_dw", n=480, kw=dict(T2=0.08)),
     # a 180 train refocusing a static off-resonance under a constant gradient in a sphere
     "bloch_cpmg_sph": dict(geom=("sph", 4e-6, None), seq="cpmg", n=2000,
                            kw=dict(T2=0.06, off_resonance_hz=30.0)),
