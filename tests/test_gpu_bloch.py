@@ -76,7 +76,8 @@ def test_cpmg_refocuses_static_offset(cuda):
     ec = d.simulate_bloch(4000, D, _zero(n_t, dt), d.FreeDiffusion(), EXC_Y + refocus, T2=T2,
                           off_resonance_hz=f, seed=0, echo_steps=echo)[0]
     for k in range(n_echo):
-        assert abs(ec[k]) == pytest.approx(np.exp(-(k + 1) * TE / T2), rel=1e-3)
+        # an echo is read after its sample's relaxation: samples 0 .. echo[k] each decay
+        assert abs(ec[k]) == pytest.approx(np.exp(-(echo[k] + 1) * dt / T2), rel=1e-4)
         assert abs(np.angle(ec[k])) < 0.15
     free = d.simulate_bloch(4000, D, _zero(n_t, dt), d.FreeDiffusion(), EXC_Y, T2=T2,
                             off_resonance_hz=f, seed=0, echo_steps=echo)[0]
