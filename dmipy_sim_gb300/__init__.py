@@ -24,7 +24,7 @@ from .autotune import autotune
 from . import compression, bank, replay
 from .replay import ReplayPack, read_rpk, write_rpk, compile_scheme, replay_signal
 from .bank import build_replay_pack, build_to_floor
-from . import bloch, pulse_sequence
+from . import bloch, mt, pulse_sequence
 from .bloch import simulate_bloch
 from .pulse_sequence import (BlochSequence, gradient_echo, spin_echo, prepend_mt_prep,
                              run_bloch_sequence, emergent_z_spectrum)
@@ -41,7 +41,7 @@ __all__ = [
     "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
     "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune", "compression", "bank", "replay",
     "ReplayPack", "read_rpk", "write_rpk", "compile_scheme", "replay_signal", "build_replay_pack",
-    "build_to_floor", "bloch", "pulse_sequence", "simulate_bloch",
+    "build_to_floor", "bloch", "mt", "pulse_sequence", "simulate_bloch",
     "BlochSequence", "gradient_echo", "spin_echo", "prepend_mt_prep", "run_bloch_sequence",
     "emergent_z_spectrum",
 ]

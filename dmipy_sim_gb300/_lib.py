@@ -31,7 +31,8 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_pack",
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
             "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes",
-            "dmsim_bloch_workspace_bytes", "dmsim_bloch")
+            "dmsim_bloch_workspace_bytes", "dmsim_bloch", "dmsim_bloch_mt_workspace_bytes",
+            "dmsim_bloch_mt")
 
 EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
@@ -95,6 +96,20 @@ class BlochParams(C.Structure):
     ]
 
 
+class MtParams(C.Structure):
+    _fields_ = [
+        ("n_walkers", C.c_int64), ("seed", C.c_uint64), ("substep_offset", C.c_uint32),
+        ("n_t", C.c_int32), ("n_meas", C.c_int32), ("n_sub", C.c_int32), ("n_echo", C.c_int32),
+        ("spin", C.c_int32), ("echo_idx", C.POINTER(C.c_int32)), ("step_length", C.c_float),
+        ("kappa_mt_over_D", C.c_float), ("dwell_substeps", C.c_float), ("rho_over_D", C.c_float),
+        ("gamma_dt", C.c_double), ("m0", C.c_double), ("e2h", C.c_double * 2),
+        ("e1h", C.c_double * 2), ("G", C.c_void_p), ("rot", C.c_void_p), ("crush", C.c_void_p),
+        ("r0", C.c_void_p), ("brem_in", C.c_void_p), ("brem_out", C.c_void_p),
+        ("r_end", C.c_void_p), ("occ", C.c_void_p), ("occ_total", C.c_void_p),
+        ("sums", C.c_void_p), ("status", C.c_void_p),
+    ]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [
         ("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("order", C.c_int32),
@@ -136,6 +151,11 @@ def load():
     lib.dmsim_bloch.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
                                 C.POINTER(BlochParams), C.POINTER(WalkOutputs), C.c_void_p,
                                 C.c_size_t, C.c_void_p]
+    lib.dmsim_bloch_mt_workspace_bytes.restype = C.c_size_t
+    lib.dmsim_bloch_mt_workspace_bytes.argtypes = [C.POINTER(MtParams), C.POINTER(Geometry)]
+    lib.dmsim_bloch_mt.restype = C.c_int
+    lib.dmsim_bloch_mt.argtypes = [C.POINTER(MtParams), C.POINTER(Geometry), C.c_void_p,
+                                   C.c_size_t, C.c_void_p]
     lib.dmsim_walk_noalloc.restype = C.c_int
     lib.dmsim_walk_noalloc.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
                                        C.POINTER(WalkOutputs), C.c_void_p]

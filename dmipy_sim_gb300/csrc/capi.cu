@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "dmsim.h"
+#include "mt_kernel.cuh"
 #include "walk_kernel.cuh"
 
 namespace dmsim {
@@ -714,6 +715,81 @@ int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dms
   return DMSIM_OK;
 }
 
+// ---- magnetisation-transfer walk --------------------------------------------------------------
+struct MtPlan {
+  MtFn fn = nullptr;
+  int width = 0, n_pass = 0, grid = 0;
+  size_t total = 0;
+};
+
+int mt_plan(const dmsim_mt_params* p, const dmsim_geometry* g, MtPlan* pl) {
+  if (!p || !g) return fail(DMSIM_EINVAL, "null MT params or geometry");
+  if (p->n_walkers < 0 || p->n_t < 1 || p->n_sub < 1 || p->n_meas < 1)
+    return fail(DMSIM_EINVAL, "MT walk needs n_walkers >= 0, n_t, n_sub, n_meas >= 1");
+  if (p->n_walkers > 0 && !p->r0) return fail(DMSIM_EINVAL, "MT walk needs start positions");
+  if (p->spin) {
+    if (p->n_echo < 1 || p->n_echo > kMtMaxEcho)
+      return fail(DMSIM_ETOOBIG, "n_echo must be in [1, %d]", kMtMaxEcho);
+    if (!p->echo_idx || !p->G || !p->rot || !p->sums)
+      return fail(DMSIM_EINVAL, "MT spin walk needs echo_idx, G, rot and sums");
+    for (int e = 0; e < p->n_echo; ++e) {
+      if (p->echo_idx[e] < 0 || p->echo_idx[e] >= p->n_t)
+        return fail(DMSIM_EINVAL, "echo index %d out of range", p->echo_idx[e]);
+      if (e > 0 && p->echo_idx[e] <= p->echo_idx[e - 1])
+        return fail(DMSIM_EINVAL, "echo indices must be strictly ascending");
+    }
+  }
+  if (!p->status) return fail(DMSIM_EINVAL, "MT walk needs the status words");
+  if (!(p->dwell_substeps > 0.f)) return fail(DMSIM_EINVAL, "dwell must be > 0");
+  const bool packed =
+      g->kind == DMSIM_GEOM_PACKED_CYLINDERS || g->kind == DMSIM_GEOM_PACKED_SPHERES;
+  if (packed) {
+    if (!g->cell_start || !g->cand || g->grid_n < 1 || !(g->L > 0.f))
+      return fail(DMSIM_EINVAL, "packed geometry needs a cell list");
+    if (!(g->reach >= p->step_length))
+      return fail(DMSIM_EINVAL, "cell list reach %g is shorter than the step %g", g->reach,
+                  p->step_length);
+  }
+  if ((g->kind == DMSIM_GEOM_BOX1D || g->kind == DMSIM_GEOM_SLAB) && !(g->L > 0.f))
+    return fail(DMSIM_EINVAL, "slab geometry needs its length L > 0");
+  if (g->kind == DMSIM_GEOM_ELLIPSOID &&
+      !(g->radius > 0.f && g->ell_inv2[0] > 0.f && g->ell_inv2[1] > 0.f && g->ell_inv2[2] > 0.f))
+    return fail(DMSIM_EINVAL, "ellipsoid needs positive semi-axes");
+  pl->width = p->n_meas <= 1 ? 1 : 4;
+  pl->fn = mt_fn(g->kind, pl->width);
+  if (!pl->fn)
+    return fail(DMSIM_EINVAL, "no MT walk for geometry kind %d (its walls have no log-weight "
+                              "rule)", g->kind);
+  pl->n_pass = (p->n_meas + pl->width - 1) / pl->width;
+  int dev = 0, n_sm = 0, nb = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(DMSIM_ECUDA, "cudaGetDevice failed");
+  if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return fail(DMSIM_ECUDA, "cudaDeviceGetAttribute failed");
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)pl->fn, kMtBlock, 0) !=
+          cudaSuccess ||
+      nb < 1)
+    return fail(DMSIM_ECUDA, "MT kernel does not fit on an SM");
+  const int64_t n_tiles = (p->n_walkers + kMtBlock - 1) / kMtBlock;
+  int64_t grid = (int64_t)nb * n_sm;
+  if (grid > n_tiles) grid = n_tiles;
+  pl->grid = (int)(grid < 1 ? 1 : grid);
+  pl->total = align256((size_t)pl->grid * (p->spin ? p->n_echo : 1) * pl->width * 3 * 8);
+  return DMSIM_OK;
+}
+
+// Fixed-order sum of the per-block partials of one pass into its measurements' sums.
+__global__ void k_mt_reduce(const double* __restrict__ part, int grid, int n_echo, int W, int M,
+                            int m_off, double* __restrict__ sums) {
+  const int n = n_echo * W * 3;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int e = i / (W * 3), r = i % (W * 3), m = m_off + r / 3;
+    if (m >= M) continue;
+    double acc = 0.0;
+    for (int b = 0; b < grid; ++b) acc += part[((size_t)b * n_echo + e) * W * 3 + r];
+    sums[((size_t)e * M + m) * 3 + r % 3] = acc;
+  }
+}
+
 }  // namespace
 
 namespace dmsim {
@@ -744,6 +820,76 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
     return fail(DMSIM_EWORKSPACE, "workspace %zu B < required %zu B", workspace_bytes, pl.total);
   if (((uintptr_t)workspace & 255) != 0) return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
   return launch_single(p, g, o, pl, static_cast<uint8_t*>(workspace), (cudaStream_t)stream);
+}
+
+size_t dmsim_bloch_mt_workspace_bytes(const dmsim_mt_params* p, const dmsim_geometry* g) {
+  MtPlan pl;
+  if (mt_plan(p, g, &pl) != DMSIM_OK) return 0;
+  return pl.total;
+}
+
+int dmsim_bloch_mt(const dmsim_mt_params* p, const dmsim_geometry* g, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  MtPlan pl;
+  int rc = mt_plan(p, g, &pl);
+  if (rc != DMSIM_OK) return rc;
+  if (!workspace || workspace_bytes < pl.total)
+    return fail(DMSIM_EWORKSPACE, "workspace %zu B < required %zu B", workspace_bytes, pl.total);
+  if (((uintptr_t)workspace & 255) != 0) return fail(DMSIM_EINVAL, "workspace must be 256-B aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (p->n_walkers == 0) {
+    if (p->spin) cudaMemsetAsync(p->sums, 0, sizeof(double) * p->n_echo * p->n_meas * 3, st);
+    return DMSIM_OK;
+  }
+  MtArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n_walkers = p->n_walkers;
+  a.seed = p->seed;
+  a.s0 = p->substep_offset;
+  a.n_t = p->n_t;
+  a.n_sub = p->n_sub;
+  a.M = p->n_meas;
+  a.n_echo = p->spin ? p->n_echo : 0;
+  a.spin = p->spin ? 1 : 0;
+  a.step_l = p->step_length;
+  a.kod_mt = p->kappa_mt_over_D;
+  a.dwell = p->dwell_substeps;
+  a.rho = p->rho_over_D;
+  a.gamma_dt = p->gamma_dt;
+  a.m0 = p->m0;
+  for (int k = 0; k < 2; ++k) {
+    a.e2h[k] = p->e2h[k];
+    a.e1h[k] = p->e1h[k];
+  }
+  a.g = make_geok(g);
+  a.cs = g->cell_start;
+  a.cand = reinterpret_cast<const float4*>(g->cand);
+  a.G = p->G;
+  a.rot = p->rot;
+  a.crush = p->crush;
+  a.r0 = p->r0;
+  a.brem_in = p->brem_in;
+  a.brem_out = p->brem_out;
+  a.r_end = p->r_end;
+  a.occ = p->occ;
+  a.occ_total = p->occ_total;
+  a.part = reinterpret_cast<double*>(workspace);
+  a.status = p->status;
+  for (int e = 0; e < a.n_echo; ++e) a.echo[e] = p->echo_idx[e];
+  const int passes = p->spin ? pl.n_pass : 1;
+  for (int pass = 0; pass < passes; ++pass) {
+    a.pass = pass;
+    a.m_off = pass * pl.width;
+    pl.fn<<<pl.grid, kMtBlock, 0, st>>>(a);
+    if (p->spin) {
+      const int nred = a.n_echo * pl.width * 3;
+      k_mt_reduce<<<(nred + 255) / 256, 256, 0, st>>>(a.part, pl.grid, a.n_echo, pl.width,
+                                                      p->n_meas, a.m_off, p->sums);
+    }
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));
+  return DMSIM_OK;
 }
 
 size_t dmsim_bloch_workspace_bytes(const dmsim_walk_params* p, const dmsim_geometry* g) {

@@ -326,6 +326,55 @@ int dmsim_bloch(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim
                 const dmsim_walk_outputs* o, void* workspace, size_t workspace_bytes,
                 void* stream);
 
+/* ---- magnetisation-transfer Bloch walk ---------------------------------------------------------
+   The binding walk of bloch.py:343-671 (simulate_bloch with kappa_MT > 0): every sample of dt is
+   n_sub sub-steps; in each a free walker takes a reflecting step of step_length (the boundary
+   log-weight dl = -2 sum d_perp of the wall hits, geometries' reflect_with_log_weight), sticks
+   with probability min(1, kappa_mt_over_D * (-dl)) on the third uniform of its Philox draw and
+   then stays put for -ln(max(u4, 1e-20)) * dwell_substeps sub-steps (u4 the fourth uniform); a
+   bound walker counts its dwell down.  With spin = 1 each walker's magnetisation M_m (FP64) is
+   carried through every sub-step by a Strang split -- half relaxation with the walker's current
+   pool (e2h, e1h [free, bound]), the rotation rot[t][pool] (RF nutation and off-resonance over
+   one sub-step, row-major 3x3), the second half relaxation and, for a free walker that did not
+   just bind, Mxy *= exp(rho_over_D * dl) -- and, after the sample's sub-steps, Mxy is rotated by
+   gamma_dt * G[t, m] . r + crush[t] * u_w (u_w from Philox stream 2, as dmsim_bloch).  The
+   uniforms of sub-step s come from Philox stream 0, counter substep_offset + s, so a burn-in
+   (spin = 0) continued by the sequence's walk draws the walk the reference's carried keys draw.
+   Geometries: cylinder, sphere, ellipsoid, Box1D, PermeableSlab1D and packed cylinders / spheres
+   (their walls always reflect here).  Outputs: sums (n_echo, n_meas, 3) of Mx, My, Mz at each
+   echo sample (after its update); per walker the end position, the residual dwell, the bound
+   fraction per sample and its sum over the samples. */
+typedef struct dmsim_mt_params {
+  int64_t n_walkers;
+  uint64_t seed;
+  uint32_t substep_offset;  /* Philox counter of the first sub-step                             */
+  int32_t n_t, n_meas, n_sub, n_echo;
+  int32_t spin;             /* 1: evolve the magnetisation; 0: walk and binding only (burn-in)  */
+  const int32_t* echo_idx;  /* HOST array of n_echo ascending sample indices (spin = 1)          */
+  float step_length;        /* sqrt(6 D dt / n_sub)                                             */
+  float kappa_mt_over_D;    /* binding reactivity over D (1/m)                                  */
+  float dwell_substeps;     /* mean dwell in sub-steps                                          */
+  float rho_over_D;         /* transverse surface relaxivity over D at free wall contacts       */
+  double gamma_dt;          /* gamma * dt                                                       */
+  double m0;                /* equilibrium longitudinal magnetisation                           */
+  double e2h[2], e1h[2];    /* exp(-dt_sub / (2 T2)), exp(-dt_sub / (2 T1)): free, bound         */
+  const float* G;           /* DEVICE (n_t, n_meas, 3) walk frame, T/m (spin = 1)               */
+  const double* rot;        /* DEVICE (n_t, 2, 9) per-sub-step rotation, free / bound (spin = 1)*/
+  const float* crush;       /* DEVICE (n_t) crusher rate or NULL                                */
+  const float* r0;          /* DEVICE (n_walkers, 3) walk-frame start positions                 */
+  const float* brem_in;     /* DEVICE (n_walkers) residual dwell at the start, or NULL (free)    */
+  float* brem_out;          /* DEVICE (n_walkers) residual dwell at the end, or NULL            */
+  float* r_end;             /* DEVICE (n_walkers, 3) end positions (unfolded) or NULL           */
+  float* occ;               /* DEVICE (n_walkers, n_t) bound fraction of each sample, or NULL   */
+  float* occ_total;         /* DEVICE (n_walkers) sum of the samples' bound fractions, or NULL  */
+  double* sums;             /* DEVICE (n_echo, n_meas, 3), overwritten (spin = 1)               */
+  uint32_t* status;         /* DEVICE DMSIM_STATUS_WORDS counters                               */
+} dmsim_mt_params;
+
+size_t dmsim_bloch_mt_workspace_bytes(const dmsim_mt_params* p, const dmsim_geometry* g);
+int dmsim_bloch_mt(const dmsim_mt_params* p, const dmsim_geometry* g, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
 /* Temporal-mode projection, the compressed trajectory export of simulate_trajectories(compress=K)
    (core.py:1370-1407) and the temporal_dct / boundary_dct codecs of compression.py:55-62, 224-249:
    out[w,k,c] = sum_t basis[k,t] * x[w,t,c] with x (n_walkers, n_t, n_ch) float16 (x_f16 = 1) or

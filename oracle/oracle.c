@@ -50,6 +50,7 @@ static double round_half(float f) {
 #define SIN sinf
 #define COS cosf
 #define EXP expf
+#define LOG logf
 #define MAX(a, b) fmaxf((a), (b))
 #define MIN(a, b) fminf((a), (b))
 #include "oracle_impl.inc"
@@ -63,6 +64,7 @@ static double round_half(float f) {
 #undef SIN
 #undef COS
 #undef EXP
+#undef LOG
 #undef MAX
 #undef MIN
 
@@ -76,6 +78,7 @@ static double round_half(float f) {
 #define SIN sin
 #define COS cos
 #define EXP exp
+#define LOG log
 #define MAX(a, b) fmax((a), (b))
 #define MIN(a, b) fmin((a), (b))
 #include "oracle_impl.inc"

@@ -169,6 +169,38 @@ int or_bloch_f32(const or_geom* g, const or_walk_params* p, const or_bloch_param
 int or_bloch_f64(const or_geom* g, const or_walk_params* p, const or_bloch_params* b,
                  const float* G, const float* r0, double* sums, int n_threads);
 
+/* Magnetisation-transfer Bloch walk (bloch.py:468-553), restated eagerly: per sub-step one
+   Philox draw (stream 0, counter s0 + s: x, y the direction, z the binding test, w the dwell); a
+   free walker takes a reflecting step with its boundary log-weight dl and sticks with
+   min(1, kod_mt * (-dl)), then stays put for -ln(max(w, 1e-20)) * dwell_substeps sub-steps; the
+   FP64 magnetisation takes half relaxation of the walker's pool, the exact rotation about
+   (f cos ax, f sin ax, dphi_pool) (f = flip / n_sub, dphi the pool's carrier over a sub-step),
+   the second half relaxation and, for a free walker that did not just bind, the factor
+   exp(rho_over_D dl); after the sub-steps Mxy turns by gamma_dt G.r + crush u_w.  T2/T1 of 0
+   mean none.  Per-sample arrays are host arrays of n_t floats (carrier, crush may be NULL);
+   r0 is required, brem0 optional.  sums (n_echo, M, 3): sum Mx, My, Mz at each echo sample. */
+typedef struct {
+  int64_t n_walkers;
+  uint64_t seed;
+  uint32_t s0;
+  int32_t n_t, n_meas, n_sub, n_echo;
+  const int32_t* echo_idx;
+  double step_length, kod_mt, dwell_substeps, rho_over_D, gamma_dt, m0, dt;
+  double T2[2], T1[2], off[2];  /* free, bound */
+  const float* G;               /* (n_t, M, 3) */
+  const float* rf_flip;
+  const float* rf_axis;
+  const float* carrier;
+  const float* crush;
+  const float* r0;
+  const float* brem0;
+  float* r_end;
+  float* brem_end;
+  float* occ_total;
+} or_mt_params;
+int or_bloch_mt_f32(const or_geom* g, const or_mt_params* p, double* sums, int n_threads);
+int or_bloch_mt_f64(const or_geom* g, const or_mt_params* p, double* sums, int n_threads);
+
 /* Philox4x32-10 draw (for cross-checking the stream contract). */
 void or_philox(uint64_t seed, uint64_t walker, uint32_t stream, uint32_t j, uint32_t out[4]);
 

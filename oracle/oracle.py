@@ -68,6 +68,20 @@ class OrBloch(C.Structure):
                 ("e1", C.c_double)]
 
 
+class OrMt(C.Structure):
+    _fields_ = [("n_walkers", C.c_int64), ("seed", C.c_uint64), ("s0", C.c_uint32),
+                ("n_t", C.c_int32), ("n_meas", C.c_int32), ("n_sub", C.c_int32),
+                ("n_echo", C.c_int32), ("echo_idx", C.POINTER(C.c_int32)),
+                ("step_length", C.c_double), ("kod_mt", C.c_double),
+                ("dwell_substeps", C.c_double), ("rho_over_D", C.c_double),
+                ("gamma_dt", C.c_double), ("m0", C.c_double), ("dt", C.c_double),
+                ("T2", C.c_double * 2), ("T1", C.c_double * 2), ("off", C.c_double * 2),
+                ("G", C.c_void_p), ("rf_flip", C.c_void_p), ("rf_axis", C.c_void_p),
+                ("carrier", C.c_void_p), ("crush", C.c_void_p), ("r0", C.c_void_p),
+                ("brem0", C.c_void_p), ("r_end", C.c_void_p), ("brem_end", C.c_void_p),
+                ("occ_total", C.c_void_p)]
+
+
 _lib = None
 
 
@@ -95,6 +109,10 @@ def load():
                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         lib.or_philox.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
                                   C.POINTER(C.c_uint32)]
+        for suf in ("_f32", "_f64"):
+            f = getattr(lib, "or_bloch_mt" + suf)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(OrGeom), C.POINTER(OrMt), C.c_void_p, C.c_int]
         for suf in ("_f32", "_f64"):
             f = getattr(lib, "or_bloch" + suf)
             f.restype = C.c_int
@@ -572,6 +590,51 @@ def bloch(g, *, n_walkers, G, dt, sub_steps, seed, rf_flip, rf_axis, carrier=Non
     if rc != 0:
         raise RuntimeError("oracle Bloch walk failed")
     return sums
+
+
+def bloch_mt(g, *, n_walkers, G, dt, n_sub, seed, r0, rf_flip, rf_axis, carrier=None,
+             crush=None, kappa_MT, dwell_time, D=2e-9, T2=None, T1=None, T2_bound=1e-5,
+             T1_bound=1.0, off_resonance_hz=0.0, off_resonance_bound=0.0, rho=0.0, M0=1.0,
+             echo_idx=None, brem0=None, s0=0, fp64=False, n_threads=0):
+    """Restated magnetisation-transfer walk (bloch.py:468-553).  Returns a dict with ``sums``
+    (n_echo, M, 3) of Mx, My, Mz and the walkers' ``r_end``, ``brem`` and ``occ_total``."""
+    from dmipy_sim_gb300.constants import GAMMA
+    lib = load()
+    G = np.asarray(G, dtype=np.float32)
+    M, n_t, _ = G.shape
+    Gt = np.ascontiguousarray(G.transpose(1, 0, 2))
+    dt = float(dt)
+    dt_sub = dt / int(n_sub)
+    echo = np.asarray([n_t - 1] if echo_idx is None else echo_idx, dtype=np.int32)
+    p = OrMt()
+    p.n_walkers, p.seed, p.s0 = int(n_walkers), int(seed), int(s0)
+    p.n_t, p.n_meas, p.n_sub, p.n_echo = n_t, M, int(n_sub), len(echo)
+    echo_c = (C.c_int32 * len(echo))(*echo.tolist())
+    p.echo_idx = echo_c
+    p.step_length = float(np.float32(np.sqrt(6.0 * D * dt_sub)))
+    p.kod_mt = float(np.float32(kappa_MT / D))
+    p.dwell_substeps = float(np.float32(dwell_time / dt_sub))
+    p.rho_over_D = float(rho) / D
+    p.gamma_dt = GAMMA * dt
+    p.m0, p.dt = float(M0), dt
+    p.T2[0], p.T2[1] = (0.0 if T2 is None else T2), T2_bound
+    p.T1[0], p.T1[1] = (0.0 if T1 is None else T1), T1_bound
+    p.off[0], p.off[1] = off_resonance_hz, off_resonance_bound
+    keep = [Gt] + [None if a is None else np.ascontiguousarray(a, np.float32)
+                   for a in (rf_flip, rf_axis, carrier, crush, r0, brem0)]
+    p.G = Gt.ctypes.data
+    p.rf_flip, p.rf_axis, p.carrier, p.crush, p.r0, p.brem0 = [
+        None if a is None else a.ctypes.data for a in keep[1:]]
+    out = {"r_end": np.zeros((n_walkers, 3), np.float32), "brem": np.zeros(n_walkers, np.float32),
+           "occ_total": np.zeros(n_walkers, np.float32)}
+    p.r_end, p.brem_end = out["r_end"].ctypes.data, out["brem"].ctypes.data
+    p.occ_total = out["occ_total"].ctypes.data
+    sums = np.zeros((len(echo), M, 3), dtype=np.float64)
+    f = lib.or_bloch_mt_f64 if fp64 else lib.or_bloch_mt_f32
+    if f(C.byref(g), C.byref(p), sums.ctypes.data, int(n_threads)) != 0:
+        raise RuntimeError("oracle MT walk failed")
+    out["sums"] = sums
+    return out
 
 
 def philox(seed, walker, stream, j):

@@ -22,6 +22,16 @@ CASES = {
                               kw=dict(T2=0.05, T1=0.3, off_resonance_hz=40.0, return_mz=True)),
     # spin echo in a square lattice of reflecting cylinders (packed single-reflection rule)
     "bloch_se_pcyl": dict(geom=("lattice", 0.6), seq="se_dw", n=2000, kw=dict(T2=0.08)),
+    # magnetisation transfer: a gradient echo from the equilibrium bound occupancy ('fast'
+    # start), and an off-resonance CW saturation from an all-free start; few explicit sub-steps
+    # keep the reference's per-walker walk tractable
+    "bloch_mt_gre_fast": dict(geom=("sph", 2e-6, None), seq="gre3", n=1600, kw=dict(
+        T2=0.08, T1=1.0, kappa_MT=40.0 * 2e-6 / 3.0, dwell_time=1.0 / 80.0, T2_bound=1e-5,
+        T1_bound=1.0, sub_steps=4, equilibrate_binding='fast', return_mz=True,
+        return_bound_frac=True)),
+    "bloch_mt_sat_off": dict(geom=("sph", 2e-6, None), seq="cw_sat", n=800, kw=dict(
+        T2=0.08, T1=1.0, kappa_MT=40.0 * 2e-6 / 3.0, dwell_time=1.0 / 80.0, T2_bound=1e-5,
+        T1_bound=1.0, sub_steps=3, equilibrate_binding='off', return_mz=True)),
 }
 
 
@@ -50,6 +60,14 @@ def sequence(ps, name):
         return ps.BlochSequence(G=G, dt=dt, rf_events=rf, echo_steps=echo, family="cpmg")
     if name == "fexi":
         return ps.fexi(3e-3, 6e-3, 1e-4, g_filter=0.15, g_detect=[0.0, 0.15], Delta=6e-3)
+    if name == "gre3":
+        return ps.gradient_echo(3e-3, 1e-4)
+    if name == "cw_sat":
+        dt, t_sat = 5e-5, 5e-3
+        rf = [{'t_s': t_sat / 2, 'flip_deg': 360.0 * 200.0 * t_sat, 'axis_deg': 0.0,
+               'duration_s': t_sat, 'offset_hz': 1000.0}]
+        return ps.BlochSequence(G=np.zeros((1, int(round(t_sat / dt)) + 1, 3)), dt=dt,
+                                rf_events=rf, family="cw")
     if name == "finite":
         dt, n_t = 1e-4, 100
         rf = [{'t_s': 1e-3, 'flip_deg': 90.0, 'axis_deg': 30.0, 'duration_s': 2e-3,
@@ -77,13 +95,10 @@ def geometry(geo, spec):
 
 
 def flatten(out, return_mz=False):
-    """simulate_bloch's return as one real vector: Re S, Im S (and the final Mz)."""
-    if return_mz:
-        s, mz = out
-    else:
-        s, mz = out, None
-    s = np.asarray(s)
+    """simulate_bloch's return as one real vector: Re S, Im S, then whatever follows (the final
+    Mz, the bound-fraction series)."""
+    items = list(out) if isinstance(out, tuple) else [out]
+    s = np.asarray(items[0])
     parts = [s.real.ravel(), s.imag.ravel()]
-    if mz is not None:
-        parts.append(np.asarray(mz, np.float64).ravel())
+    parts += [np.asarray(x, np.float64).ravel() for x in items[1:]]
     return np.concatenate(parts).astype(np.float64)

@@ -172,6 +172,7 @@ def install():
     jax.vmap = vmap
     jax.jit = jit
     jax.Array = object
+    jax.config = types.SimpleNamespace(update=lambda *a, **k: None)   # numpy is FP64-capable
     jax.devices = lambda *a, **k: ["cpu"]
     jax.default_backend = lambda: "cpu"
     sys.modules["jax"] = jax

@@ -935,6 +935,37 @@ def make_bloch_kat(root):
     print(f"bloch_kat.npz: {len(out)} arrays")
 
 
+def make_mt_kat(root):
+    """mt_kat.npz: dmipy-sim's own two-pool Bloch-McConnell model and binding bookkeeping
+    (mt.py) on fixed inputs."""
+    _ref(root)
+    import importlib
+    mt = importlib.import_module("dmipy_sim.mt")
+    out = {}
+    out["gen"] = mt.two_pool_generator(R1a=1.1, R2a=12.5, R1b=0.9, R2b=1e5, k_f=40.0, k_r=80.0,
+                                       dw_a=300.0, dw_b=-50.0, w1=700.0, rf_phase=0.4)
+    out["gen_m0b"] = mt.two_pool_generator(R1a=1.0, R2a=10.0, R1b=1.0, R2b=1e4, k_f=30.0,
+                                           k_r=100.0, M0a=0.8, M0b=0.1)
+    t = np.array([0.0, 1e-3, 5e-3, 0.02, 0.08])
+    out["bmt"] = mt.bloch_mcconnell_transverse(t, T2a=80e-3, T2b=1e-5, k_f=30.0, k_r=100.0)
+    out["bmt_dw"] = mt.bloch_mcconnell_transverse(t, T2a=60e-3, T2b=2e-3, k_f=20.0, k_r=50.0,
+                                                  dw_a=100.0, dw_b=400.0, T1a=0.9, T1b=0.5)
+    out["bml"] = mt.bloch_mcconnell_longitudinal(t * 10, T1a=1.0, T1b=0.7, k_f=30.0, k_r=90.0)
+    out["bml_sat"] = mt.bloch_mcconnell_longitudinal(t * 10, T1a=1.2, T1b=1.0, k_f=30.0,
+                                                     k_r=90.0, Mza0=1.0, Mzb0=0.0)
+    off = np.array([-5000.0, -500.0, 0.0, 200.0, 2000.0, 20000.0])
+    kw = dict(w1_hz=200.0, t_sat=0.025, T1a=1.0, T2a=80e-3, T1b=1.0, T2b=1e-5, k_f=40.0,
+              k_r=80.0)
+    out["z_a"] = mt.mt_z_spectrum(off, **kw)
+    out["z_b"] = mt.mt_z_spectrum(off, read_pool="b", **kw)
+    out["misc"] = np.array([
+        mt.forward_rate(2e-6, 3e5), mt.backward_rate(0.0125), mt.bound_fraction(2e-6, 0.0125, 3e5),
+        mt.kappa_MT_from_forward_rate(40.0, 1.5e6), mt.dwell_time_from_fraction(0.3, 40.0)])
+    out["stick"] = mt.stick_probability(np.array([0.0, 1e-9, 1e-8, 1e-6]), 2e-5, 2e-9)
+    np.savez_compressed(HERE / "mt_kat.npz", **out)
+    print(f"mt_kat.npz: {len(out)} arrays")
+
+
 def _jsonable(cfg):
     return {k: (list(v) if isinstance(v, tuple) else v) for k, v in cfg.items()}
 
@@ -950,6 +981,8 @@ if __name__ == "__main__":
     ap.add_argument("--replay-kat", action="store_true",
                     help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
+    ap.add_argument("--mt-kat", action="store_true",
+                    help="write mt_kat.npz (the two-pool model and binding bookkeeping)")
     ap.add_argument("--mc-bloch", action="store_true",
                     help="write mc_bloch.json (the reference's simulate_bloch on bloch_cases.py)")
     ap.add_argument("--bloch-kat", action="store_true",
@@ -967,6 +1000,8 @@ if __name__ == "__main__":
         make_myelin_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)
+    if a.mt_kat:
+        make_mt_kat(a.ref)
     if a.mc_bloch:
         make_mc_bloch(a.ref, a.procs, a.only)
     if a.bloch_kat:

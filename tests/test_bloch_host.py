@@ -101,12 +101,105 @@ def test_echo_read_out_order_duplicates_and_mz():
 
 
 def test_refused_options_fail_before_any_walk():
+    """The reference's argument errors, raised before the device is touched."""
     wf = ps.gradient_echo(1e-3, 1e-4)
     with pytest.raises(NotImplementedError):
-        d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, kappa_MT=1e-5,
-                         dwell_time=1e-3)
-    with pytest.raises(NotImplementedError):
         d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, susceptibility=object())
+    with pytest.raises(ValueError):
+        d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, kappa_MT=1e-5,
+                         dwell_time=0.0)
+    with pytest.raises(TypeError):
+        d.simulate_bloch(10, 2e-9, wf, d.FreeDiffusion(), wf.rf_events, kappa_MT=1e-5,
+                         dwell_time=1e-3)
+    with pytest.raises(ValueError):
+        d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, kappa_MT=1e-5,
+                         dwell_time=1e-3, equilibrate_binding="later")
+
+
+def test_mt_fast_mode_falls_back_when_unsafe():
+    from dmipy_sim_gb300.bloch import _mt_mode
+    G = np.zeros((1, 5, 3))
+    assert _mt_mode("fast", G, 0.08, 1e-5, d.Sphere(2e-6)) == "fast"
+    assert _mt_mode("auto", G, 0.08, 1e-5, d.Sphere(2e-6)) == "burnin"
+    assert _mt_mode("off", G, 0.08, 1e-5, d.Sphere(2e-6)) == "off"
+    with pytest.warns(UserWarning):
+        assert _mt_mode("fast", G, 0.08, 1e-5, d.Box1D(4e-6)) == "burnin"
+    G[0, 2, 0] = 0.1
+    with pytest.warns(UserWarning):
+        assert _mt_mode("fast", G, 0.08, 0.05, d.Sphere(2e-6)) == "burnin"
+    assert _mt_mode("fast", G, 0.08, 1e-5, d.Sphere(2e-6)) == "fast"
+
+
+def test_mt_rotation_tables_are_rodrigues_rotations():
+    """The per-sub-step rotations the MT kernel applies: orthogonal, determinant 1, axis
+    (f cos ax, f sin ax, dphi) fixed, angle |k|; the bound pool's adds its offset."""
+    from dmipy_sim_gb300.bloch import _mt_rotations
+    fl, ax, ca = B._build_rf_schedule(RF_EVENTS[2], 1e-4, 100)
+    R = _mt_rotations(fl, ax, ca, 7, 1e-4, 120.0, -900.0)
+    for t in (0, 12, 99):
+        for p in range(2):
+            Q = R[t, p]
+            np.testing.assert_allclose(Q @ Q.T, np.eye(3), atol=1e-14)
+            assert np.linalg.det(Q) == pytest.approx(1.0, abs=1e-14)
+            f = np.float64(np.float32(fl[t])) / 7.0
+            a = np.float32(ax[t])
+            kz = (2 * np.pi * 120.0 * 1e-4 + np.float64(np.float32(ca[t]))) / 7.0
+            kz += 2 * np.pi * (-900.0) * 1e-4 / 7.0 if p else 0.0
+            k = np.array([f * np.float64(np.cos(a)), f * np.float64(np.sin(a)), kz])
+            np.testing.assert_allclose(Q @ k, k, rtol=0, atol=1e-14 * np.linalg.norm(k))
+            th = np.linalg.norm(k)
+            assert np.arccos(np.clip((np.trace(Q) - 1) / 2, -1, 1)) == pytest.approx(th, abs=1e-7)
+
+
+def test_two_pool_model_matches_reference():
+    from dmipy_sim_gb300 import mt
+    z = np.load(Path(__file__).parent / "golden" / "mt_kat.npz")
+    np.testing.assert_array_equal(
+        mt.two_pool_generator(R1a=1.1, R2a=12.5, R1b=0.9, R2b=1e5, k_f=40.0, k_r=80.0,
+                              dw_a=300.0, dw_b=-50.0, w1=700.0, rf_phase=0.4), z["gen"])
+    np.testing.assert_array_equal(
+        mt.two_pool_generator(R1a=1.0, R2a=10.0, R1b=1.0, R2b=1e4, k_f=30.0, k_r=100.0,
+                              M0a=0.8, M0b=0.1), z["gen_m0b"])
+    t = np.array([0.0, 1e-3, 5e-3, 0.02, 0.08])
+    np.testing.assert_allclose(mt.bloch_mcconnell_transverse(t, T2a=80e-3, T2b=1e-5, k_f=30.0,
+                                                             k_r=100.0), z["bmt"], rtol=1e-12)
+    np.testing.assert_allclose(
+        mt.bloch_mcconnell_transverse(t, T2a=60e-3, T2b=2e-3, k_f=20.0, k_r=50.0, dw_a=100.0,
+                                      dw_b=400.0, T1a=0.9, T1b=0.5), z["bmt_dw"], rtol=1e-12)
+    np.testing.assert_allclose(mt.bloch_mcconnell_longitudinal(t * 10, T1a=1.0, T1b=0.7,
+                                                               k_f=30.0, k_r=90.0), z["bml"],
+                               rtol=1e-12)
+    np.testing.assert_allclose(
+        mt.bloch_mcconnell_longitudinal(t * 10, T1a=1.2, T1b=1.0, k_f=30.0, k_r=90.0, Mza0=1.0,
+                                        Mzb0=0.0), z["bml_sat"], rtol=1e-12)
+    off = np.array([-5000.0, -500.0, 0.0, 200.0, 2000.0, 20000.0])
+    kw = dict(w1_hz=200.0, t_sat=0.025, T1a=1.0, T2a=80e-3, T1b=1.0, T2b=1e-5, k_f=40.0,
+              k_r=80.0)
+    np.testing.assert_allclose(mt.mt_z_spectrum(off, **kw), z["z_a"], rtol=1e-12)
+    np.testing.assert_allclose(mt.mt_z_spectrum(off, read_pool="b", **kw), z["z_b"], rtol=1e-12)
+    np.testing.assert_allclose([mt.forward_rate(2e-6, 3e5), mt.backward_rate(0.0125),
+                                mt.bound_fraction(2e-6, 0.0125, 3e5),
+                                mt.kappa_MT_from_forward_rate(40.0, 1.5e6),
+                                mt.dwell_time_from_fraction(0.3, 40.0)], z["misc"], rtol=1e-15)
+    np.testing.assert_array_equal(mt.stick_probability(np.array([0.0, 1e-9, 1e-8, 1e-6]), 2e-5,
+                                                       2e-9), z["stick"])
+
+
+def test_oracle_mt_exchange_reaches_equilibrium_fraction():
+    """The restated MT walk on a sphere: the bound occupancy relaxes to k_f/(k_f + k_r)."""
+    R, D, k_f, k_r = 5e-6, 1e-9, 50.0, 100.0
+    dt, n_t = 1e-3, 61
+    n_sub = int(np.ceil(dt / (R ** 2 / (3750 * D))))
+    g = d.Sphere(R)
+    r0 = g.init_positions(2000, 3).astype(np.float32)
+    fl, ax, _ = B._build_rf_schedule([{'t_s': 0.0, 'flip_deg': 90.0, 'axis_deg': 90.0}], dt, n_t)
+    o1 = O.bloch_mt(O.geom_from(g), n_walkers=2000, G=np.zeros((1, 40, 3)), dt=dt, n_sub=n_sub,
+                    seed=3, r0=r0, rf_flip=fl[:40], rf_axis=ax[:40], kappa_MT=k_f * R / 3,
+                    dwell_time=1 / k_r, D=D)
+    o2 = O.bloch_mt(O.geom_from(g), n_walkers=2000, G=np.zeros((1, 21, 3)), dt=dt, n_sub=n_sub,
+                    seed=3, r0=o1["r_end"], brem0=o1["brem"], s0=40 * n_sub, rf_flip=fl[:21],
+                    rf_axis=ax[:21], kappa_MT=k_f * R / 3, dwell_time=1 / k_r, D=D)
+    assert o2["occ_total"].mean() / 21 == pytest.approx(k_f / (k_f + k_r), rel=0.08)
 
 
 # ---- the oracle's Bloch walk ----------------------------------------------------------------

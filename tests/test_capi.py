@@ -51,6 +51,7 @@ def _c_layout(struct, fields):
                                           ("dmsim_walk_outputs", "WalkOutputs"),
                                           ("dmsim_batch_tuning", "BatchTuning"),
                                           ("dmsim_bloch_params", "BlochParams"),
+                                          ("dmsim_mt_params", "MtParams"),
                                           ("dmsim_gemm", "Gemm")])
 def test_struct_layout_matches_header(cname, pyname):
     from dmipy_sim_gb300 import _lib
