@@ -184,7 +184,9 @@ T2a, T1a, T2b, T1b = 80e-3, 1.0, 1e-5, 1.0
 W1_HZ, T_SAT, DT = 200.0, 0.025, 2e-5
 
 
-def _mz(offset_hz, *, with_mt, equilibrate='auto', n=8000):
+def _mz(offset_hz, *, with_mt, equilibrate='auto', n=32000):
+    # on resonance the walker-to-walker spread of Mz (binding histories) makes the 4 % relative
+    # tolerance ~3 SE at 8000 walkers; 32000 keep it at ~6 SE
     n_t = int(round(T_SAT / DT)) + 1
     rf = [{'t_s': T_SAT / 2, 'flip_deg': 360.0 * W1_HZ * T_SAT, 'axis_deg': 0.0,
            'duration_s': T_SAT, 'offset_hz': offset_hz}]
