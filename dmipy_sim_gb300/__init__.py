@@ -16,6 +16,8 @@ from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, Wal
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
                    fused_sub_steps)
 from . import trajectories
+from .trajectories import (replay_bloch, replay_bloch_jax, unwrap_periodic, pathway_sign_se,
+                           finite_180_longitudinal_dwell, pre_pulse_gradient_phase)
 from .mesh import Mesh, load_ply, icosphere, random_ellipsoid_cells, mesh_contains
 from .batched import Instance, Tuning, PreparedBatch, simulate_batch
 from .autotune import autotune
@@ -36,7 +38,9 @@ __all__ = [
     "Cylinder", "Sphere", "MyelinatedCylinder", "PackedMyelinatedCylinders",
     "pack_myelinated_cylinders", "Box1D", "PermeableSlab1D", "PermeableShell", "Ellipsoid",
     "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
-    "simulate", "simulate_cpmg", "simulate_trajectories", "trajectories", "run_walk", "WalkResult",
+    "simulate", "simulate_cpmg", "simulate_trajectories", "trajectories", "replay_bloch",
+    "replay_bloch_jax", "unwrap_periodic", "pathway_sign_se", "finite_180_longitudinal_dwell",
+    "pre_pulse_gradient_phase", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
     "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
     "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune", "compression", "bank", "replay",

@@ -32,7 +32,7 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
             "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes",
             "dmsim_bloch_workspace_bytes", "dmsim_bloch", "dmsim_bloch_mt_workspace_bytes",
-            "dmsim_bloch_mt")
+            "dmsim_bloch_mt", "dmsim_replay_bloch_workspace_bytes", "dmsim_replay_bloch")
 
 EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
@@ -110,6 +110,23 @@ class MtParams(C.Structure):
     ]
 
 
+class ReplayBlochParams(C.Structure):
+    _fields_ = [
+        ("n_walkers", C.c_int64), ("n_t", C.c_int32), ("n_meas", C.c_int32),
+        ("n_echo", C.c_int32), ("traj_f16", C.c_int32), ("traj", C.c_void_p), ("G", C.c_void_p),
+        ("gamma_dt", C.c_double), ("dt_traj", C.c_double), ("e2", C.c_double),
+        ("e1", C.c_double), ("inv_t2", C.c_double), ("inv_t1", C.c_double),
+        ("comp", C.c_void_p), ("inv_t2_comp", C.c_void_p), ("inv_t1_comp", C.c_void_p),
+        ("bound_frac", C.c_void_p), ("inv_t2_bound", C.c_double),
+        ("inv_t1_bound", C.c_double), ("dphi_bound", C.c_double), ("dlog", C.c_void_p),
+        ("rho_over_D", C.c_double), ("extra_phase", C.c_void_p), ("rf_start", C.c_void_p),
+        ("rf_flip", C.c_void_p), ("rf_axis", C.c_void_p), ("rf_offset", C.c_void_p),
+        ("rf_active", C.c_void_p), ("b1_scale", C.c_void_p), ("slice_dphi", C.c_void_p),
+        ("weights", C.c_void_p), ("echo_idx", C.c_void_p), ("sums", C.c_void_p),
+        ("echo_walker", C.c_void_p), ("m_last", C.c_void_p),
+    ]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [
         ("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("order", C.c_int32),
@@ -156,6 +173,11 @@ def load():
     lib.dmsim_bloch_mt.restype = C.c_int
     lib.dmsim_bloch_mt.argtypes = [C.POINTER(MtParams), C.POINTER(Geometry), C.c_void_p,
                                    C.c_size_t, C.c_void_p]
+    lib.dmsim_replay_bloch_workspace_bytes.restype = C.c_size_t
+    lib.dmsim_replay_bloch_workspace_bytes.argtypes = [C.POINTER(ReplayBlochParams)]
+    lib.dmsim_replay_bloch.restype = C.c_int
+    lib.dmsim_replay_bloch.argtypes = [C.POINTER(ReplayBlochParams), C.c_void_p, C.c_size_t,
+                                       C.c_void_p]
     lib.dmsim_walk_noalloc.restype = C.c_int
     lib.dmsim_walk_noalloc.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
                                        C.POINTER(WalkOutputs), C.c_void_p]

@@ -375,6 +375,52 @@ size_t dmsim_bloch_mt_workspace_bytes(const dmsim_mt_params* p, const dmsim_geom
 int dmsim_bloch_mt(const dmsim_mt_params* p, const dmsim_geometry* g, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* ---- vector-Bloch replay of a stored walk --------------------------------------------------------
+   trajectories.py:734-949 (replay_bloch): every walker's magnetisation M_m, starting at
+   (0, 0, 1), is carried through the samples of its saved positions in the order: the sample's RF
+   increments rf_start[t] .. rf_start[t+1] (rotation by rf_flip * b1_scale[w] about
+   (cos rf_axis, sin rf_axis, 0)); precession of Mxy by gamma_dt * G[t, m] . r(t) + extra_phase
+   + bound_frac * dphi_bound + rf_offset[t] + (rf_active[t] ? slice_dphi[w] : 0); Mxy *=
+   exp(rho_over_D * dlog); Mxy *= E2, Mz *= E1 with E = exp(-dt_traj * rate), the rate the
+   compartment's (comp, inv_t*_comp) or the constant one, blended toward the bound pool by
+   bound_frac (without compartments or bound_frac, e2 / e1 are used as given).  All FP64.  At
+   each echo sample sums[m][e] = (sum_w weight_w Mx, sum_w weight_w My); optional per-walker
+   echoes and the last measurement's final magnetisation.  Per-walker-sample arrays are
+   (n_walkers, n_t); every pointer is DEVICE memory. */
+typedef struct dmsim_replay_bloch_params {
+  int64_t n_walkers;
+  int32_t n_t, n_meas, n_echo, traj_f16;
+  const void* traj;            /* (n_walkers, n_t, 3) float16 or float32                        */
+  const double* G;             /* (n_t, n_meas, 3) on the walk's sample grid                    */
+  double gamma_dt, dt_traj;
+  double e2, e1;               /* per-sample factors without per-sample rates                  */
+  double inv_t2, inv_t1;       /* base rates (1/s) blended with bound_frac                      */
+  const int32_t* comp;         /* compartment per walker-sample or NULL                         */
+  const double* inv_t2_comp;   /* rates per compartment                                         */
+  const double* inv_t1_comp;
+  const float* bound_frac;     /* bound-pool occupancy per walker-sample or NULL                */
+  double inv_t2_bound, inv_t1_bound, dphi_bound;
+  const float* dlog;           /* boundary log-weight at rho/D = 1 per walker-sample or NULL     */
+  double rho_over_D;
+  const double* extra_phase;   /* per walker-sample phase (rad) or NULL                         */
+  const int32_t* rf_start;     /* (n_t + 1) offsets into rf_flip / rf_axis                      */
+  const double* rf_flip;
+  const double* rf_axis;
+  const double* rf_offset;     /* (n_t) pulse carrier per sample or NULL                        */
+  const uint8_t* rf_active;    /* (n_t) 1 while a pulse is on                                    */
+  const double* b1_scale;      /* (n_walkers) or NULL                                           */
+  const double* slice_dphi;    /* (n_walkers) slice-select phase per sample, or NULL            */
+  const double* weights;       /* (n_walkers) or NULL (all 1)                                   */
+  const int32_t* echo_idx;     /* (n_echo) ascending sample indices                             */
+  double* sums;                /* (n_meas, n_echo, 2)                                           */
+  double* echo_walker;         /* (n_meas, n_echo, n_walkers, 2) or NULL                        */
+  double* m_last;              /* (3, n_walkers) of the last measurement, or NULL               */
+} dmsim_replay_bloch_params;
+
+size_t dmsim_replay_bloch_workspace_bytes(const dmsim_replay_bloch_params* p);
+int dmsim_replay_bloch(const dmsim_replay_bloch_params* p, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
 /* Temporal-mode projection, the compressed trajectory export of simulate_trajectories(compress=K)
    (core.py:1370-1407) and the temporal_dct / boundary_dct codecs of compression.py:55-62, 224-249:
    out[w,k,c] = sum_t basis[k,t] * x[w,t,c] with x (n_walkers, n_t, n_ch) float16 (x_f16 = 1) or

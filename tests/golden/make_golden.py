@@ -935,6 +935,81 @@ def make_bloch_kat(root):
     print(f"bloch_kat.npz: {len(out)} arrays")
 
 
+def replay_bloch_inputs():
+    """The seeded walk and per-step inputs of the replay_bloch known answers (also rebuilt by
+    the tests): 96 walkers x 150 samples in a 4 um cylinder, two compartments."""
+    rng = np.random.default_rng(21)
+    n_w, n_t, dt = 96, 150, 1e-4
+    r = np.zeros((n_w, n_t, 3))
+    r[:, 0, :2] = rng.uniform(-2e-6, 2e-6, (n_w, 2))
+    for t in range(1, n_t):
+        r[:, t] = r[:, t - 1] + rng.normal(0, 0.6e-6, (n_w, 3))
+        rad = np.linalg.norm(r[:, t, :2], axis=1)
+        out = rad > 4e-6
+        r[out, t, :2] *= (8e-6 / rad[out] - 1.0)[:, None]
+    traj = r.astype(np.float32)
+    comp = (np.linalg.norm(traj[..., :2], axis=-1) > 2.5e-6).astype(np.int64)
+    G = np.zeros((3, 301, 3))
+    G[0, 20:80, 0] = G[0, 160:220, 0] = 0.06
+    G[1, 20:80, 1] = G[1, 160:220, 1] = 0.06
+    G[2, 30:250, 2] = 0.02 * np.sin(np.linspace(0, 6 * np.pi, 220))
+    rf = [{'t_s': 0.0, 'flip_deg': 90.0, 'axis_deg': 90.0},
+          {'t_s': 7.5e-3, 'flip_deg': 180.0, 'axis_deg': 0.0, 'duration_s': 8e-4,
+           'offset_hz': 250.0},
+          {'t_s': 11e-3, 'flip_deg': 60.0, 'axis_deg': 30.0, 'duration_s': 1.2e-3,
+           'b1_envelope': [0.2, 1.0, 0.6, 0.1]}]
+    dlog = -np.abs(rng.normal(0, 2e-8, (n_w, n_t))).astype(np.float32)
+    dlog[rng.random((n_w, n_t)) < 0.7] = 0.0
+    bf = np.clip(rng.random((n_w, n_t)) * 1.5 - 0.7, 0.0, 1.0).astype(np.float32)
+    xph = rng.normal(0, 0.02, (n_w, n_t))
+    wts = rng.uniform(0.5, 1.5, n_w)
+    b1s = rng.uniform(0.85, 1.1, n_w)
+    sl = rng.uniform(-1e-3, 1e-3, n_w)
+    return dict(traj=traj, dt_traj=dt, G=G, dt_wf=0.5e-4, rf=rf, comp=comp, dlog=dlog, bf=bf,
+                xph=xph, wts=wts, b1s=b1s, slice=sl)
+
+
+def replay_bloch_cases(x):
+    """name -> keyword arguments of the replay_bloch known answers."""
+    return {
+        "plain": dict(T2=0.07),
+        "relax": dict(T2=0.07, T1=0.9, echo_steps=[40, 75, 149, 75]),
+        "comp": dict(comp_traj=x["comp"], T2_per_comp=[0.06, 0.09], T1_per_comp=[0.8, 1.2],
+                     dlog_boundary_unit=x["dlog"], surface_relaxivity=3e-5, D=2e-9,
+                     weights=x["wts"]),
+        "mt": dict(T2=0.07, T1=1.0, bound_frac=x["bf"], T2_bound=1e-4, T1_bound=0.6,
+                   off_resonance_bound=-600.0, echo_steps=[60, 120], echo_per_walker=True),
+        "susc": dict(T2=0.08, extra_phase_per_step=x["xph"], b1_scale=x["b1s"],
+                     slice_offsets=x["slice"], slice_gradient=0.01, return_walker_signals=True),
+    }
+
+
+def make_replay_bloch_kat(root):
+    """replay_bloch_kat.npz: dmipy-sim's own trajectories.replay_bloch (numpy, FP64) on the
+    seeded walk of replay_bloch_inputs(), one case per option group."""
+    m = _ref(root)
+    x = replay_bloch_inputs()
+    out = {}
+    for name, kw in replay_bloch_cases(x).items():
+        res = m["trajectories"].replay_bloch(x["traj"], x["dt_traj"], x["G"], x["dt_wf"],
+                                             x["rf"], **kw)
+        if isinstance(res, tuple):
+            out[f"{name}_mlast"] = np.asarray(res[0])
+            res = res[1]
+        out[name] = np.asarray(res)
+    tr = m["trajectories"]
+    out["sign_se"] = tr.pathway_sign_se(37, 1e-4, 2.2e-3, te_frac=0.45)
+    rng = np.random.default_rng(8)
+    walk = np.cumsum(rng.normal(0, 0.7e-6, (5, 60, 3)), axis=1)
+    out["wrapped"] = (walk - 6e-6 * np.floor(walk / 6e-6 + 0.5)).astype(np.float32)
+    out["unwrapped"] = tr.unwrap_periodic(out["wrapped"], 6e-6)
+    out["unwrapped_xyz"] = tr.unwrap_periodic(out["wrapped"], 6e-6, periodic_axes=(0, 1, 2))
+    out["dwell180"] = tr.finite_180_longitudinal_dwell(np.linspace(-3, 3, 11), 2e-3, 0.3)
+    out["phi_pre"] = tr.pre_pulse_gradient_phase(x["traj"], x["dt_traj"], x["G"], x["dt_wf"], 150)
+    np.savez_compressed(HERE / "replay_bloch_kat.npz", **out)
+    print(f"replay_bloch_kat.npz: {sorted(out)}")
+
+
 def make_mt_kat(root):
     """mt_kat.npz: dmipy-sim's own two-pool Bloch-McConnell model and binding bookkeeping
     (mt.py) on fixed inputs."""
@@ -981,6 +1056,8 @@ if __name__ == "__main__":
     ap.add_argument("--replay-kat", action="store_true",
                     help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
+    ap.add_argument("--replay-bloch-kat", action="store_true",
+                    help="write replay_bloch_kat.npz (the Bloch replay on a stored walk)")
     ap.add_argument("--mt-kat", action="store_true",
                     help="write mt_kat.npz (the two-pool model and binding bookkeeping)")
     ap.add_argument("--mc-bloch", action="store_true",
@@ -1000,6 +1077,8 @@ if __name__ == "__main__":
         make_myelin_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)
+    if a.replay_bloch_kat:
+        make_replay_bloch_kat(a.ref)
     if a.mt_kat:
         make_mt_kat(a.ref)
     if a.mc_bloch:

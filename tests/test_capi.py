@@ -52,6 +52,7 @@ def _c_layout(struct, fields):
                                           ("dmsim_batch_tuning", "BatchTuning"),
                                           ("dmsim_bloch_params", "BlochParams"),
                                           ("dmsim_mt_params", "MtParams"),
+                                          ("dmsim_replay_bloch_params", "ReplayBlochParams"),
                                           ("dmsim_gemm", "Gemm")])
 def test_struct_layout_matches_header(cname, pyname):
     from dmipy_sim_gb300 import _lib
