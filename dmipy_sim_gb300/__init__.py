@@ -14,7 +14,7 @@ from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, MyelinatedCy
                          PackedCylinders, pack_spheres, PackedSpheres, lattice_cylinders)
 from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
-                   fused_sub_steps)
+                   fused_sub_steps, mt_sub_steps)
 from . import trajectories
 from .trajectories import (replay_bloch, replay_bloch_jax, unwrap_periodic, pathway_sign_se,
                            finite_180_longitudinal_dwell, pre_pulse_gradient_phase)
@@ -26,7 +26,8 @@ from .autotune import autotune
 from . import compression, bank, replay
 from .replay import ReplayPack, read_rpk, write_rpk, compile_scheme, replay_signal
 from .bank import build_replay_pack, build_to_floor
-from . import bloch, mt, pulse_sequence
+from . import bloch, mt, mt_walk, pulse_sequence
+from .mt_walk import simulate_mt_trajectories
 from .bloch import simulate_bloch
 from .pulse_sequence import (BlochSequence, gradient_echo, spin_echo, prepend_mt_prep,
                              run_bloch_sequence, emergent_z_spectrum)
@@ -42,10 +43,10 @@ __all__ = [
     "replay_bloch_jax", "unwrap_periodic", "pathway_sign_se", "finite_180_longitudinal_dwell",
     "pre_pulse_gradient_phase", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",
-    "fused_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
+    "fused_sub_steps", "mt_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
     "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune", "compression", "bank", "replay",
     "ReplayPack", "read_rpk", "write_rpk", "compile_scheme", "replay_signal", "build_replay_pack",
-    "build_to_floor", "bloch", "mt", "pulse_sequence", "simulate_bloch",
+    "build_to_floor", "bloch", "mt", "mt_walk", "simulate_mt_trajectories", "pulse_sequence", "simulate_bloch",
     "BlochSequence", "gradient_echo", "spin_echo", "prepend_mt_prep", "run_bloch_sequence",
     "emergent_z_spectrum",
 ]

@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 7
+DMSIM_ABI_VERSION = 8
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
@@ -106,7 +106,8 @@ class MtParams(C.Structure):
         ("e1h", C.c_double * 2), ("G", C.c_void_p), ("rot", C.c_void_p), ("crush", C.c_void_p),
         ("r0", C.c_void_p), ("brem_in", C.c_void_p), ("brem_out", C.c_void_p),
         ("r_end", C.c_void_p), ("occ", C.c_void_p), ("occ_total", C.c_void_p),
-        ("sums", C.c_void_p), ("status", C.c_void_p),
+        ("sums", C.c_void_p), ("status", C.c_void_p), ("traj", C.c_void_p),
+        ("traj_f16", C.c_int32), ("pad0", C.c_int32), ("dlog_free", C.c_void_p),
     ]
 
 

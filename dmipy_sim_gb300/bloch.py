@@ -393,11 +393,19 @@ class MTWalk:
         self.brem, self.brem_next = self.brem_next, self.brem
         self.counter += int(n_t) * self.n_sub
 
-    def burn_chunk(self, n_chunk):
-        """Walk n_chunk samples without RF or gradient; returns the mean bound occupancy."""
+    def burn_chunk(self, n_chunk, sub=None):
+        """Walk n_chunk samples (of ``sub`` sub-steps, default the walk's) without RF, gradient
+        or magnetisation; returns the mean bound occupancy."""
         self.p.n_meas = 1
-        self._run(n_chunk, 0, {"occ": None, "sums": None, "G": None, "rot": None,
-                               "crush": None, "n_echo": 0, "echo_idx": None})
+        n_sub = self.n_sub
+        if sub is not None:
+            self.n_sub = self.p.n_sub = int(sub)
+        try:
+            self._run(n_chunk, 0, {"occ": None, "sums": None, "G": None, "rot": None,
+                                   "crush": None, "n_echo": 0, "echo_idx": None,
+                                   "traj": None, "dlog_free": None})
+        finally:
+            self.n_sub = self.p.n_sub = n_sub
         return float(self.occ_total.sum().item()) / (self.n * n_chunk)
 
 

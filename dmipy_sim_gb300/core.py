@@ -94,6 +94,21 @@ def surface_sub_steps(geometry, diffusivity, dt, frac=8.0):
     return max(1, int(np.ceil(dt / ((Rc / frac) ** 2 / (6.0 * diffusivity)))))
 
 
+def mt_sub_steps(geometry, diffusivity, dt, dwell_time, frac=8.0, dwell_frac=20.0):
+    """Sub-steps of a magnetisation-transfer walk (physics.py:98-160): a mesh's collision rule,
+    else steps of R/frac (the boundary local time's accuracy), and at least dwell_frac
+    sub-steps per mean dwell."""
+    if getattr(geometry, 'cell_size', None):
+        n = collision_sub_steps(geometry, diffusivity, dt)
+    else:
+        R = _geometry_radius(geometry)
+        n = 1 if R is None else max(1, int(np.ceil(dt / ((R / float(frac)) ** 2
+                                                         / (6.0 * diffusivity)))))
+    if dwell_time and dwell_time > 0:
+        n = max(n, int(np.ceil(dt * float(dwell_frac) / float(dwell_time))))
+    return max(1, int(n))
+
+
 def replay_sub_steps(geometry, diffusivity, dt):
     """Producer-walk sub-steps: step <= R/6 (216), or R/25 (3750) when permeable (core.py:1089-1120)."""
     R = getattr(geometry, 'radius', None)

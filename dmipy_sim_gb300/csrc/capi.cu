@@ -875,6 +875,9 @@ int dmsim_bloch_mt(const dmsim_mt_params* p, const dmsim_geometry* g, void* work
   a.occ_total = p->occ_total;
   a.part = reinterpret_cast<double*>(workspace);
   a.status = p->status;
+  a.traj = p->traj;
+  a.traj_f16 = p->traj_f16;
+  a.dlog_free = p->dlog_free;
   for (int e = 0; e < a.n_echo; ++e) a.echo[e] = p->echo_idx[e];
   const int passes = p->spin ? pl.n_pass : 1;
   for (int pass = 0; pass < passes; ++pass) {

@@ -34,6 +34,9 @@ struct MtArgs {
   float* occ_total;
   double* part;  // [gridDim.x][n_echo][W][3]
   uint32_t* status;
+  void* traj;
+  int traj_f16;
+  float* dlog_free;
   int echo[kMtMaxEcho];
 };
 

@@ -9,6 +9,7 @@
 // for every walker in that pool), half relaxation and the free-contact surface weight -- and
 // after the sample's sub-steps the gradient (and crusher) phase rotates Mxy.  Echo samples are
 // reduced per block in FP64 in a fixed order.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "mt_kernel.cuh"
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(kMtBlock) k_bloch_mt(const __grid_constant__ M
         }
       }
       int n_bound = 0;
+      float dl_free = 0.f;  // the sample's boundary log-weight over free, non-binding sub-steps
 #pragma unroll 1
       for (int sub = 0; sub < a.n_sub; ++sub, ++s) {
         const u32x4 rr = draw(a.seed, gw, 0u, s);
@@ -122,6 +124,7 @@ __global__ void __launch_bounds__(kMtBlock) k_bloch_mt(const __grid_constant__ M
         const float dwell = -logf(fmaxf(u01(rr.w), 1e-20f)) * a.dwell;
         brem = bound ? brem - 1.f : (newly ? dwell : 0.f);
         n_bound += bound ? 1 : 0;
+        if (!(bound || newly)) dl_free += dl;
         if (a.spin) {
           // Strang split with the pool of this sub-step (bloch.py:488-538)
           const double e2h = bound ? a.e2h[1] : a.e2h[0];
@@ -146,7 +149,25 @@ __global__ void __launch_bounds__(kMtBlock) k_bloch_mt(const __grid_constant__ M
       }
       const float bf = (float)n_bound / (float)a.n_sub;
       occ_sum += bf;
-      if (act && a.occ) a.occ[(size_t)w * a.n_t + t] = bf;
+      if (act && a.pass == 0) {
+        if (a.occ) a.occ[(size_t)w * a.n_t + t] = bf;
+        if (a.dlog_free) a.dlog_free[(size_t)w * a.n_t + t] = dl_free;
+        if (a.traj) {
+          const size_t o = ((size_t)w * a.n_t + t) * 3;
+          const float px = x + g.L * (float)ix, py = y + g.L * (float)iy, pz = z + g.L * (float)iz;
+          if (a.traj_f16) {
+            __half* tp = reinterpret_cast<__half*>(a.traj);
+            tp[o] = __float2half_rn(px);
+            tp[o + 1] = __float2half_rn(py);
+            tp[o + 2] = __float2half_rn(pz);
+          } else {
+            float* tp = reinterpret_cast<float*>(a.traj);
+            tp[o] = px;
+            tp[o + 1] = py;
+            tp[o + 2] = pz;
+          }
+        }
+      }
       if (a.spin) {
         // the sample's gradient and crusher phase at the walker's position (bloch.py:544-548)
         const float ux = x + g.L * (float)ix, uy = y + g.L * (float)iy, uz = z + g.L * (float)iz;

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 7
+#define DMSIM_ABI_VERSION 8
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -369,6 +369,13 @@ typedef struct dmsim_mt_params {
   float* occ_total;         /* DEVICE (n_walkers) sum of the samples' bound fractions, or NULL  */
   double* sums;             /* DEVICE (n_echo, n_meas, 3), overwritten (spin = 1)               */
   uint32_t* status;         /* DEVICE DMSIM_STATUS_WORDS counters                               */
+  /* the saved walk of mt_walk.py:43-239 (simulate_mt_trajectories), each optional: positions
+     after every sample (unfolded), and the free-pool boundary log-weight of every sample (the
+     dl of the sub-steps on which the walker was free and did not bind) */
+  void* traj;               /* DEVICE (n_walkers, n_t, 3) float16 (traj_f16 = 1) or float32    */
+  int32_t traj_f16;
+  int32_t pad0;
+  float* dlog_free;         /* DEVICE (n_walkers, n_t) or NULL                                   */
 } dmsim_mt_params;
 
 size_t dmsim_bloch_mt_workspace_bytes(const dmsim_mt_params* p, const dmsim_geometry* g);

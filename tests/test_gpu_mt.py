@@ -272,3 +272,49 @@ def test_crusher_dephases_transverse(cuda):
                                crusher={'windows_s': [(0.0, n_t * dt)], 'n_cycles': 32.0})
     assert abs(free[0]) == pytest.approx(1.0, rel=1e-2)
     assert abs(crushed[0]) < 0.1
+
+
+# ---- the saved MT walk (dmipy-sim mt_walk.py) and its replay -----------------------------------
+def test_mt_trajectories_follow_the_oracle_walk(cuda):
+    """All-free start: the saved walk is the oracle's MT walk from the same start and draws
+    (end positions to float16 precision, occupancy summed over the samples)."""
+    R, D, n = 2e-6, 2e-9, 2048
+    g = d.Sphere(R)
+    traj, dt, nsub, dt_sim, bf, dlog = d.simulate_mt_trajectories(
+        n, D, g, 0.004, 1e-4, 3e-5, 2e-3, seed=11, sub_steps=4, equilibrate_binding='off')
+    assert traj.dtype == np.float16 and traj.shape == (n, 41, 3) and nsub == 4
+    assert bf.shape == dlog.shape == (n, 41)
+    r0 = np.asarray(g.init_positions(n, 11), np.float32)
+    ora = O.bloch_mt(O.geom_from(g), n_walkers=n, G=np.zeros((1, 41, 3)), dt=dt, n_sub=4,
+                     seed=11, r0=r0, rf_flip=np.zeros(41), rf_axis=np.zeros(41), kappa_MT=3e-5,
+                     dwell_time=2e-3, D=D)
+    err = np.max(np.abs(traj[:, -1].astype(np.float64) - ora["r_end"]), axis=1)
+    assert np.mean(err < 2e-3 * R) > 0.97
+    np.testing.assert_allclose(bf.astype(np.float64).sum(1), ora["occ_total"], atol=41 * 1e-3)
+    assert np.all(dlog <= 0) and np.any(dlog < 0) and np.any(bf > 0)
+
+
+def test_mt_trajectories_bound_fraction_and_replayed_exchange(cuda):
+    R, D, k_f, k_r = 2e-6, 2e-9, 30.0, 100.0
+    g = d.Sphere(R)
+    traj, dt, nsub, _, bf, dlog = d.simulate_mt_trajectories(
+        12000, D, g, 0.03, 1e-3, k_f * R / 3.0, 1.0 / k_r, seed=3)
+    assert nsub == d.mt_sub_steps(g, D, dt, 1.0 / k_r)
+    assert np.all(np.linalg.norm(traj.astype(np.float64), axis=-1) < R * 1.002)
+    assert float(bf.astype(np.float64).mean()) == pytest.approx(k_f / (k_f + k_r), rel=0.08)
+    # replay with the bound-pool blend from an all-free start: transverse exchange against the
+    # two-pool model, as for the forward MT walk
+    traj0, dt0, _, _, bf0, _ = d.simulate_mt_trajectories(
+        12000, D, g, 0.03, 1e-3, k_f * R / 3.0, 1.0 / k_r, seed=4, equilibrate_binding='off')
+    echo = list(range(1, 31))
+    G0 = np.zeros((1, 31, 3))
+    S_mt = np.abs(d.replay_bloch(traj0, dt0, G0, dt0, EXC, T2=80e-3, bound_frac=bf0,
+                                 T2_bound=1e-5, T1_bound=1.0, echo_steps=echo))[0]
+    S0 = np.abs(d.replay_bloch(traj0, dt0, G0, dt0, EXC, T2=80e-3, echo_steps=echo))[0]
+    A = mt.two_pool_generator(R1a=0.1, R2a=1 / 80e-3, R1b=1.0, R2b=1e5, k_f=k_f, k_r=k_r)
+    t = np.array(echo) * dt0
+    S_or = np.array([abs(complex(*mt.evolve_two_pool(np.array([1., 0, 0, 0, 0, 0, 1.]), tt,
+                                                     A)[[0, 1]])) for tt in t])
+    m = t > 0.006
+    rel = np.abs(S_mt / S0 - S_or / np.exp(-t / 80e-3))[m] / (S_or / np.exp(-t / 80e-3))[m]
+    assert np.max(rel) < 0.1, rel
