@@ -1010,6 +1010,46 @@ def make_replay_bloch_kat(root):
     print(f"replay_bloch_kat.npz: {sorted(out)}")
 
 
+def rf_pulses(rf):
+    """The pulses of the RF known answers, from an rf module (the reference's or this
+    package's, same constructors)."""
+    return {
+        "hard": rf.B1Pulse.hard(90.0, 1e-3, 1e-5, phase_deg=30.0),
+        "sinc": rf.B1Pulse.windowed_sinc(90.0, 2e-3, 1e-5, time_bw=6.0),
+        "sinc_rect": rf.B1Pulse.windowed_sinc(30.0, 1.5e-3, 1e-5, n_zeros=2, window=None),
+        "hs": rf.B1Pulse.adiabatic_hs(8e-3, 1e-5, peak_b1=15e-6),
+        "ahp": rf.B1Pulse.adiabatic_half_passage(4e-3, 1e-5, peak_b1=12e-6),
+        "bir4": rf.B1Pulse.bir4(60.0, 8e-3, 1e-5, peak_b1=15e-6),
+        "comp": rf.B1Pulse.composite([(90, 0), (180, 90), (90, 0)], 1e-5, peak_b1=10e-6),
+        "samples": rf.B1Pulse.from_magnitude_phase(np.linspace(0, 5e-6, 50),
+                                                   np.linspace(0, 1, 50), 2e-5),
+    }
+
+
+def make_rf_kat(root):
+    """rf_kat.npz: dmipy-sim's own RF pulse constructors and Bloch integrator (rf.py)."""
+    _ref(root)
+    import importlib
+    rf = importlib.import_module("dmipy_sim.rf")
+    out = {}
+    df = np.linspace(-2000.0, 2000.0, 9)
+    for k, p in rf_pulses(rf).items():
+        out[f"{k}_b1"] = p.b1
+        out[f"{k}_props"] = np.array([p.duration, p.peak_b1, p.b1_rms, p.sar_proxy,
+                                      p.nominal_flip_deg, p.max_slew_b1])
+        mxy, mz = rf.bloch_simulate(p, df_hz=df, b1_scale=np.linspace(0.8, 1.2, 9), T1=0.9,
+                                    T2=0.05)
+        out[f"{k}_mxy"], out[f"{k}_mz"] = mxy, mz
+    p = rf_pulses(rf)["hard"]
+    mxy, mz, hist = rf.bloch_simulate(p, df_hz=[0.0, 300.0], M0=[0.0, 1.0, 0.0],
+                                      return_history=True)
+    out["hist"], out["hist_mxy"], out["hist_mz"] = hist, mxy, mz
+    z, mxy, mz = rf.slice_profile(rf_pulses(rf)["sinc"], 0.01, np.linspace(-5e-3, 5e-3, 21))
+    out["slice_mxy"], out["slice_mz"] = mxy, mz
+    np.savez_compressed(HERE / "rf_kat.npz", **out)
+    print(f"rf_kat.npz: {len(out)} arrays")
+
+
 def make_mt_kat(root):
     """mt_kat.npz: dmipy-sim's own two-pool Bloch-McConnell model and binding bookkeeping
     (mt.py) on fixed inputs."""
@@ -1056,6 +1096,8 @@ if __name__ == "__main__":
     ap.add_argument("--replay-kat", action="store_true",
                     help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
+    ap.add_argument("--rf-kat", action="store_true",
+                    help="write rf_kat.npz (RF pulse constructors, Bloch integrator)")
     ap.add_argument("--replay-bloch-kat", action="store_true",
                     help="write replay_bloch_kat.npz (the Bloch replay on a stored walk)")
     ap.add_argument("--mt-kat", action="store_true",
@@ -1077,6 +1119,8 @@ if __name__ == "__main__":
         make_myelin_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)
+    if a.rf_kat:
+        make_rf_kat(a.ref)
     if a.replay_bloch_kat:
         make_replay_bloch_kat(a.ref)
     if a.mt_kat:
