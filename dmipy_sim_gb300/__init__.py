@@ -26,7 +26,8 @@ from .autotune import autotune
 from . import compression, bank, replay
 from .replay import ReplayPack, read_rpk, write_rpk, compile_scheme, replay_signal
 from .bank import build_replay_pack, build_to_floor
-from . import bloch, mt, mt_walk, pulse_sequence, rf
+from . import bloch, mt, mt_walk, pulse_sequence, rf, susceptibility
+from .susceptibility import SusceptibilitySources, MyelinSusceptibility, GridSusceptibility
 from .rf import B1Pulse, bloch_simulate, slice_profile
 from .mt_walk import simulate_mt_trajectories
 from .bloch import simulate_bloch
@@ -47,7 +48,8 @@ __all__ = [
     "fused_sub_steps", "mt_sub_steps", "Mesh", "load_ply", "icosphere", "random_ellipsoid_cells", "mesh_contains",
     "Instance", "Tuning", "PreparedBatch", "simulate_batch", "autotune", "compression", "bank", "replay",
     "ReplayPack", "read_rpk", "write_rpk", "compile_scheme", "replay_signal", "build_replay_pack",
-    "build_to_floor", "bloch", "mt", "mt_walk", "rf", "B1Pulse", "bloch_simulate", "slice_profile", "simulate_mt_trajectories", "pulse_sequence", "simulate_bloch",
+    "build_to_floor", "bloch", "mt", "mt_walk", "rf", "susceptibility", "SusceptibilitySources",
+    "MyelinSusceptibility", "GridSusceptibility", "B1Pulse", "bloch_simulate", "slice_profile", "simulate_mt_trajectories", "pulse_sequence", "simulate_bloch",
     "BlochSequence", "gradient_echo", "spin_echo", "prepend_mt_prep", "run_bloch_sequence",
     "emergent_z_spectrum",
 ]

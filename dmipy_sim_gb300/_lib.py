@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 8
+DMSIM_ABI_VERSION = 9
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
@@ -93,6 +93,9 @@ class BlochParams(C.Structure):
     _fields_ = [
         ("rf_flip", C.c_void_p), ("rf_axis", C.c_void_p), ("carrier", C.c_void_p),
         ("crush", C.c_void_p), ("m0", C.c_float), ("t1_sample", C.c_float),
+        ("field_kind", C.c_int32), ("field_n", C.c_int32), ("field_tab", C.c_void_p),
+        ("field_rot", C.c_float * 9), ("field_par", C.c_float * 8),
+        ("field_dims", C.c_int32 * 3), ("field_gamma_dt", C.c_float),
     ]
 
 

@@ -12,7 +12,9 @@ With ``kappa_MT > 0`` the walk binds at the walls (bloch.py:343-671): a free wal
 p = min(1, 2 kappa_MT d_perp / D) per hit and stays put for an exponential dwell, the FP64
 magnetisation takes a Strang split per sub-step with the walker's pool (free or bound: its own
 T2, T1 and offset), and a burn-in brings the bound occupancy to equilibrium before the sequence
-(``dmsim_bloch_mt``).  Susceptibility fields are not built (``NotImplementedError``).
+(``dmsim_bloch_mt``).  A susceptibility field provider (``susceptibility.py``: magnetised spheres,
+myelin cylinders, a solved grid) is evaluated on the device at every sample; the MT walk takes
+none.
 """
 import ctypes
 import warnings
@@ -72,13 +74,48 @@ def _build_crusher(crusher, dt, n_t):
     return rate, True
 
 
+def _field_params(susceptibility, geometry, dt, b, dev, keep):
+    """Fill the susceptibility fields of ``b`` (dmsim_bloch_params) from a provider."""
+    from . import susceptibility as su
+    frame = geometry._frame()
+    rot = np.eye(3) if frame is None else np.asarray(frame, np.float64).T   # walk -> lab
+    if isinstance(susceptibility, su.SusceptibilitySources):
+        tab, kind = susceptibility._table(), 1
+    elif isinstance(susceptibility, su.MyelinSusceptibility):
+        tab, (L, scale, c2a, s2a) = susceptibility._table()
+        kind = 2
+        if susceptibility.R is not None:
+            rot = np.asarray(susceptibility.R, np.float64) @ rot
+        b.field_par[:6] = [L, scale, c2a, s2a, float(susceptibility.n_images),
+                           1.0 if susceptibility.periodic else 0.0]
+    elif isinstance(susceptibility, su.GridSusceptibility):
+        tab = np.ascontiguousarray(np.asarray(susceptibility.dB, np.float32))
+        kind = 3
+        vs = su._voxel(susceptibility.voxel_size, 3)
+        b.field_par[:7] = list(np.asarray(susceptibility.origin, float).ravel()) + list(vs) + [
+            1.0 if susceptibility.periodic else 0.0]
+        b.field_dims[:] = list(tab.shape)
+    else:
+        raise NotImplementedError(
+            "the device walk evaluates SusceptibilitySources, MyelinSusceptibility and "
+            "GridSusceptibility; a bare r -> dBz callable is sampled on the host by "
+            "trajectories.replay_bloch")
+    t = torch.from_numpy(np.ascontiguousarray(tab, np.float32).ravel()).to(dev)
+    keep.append(t)
+    b.field_kind = kind
+    b.field_n = int(tab.shape[0]) if kind != 3 else 0
+    b.field_tab = t.data_ptr()
+    b.field_rot[:] = [float(v) for v in rot.ravel()]
+    b.field_gamma_dt = float(np.float32(GAMMA * dt))
+
+
 class BlochWalk:
     """One vector-Bloch walk with its device buffers: ``launch()`` enqueues it on the current
     stream, ``result()`` synchronises and returns the sums (n_echo, M, 3) of Mx, My, Mz."""
 
     def __init__(self, geometry, *, n_walkers, diffusivity, G, dt, flip, axis, carrier, crush,
                  T2, T1, M0, seed, echo_idx, surface_relaxivity=0.0, r0=None,
-                 want_positions=False):
+                 want_positions=False, susceptibility=None):
         if getattr(geometry, '_is_myelinated', False) or getattr(geometry, '_is_packed_myelinated',
                                                                 False):
             raise NotImplementedError("the vector-Bloch walk does not take myelinated cylinders")
@@ -130,6 +167,9 @@ class BlochWalk:
         b.crush = None if self.crush_dev is None else self.crush_dev.data_ptr()
         b.m0 = float(M0)
         b.t1_sample = float(np.float32(dt / T1)) if T1 is not None else 0.0
+        self._field_keep = []
+        if susceptibility is not None:
+            _field_params(susceptibility, geometry, dt, b, dev, self._field_keep)
         self.sums = torch.zeros((len(echo), n_meas, 3), dtype=torch.float64, device=dev)
         self.status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
         o = self.o = _lib.WalkOutputs()
@@ -157,7 +197,7 @@ class BlochWalk:
 
 def _prepare(n_walkers, diffusivity, waveform, geometry, rf_events, *, T2, T1, M0,
              off_resonance_hz, seed, echo_steps, return_mz, crusher, surface_relaxivity, r0=None,
-             want_positions=False):
+             want_positions=False, susceptibility=None):
     if hasattr(waveform, 'waveform'):
         waveform = waveform.waveform
     G, _ = _waveform_arrays(waveform, geometry)      # walk frame, Mesh placement applied
@@ -180,7 +220,7 @@ def _prepare(n_walkers, diffusivity, waveform, geometry, rf_events, *, T2, T1, M
                   axis=axis, carrier=carrier if np.any(carrier) else None,
                   crush=rate if has_crush else None, T2=T2, T1=T1, M0=M0, seed=seed,
                   echo_idx=uniq, surface_relaxivity=surface_relaxivity, r0=r0,
-                  want_positions=want_positions)
+                  want_positions=want_positions, susceptibility=susceptibility)
     return w, uniq, idx
 
 
@@ -213,9 +253,10 @@ def simulate_bloch(n_walkers, diffusivity, waveform, geometry, rf_events, *,
     (n_meas,) or at ``echo_steps`` (n_meas, n_echo), followed by the final walker-mean ``Mz``
     (n_meas,) with ``return_mz``.
     """
-    if susceptibility is not None:
-        raise NotImplementedError("susceptibility fields are not built in this engine")
     if kappa_MT and float(kappa_MT) > 0.0:
+        if susceptibility is not None:
+            raise NotImplementedError("the magnetisation-transfer walk takes no susceptibility "
+                                      "field")
         return _simulate_bloch_mt(
             n_walkers, diffusivity, waveform, geometry, rf_events, T2=T2, T1=T1, M0=M0,
             off_resonance_hz=off_resonance_hz, seed=seed, echo_steps=echo_steps,
@@ -228,7 +269,7 @@ def simulate_bloch(n_walkers, diffusivity, waveform, geometry, rf_events, *,
     w, uniq, idx = _prepare(n_walkers, diffusivity, waveform, geometry, rf_events, T2=T2, T1=T1,
                             M0=M0, off_resonance_hz=off_resonance_hz, seed=seed,
                             echo_steps=echo_steps, return_mz=return_mz, crusher=crusher,
-                            surface_relaxivity=surface_relaxivity)
+                            surface_relaxivity=surface_relaxivity, susceptibility=susceptibility)
     w.launch()
     return _finish(w.result(), n_walkers, uniq, idx, return_mz)
 

@@ -698,6 +698,13 @@ int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dms
     a.crush = bl->crush;
     a.m0 = bl->m0;
     a.t1_sample = bl->t1_sample;
+    a.fkind = bl->field_kind;
+    a.fn = bl->field_n;
+    a.ftab = bl->field_tab;
+    for (int k = 0; k < 9; ++k) a.frot[k] = bl->field_rot[k];
+    for (int k = 0; k < 8; ++k) a.fpar[k] = bl->field_par[k];
+    for (int k = 0; k < 3; ++k) a.fdims[k] = bl->field_dims[k];
+    a.fgdt = bl->field_gamma_dt;
   }
   BatchCtl none;
   memset(&none, 0, sizeof(none));
@@ -907,6 +914,16 @@ int dmsim_bloch(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim
   if (!b || !b->rf_flip || !b->rf_axis)
     return fail(DMSIM_EINVAL, "Bloch parameters need the per-sample flip and axis");
   if (!(b->t1_sample >= 0.f)) return fail(DMSIM_EINVAL, "t1_sample must be >= 0");
+  if (b->field_kind < 0 || b->field_kind > 3)
+    return fail(DMSIM_EINVAL, "unknown susceptibility field kind %d", b->field_kind);
+  if (b->field_kind && !b->field_tab)
+    return fail(DMSIM_EINVAL, "susceptibility field needs its table");
+  if ((b->field_kind == 1 || b->field_kind == 2) && b->field_n < 0)
+    return fail(DMSIM_EINVAL, "negative susceptibility source count");
+  if (b->field_kind == 3 && (b->field_dims[0] < 1 || b->field_dims[1] < 1 ||
+                             b->field_dims[2] < 1 || !(b->field_par[3] > 0.f) ||
+                             !(b->field_par[4] > 0.f) || !(b->field_par[5] > 0.f)))
+    return fail(DMSIM_EINVAL, "susceptibility grid needs positive dims and voxel sizes");
   if (o && o->phi) return fail(DMSIM_EINVAL, "the Bloch walk has no per-walker phase output");
   Plan pl;
   int rc = make_plan(p, g, &pl, kTabSmemBudget, true);

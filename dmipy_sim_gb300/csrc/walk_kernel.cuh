@@ -83,8 +83,101 @@ struct KArgs {
   const float* carrier;
   const float* crush;
   float m0, t1_sample;
+  // susceptibility field of the Bloch form: kind (0 none, 1 spheres, 2 myelin cylinders, 3 grid),
+  // table or grid, rotation into the field frame, parameters, grid dims, gamma * dt
+  int fkind, fn;
+  const float* ftab;
+  float frot[9], fpar[8];
+  int fdims[3];
+  float fgdt;
   int echo[kMaxEcho];
 };
+
+// dBz (T) of the susceptibility field at a walk-frame position (susceptibility.py:78-205,
+// 348-365): superposed magnetised spheres (distance clamped to the radius inside), periodic
+// hollow myelin cylinders, or a trilinearly sampled grid.
+static __device__ __noinline__ float field_dbz(const KArgs& a, float rx, float ry, float rz) {
+  const float* R = a.frot;
+  const float x = R[0] * rx + R[1] * ry + R[2] * rz;
+  const float y = R[3] * rx + R[4] * ry + R[5] * rz;
+  const float z = R[6] * rx + R[7] * ry + R[8] * rz;
+  if (a.fkind == 1) {
+    float sum = 0.f;
+    for (int k = 0; k < a.fn; ++k) {
+      const float* t = a.ftab + 5 * k;
+      const float dx = x - __ldg(t), dy = y - __ldg(t + 1), dz = z - __ldg(t + 2);
+      const float q = fmaxf(dx * dx + dy * dy + dz * dz, __ldg(t + 4));
+      sum += __ldg(t + 3) * (3.f * (dz * dz) / q - 1.f) / (q * sqrtf(q));
+    }
+    return sum;
+  }
+  if (a.fkind == 2) {
+    const float L = a.fpar[0];
+    float px = x, py = y;
+    if (a.fpar[5] != 0.f) {
+      px += 0.5f * L;
+      px -= L * floorf(px / L);
+      px -= 0.5f * L;
+      py += 0.5f * L;
+      py -= L * floorf(py / L);
+      py -= 0.5f * L;
+    }
+    const int ni = (int)a.fpar[4];
+    float p0 = 0.f, pc = 0.f, ps = 0.f;
+    for (int k = 0; k < a.fn; ++k) {
+      const float* t = a.ftab + 8 * k;
+      const float cx = __ldg(t), cy = __ldg(t + 1), a2 = __ldg(t + 2), b2 = __ldg(t + 3);
+      const float a4 = __ldg(t + 4), lba = __ldg(t + 5);
+      for (int jy = -ni; jy <= ni; ++jy)
+        for (int jx = -ni; jx <= ni; ++jx) {
+          const float dx = px - (cx + (float)jx * L), dy = py - (cy + (float)jy * L);
+          const float r2 = dx * dx + dy * dy, r4 = r2 * r2;
+          float f = 0.f;
+          if (r2 > b2) {
+            f = (b2 - a2) / r4;
+          } else if (r2 > a2) {
+            f = (r4 - a4) / (r4 * (b2 + a2));
+            p0 += -0.5f * logf(r2 / b2);
+          } else if (r2 < a2) {
+            p0 += lba;
+          }
+          pc += f * (dx * dx - dy * dy);
+          ps += f * 2.f * dx * dy;
+        }
+    }
+    return a.fpar[1] * p0 + a.fpar[1] * (a.fpar[2] * pc + a.fpar[3] * ps);
+  }
+  // grid: voxel (0, 0, 0) centred at origin + voxel / 2
+  const int per = a.fpar[6] != 0.f;
+  float f[3] = {(x - a.fpar[0]) / a.fpar[3] - 0.5f, (y - a.fpar[1]) / a.fpar[4] - 0.5f,
+                (z - a.fpar[2]) / a.fpar[5] - 0.5f};
+  int i0[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float n = (float)a.fdims[d];
+    if (per) f[d] -= n * floorf(f[d] / n);
+    const float fl = floorf(f[d]);
+    i0[d] = (int)fl;
+    f[d] -= fl;
+  }
+  float acc = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    float w = 1.f;
+    int ii[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int bit = (c >> d) & 1;
+      int j = i0[d] + bit;
+      w *= bit ? f[d] : 1.f - f[d];
+      const int n = a.fdims[d];
+      j = per ? ((j % n) + n) % n : min(max(j, 0), n - 1);
+      ii[d] = j;
+    }
+    acc += w * __ldg(a.ftab + ((size_t)ii[0] * a.fdims[1] + ii[1]) * a.fdims[2] + ii[2]);
+  }
+  return acc;
+}
 
 // Batched launch: a table of instances (one KArgs each, in global memory) walked by persistent
 // blocks that pull work items from a global counter.  A work item is up to `tiles_per_item`
@@ -766,8 +859,9 @@ __global__ void __launch_bounds__(kBlock, BATCH ? batch_min_blocks(PM, W) : DMSI
         }
         if constexpr (BLOCH) {
           // carriers of this sample: off-resonance + pulse carrier + crusher (bloch.py:126)
-          const float dpsi = (a.carrier ? __ldg(a.carrier + t) : 0.f) +
-                             (a.crush ? __ldg(a.crush + t) * uc : 0.f);
+          float dpsi = (a.carrier ? __ldg(a.carrier + t) : 0.f) +
+                       (a.crush ? __ldg(a.crush + t) * uc : 0.f);
+          if (a.fkind) dpsi += a.fgdt * field_dbz(a, ux, uy, uz);
           const float yk = dpsi - psik;
           const float tk = psi + yk;
           psik = (tk - psi) - yk;

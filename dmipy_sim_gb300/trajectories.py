@@ -334,7 +334,10 @@ def replay_bloch(trajectory, dt_traj, G, dt_wf, rf_events, *, T2=None, T1=None, 
                  else susceptibility)
         r = (traj_t.float().cpu().numpy() if isinstance(trajectory, torch.Tensor)
              else np.asarray(trajectory, np.float32))
-        dbz = np.array([[float(field(r[w, t])) for t in range(n_t)] for w in range(n_w)])
+        try:                                      # providers of this package take (..., 3)
+            dbz = np.asarray(field(r), np.float64).reshape(n_w, n_t)
+        except Exception:                         # a callable of one position
+            dbz = np.array([[float(field(r[w, t])) for t in range(n_t)] for w in range(n_w)])
         extra_phase_per_step = GAMMA * dt_traj * dbz
     p.extra_phase = dv(extra_phase_per_step, np.float64)
     if (surface_relaxivity is not None and dlog_boundary_unit is not None

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 8
+#define DMSIM_ABI_VERSION 9
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -319,6 +319,19 @@ typedef struct dmsim_bloch_params {
   const float* crush;    /* DEVICE (n_t) crusher rate (rad per unit coordinate) or NULL          */
   float m0;              /* equilibrium longitudinal magnetisation                                */
   float t1_sample;       /* dt/T1 per waveform sample, 0 if none                                  */
+  /* susceptibility field (bloch.py:126-128, susceptibility.py): evaluated at the walker's
+     position after each sample, rotated into the field frame by field_rot (row-major), and added
+     to its precession as field_gamma_dt * dBz.  field_kind 0 none; 1 magnetised spheres, table
+     (field_n, 5) = (cx, cy, cz, (dchi B0/3) a^3, a^2); 2 hollow myelin cylinders, table
+     (field_n, 8) = (cx, cy, a^2, b^2, a^4, ln(b/a), 0, 0), field_par = (L, dchi_a B0 sin^2/2,
+     cos 2 alpha, sin 2 alpha, images per side, periodic); 3 a grid of field_dims (x-major,
+     C order), field_par = (origin xyz, voxel xyz, periodic), trilinear. */
+  int32_t field_kind, field_n;
+  const float* field_tab; /* DEVICE table or grid                                                 */
+  float field_rot[9];
+  float field_par[8];
+  int32_t field_dims[3];
+  float field_gamma_dt;   /* gamma * dt                                                           */
 } dmsim_bloch_params;
 
 size_t dmsim_bloch_workspace_bytes(const dmsim_walk_params* p, const dmsim_geometry* g);

@@ -1050,6 +1050,49 @@ def make_rf_kat(root):
     print(f"rf_kat.npz: {len(out)} arrays")
 
 
+def susceptibility_inputs():
+    """Sources, sample points and a small chi grid of the susceptibility known answers."""
+    rng = np.random.default_rng(31)
+    return dict(
+        sph_c=rng.uniform(-6e-6, 6e-6, (7, 3)), sph_a=rng.uniform(0.5e-6, 1.5e-6, 7),
+        sph_chi=rng.uniform(-1e-6, 2e-6, 7),
+        my_c=np.array([[-2e-6, -2e-6], [2e-6, 1.5e-6], [1.8e-6, -2.2e-6]]),
+        my_a=np.array([0.9e-6, 0.7e-6, 0.8e-6]), my_b=np.array([1.3e-6, 1.1e-6, 1.2e-6]),
+        pts=rng.uniform(-5e-6, 5e-6, (64, 3)),
+        mask=(rng.random((12, 10, 8)) > 0.6).astype(float), rad=rng.normal(size=(12, 10, 8, 3)),
+        grid=rng.normal(size=(9, 7, 6)))
+
+
+def make_susceptibility_kat(root):
+    """susceptibility_kat.npz: dmipy-sim's own susceptibility fields (susceptibility.py)."""
+    _ref(root)
+    import importlib
+    su = importlib.import_module("dmipy_sim.susceptibility")
+    x = susceptibility_inputs()
+    out = {}
+    f = su.SusceptibilitySources(x["sph_c"], x["sph_a"], x["sph_chi"], B0=3.0).delta_bz_fn()
+    out["sph"] = np.array([float(f(p)) for p in x["pts"]])
+    for k, (th, al, per) in enumerate(((0.7, 0.3, True), (np.pi / 2, 1.1, True),
+                                       (1.2, 0.0, False))):
+        g = su.MyelinSusceptibility(x["my_c"], x["my_a"], x["my_b"], 8e-6, delta_chi_a=-0.1e-6,
+                                    B0=3.0, theta=th, alpha=al, periodic=per).delta_bz_fn()
+        out[f"my{k}"] = np.array([float(g(p)) for p in x["pts"]])
+    chi6 = su.myelin_susceptibility_tensor(x["mask"], x["rad"], chi_iso=-0.05e-6,
+                                           chi_aniso=-0.1e-6)
+    out["chi6"] = chi6
+    out["dB"] = su.dipole_field(chi6, [0.2e-6, 0.25e-6, 0.3e-6], [0.3, 0.2, 1.0], B0=3.0)
+    sdf = np.linalg.norm(np.stack(np.meshgrid(*[np.arange(n) - n / 2 for n in (12, 10, 8)],
+                                              indexing="ij"), -1), axis=-1) - 3.0
+    out["radial"] = su.radial_from_sdf(sdf, 0.2e-6)
+    org = np.array([-1e-6, -0.5e-6, 0.2e-6])
+    q = np.random.default_rng(5).uniform(-2e-6, 3e-6, (50, 3))
+    out["samp_clamp"] = su.sample_grid(x["grid"], q, org, 0.4e-6, periodic=False)
+    out["samp_wrap"] = su.sample_grid(x["grid"], q, org, 0.4e-6, periodic=True)
+    out["samp_q"] = q
+    np.savez_compressed(HERE / "susceptibility_kat.npz", **out)
+    print(f"susceptibility_kat.npz: {sorted(out)}")
+
+
 def make_mt_kat(root):
     """mt_kat.npz: dmipy-sim's own two-pool Bloch-McConnell model and binding bookkeeping
     (mt.py) on fixed inputs."""
@@ -1096,6 +1139,8 @@ if __name__ == "__main__":
     ap.add_argument("--replay-kat", action="store_true",
                     help="write replay_kat.npz (compression / replay-pack known answers)")
     ap.add_argument("--mc", action="store_true")
+    ap.add_argument("--susceptibility-kat", action="store_true",
+                    help="write susceptibility_kat.npz (field providers, dipole solver)")
     ap.add_argument("--rf-kat", action="store_true",
                     help="write rf_kat.npz (RF pulse constructors, Bloch integrator)")
     ap.add_argument("--replay-bloch-kat", action="store_true",
@@ -1119,6 +1164,8 @@ if __name__ == "__main__":
         make_myelin_kat(a.ref)
     if a.mc:
         make_mc(a.ref, a.procs, a.only)
+    if a.susceptibility_kat:
+        make_susceptibility_kat(a.ref)
     if a.rf_kat:
         make_rf_kat(a.ref)
     if a.replay_bloch_kat:

@@ -104,7 +104,8 @@ def test_refused_options_fail_before_any_walk():
     """The reference's argument errors, raised before the device is touched."""
     wf = ps.gradient_echo(1e-3, 1e-4)
     with pytest.raises(NotImplementedError):
-        d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, susceptibility=object())
+        d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, kappa_MT=1e-5,
+                         dwell_time=1e-3, susceptibility=object())
     with pytest.raises(ValueError):
         d.simulate_bloch(10, 2e-9, wf, d.Sphere(4e-6), wf.rf_events, kappa_MT=1e-5,
                          dwell_time=0.0)

@@ -208,3 +208,38 @@ def test_within_4_standard_errors_of_reference(cuda, mc_bloch, name):
     se = np.maximum(se, 2e-6 + 2e-5 * np.abs(np.asarray(ref["value"])))
     z = (mean - np.asarray(ref["value"])) / se
     assert np.max(np.abs(z)) < 4.0, (name, z)
+
+
+# ---- susceptibility fields on the device ---------------------------------------------------------
+def _provider(kind):
+    rng = np.random.default_rng(12)
+    if kind == "spheres":
+        return d.SusceptibilitySources(rng.uniform(-5e-6, 5e-6, (6, 3)),
+                                       rng.uniform(0.6e-6, 1.2e-6, 6), 1e-6, B0=3.0)
+    if kind == "myelin":
+        return d.MyelinSusceptibility([[-2e-6, -2e-6], [2e-6, 1.5e-6]], [0.9e-6, 0.7e-6],
+                                      [1.4e-6, 1.1e-6], 8e-6, delta_chi_a=-1e-6, B0=3.0,
+                                      theta=1.3, alpha=0.4)
+    x, y, z = np.meshgrid(*[np.linspace(0, 1, 24)] * 3, indexing="ij")
+    dB = 1e-6 * (np.sin(5 * x) * np.cos(3 * y) + 0.5 * z)
+    return d.GridSusceptibility(dB, np.array([-6e-6, -6e-6, -6e-6]), 0.5e-6, periodic=False)
+
+
+@pytest.mark.parametrize("kind", ["spheres", "myelin", "grid"])
+def test_static_field_dephases_the_gradient_echo_and_the_180_refocuses_it(cuda, kind):
+    """Walkers held still (D ~ 0): the gradient echo is the mean of exp(i n_t gamma dt dBz(r0))
+    with dBz from the host provider, and a 180 at the middle refocuses the static field."""
+    n, n_t, dt = 4096, 101, 1e-4
+    g = d.Sphere(6e-6)
+    r0 = g.init_positions(n, 3).astype(np.float32)
+    prov = _provider(kind)
+    wf = _zero(n_t, dt)
+    gre = B._bloch_walk(n, 1e-20, wf, g, EXC_Y, r0=r0, susceptibility=prov)[0]
+    phase = n_t * np.float64(np.float32(d.GAMMA * dt)) * prov.delta_bz_fn()(r0).astype(np.float64)
+    expect = np.mean(np.exp(1j * phase))
+    assert abs(complex(gre[0]) - expect) < 2e-3, (gre[0], expect)
+    assert abs(expect) < 0.9
+    se = B._bloch_walk(n, 1e-20, wf, g, EXC_Y + [{'t_s': 50 * dt, 'flip_deg': 180.0}], r0=r0,
+                       susceptibility=prov)[0]
+    one = np.mean(np.exp(-1j * phase / n_t))      # one sample's phase is left after the echo
+    assert abs(abs(complex(se[0])) - abs(one)) < 2e-3
