@@ -215,7 +215,7 @@ def _provider(kind):
     rng = np.random.default_rng(12)
     if kind == "spheres":
         return d.SusceptibilitySources(rng.uniform(-5e-6, 5e-6, (6, 3)),
-                                       rng.uniform(0.6e-6, 1.2e-6, 6), 1e-6, B0=3.0)
+                                       rng.uniform(0.6e-6, 1.2e-6, 6), 5e-6, B0=3.0)
     if kind == "myelin":
         return d.MyelinSusceptibility([[-2e-6, -2e-6], [2e-6, 1.5e-6]], [0.9e-6, 0.7e-6],
                                       [1.4e-6, 1.1e-6], 8e-6, delta_chi_a=-1e-6, B0=3.0,
