@@ -299,7 +299,8 @@ int dmsim_replay(const void* traj, int32_t traj_f16, int64_t n_walkers, int32_t 
 
 /* ---- vector Bloch ------------------------------------------------------------------------------
    The forward vector-Bloch walk of bloch.py:212-340 (simulate_bloch without magnetisation
-   transfer or susceptibility): every walker carries M_m = (Mx, My, Mz) for each measurement m,
+   transfer; a susceptibility field is optional, below): every walker carries M_m = (Mx, My, Mz)
+   for each measurement m,
    starting from (0, 0, m0), and each waveform sample t applies, after the move of the walk
    (the same walk, stream and sub-steps as dmsim_walk for the same parameters):
      an RF rotation by rf_flip[t] about (cos rf_axis[t], sin rf_axis[t], 0)    (bloch.py:44-57),
