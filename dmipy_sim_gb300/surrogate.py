@@ -9,7 +9,7 @@ Scope: packed parallel cylinders (the axis is the encoding's reference axis), wi
 inside the hull it was trained on (:data:`HULL`) and echo times up to ``t_max``.  Every query
 outside the hull -- another substrate kind, a parameter out of range, a longer waveform -- is
 answered by the batched Monte-Carlo walk (:meth:`Surrogate.signals` does the routing), and the
-same walk at 1e6 walkers is the judge of the surrogate's error on held-out substrates.
+same walk at 1e6 walkers is what the surrogate's error on held-out substrates is measured against.
 """
 import dataclasses
 import time
