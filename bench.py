@@ -237,7 +237,12 @@ def profile_case(a):
     batched   a 32-instance slice of the batched study at 4096 walkers per instance;
     bloch     the vector-Bloch walk of a diffusion-weighted spin echo (2 measurements, 201
               samples) in a 4 um cylinder with surface relaxivity, 1,048,576 walkers; also
-              times the scalar walk of the same gradient, geometry and walk."""
+              times the scalar walk of the same gradient, geometry and walk;
+    mt        the magnetisation-transfer walk of a CW saturation (200 Hz, 1 kHz off, 25 ms at
+              dt 20 us) in a 2 um sphere, 131,072 walkers x 1251 samples x 38 sub-steps, FP64
+              magnetisation, no burn-in (times the sequence walk alone);
+    rbloch    the vector-Bloch replay of a stored float16 walk, 262,144 walkers x 500 samples,
+              4 measurements, a spin echo with T2 and T1 (FP64)."""
     import dataclasses
     import torch
     import dmipy_sim_gb300 as d
@@ -272,6 +277,51 @@ def profile_case(a):
         extra = {"walker_steps_per_launch": n_w * seq.n_t,
                  "scalar_walk_ms": ms,
                  "scalar_walker_steps_per_s": n_w * seq.n_t / (ms * 1e-3)}
+    if a.profile_case in ("mt", "rbloch"):
+        import time
+        if a.profile_case == "mt":
+            from dmipy_sim_gb300 import bloch as B
+            n_w, n_t, n_sub, dt = 1 << 17, 1251, 38, 2e-5
+            sph = d.Sphere(2e-6)
+            rf = [{'t_s': 0.0125, 'flip_deg': 360.0 * 200.0 * 0.025, 'axis_deg': 0.0,
+                   'duration_s': 0.025, 'offset_hz': 1000.0}]
+            r0 = torch.from_numpy(np.asarray(sph.init_positions(n_w, 3), np.float32))
+            kw = dict(T2=0.08, T1=1.0, M0=1.0, off_resonance_hz=0.0, off_resonance_bound=0.0,
+                      T2_bound=1e-5, T1_bound=1.0, echo_steps=None, return_mz=True,
+                      crusher=None, return_bound_frac=False)
+
+            def run():
+                w = B.MTWalk(sph, n_w, D, dt, n_sub, 3, kappa_MT=40.0 * 2e-6 / 3.0,
+                             dwell_time=1.0 / 80.0, surface_relaxivity=0.0)
+                w.r.copy_(r0)
+                B._mt_run(w, np.zeros((1, n_t, 3)), dt, rf, **kw)
+            units, unit = n_w * n_t * n_sub, "walker_substeps"
+        else:
+            from dmipy_sim_gb300.trajectories import replay_bloch
+            n_w, n_t, dt = 1 << 18, 500, 1e-4
+            g = torch.Generator(device=dev).manual_seed(0)
+            traj = (torch.randn((n_w, n_t, 3), generator=g, device=dev) * 2e-6).half()
+            G = np.zeros((4, n_t, 3))
+            for m in range(4):
+                G[m, 50:150, m % 3] = G[m, 300:400, m % 3] = 0.04
+            rf = [{'t_s': 0.0, 'flip_deg': 90.0, 'axis_deg': 90.0},
+                  {'t_s': 0.0225, 'flip_deg': 180.0}]
+
+            def run():
+                replay_bloch(traj, dt, G, dt, rf, T2=0.08, T1=1.0)
+            units, unit = n_w * n_t, "walker_samples"
+        for _ in range(max(1, a.warmup)):
+            run()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(max(1, a.steps)):
+            run()
+        torch.cuda.synchronize(dev)
+        ms = (time.perf_counter() - t0) * 1e3 / max(1, a.steps)
+        print(json.dumps({"profile_case": a.profile_case, "ok": True, "ms_per_call": ms,
+                          unit + "_per_call": units, unit + "_per_s": units / (ms * 1e-3),
+                          "timing": "host clock around synchronised calls (incl. host setup)"}))
+        return
     for _ in range(max(1, a.warmup) + a.steps):
         if _ == max(1, a.warmup):
             torch.cuda.synchronize(dev)
@@ -489,7 +539,8 @@ def main():
                     help="walkers per instance of the batched study (20000: <= 0.005 error)")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per GPU (smaller only for profiling captures)")
-    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched", "bloch"], default=None,
+    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched", "bloch", "mt", "rbloch"],
+                    default=None,
                     help="run one small kernel case for a profiler capture and exit")
     a = ap.parse_args()
     if a.profile_case:
