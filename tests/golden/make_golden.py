@@ -1096,7 +1096,7 @@ def make_susceptibility_kat(root):
 def make_mt_kat(root):
     """mt_kat.npz: dmipy-sim's own two-pool Bloch-McConnell model and binding bookkeeping
     (mt.py) on fixed inputs."""
-    _ref(root)
+    m = _ref(root)
     import importlib
     mt = importlib.import_module("dmipy_sim.mt")
     out = {}
@@ -1120,6 +1120,13 @@ def make_mt_kat(root):
         mt.forward_rate(2e-6, 3e5), mt.backward_rate(0.0125), mt.bound_fraction(2e-6, 0.0125, 3e5),
         mt.kappa_MT_from_forward_rate(40.0, 1.5e6), mt.dwell_time_from_fraction(0.3, 40.0)])
     out["stick"] = mt.stick_probability(np.array([0.0, 1e-9, 1e-8, 1e-6]), 2e-5, 2e-9)
+    geo, phys = m["geometries"], m["physics"]
+    out["mt_sub"] = np.array([
+        phys.mt_sub_steps(geo.Sphere(2e-6), 2e-9, 2e-5, 1.0 / 80.0),
+        phys.mt_sub_steps(geo.Sphere(5e-6), 1e-9, 1e-3, 0.01),
+        phys.mt_sub_steps(geo.Cylinder(3e-6, (0, 0, 1)), 2e-9, 1e-4, 1e-5),
+        phys.mt_sub_steps(geo.Box1D(4e-6), 2e-9, 1e-4, 0.02),
+        phys.mt_sub_steps(geo.Box1D(4e-6), 2e-9, 1e-4, 0.0)])
     np.savez_compressed(HERE / "mt_kat.npz", **out)
     print(f"mt_kat.npz: {len(out)} arrays")
 

@@ -186,6 +186,16 @@ def test_two_pool_model_matches_reference():
                                                        2e-9), z["stick"])
 
 
+def test_mt_sub_step_rule_matches_reference():
+    z = np.load(Path(__file__).parent / "golden" / "mt_kat.npz")
+    got = [d.mt_sub_steps(d.Sphere(2e-6), 2e-9, 2e-5, 1.0 / 80.0),
+           d.mt_sub_steps(d.Sphere(5e-6), 1e-9, 1e-3, 0.01),
+           d.mt_sub_steps(d.Cylinder(3e-6, (0, 0, 1)), 2e-9, 1e-4, 1e-5),
+           d.mt_sub_steps(d.Box1D(4e-6), 2e-9, 1e-4, 0.02),
+           d.mt_sub_steps(d.Box1D(4e-6), 2e-9, 1e-4, 0.0)]
+    np.testing.assert_array_equal(got, z["mt_sub"])
+
+
 def test_oracle_mt_exchange_reaches_equilibrium_fraction():
     """The restated MT walk on a sphere: the bound occupancy relaxes to k_f/(k_f + k_r)."""
     R, D, k_f, k_r = 5e-6, 1e-9, 50.0, 100.0
