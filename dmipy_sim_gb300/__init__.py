@@ -12,7 +12,8 @@ from .geometries import (Geometry, FreeDiffusion, Cylinder, Sphere, MyelinatedCy
                          PackedMyelinatedCylinders, pack_myelinated_cylinders, Box1D,
                          PermeableSlab1D, PermeableShell, Ellipsoid, pack_cylinders,
                          PackedCylinders, pack_spheres, PackedSpheres, lattice_cylinders)
-from .core import (simulate, simulate_cpmg, simulate_trajectories, run_walk, WalkResult,
+from .core import (simulate, simulate_mixture, simulate_cpmg, simulate_trajectories, run_walk,
+                   WalkResult,
                    permeable_sub_steps, surface_sub_steps, collision_sub_steps, replay_sub_steps,
                    fused_sub_steps, mt_sub_steps)
 from . import trajectories
@@ -41,7 +42,7 @@ __all__ = [
     "Cylinder", "Sphere", "MyelinatedCylinder", "PackedMyelinatedCylinders",
     "pack_myelinated_cylinders", "Box1D", "PermeableSlab1D", "PermeableShell", "Ellipsoid",
     "pack_cylinders", "PackedCylinders", "pack_spheres", "PackedSpheres", "lattice_cylinders",
-    "simulate", "simulate_cpmg", "simulate_trajectories", "trajectories", "replay_bloch",
+    "simulate", "simulate_mixture", "simulate_cpmg", "simulate_trajectories", "trajectories", "replay_bloch",
     "replay_bloch_jax", "unwrap_periodic", "pathway_sign_se", "finite_180_longitudinal_dwell",
     "pre_pulse_gradient_phase", "run_walk", "WalkResult",
     "permeable_sub_steps", "surface_sub_steps", "collision_sub_steps", "replay_sub_steps",

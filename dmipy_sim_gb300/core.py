@@ -574,6 +574,21 @@ def _simulate_in_walker_batches(n_walkers, walker_batch_size, *, seed, diffusivi
     return res[0] if len(res) == 1 else tuple(res)
 
 
+def simulate_mixture(compartments, waveform, seed=123):
+    """Compartments without exchange (core.py:821-858): each dict (``fraction``, ``n_walkers``,
+    ``diffusivity``, ``geometry``) is walked on its own by ``simulate`` with seed + its index,
+    and the signals are summed weighted by the fractions, which must sum to 1."""
+    total = sum(c['fraction'] for c in compartments)
+    if abs(total - 1.0) > 1e-6:
+        raise ValueError(f"Compartment fractions must sum to 1, got {total}")
+    signal = None
+    for i, c in enumerate(compartments):
+        s = c['fraction'] * simulate(n_walkers=c['n_walkers'], diffusivity=c['diffusivity'],
+                                     waveform=waveform, geometry=c['geometry'], seed=seed + i)
+        signal = s if signal is None else signal + s
+    return signal
+
+
 def simulate_cpmg(n_walkers, diffusivity, waveform, geometry, *, T2=None, seed=123,
                   walker_batch_size=None, require_gpu=None):
     """Multi-echo CPMG signal (n_echoes, n_meas) from one walk (core.py:861-969): the ensemble is

@@ -272,3 +272,22 @@ def test_oracle_spin_echo_refocuses_free_diffusion():
     q = GAMMA * g * nd * dt
     b = q * q * (0.02 - nd * dt / 3.0)
     assert abs(s[0] + 1j * s[1]) == pytest.approx(np.exp(-b * D - n_t * dt / 0.08), abs=0.02)
+
+
+def test_simulate_mixture_weights_compartments_with_their_own_seeds(monkeypatch):
+    from dmipy_sim_gb300 import core
+    calls = []
+
+    def fake(n_walkers, diffusivity, waveform, geometry, seed):
+        calls.append((n_walkers, diffusivity, geometry, seed))
+        return np.full(3, float(seed), np.float32)
+
+    monkeypatch.setattr(core, "simulate", fake)
+    wf = d.set_b(d.pgse(0.01, 0.03, 0.05, [[1, 0, 0]] * 3, 50), [0, 1e9, 2e9])
+    comps = [dict(fraction=0.3, n_walkers=10, diffusivity=1e-9, geometry="a"),
+             dict(fraction=0.7, n_walkers=20, diffusivity=2e-9, geometry="b")]
+    s = core.simulate_mixture(comps, wf, seed=5)
+    assert [c[3] for c in calls] == [5, 6] and [c[2] for c in calls] == ["a", "b"]
+    np.testing.assert_allclose(s, 0.3 * 5 + 0.7 * 6, rtol=1e-6)
+    with pytest.raises(ValueError):
+        core.simulate_mixture([dict(comps[0], fraction=0.5)], wf)
