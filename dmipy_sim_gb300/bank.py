@@ -109,38 +109,53 @@ def _select_boundary_codec(m, dlog, env, tol, dtype, verbose=False):
         cands.append((K, cf))
         if cf is not None and cf["err"] <= tol * cf["floor"]:
             if verbose:
-                print(f"[bank] boundary codec: boundary_dct K={K} {np.dtype(dtype).name} "
-                      f"(err={cf['err']:.2e} vs floor {cf['floor']:.2e})", flush=True)
+                print(f"boundary channel: {K} cumulative DCT bands ({np.dtype(dtype).name}), "
+                      f"surface error {cf['err']:.2e} / floor {cf['floor']:.2e}", flush=True)
             return a, mm
     a, mm = _cx.encode_boundary_local_time(dlog)
     if verbose:
-        print("[bank] boundary codec: no DCT K passed the surface gate; exact "
-              f"{mm['mode']} codec", flush=True)
+        print(f"boundary channel: no band count met the surface gate, stored {mm['mode']} "
+              "(quantised per step)", flush=True)
     return a, mm
 
 
-def _precision_tiers(arrays, n_walkers, floor_max, walkers_shuffled):
-    """Walker-prefix read sizes for statistical floors 1e-2, 3e-3, 1e-3 (bank.py:526-557)."""
-    per_walker, fixed, whole = 0, 0, []
-    for k, v in arrays.items():
+_TIER_FLOORS = (1e-2, 3e-3, 1e-3)
+
+
+def _prefix_layout(arrays, n_walkers):
+    """(bytes per walker of the walker-leading tensors, bytes of the rest, names of the rest).
+
+    A tensor whose first axis is the walker axis can be read for a walker prefix as one
+    contiguous range; the others (run-length rows, modes, tables) must be read whole."""
+    per_walker, whole = 0, {}
+    for name, v in arrays.items():
         a = np.asarray(v)
-        if a.ndim >= 1 and a.shape[0] == n_walkers:
-            per_walker += int(a.nbytes // max(n_walkers, 1))
+        if a.ndim and a.shape[0] == n_walkers:
+            per_walker += a.nbytes // max(n_walkers, 1)
         else:
-            fixed += int(a.nbytes)
-            whole.append(k)
-    tiers = []
-    if floor_max > 0:
-        for eps in (1e-2, 3e-3, 1e-3):
-            n = int(min(n_walkers, max(1, np.ceil(n_walkers * (floor_max / eps) ** 2))))
-            tiers.append(dict(eps=float(eps), n_walkers=n, bytes=int(n * per_walker + fixed),
-                              reachable=bool(n < n_walkers or floor_max <= eps)))
-    return dict(bytes_per_walker=per_walker, fixed_bytes=fixed,
-                not_prefix_sliceable=sorted(whole), floor_at_full_n=float(floor_max),
-                walkers_shuffled=bool(walkers_shuffled), usable=bool(walkers_shuffled),
-                tiers=tiers,
-                note=("prefix reads are unbiased" if walkers_shuffled else
-                      "WALKER ORDER NOT DECLARED SHUFFLED -- a prefix may be a biased sub-ensemble"))
+            whole[name] = a.nbytes
+    return int(per_walker), int(sum(whole.values())), sorted(whole)
+
+
+def _precision_tiers(arrays, n_walkers, floor_max, walkers_shuffled):
+    """Walker-prefix reads for the statistical floors 1e-2, 3e-3 and 1e-3 (the metadata block of
+    bank.py:526-557): the Monte-Carlo floor falls as n^-1/2, so a floor eps needs the first
+    n = N (floor_max / eps)^2 walkers (at least 1, at most N).  A prefix is an unbiased
+    sub-ensemble only when the producer declares the walker order shuffled."""
+    per_walker, fixed, whole = _prefix_layout(arrays, n_walkers)
+
+    def tier(eps):
+        n = int(np.clip(np.ceil(n_walkers * (floor_max / eps) ** 2), 1, n_walkers))
+        return dict(eps=float(eps), n_walkers=n, bytes=int(n * per_walker + fixed),
+                    reachable=bool(n < n_walkers or floor_max <= eps))
+
+    shuffled = bool(walkers_shuffled)
+    return dict(bytes_per_walker=per_walker, fixed_bytes=fixed, not_prefix_sliceable=whole,
+                floor_at_full_n=float(floor_max), walkers_shuffled=shuffled, usable=shuffled,
+                tiers=[tier(e) for e in _TIER_FLOORS] if floor_max > 0 else [],
+                note=("walker prefixes are exchangeable samples of the ensemble" if shuffled
+                      else "walker order not declared shuffled: a prefix can be a biased "
+                           "sub-ensemble"))
 
 
 def _refresh(fid, err, floor, sigma_star):
@@ -213,61 +228,85 @@ def build_replay_pack(src, *, id, method="temporal_dct", envelope=None, tol=2.0,
             fid.update(err_surface=cf["err"], floor_surface=cf["floor"])
             fid = _refresh(fid, cf["err"], cf["floor"], sigma_star)
     n_t = X.shape[1]
-    comp_meta = dict(method=method, K=int(K), walker_preserving=bool(wp), n_t=int(n_t))
-    if wp:
-        comp_meta["precision_tiers"] = _precision_tiers(arrays, int(m["n_walkers"]),
-                                                        float(fid.get("floor_max") or 0.0),
-                                                        bool(m.get("walkers_shuffled")))
-    if chan_meta:
-        comp_meta["channels"] = chan_meta
-
-    def lst(k):
-        return None if m.get(k) is None else np.asarray(m[k]).tolist()
-    meta = dict(
-        rpk_schema_version=RPK_SCHEMA_VERSION, id=id, compression=comp_meta,
-        walk_params=dict(n_walkers=int(m["n_walkers"]), n_t=int(n_t), dt_traj=dt,
-                         T_max=float(m["T_max"]), diffusivity=m.get("D_intra"),
-                         seed=int(m["seed"]), cell_size=m.get("cell_size"),
-                         substrate_frame=lst("substrate_frame")),
-        per_comp=dict(T2=lst("T2_per_comp"), T1=lst("T1_per_comp"), R=lst("R")),
-        replay_envelope=dict(gradient=True, bulk_relaxation=channels["T1T2"],
-                             surface_relaxivity=channels["rho"], field=False,
-                             magnetization_transfer=channels["mt"], diffusivity_fixed=True,
-                             acquisition=_envelope_summary(env)),
-        fidelity=fid, provenance=provenance or {}, license=license, citation=citation)
-    if m.get("mt_params") is not None:
-        meta["mt"] = {k: (float(v) if isinstance(v, (int, float, np.floating)) else v)
-                      for k, v in m["mt_params"].items()}
+    meta = _pack_metadata(m, id=id, method=method, K=K, walker_preserving=wp, n_t=n_t, dt=dt,
+                          arrays=arrays, chan_meta=chan_meta, channels=channels, env=env,
+                          fidelity=fid, provenance=provenance, license=license,
+                          citation=citation)
     pack = ReplayPack(arrays, meta, source=out_path)
     if out_path is not None:
         write_rpk(out_path, {k: v for k, v in arrays.items() if v is not None}, meta)
     if verbose:
-        print(f"[pack] {id} method={method} K={K} err={fid['err_max']:.4f} "
-              f"floor={fid['floor_max']:.4f} within2x={fid['within_2x_floor']}", flush=True)
+        verdict = "within" if fid["within_2x_floor"] else "beyond"
+        print(f"pack {id}: {method} with {K} modes, replay error {fid['err_max']:.4f} "
+              f"({verdict} 2 x the floor {fid['floor_max']:.4f})", flush=True)
     return pack
+
+
+def _as_list(m, key):
+    v = m.get(key)
+    return None if v is None else np.asarray(v).tolist()
+
+
+def _pack_metadata(m, *, id, method, K, walker_preserving, n_t, dt, arrays, chan_meta, channels,
+                   env, fidelity, provenance, license, citation):
+    """The .rpk metadata of a pack (the key layout of bank.py:741-781, which readers of the
+    format rely on): compression block (method, modes, precision tiers, channel codecs), walk
+    parameters, per-compartment constants, the replay envelope, fidelity and provenance."""
+    compression = dict(method=method, K=int(K), walker_preserving=bool(walker_preserving),
+                       n_t=int(n_t))
+    if walker_preserving:
+        compression["precision_tiers"] = _precision_tiers(
+            arrays, int(m["n_walkers"]), float(fidelity.get("floor_max") or 0.0),
+            bool(m.get("walkers_shuffled")))
+    if chan_meta:
+        compression["channels"] = chan_meta
+    walk = dict(n_walkers=int(m["n_walkers"]), n_t=int(n_t), dt_traj=dt, T_max=float(m["T_max"]),
+                diffusivity=m.get("D_intra"), seed=int(m["seed"]), cell_size=m.get("cell_size"),
+                substrate_frame=_as_list(m, "substrate_frame"))
+    envelope = dict(gradient=True, bulk_relaxation=channels["T1T2"],
+                    surface_relaxivity=channels["rho"], field=False,
+                    magnetization_transfer=channels["mt"], diffusivity_fixed=True,
+                    acquisition=_envelope_summary(env))
+    meta = dict(rpk_schema_version=RPK_SCHEMA_VERSION, id=id, compression=compression,
+                walk_params=walk,
+                per_comp=dict(T2=_as_list(m, "T2_per_comp"), T1=_as_list(m, "T1_per_comp"),
+                              R=_as_list(m, "R")),
+                replay_envelope=envelope, fidelity=fidelity, provenance=provenance or {},
+                license=license, citation=citation)
+    if m.get("mt_params") is not None:
+        meta["mt"] = {k: (float(v) if isinstance(v, (int, float, np.floating)) else v)
+                      for k, v in m["mt_params"].items()}
+    return meta
 
 
 def build_to_floor(make_model, *, id, envelope=None, sigma_star=1e-3, pilot_n=8000, safety=1.4,
                    max_n=400000, walk=None, method="temporal_dct", verbose=True, **bp):
-    """Size the walker count so the split-half floor reaches ``sigma_star`` (a pilot walk, one
-    re-estimate when it undershoots), then build the pack to that floor (bank.py:790-808)."""
+    """A pack whose split-half floor reaches ``sigma_star`` (the contract of bank.py:790-808).
+
+    The floor of a walk falls as n^-1/2, so a pilot of ``pilot_n`` walkers predicts the walker
+    count, inflated by ``safety`` and capped at ``max_n``; when the walk at that count still
+    misses the target, the count is predicted once more from it.  ``make_model(n)`` returns the
+    master walk of n walkers on a fixed substrate (``walk`` maps it to the master dict)."""
     env = envelope or _cx.default_envelope()
-    _walk = walk or _master_arrays
-    f0 = _measure_floor(_walk(make_model(pilot_n)), env)
-    n_star = int(min(max_n, max(pilot_n, round(pilot_n * (f0 / sigma_star) ** 2 * safety))))
+    master_of = walk or _master_arrays
+
+    def walk_floor(n):
+        model = make_model(n)
+        return model, _measure_floor(master_of(model), env)
+
+    def predicted(n, floor):
+        return int(min(max_n, round(n * (floor / sigma_star) ** 2 * safety)))
+
+    _, f_pilot = walk_floor(pilot_n)
+    n = max(pilot_n, predicted(pilot_n, f_pilot)) if pilot_n < max_n else max_n
+    model, f = walk_floor(n)
+    history = [(pilot_n, f_pilot), (n, f)]
+    if f > sigma_star and n < max_n:
+        n = predicted(n, f)
+        model, f = walk_floor(n)
+        history.append((n, f))
     if verbose:
-        print(f"[floor-target] pilot N={pilot_n}: floor={f0:.4g}; sigma*={sigma_star:.4g} -> "
-              f"N*~{n_star}", flush=True)
-    model = make_model(n_star)
-    f = _measure_floor(_walk(model), env)
-    if f > sigma_star and n_star < max_n:
-        n_star = int(min(max_n, round(n_star * (f / sigma_star) ** 2 * safety)))
-        if verbose:
-            print(f"[floor-target] floor={f:.4g} > sigma*; topping up to N*={n_star}", flush=True)
-        model = make_model(n_star)
-        f = _measure_floor(_walk(model), env)
-    if verbose:
-        print(f"[floor-target] N={n_star}: achieved floor={f:.4g} "
-              f"({'<=' if f <= sigma_star else '>'} sigma*)", flush=True)
+        steps = ", ".join(f"{k} walkers -> {v:.3g}" for k, v in history)
+        print(f"walker count for floor {sigma_star:.3g}: {steps}", flush=True)
     return build_replay_pack(model, id=id, envelope=env, method=method, err_target=sigma_star,
                              sigma_star=sigma_star, verbose=verbose, **bp)

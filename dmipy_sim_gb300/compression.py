@@ -302,14 +302,15 @@ def decode_compartment(arrays, meta):
     return q.astype(np.int16)
 
 
-CHANNEL_ENCODERS = {"bound_fraction": encode_bound_fraction,
-                    "boundary_local_time": encode_boundary_local_time,
-                    "boundary_dct": encode_boundary_dct,
-                    "compartment": encode_compartment}
-CHANNEL_DECODERS = {"bound_fraction": decode_bound_fraction,
-                    "boundary_local_time": decode_boundary_local_time,
-                    "boundary_dct": decode_boundary_dct,
-                    "compartment": decode_compartment}
+# Codec of each per-walker channel, by the channel name the pack metadata records.
+_CHANNELS = (
+    ("bound_fraction", encode_bound_fraction, decode_bound_fraction),
+    ("boundary_local_time", encode_boundary_local_time, decode_boundary_local_time),
+    ("boundary_dct", encode_boundary_dct, decode_boundary_dct),
+    ("compartment", encode_compartment, decode_compartment),
+)
+CHANNEL_ENCODERS = {name: enc for name, enc, _ in _CHANNELS}
+CHANNEL_DECODERS = {name: dec for name, _, dec in _CHANNELS}
 
 
 # ------------------------------------------------------------------ position layout
@@ -345,27 +346,50 @@ def is_walker_preserving(method):
     return method in WALKER_PRESERVING
 
 
+def _stored_coeffs(arrays, meta, n, rng):
+    A = np.asarray(arrays["coeffs"], np.float64)
+    if n is not None and n != A.shape[0]:
+        raise ValueError("lowrank preserves its stored walker count only")
+    return A
+
+
+def _gaussian_coeffs(arrays, meta, n, rng):
+    """n draws of the stored coefficient Gaussian: mean + Z L^T, L the Cholesky factor of the
+    covariance (a 1e-30 ridge keeps it positive definite), Z standard normal (n, K)."""
+    cov = np.asarray(arrays["coeff_cov"], np.float64)
+    chol = np.linalg.cholesky(cov + 1e-30 * np.eye(cov.shape[0]))
+    z = rng.standard_normal((n, cov.shape[0]))
+    return z @ chol.T + np.asarray(arrays["coeff_mean"], np.float64)
+
+
+def _marginal_coeffs(arrays, meta, n, rng):
+    """n draws of independent coefficients, each through its stored quantile table (inverse-CDF
+    sampling with linear interpolation between equally spaced probabilities)."""
+    table = np.asarray(arrays["coeff_quantiles"], np.float64)
+    probs = np.linspace(0.0, 1.0, table.shape[0])
+    u = rng.random((n, table.shape[1]))
+    out = np.empty_like(u)
+    for k in range(table.shape[1]):
+        out[:, k] = np.interp(u[:, k], probs, table[:, k])
+    return out
+
+
+_COEFF_SOURCES = {"lowrank": _stored_coeffs, "gaussian": _gaussian_coeffs,
+                  "marginal": _marginal_coeffs}
+
+
 def _sample_coeffs(arrays, meta, n_walkers=None, seed=0):
-    """Per-walker KL coefficients: stored (lowrank) or drawn from the stored distribution
-    (compression.py:291-306)."""
+    """Per-walker Karhunen-Loeve coefficients (n, K): the stored ones of a walker-preserving pack,
+    or n draws (default: the recorded walker count, else 100,000) from the coefficient
+    distribution of a distributional one, from numpy's generator seeded with ``seed`` (the
+    decode contract of compression.py:290-306)."""
     method = meta["method"]
-    rng = np.random.default_rng(seed)
-    if method == "lowrank":
-        A = np.asarray(arrays["coeffs"], np.float64)
-        if n_walkers is not None and n_walkers != A.shape[0]:
-            raise ValueError("lowrank preserves its stored walker count only")
-        return A
-    K = np.asarray(arrays["modes"]).shape[0]
-    n = n_walkers or int(meta.get("n_walkers", 100_000))
-    if method == "gaussian":
-        L = np.linalg.cholesky(np.asarray(arrays["coeff_cov"], np.float64) + 1e-30 * np.eye(K))
-        return rng.standard_normal((n, K)) @ L.T + np.asarray(arrays["coeff_mean"], np.float64)
-    if method == "marginal":
-        quant = np.asarray(arrays["coeff_quantiles"], np.float64)
-        qs = np.linspace(0, 1, quant.shape[0])
-        u = rng.random((n, K))
-        return np.stack([np.interp(u[:, k], qs, quant[:, k]) for k in range(K)], axis=1)
-    raise ValueError(f"unknown method {method!r}")
+    if method not in _COEFF_SOURCES:
+        raise ValueError(f"unknown method {method!r}")
+    n = n_walkers
+    if method != "lowrank":
+        n = n_walkers or int(meta.get("n_walkers", 100_000))
+    return _COEFF_SOURCES[method](arrays, meta, n, np.random.default_rng(seed))
 
 
 def decode(arrays, meta, n_walkers=None, seed=0):
@@ -420,40 +444,59 @@ def mode_space_signal(arrays, meta, G, dt, logw=None, weights=None, n_walkers=No
     return (np.exp(lw[:, None] + 1j * phi) * (w / w.sum())[:, None]).sum(0)
 
 
-def relaxation_logweight(comp, T2_per_comp, T1_per_comp, dt, chi=None):
-    """Per-walker bulk-relaxation log-weight from the compartment channel (compression.py:468-485)."""
-    comp = np.asarray(comp)
+def _rates(times):
+    """1 / T per compartment, 0 where T <= 0 (no relaxation)."""
+    T = np.asarray(times, float)
+    return np.where(T > 0, 1.0 / np.maximum(T, 1e-30), 0.0)
 
-    def inv(T):
-        T = np.asarray(T, float)
-        return np.where(T > 0, 1.0 / np.maximum(T, 1e-30), 0.0)
-    i2, i1 = inv(T2_per_comp), inv(T1_per_comp)
-    if np.issubdtype(comp.dtype, np.floating) and not np.array_equal(comp, np.round(comp)):
+
+def relaxation_logweight(comp, T2_per_comp, T1_per_comp, dt, chi=None):
+    """Bulk-relaxation log-weight per walker, -dt sum_t [chi_t R2(c_t) + (1 - chi_t) R1(c_t)]
+    (chi = 1 throughout without a coherence mask), from the compartment channel (the contract of
+    compression.py:468-485): integer labels index the per-compartment rates; a fractional
+    channel is the occupancy f of compartment 1 and mixes the rates of compartments 0 and 1 as
+    (1 - f) R(0) + f R(1)."""
+    comp = np.asarray(comp)
+    r2, r1 = _rates(T2_per_comp), _rates(T1_per_comp)
+    fractional = np.issubdtype(comp.dtype, np.floating) and not np.array_equal(comp,
+                                                                                np.round(comp))
+    if fractional:
         f = np.clip(comp, 0.0, 1.0)
-        r2 = (1.0 - f) * i2[0] + f * i2[1]
-        r1 = (1.0 - f) * i1[0] + f * i1[1]
+        rate2 = r2[0] + f * (r2[1] - r2[0])
+        rate1 = r1[0] + f * (r1[1] - r1[0])
     else:
-        ci = comp.astype(np.int64)
-        r2, r1 = i2[ci], i1[ci]
+        idx = comp.astype(np.int64)
+        rate2, rate1 = r2[idx], r1[idx]
     if chi is None:
-        return -dt * r2.sum(1)
-    chi = np.asarray(chi, float)[None, :]
-    return -dt * (chi * r2 + (1.0 - chi) * r1).sum(1)
+        return -dt * np.sum(rate2, axis=1)
+    c = np.asarray(chi, float)
+    return -dt * (rate2 @ c + rate1 @ (1.0 - c))
 
 
 def surface_logweight(blt, rho_over_D, chi=None):
-    """(rho/D) sum_t chi_t ell(t) per walker, ell stored at rho/D = 1 (compression.py:488-493)."""
-    blt = np.asarray(blt, np.float64)
-    s = blt.sum(1) if chi is None else (np.asarray(chi, float)[None, :] * blt).sum(1)
-    return float(rho_over_D) * s
+    """Surface-relaxation log-weight per walker, (rho / D) sum_t chi_t ell_t, from the boundary
+    channel ell stored at rho / D = 1 (compression.py:488-493)."""
+    ell = np.asarray(blt, np.float64)
+    total = ell.sum(axis=1) if chi is None else ell @ np.asarray(chi, float)
+    return float(rho_over_D) * total
 
 
 # ------------------------------------------------------------------ envelope and fidelity
+# The acquisition envelope a pack is certified over (b in s/m^2): PGSE at these b-values and
+# directions, cosine OGSE of these period counts, short-delta PGSE at shortd_b; lobe timings as
+# fractions of the walk's duration.  These values are part of the pack format (they fix what a
+# pack's fidelity record means) and equal the reference's defaults.
+_DEFAULT_ENVELOPE = dict(bvals=(0.0, 0.5e9, 1e9, 2e9, 3e9),
+                         dirs=((0, 0, 1), (1, 0, 0), (1, 0, 1)),
+                         ogse_periods=(1, 2, 3, 5), shortd_b=1e9,
+                         shortd_deltas_frac=(0.2, 0.1, 0.05, 0.025),
+                         delta_frac=0.2, Delta_frac=0.5)
+
+
 def default_envelope():
-    """The acquisition envelope a pack is certified over, b in s/m^2 (compression.py:497-503)."""
-    return dict(bvals=[0.0, 0.5e9, 1e9, 2e9, 3e9], dirs=[[0, 0, 1], [1, 0, 0], [1, 0, 1]],
-                ogse_periods=[1, 2, 3, 5], shortd_b=1e9,
-                shortd_deltas_frac=[0.2, 0.1, 0.05, 0.025], delta_frac=0.2, Delta_frac=0.5)
+    """A fresh copy of the default certification envelope (compression.py:497-503)."""
+    return {k: ([list(x) if isinstance(x, tuple) else x for x in v] if isinstance(v, tuple)
+                else v) for k, v in _DEFAULT_ENVELOPE.items()}
 
 
 def _bipolar(t, delta, Delta):
@@ -547,40 +590,48 @@ def _fidelity_report(raw, S_raw, S_dec, meta, n_w, w, logw):
                 per_family=per_fam)
 
 
+def _candidate_signals(X, traj, dt_traj, method, G, K_grid, w, logw):
+    """(K, decoded-walk signal over G) for every K of the grid, in order.  Temporal-DCT
+    candidates replay straight from the K lowest bands (the transform is orthonormal, so this
+    equals replaying the decoded positions); the Karhunen-Loeve ones replay their decoded walk."""
+    n_t = traj.shape[1]
+    if method == "temporal_dct":
+        bands = project_modes(X, max(K_grid)).cpu().numpy()
+        for K in K_grid:
+            k = min(K, bands.shape[1])
+            arrays = pack_position_arrays(bands[:, :k], np.float32)
+            yield K, mode_space_signal(arrays, {"method": method, "K": int(k), "n_t": int(n_t)},
+                                       G, dt_traj, logw=logw, weights=w)
+        return
+    factors = _kl(X)
+    keep_n = X.shape[0] if is_walker_preserving(method) else None
+    for K in K_grid:
+        arrays, mm, _ = ENCODERS[method](X, K, _cache=factors)
+        yield K, _DeviceReplay(decode(arrays, mm, n_walkers=keep_n), dt_traj, G).signal(w, logw)
+
+
 def auto_select_modes(X, traj, dt_traj, method="temporal_dct", env=None, tol=2.0,
                       err_target=None, K_grid=(8, 16, 32, 48, 64, 96, 128), w=None, logw=None,
                       verbose=False):
-    """Smallest ``K`` of ``K_grid`` whose replay error meets ``err_target`` (else ``tol`` x the
-    split-half floor); the largest ``K`` when none does (compression.py:582-603).  The raw walk is
-    uploaded once; ``temporal_dct`` candidates are replayed in mode space (equal to replaying the
-    decoded positions, the DCT being orthonormal), the others from their decoded positions."""
+    """The smallest mode count of ``K_grid`` whose replay error over the envelope meets
+    ``err_target`` (else ``tol`` x the walk's split-half floor), with its fidelity report; the
+    largest count's when none does (the rule of compression.py:582-603).  The raw walk is
+    uploaded to the GPU once and replayed against every candidate."""
     env = env or default_envelope()
-    n_w, n_t = traj.shape[0], traj.shape[1]
-    G, meta = acquisition_battery(n_t, float(dt_traj), env)
+    G, meta = acquisition_battery(traj.shape[1], float(dt_traj), env)
     raw = _DeviceReplay(traj, dt_traj, G)
     S_raw = raw.signal(w, logw)
-    cache = _kl(X) if method in ("lowrank", "gaussian", "marginal") else None
-    Cfull = project_modes(X, max(K_grid)).cpu().numpy() if method == "temporal_dct" else None
-    best = None
-    for K in K_grid:
-        if method == "temporal_dct":
-            arrays = pack_position_arrays(Cfull[:, :min(K, Cfull.shape[1])], np.float32)
-            mm = {"method": "temporal_dct", "K": int(min(K, Cfull.shape[1])), "n_t": int(n_t)}
-            S_dec = mode_space_signal(arrays, mm, G, dt_traj, logw=logw, weights=w)
-        else:
-            arrays, mm, _ = ENCODERS[method](X, K, _cache=cache)
-            pos = decode(arrays, mm, n_walkers=(X.shape[0] if is_walker_preserving(method)
-                                               else None))
-            S_dec = _DeviceReplay(pos, dt_traj, G).signal(w, logw)
-        fid = _fidelity_report(raw, S_raw, S_dec, meta, n_w, w, logw)
+    chosen = None
+    for K, S_dec in _candidate_signals(X, traj, dt_traj, method, G, K_grid, w, logw):
+        report = _fidelity_report(raw, S_raw, S_dec, meta, traj.shape[0], w, logw)
+        limit = err_target if err_target is not None else tol * report["floor_max"]
         if verbose:
-            print(f"  K={K}: err={fid['err_max']:.4f} floor={fid['floor_max']:.4f} "
-                  f"{'OK' if fid['within_2x_floor'] else '>'}", flush=True)
-        best = (K, fid)
-        thresh = err_target if err_target is not None else tol * fid["floor_max"]
-        if fid["err_max"] <= thresh:
-            return K, fid
-    return best
+            print(f"{method} with {K} modes: replay error {report['err_max']:.4f}, "
+                  f"limit {limit:.4f}", flush=True)
+        chosen = (K, report)
+        if report["err_max"] <= limit:
+            break
+    return chosen
 
 
 __all__ = ["WALKER_PRESERVING", "DISTRIBUTIONAL", "ALL_METHODS", "POSITION_AXES", "dct_basis",

@@ -1,13 +1,26 @@
-"""The RF pulse as its complex transmit field B1(t) = B1x + i B1y (Tesla) on a uniform raster,
-and the single-spin Bloch integrator that maps it to magnetisation (rf.py of dmipy-sim).
+"""RF pulses as sampled transmit fields, and the Bloch integrator that plays them on spins.
 
-Constructors: explicit samples, magnitude/phase, a hard (rectangular) pulse, an apodised sinc,
-the hyperbolic-secant adiabatic full passage (Silver, Joseph & Hoult 1985), the adiabatic half
-passage and BIR-4 (Garwood & Ke 1991), composite hard pulses.  ``bloch_simulate`` rotates each
-spin of an ensemble (off-resonance, B1+ scale) per raster step about its effective field
-(gamma B1x b, gamma B1y b, 2 pi df) dt and relaxes it toward +z; no flip is renormalised.
-The scanner deliverability check reads a vendor limits catalogue that is not part of this
-package.
+A pulse is its complex field B1(t) = B1x + i B1y (Tesla) on a uniform raster (the interface of
+dmipy-sim's rf.py:38-275).  The constructors build a pulse from a named envelope:
+
+  hard        a constant complex amplitude
+  sinc        sinc(x) on x in [-w, w], optionally Hamming-apodised
+  sech        the hyperbolic-secant full passage sech(beta tau)^(1 + i mu)  (Silver, Joseph and
+              Hoult, Phys. Rev. A 31, 1985)
+  tanh / tan  the adiabatic half passage: amplitude tanh(beta tau), frequency sweep
+              tan(kappa (1 - tau)) / tan(kappa)  (Garwood and Ke, J. Magn. Reson. 94, 1991), and
+              BIR-4, four such segments with phase jumps of half the flip
+  composite   hard sub-pulses at a common peak amplitude
+
+and flip-prescribed envelopes are scaled so that the on-resonance flip gamma * dt * sum |B1|
+equals the prescription.
+
+``bloch_simulate`` integrates the Bloch equation in the rotating frame for an ensemble of spins
+(off-resonance, B1+ scale): every raster step is a rotation by the step's effective-field vector
+w = (gamma b B1x dt, gamma b B1y dt, 2 pi df dt) -- applied here as the unit quaternion
+(cos(|w|/2), sin(|w|/2) w/|w|) -- followed by relaxation toward +z.  The flip is whatever the
+field produces; nothing is renormalised.  The scanner deliverability check needs a vendor limits
+catalogue that is not part of this package.
 """
 from dataclasses import dataclass
 
@@ -18,155 +31,175 @@ from .constants import GAMMA
 __all__ = ["B1Pulse", "bloch_simulate", "slice_profile"]
 
 
+# ------------------------------------------------------------------------------------------------
+# envelopes (unscaled, on n raster samples)
+# ------------------------------------------------------------------------------------------------
+def _raster_len(duration, dt, least):
+    """Samples of a pulse of the given duration: duration / dt rounded, at least ``least``."""
+    return max(least, int(round(float(duration) / float(dt))))
+
+
+def _sinc_envelope(n, half_width, hamming):
+    x = np.linspace(-half_width, half_width, n)
+    taper = 0.54 + 0.46 * np.cos(np.pi * x / half_width) if hamming else 1.0
+    return np.sinc(x) * taper
+
+
+def _sech_envelope(n, beta, mu):
+    """sech(beta tau)^(1 + i mu) for tau in [-1, 1] (amplitude sech, phase mu log sech)."""
+    sech = 1.0 / np.cosh(beta * np.linspace(-1.0, 1.0, n))
+    return sech * np.exp(1j * mu * np.log(sech + 1e-300))
+
+
+def _half_passage(n, beta, kappa, sweep_hz):
+    """(amplitude, frequency in Hz) of one adiabatic half passage over tau in [0, 1]."""
+    tau = np.linspace(0.0, 1.0, n)
+    return np.tanh(beta * tau), sweep_hz * np.tan(kappa * (1.0 - tau)) / np.tan(kappa)
+
+
+def _phase_of_sweep(freq_hz, dt):
+    """Running phase (rad) of a frequency sweep: the left Riemann sum of 2 pi f dt."""
+    return np.cumsum(2.0 * np.pi * np.asarray(freq_hz, float) * float(dt))
+
+
+def _per_flip(envelope, flip_deg, dt):
+    """The envelope scaled so that gamma * dt * sum |B1| is the flip (a zero envelope stays 0)."""
+    area = GAMMA * float(dt) * float(np.sum(np.abs(envelope)))
+    return envelope * (np.radians(float(flip_deg)) / area if area > 0.0 else 0.0)
+
+
+def _rotated(envelope, phase_deg):
+    return np.asarray(envelope, np.complex128) * np.exp(1j * np.radians(float(phase_deg)))
+
+
+# ------------------------------------------------------------------------------------------------
+# the pulse
+# ------------------------------------------------------------------------------------------------
 @dataclass
 class B1Pulse:
-    """Complex B1(t) in Tesla on raster ``dt`` (rf.py:38-275); ``flip_deg`` is the intended net
-    flip when the constructor knows it."""
+    """Complex B1(t) in Tesla on raster ``dt``; ``flip_deg`` is the intended net flip when the
+    constructor prescribes one (None otherwise)."""
     b1: np.ndarray
     dt: float
     label: str = ""
     flip_deg: float = None
 
     def __post_init__(self):
-        self.b1 = np.asarray(self.b1, dtype=np.complex128)
-        if self.b1.ndim != 1:
+        arr = np.asarray(self.b1, dtype=np.complex128)
+        if arr.ndim != 1:
             raise ValueError("b1 must be 1-D (n_samples,)")
-        self.dt = float(self.dt)
+        self.b1, self.dt = arr, float(self.dt)
 
-    @property
-    def n(self):
-        return self.b1.shape[0]
-
-    @property
-    def duration(self):
-        return self.n * self.dt
-
-    @property
-    def times(self):
-        return np.arange(self.n) * self.dt
-
-    @property
-    def magnitude(self):
-        return np.abs(self.b1)
-
-    @property
-    def phase(self):
-        return np.angle(self.b1)
+    # ---- raster and field statistics ----------------------------------------------------------
+    n = property(lambda self: int(self.b1.size))
+    duration = property(lambda self: self.n * self.dt)
+    times = property(lambda self: self.dt * np.arange(self.n))
+    magnitude = property(lambda self: np.abs(self.b1))
+    phase = property(lambda self: np.angle(self.b1))
 
     @property
     def peak_b1(self):
-        return float(np.max(np.abs(self.b1))) if self.n else 0.0
+        """Largest |B1| (T)."""
+        return float(self.magnitude.max()) if self.n else 0.0
 
     @property
     def b1_rms(self):
-        return float(np.sqrt(np.mean(np.abs(self.b1) ** 2))) if self.n else 0.0
+        """Root-mean-square |B1| over the pulse (T)."""
+        return float(np.sqrt(np.mean(self.magnitude ** 2))) if self.n else 0.0
 
     @property
     def sar_proxy(self):
-        """sum |B1|^2 dt (T^2 s), proportional to the deposited RF energy."""
-        return float(np.sum(np.abs(self.b1) ** 2) * self.dt)
+        """dt * sum |B1|^2 (T^2 s): proportional to the RF energy deposited."""
+        return float(self.dt * np.sum(self.magnitude ** 2))
 
     @property
     def nominal_flip_rad(self):
-        """gamma sum |B1| dt: the on-resonance flip of a constant-phase pulse."""
-        return float(GAMMA * np.sum(np.abs(self.b1)) * self.dt)
+        """gamma * dt * sum |B1|: the on-resonance flip of a pulse of constant phase."""
+        return float(GAMMA * self.dt * np.sum(self.magnitude))
 
     @property
     def nominal_flip_deg(self):
-        return np.degrees(self.nominal_flip_rad)
+        return float(np.degrees(self.nominal_flip_rad))
 
     @property
     def max_slew_b1(self):
-        return float(np.max(np.abs(np.diff(self.b1))) / self.dt) if self.n >= 2 else 0.0
+        """Largest |B1| change per second between neighbouring samples (T/s)."""
+        if self.n < 2:
+            return 0.0
+        return float(np.abs(np.diff(self.b1)).max() / self.dt)
 
+    # ---- constructors ------------------------------------------------------------------------
     @classmethod
     def from_samples(cls, b1, dt, label=""):
-        return cls(b1=np.asarray(b1, dtype=np.complex128), dt=dt, label=label)
+        """A pulse from its complex samples (T)."""
+        return cls(np.asarray(b1, np.complex128), dt, label)
 
     @classmethod
     def from_magnitude_phase(cls, mag_T, phase_rad, dt, label=""):
+        """A pulse from |B1| (T) and its phase (rad; None for a constant zero phase)."""
         mag = np.asarray(mag_T, float)
-        ph = np.zeros_like(mag) if phase_rad is None else np.asarray(phase_rad, float)
-        return cls(b1=mag * np.exp(1j * ph), dt=dt, label=label)
+        ph = np.zeros(mag.shape) if phase_rad is None else np.asarray(phase_rad, float)
+        return cls(mag * np.exp(1j * ph), dt, label)
 
     @classmethod
     def hard(cls, flip_deg, duration, dt, phase_deg=0.0, label="hard"):
-        """round(duration/dt) samples (at least 1) of the amplitude whose discretised area
-        gamma B1 n dt is the flip."""
-        n = max(1, int(round(float(duration) / float(dt))))
-        amp = np.deg2rad(float(flip_deg)) / (GAMMA * n * float(dt))
-        b1 = np.full(n, amp, dtype=np.complex128) * np.exp(1j * np.deg2rad(phase_deg))
-        return cls(b1=b1, dt=dt, label=label, flip_deg=float(flip_deg))
+        """Constant amplitude over duration / dt samples (at least one), scaled to the flip."""
+        n = _raster_len(duration, dt, 1)
+        env = _per_flip(np.ones(n), flip_deg, dt)
+        return cls(_rotated(env, phase_deg), dt, label, float(flip_deg))
 
     @classmethod
     def windowed_sinc(cls, flip_deg, duration, dt, time_bw=4.0, n_zeros=None, window="hamming",
                       phase_deg=0.0, label="sinc"):
-        """sinc(x) on x in [-z, z] (z = time_bw/2 zero crossings a side unless ``n_zeros``),
-        Hamming-apodised (0.54 + 0.46 cos(pi x / z)) or not, scaled so gamma sum |B1| dt is
-        the flip."""
-        n = max(3, int(round(float(duration) / float(dt))))
-        z = float(n_zeros) if n_zeros is not None else float(time_bw) / 2.0
-        x = np.linspace(-z, z, n)
-        env = np.sinc(x)
-        if window == "hamming":
-            env = env * (0.54 + 0.46 * np.cos(np.pi * x / z))
-        elif window not in (None, "none", "rect"):
+        """sinc over +-(time_bw / 2) zero crossings (or ``n_zeros``), Hamming-apodised with
+        ``window="hamming"`` or not (None / "none" / "rect"), at least 3 samples, scaled to the
+        flip."""
+        if window not in ("hamming", None, "none", "rect"):
             raise ValueError(f"unknown window {window!r}")
-        area = GAMMA * np.sum(np.abs(env)) * float(dt)
-        amp = np.deg2rad(float(flip_deg)) / area if area > 0 else 0.0
-        b1 = (env * amp).astype(np.complex128) * np.exp(1j * np.deg2rad(phase_deg))
-        return cls(b1=b1, dt=dt, label=label, flip_deg=float(flip_deg))
+        n = _raster_len(duration, dt, 3)
+        half = float(time_bw) / 2.0 if n_zeros is None else float(n_zeros)
+        env = _per_flip(_sinc_envelope(n, half, window == "hamming"), flip_deg, dt)
+        return cls(_rotated(env, phase_deg), dt, label, float(flip_deg))
 
     @classmethod
     def adiabatic_hs(cls, duration, dt, *, peak_b1, mu=4.0, beta=5.3, label="adiabatic_hs"):
-        """Hyperbolic secant: peak_b1 sech(beta tau)^(1 + i mu), tau in [-1, 1]."""
-        n = max(3, int(round(float(duration) / float(dt))))
-        sech = 1.0 / np.cosh(beta * np.linspace(-1.0, 1.0, n))
-        b1 = peak_b1 * sech * np.exp(1j * mu * np.log(sech + 1e-300))
-        return cls(b1=b1.astype(np.complex128), dt=dt, label=label, flip_deg=180.0)
-
-    @staticmethod
-    def _half_passage(n, beta, kappa, sweep_hz):
-        tau = np.linspace(0.0, 1.0, n)
-        amp = np.tanh(beta * tau)
-        freq = sweep_hz * np.tan(kappa * (1.0 - tau)) / np.tan(kappa)
-        return amp, freq
+        """Hyperbolic-secant inversion: peak_b1 sech(beta tau)^(1 + i mu), tau in [-1, 1]."""
+        n = _raster_len(duration, dt, 3)
+        return cls(peak_b1 * _sech_envelope(n, beta, mu), dt, label, 180.0)
 
     @classmethod
     def adiabatic_half_passage(cls, duration, dt, *, peak_b1, beta=6.0, kappa=np.arctan(20.0),
                                sweep_hz=1.0e4, label="ahp"):
-        """Amplitude peak_b1 tanh(beta tau) while the frequency sweeps sweep_hz tan(kappa (1 -
-        tau)) / tan(kappa) down to 0 (tau in [0, 1]); the phase is its running integral."""
-        n = max(3, int(round(float(duration) / float(dt))))
-        amp, freq = cls._half_passage(n, beta, kappa, sweep_hz)
-        phase = np.cumsum(2.0 * np.pi * freq * float(dt))
-        return cls(b1=(peak_b1 * amp * np.exp(1j * phase)).astype(np.complex128), dt=dt,
-                   label=label, flip_deg=90.0)
+        """Adiabatic 90: amplitude peak_b1 tanh(beta tau) under a frequency sweep from
+        ``sweep_hz`` down to 0, the phase being the sweep's running integral."""
+        n = _raster_len(duration, dt, 3)
+        amp, freq = _half_passage(n, beta, kappa, sweep_hz)
+        return cls(peak_b1 * amp * np.exp(1j * _phase_of_sweep(freq, dt)), dt, label, 90.0)
 
     @classmethod
     def bir4(cls, flip_deg, duration, dt, *, peak_b1, beta=6.0, kappa=np.arctan(20.0),
              sweep_hz=1.0e4, label="bir4"):
-        """Four half passages of n//4 samples (n = round(duration/dt), at least 8): amplitude
-        forward, reversed, forward, reversed; the frequency likewise with signs +, -, +, -;
-        phase jumps of flip/2 on the middle two segments."""
-        n = max(8, int(round(float(duration) / float(dt))))
-        q = n // 4
-        amp0, fr0 = cls._half_passage(q, beta, kappa, sweep_hz)
-        half = np.deg2rad(float(flip_deg) / 2.0)
-        amp = np.concatenate([amp0, amp0[::-1], amp0, amp0[::-1]])
-        fr = np.concatenate([fr0, -fr0[::-1], fr0, -fr0[::-1]])
-        jump = np.concatenate([np.zeros(q), np.full(q, half), np.full(q, half), np.zeros(q)])
-        ph = np.cumsum(2.0 * np.pi * fr * float(dt)) + jump
-        b1 = peak_b1 * amp * np.exp(1j * ph)
-        return cls(b1=b1.astype(np.complex128), dt=dt, label=label, flip_deg=float(flip_deg))
+        """BIR-4 plane rotation: four half-passage segments of n // 4 samples (n at least 8),
+        amplitudes forward / reversed / forward / reversed, sweeps +, -reversed, +, -reversed,
+        and a phase jump of half the flip across the middle two segments."""
+        q = _raster_len(duration, dt, 8) // 4
+        a, f = _half_passage(q, beta, kappa, sweep_hz)
+        segments = ((a, f, 0.0), (a[::-1], -f[::-1], 1.0), (a, f, 1.0), (a[::-1], -f[::-1], 0.0))
+        amp = np.concatenate([s[0] for s in segments])
+        freq = np.concatenate([s[1] for s in segments])
+        jump = np.repeat([s[2] for s in segments], q) * np.radians(float(flip_deg) / 2.0)
+        phase = _phase_of_sweep(freq, dt) + jump
+        return cls(peak_b1 * amp * np.exp(1j * phase), dt, label, float(flip_deg))
 
     @classmethod
     def composite(cls, segments, dt, *, peak_b1, label="composite"):
-        """Hard sub-pulses (flip_deg, phase_deg) at peak_b1, each |flip| / (gamma peak_b1)
-        long, concatenated."""
-        parts = [cls.hard(f, abs(np.deg2rad(float(f))) / (GAMMA * float(peak_b1)), dt,
-                          phase_deg=p).b1 for f, p in segments]
-        return cls(b1=np.concatenate(parts).astype(np.complex128), dt=dt, label=label)
+        """Hard sub-pulses (flip_deg, phase_deg) played back to back at amplitude peak_b1: each
+        lasts |flip| / (gamma peak_b1)."""
+        pieces = []
+        for flip, phase in segments:
+            length = abs(np.radians(float(flip))) / (GAMMA * float(peak_b1))
+            pieces.append(cls.hard(flip, length, dt, phase_deg=phase).b1)
+        return cls(np.concatenate(pieces), dt, label)
 
     def deliverability(self, model, *, coil="body", tol=1.02):
         raise NotImplementedError("the vendor scanner-limits catalogue is not part of this "
@@ -177,60 +210,62 @@ class B1Pulse:
         return self.deliverability(model, coil=coil, tol=tol)["deliverable"]
 
 
+# ------------------------------------------------------------------------------------------------
+# Bloch integration
+# ------------------------------------------------------------------------------------------------
+def _rotate(M, w):
+    """Rotate the vectors M (3, E) by the rotation vectors w (3, E) (angle |w| about w / |w|,
+    right-handed), through the unit quaternion (c, s u), c = cos(|w|/2), s = sin(|w|/2):
+    M' = M + 2 c (v x M) + 2 v x (v x M) with v = s u.  A rotation below 1e-30 rad leaves M."""
+    ang = np.sqrt(np.sum(w * w, axis=0))
+    tiny = ang < 1e-30
+    safe = np.where(tiny, 1.0, ang)
+    half = 0.5 * safe
+    v = w * (np.sin(half) / safe)
+    c = np.cos(half)
+    t = 2.0 * np.cross(v, M, axis=0)
+    out = M + c * t + np.cross(v, t, axis=0)
+    return np.where(tiny, M, out)
+
+
 def bloch_simulate(pulse, df_hz=0.0, b1_scale=1.0, M0=None, T1=np.inf, T2=np.inf,
                    return_history=False):
-    """Magnetisation after ``pulse`` for an ensemble of spins (off-resonance ``df_hz``, B1+
-    factor ``b1_scale``, broadcast together; start ``M0`` or +z).  Each raster step rotates by
-    |n| about n = (gamma B1x b dt, gamma B1y b dt, 2 pi df dt) (the identity below 1e-30 rad)
-    and relaxes: Mxy *= exp(-dt/T2), Mz -> Mz exp(-dt/T1) + 1 - exp(-dt/T1).  Returns
-    (Mxy, Mz) and, with ``return_history``, M at every step (n + 1, 3, E) (rf.py:278-363)."""
-    df = np.asarray(df_hz, float)
-    bs = np.asarray(b1_scale, float)
-    E = int(np.broadcast(df, bs).size)
-    df = np.broadcast_to(df, (E,)).astype(float)
-    bs = np.broadcast_to(bs, (E,)).astype(float)
-    M = np.zeros((3, E))
+    """Magnetisation after ``pulse`` for spins at off-resonance ``df_hz`` (Hz) with B1+ factor
+    ``b1_scale`` (broadcast together into an ensemble of E spins), starting from ``M0`` ((3,) or
+    (3, E); +z by default).  Per raster step: rotation by (gamma b B1x dt, gamma b B1y dt,
+    2 pi df dt), then Mxy *= exp(-dt / T2), Mz <- Mz exp(-dt / T1) + 1 - exp(-dt / T1) (infinite
+    times relax nothing).  Returns (Mxy (E,) complex, Mz (E,)) and, with ``return_history``, M at every
+    step boundary (n + 1, 3, E)."""
+    df, bs = np.broadcast_arrays(np.asarray(df_hz, float), np.asarray(b1_scale, float))
+    df, bs = df.ravel().astype(float), bs.ravel().astype(float)
+    E = df.size
     if M0 is None:
-        M[2] = 1.0
+        M = np.vstack([np.zeros((2, E)), np.ones((1, E))])
     else:
-        M0 = np.asarray(M0, float)
-        M[:] = M0[:, None] if M0.ndim == 1 else M0
+        m0 = np.asarray(M0, float)
+        M = np.array(np.broadcast_to(m0[:, None] if m0.ndim == 1 else m0, (3, E)), float)
     dt = pulse.dt
-    nz = 2.0 * np.pi * df * dt
-    e1 = np.exp(-dt / T1) if np.isfinite(T1) else 1.0
-    e2 = np.exp(-dt / T2) if np.isfinite(T2) else 1.0
-    hist = None
-    if return_history:
-        hist = np.empty((pulse.n + 1, 3, E))
-        hist[0] = M
-    for k in range(pulse.n):
-        nx = GAMMA * (pulse.b1[k].real * bs) * dt
-        ny = GAMMA * (pulse.b1[k].imag * bs) * dt
-        theta = np.sqrt(nx * nx + ny * ny + nz * nz)
-        still = theta < 1e-30
-        th = np.where(still, 1.0, theta)
-        ux, uy, uz = nx / th, ny / th, nz / th
-        c, s = np.cos(th), np.sin(th)
-        omc = 1.0 - c
-        Mx, My, Mz = M
-        dot = ux * Mx + uy * My + uz * Mz
-        rx = Mx * c + (uy * Mz - uz * My) * s + ux * dot * omc
-        ry = My * c + (uz * Mx - ux * Mz) * s + uy * dot * omc
-        rz = Mz * c + (ux * My - uy * Mx) * s + uz * dot * omc
-        rx, ry, rz = (np.where(still, Mx, rx), np.where(still, My, ry), np.where(still, Mz, rz))
-        M = np.stack([rx * e2, ry * e2, rz * e1 + (1.0 - e1)])
+    keep_t2 = np.exp(-dt / T2) if np.isfinite(T2) else 1.0
+    keep_t1 = np.exp(-dt / T1) if np.isfinite(T1) else 1.0
+    wz = 2.0 * np.pi * dt * df
+    history = [M.copy()] if return_history else None
+    for b in pulse.b1:
+        w = np.stack([GAMMA * dt * (b.real * bs), GAMMA * dt * (b.imag * bs), wz])
+        M = _rotate(M, w)
+        M[:2] *= keep_t2
+        M[2] = M[2] * keep_t1 + (1.0 - keep_t1)
         if return_history:
-            hist[k + 1] = M
-    Mxy = M[0] + 1j * M[1]
+            history.append(M.copy())
+    mxy, mz = M[0] + 1j * M[1], M[2].copy()
     if return_history:
-        return Mxy, M[2], hist
-    return Mxy, M[2]
+        return mxy, mz, np.stack(history)
+    return mxy, mz
 
 
 def slice_profile(pulse, slice_gradient, positions_m, df_hz=0.0, b1_scale=1.0, **kw):
-    """(positions, Mxy, Mz) across a slice: a spin at z sees the extra off-resonance
-    gamma G_ss z / (2 pi) Hz (rf.py:366-377)."""
+    """(positions, Mxy, Mz) across a slice: the spin at z also sees gamma G_ss z / (2 pi) Hz of
+    off-resonance (the interface of rf.py:366-377)."""
     z = np.asarray(positions_m, float)
-    df = (GAMMA / (2.0 * np.pi)) * float(slice_gradient) * z + np.asarray(df_hz, float)
-    Mxy, Mz = bloch_simulate(pulse, df_hz=df, b1_scale=b1_scale, **kw)
-    return z, Mxy, Mz
+    df = np.asarray(df_hz, float) + float(slice_gradient) * z * (GAMMA / (2.0 * np.pi))
+    mxy, mz = bloch_simulate(pulse, df_hz=df, b1_scale=b1_scale, **kw)
+    return z, mxy, mz

@@ -19,7 +19,9 @@ def z():
                                   "samples"])
 def test_pulses_and_bloch_integration_match_reference(z, name):
     p = rf_pulses(rf)[name]
-    np.testing.assert_array_equal(p.b1, z[f"{name}_b1"])
+    # the envelopes are the reference's to rounding (the amplitude scale is formed in another
+    # order, so a sample may differ in its last bit)
+    np.testing.assert_allclose(p.b1, z[f"{name}_b1"], rtol=1e-13, atol=1e-22)
     np.testing.assert_allclose([p.duration, p.peak_b1, p.b1_rms, p.sar_proxy,
                                 p.nominal_flip_deg, p.max_slew_b1], z[f"{name}_props"],
                                rtol=1e-14)
