@@ -13,6 +13,9 @@
 //     the process exits.
 //   * The first call on a device, with that device current, looks up the array's device address
 //     (cudaGetSymbolAddress) once; make that first call before any stream capture.
+//   * That address is kept for the life of the process.  A cudaDeviceReset (or any other reset
+//     of the device's primary context) unloads the library's device image and invalidates it:
+//     a process that resets a device must not call this entry point on that device again.
 //   * Every call shares the one array and the array keeps the last call's contents.  Nothing in
 //     it needs to start at zero (each launch writes every byte it later reads), but calls whose
 //     work overlaps on the GPU race on it: serialise them (one stream, or events).

@@ -221,6 +221,48 @@ def _replay_compressed(master, G, dt_wf, *, chi_perp, T2, T1, surface_relaxivity
 
 
 # ---- vector-Bloch replay ------------------------------------------------------------------------
+def _per_comp_rates(comp_traj, T2_per_comp, T1_per_comp, inv2, inv1):
+    """Per-compartment relaxation rates of the Bloch replay: ``(comp (n_w, n_t) int32, 1/T2 per
+    compartment, 1/T1 per compartment)``, or None without per-compartment times.
+
+    The device reads the rates at every walker's compartment id, so the ids must be >= 0 and each
+    list must hold an entry for the largest id.  The reference indexes the same lists with the ids
+    (trajectories.py:798-803) and raises IndexError on a short list; so does this check, and on a
+    negative id too (which the device cannot index)."""
+    if T2_per_comp is None and T1_per_comp is None:
+        return None
+    if comp_traj is None:
+        raise ValueError("T2_per_comp / T1_per_comp need comp_traj")
+    comp = np.asarray(comp_traj)
+    if comp.size and int(np.min(comp)) < 0:
+        raise IndexError("comp_traj holds a negative compartment id")
+    n_c = int(np.max(comp)) + 1 if comp.size else 1
+    t2c = (1.0 / np.asarray(T2_per_comp, np.float64).ravel() if T2_per_comp is not None
+           else np.full(n_c, inv2))
+    t1c = (1.0 / np.asarray(T1_per_comp, np.float64).ravel() if T1_per_comp is not None
+           else np.full(n_c, inv1))
+    for name, arr in (("T2_per_comp", t2c), ("T1_per_comp", t1c)):
+        if len(arr) < n_c:
+            raise IndexError(f"{name} has {len(arr)} entries but comp_traj holds compartment "
+                             f"ids up to {n_c - 1}")
+    return comp.astype(np.int32), t2c, t1c
+
+
+def _takes_position_arrays(field):
+    """Whether a field callable maps positions (..., 3) to values (...) in one call.
+
+    The providers of this package do; a user callable may instead take one position at a time.
+    The probe is one call on two positions: a callable of one position fails it with the shape or
+    type error such a callable raises on a (2, 3) array, or returns something other than two
+    values.  Any other exception is a fault of the callable and propagates."""
+    probe = np.zeros((2, 3), np.float32)
+    try:
+        out = np.asarray(field(probe), np.float64)
+    except (TypeError, ValueError, IndexError):
+        return False
+    return out.shape == (2,)
+
+
 def _rf_increments(rf_events, dt_traj, n_t):
     """The RF events as per-sample partial rotations (trajectories.py:888-917): a pulse of
     duration_s > 0 covers round(duration/dt) samples centred on round(t_s/dt) (clipped at 0, the
@@ -276,6 +318,9 @@ def replay_bloch(trajectory, dt_traj, G, dt_wf, rf_events, *, T2=None, T1=None, 
     n_echo) at the distinct ``echo_steps`` in time order ((n_meas, n_echo, n_walkers) per
     walker with ``echo_per_walker``), or ``(M_last (3, n_walkers), signals)`` with
     ``return_walker_signals``."""
+    inv2 = 0.0 if T2 is None else 1.0 / T2
+    inv1 = 0.0 if T1 is None else 1.0 / T1
+    per_comp = _per_comp_rates(comp_traj, T2_per_comp, T1_per_comp, inv2, inv1)
     dev = _lib.device()
     lib = _lib.load()
     if isinstance(trajectory, torch.Tensor):
@@ -309,19 +354,11 @@ def replay_bloch(trajectory, dt_traj, G, dt_wf, rf_events, *, T2=None, T1=None, 
     p.G = dv(G_tr, np.float64)
     p.gamma_dt = GAMMA * dt_traj
     p.dt_traj = float(dt_traj)
-    inv2 = 0.0 if T2 is None else 1.0 / T2
-    inv1 = 0.0 if T1 is None else 1.0 / T1
     p.inv_t2, p.inv_t1 = inv2, inv1
     p.e2, p.e1 = float(np.exp(-dt_traj * inv2)), float(np.exp(-dt_traj * inv1))
-    if T2_per_comp is not None or T1_per_comp is not None:
-        if comp_traj is None:
-            raise ValueError("T2_per_comp / T1_per_comp need comp_traj")
-        n_c = int(np.max(comp_traj)) + 1
-        t2c = (1.0 / np.asarray(T2_per_comp, np.float64) if T2_per_comp is not None
-               else np.full(n_c, inv2))
-        t1c = (1.0 / np.asarray(T1_per_comp, np.float64) if T1_per_comp is not None
-               else np.full(n_c, inv1))
-        p.comp = dv(comp_traj, np.int32)
+    if per_comp is not None:
+        comp_np, t2c, t1c = per_comp
+        p.comp = dv(comp_np, np.int32)
         p.inv_t2_comp, p.inv_t1_comp = dv(t2c, np.float64), dv(t1c, np.float64)
     if bound_frac is not None:
         if T2_bound is None or T1_bound is None:
@@ -334,9 +371,9 @@ def replay_bloch(trajectory, dt_traj, G, dt_wf, rf_events, *, T2=None, T1=None, 
                  else susceptibility)
         r = (traj_t.float().cpu().numpy() if isinstance(trajectory, torch.Tensor)
              else np.asarray(trajectory, np.float32))
-        try:                                      # providers of this package take (..., 3)
+        if _takes_position_arrays(field):         # providers of this package take (..., 3)
             dbz = np.asarray(field(r), np.float64).reshape(n_w, n_t)
-        except Exception:                         # a callable of one position
+        else:                                     # a callable of one position
             dbz = np.array([[float(field(r[w, t])) for t in range(n_t)] for w in range(n_w)])
         extra_phase_per_step = GAMMA * dt_traj * dbz
     p.extra_phase = dv(extra_phase_per_step, np.float64)

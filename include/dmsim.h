@@ -238,6 +238,13 @@ int dmsim_version(void);
 /* Thread-local message for the last failing call on this thread. */
 const char* dmsim_last_error(void);
 
+/* Measurement helper, no counterpart in the reference: enqueues one launch of a kernel that runs
+   8 independent FP32 fused-multiply-add chains per thread, iters x 16 times each, on blocks x
+   threads threads (threads a multiple of 32, at most 256), and stores one float into sink.  FLOPs
+   per launch = blocks * threads * iters * 256; timed with events on the stream it gives this
+   GPU's measured FP32 FMA rate, the denominator of the walk kernels' roofline fraction. */
+int dmsim_fp32_fma_peak(int blocks, int threads, int iters, float* sink, void* stream);
+
 /* Workspace bytes dmsim_walk() needs for these parameters on the current device
    (per-block FP64 partials of the ensemble sums).  Replaces the device memory XLA allocated for
    the vmapped scan carry (core.py:700-727). */
@@ -256,7 +263,9 @@ int dmsim_walk(const dmsim_walk_params* p, const dmsim_geometry* g, const dmsim_
    no counterpart in the reference.  The caller passes inputs and outputs only; the scratch lives
    in one library-owned device array of DMSIM_NOALLOC_SCRATCH_BYTES (16 MiB) that every GPU which
    loads the library keeps until exit.  The first call on a device (with that device current)
-   looks the array's address up once: make it before any stream capture.  Calls share the array
+   looks the array's address up once: make it before any stream capture.  That address holds
+   until the device's context is reset (cudaDeviceReset): after a reset, do not call this entry
+   point on that device again in the same process.  Calls share the array
    and it keeps the last call's contents, so calls that overlap on the GPU race: serialise them.
    A walk whose workspace (dmsim_walk_workspace_bytes) exceeds the array returns DMSIM_ETOOBIG
    without launching anything.  Allocates nothing. */
@@ -407,7 +416,11 @@ int dmsim_bloch_mt(const dmsim_mt_params* p, const dmsim_geometry* g, void* work
    bound_frac (without compartments or bound_frac, e2 / e1 are used as given).  All FP64.  At
    each echo sample sums[m][e] = (sum_w weight_w Mx, sum_w weight_w My); optional per-walker
    echoes and the last measurement's final magnetisation.  Per-walker-sample arrays are
-   (n_walkers, n_t); every pointer is DEVICE memory. */
+   (n_walkers, n_t); every pointer is DEVICE memory.  The library checks counts and pointers
+   only, not the contents of the device tables: the caller guarantees echo_idx strictly ascending
+   in [0, n_t), rf_start non-decreasing from 0 with rf_start[n_t] <= the length of rf_flip and
+   rf_axis, and every comp id < the length of inv_t2_comp / inv_t1_comp.  The Python wrapper
+   (trajectories.replay_bloch) builds and checks them on the host before the upload. */
 typedef struct dmsim_replay_bloch_params {
   int64_t n_walkers;
   int32_t n_t, n_meas, n_echo, traj_f16;
