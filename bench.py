@@ -11,15 +11,24 @@ One step = one complete walk of that workload (all walkers, all samples, all sub
 reduction).  Metric: walker-steps/s, a walker-step being one walker advanced one physics sub-step
 with every measurement's phase updated.
 
-The same JSON line carries the metric's second half (rank 0, N = 1):
+The roofline fraction is quoted against the FP32 FMA rate measured in the same process
+(``dmsim_fp32_fma_peak``: FMA chains on every SM, CUDA-event timed).
+
+The same JSON line carries, at N = 1:
+  "legs"       every other configuration of the metric at its own size, inputs resident:
+               free diffusion + PGSE (50,000 walkers), a cylinder with surface relaxivity and a
+               permeable sphere (30 directions, 100,000 walkers), the lattice with permeable
+               walls (kappa = 2e-5 m/s, 460 sub-steps per sample), the lattice as a 16-echo CPMG
+               train (5 ms spacing) and the headline walk in the direct phase form (every
+               measurement's phase accumulated separately); each with walker-steps/s, its
+               roofline fraction and the oracle's CPU rate on a bounded sample;
   "batched"    signals/s of the batched walk on the 256-instance study (packed cylinders, packed
                spheres and a periodic mesh of 200 ellipsoid cells with ~500k triangles; radius,
                volume fraction, permeability, relaxivity, D, n_t and free waveforms of 8-96
                measurements drawn from seed 0), one graph-captured launch with every instance at
-               --batched-walkers walkers (default 2,000), and the signals/s at <= 0.005 error:
-               20,000 walkers per instance bound every signal's standard error by 0.005, and a
-               walk's cost is linear in its walkers, so that figure is the measured rate x
-               (batched-walkers / 20,000) unless --batched-walkers is 20,000 itself;
+               --batched-walkers walkers (default 20,000, which bounds every signal's standard
+               error by 0.005: the variance of w cos(phi) is at most 0.5), measured, with and
+               without the host set-up;
   "surrogate"  signals/s of the trained MLP surrogate on 1,000,000 queries in one batch, its
                absolute error against the walk on held-out substrates, and its speed-up over
                the batched walk's signals/s.
@@ -145,6 +154,164 @@ def cpu_baseline(geom, wf, S, threads, budget_s=15.0):
     return steps / el, f"{n2} walkers x {wf.G.shape[1]} samples x {S} sub-steps in {el:.1f} s"
 
 
+def fp32_peak_tflops(dev):
+    """The measured FP32 FMA rate of this GPU (TFLOP/s): the library's FMA-chain kernel on 8
+    blocks per SM x 256 threads, best of 5 launches timed with CUDA events."""
+    import torch
+    from dmipy_sim_gb300 import _lib
+    lib = _lib.load()
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, threads, iters = 8 * n_sm, 256, 4096
+    sink = torch.zeros(1, dtype=torch.float32, device=dev)
+    best = None
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.check(lib.dmsim_fp32_fma_peak(blocks, threads, iters, _lib.ptr(sink),
+                                           _lib.stream_handle()), "dmsim_fp32_fma_peak")
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    flops = float(blocks) * threads * iters * 16 * 8 * 2
+    return flops / (best * 1e-3) / 1e12
+
+
+def _pgse30():
+    rng = np.random.default_rng(0)
+    bv = rng.normal(size=(30, 3))
+    return bv / np.linalg.norm(bv, axis=1, keepdims=True)
+
+
+def leg_workloads():
+    """The configurations of the metric besides the headline, as simulate() / simulate_cpmg()
+    would walk them: name -> (geometry, waveform, api, walkers, T2, engine, timed steps)."""
+    import warnings
+    import dmipy_sim_gb300 as d
+    radii, centers, L = d.lattice_cylinders(16, 0.6, 2e-6, 0.5e-6, seed=0)
+    _, wf64 = build_workload()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        c1 = d.set_b(d.pgse(0.01, 0.04, 0.05, [[1, 0, 0]] * 3, 300), [0.0, 1e9, 2e9])
+        c2 = d.set_b(d.pgse(0.01, 0.04, 0.05, _pgse30(), 300), 1e9)
+        cp = d.cpmg(16, 5e-3, 0.02, [[1, 0, 0], [0, 1, 0], [0, 0, 1], [0.6, 0.8, 0]],
+                    n_t_per_echo=100)
+    return {
+        "c1_free_pgse": (d.FreeDiffusion(), c1, "simulate", 50_000, None, "auto", 20),
+        "c2_cylinder_rho1e-6": (d.Cylinder(5e-6, (0, 0, 1), surface_relaxivity_t2=1e-6), c2,
+                                "simulate", 100_000, None, "auto", 20),
+        "c2_sphere_kappa1e-5": (d.Sphere(5e-6, permeability=1e-5), c2, "simulate", 100_000, None,
+                                "auto", 5),
+        "c3_lattice_kappa2e-5": (d.PackedCylinders(radii, centers, L, permeability=2e-5), wf64,
+                                 "simulate", N_WALKERS, None, "auto", 1),
+        "c3_lattice_cpmg16": (d.PackedCylinders(radii, centers, L), cp, "cpmg", N_WALKERS, 0.08,
+                              "auto", 5),
+        "c3_lattice_direct_form": (d.PackedCylinders(radii, centers, L), wf64, "simulate",
+                                   N_WALKERS, None, "direct", 2),
+    }
+
+
+def _leg_plan(geom, wf, api, engine):
+    """(G, chi, sub_steps, phase_per_substep, echo_idx) as simulate() / simulate_cpmg() pick
+    them."""
+    from dmipy_sim_gb300 import core
+    G, chi = core._waveform_arrays(wf, geom)
+    if api == "cpmg":
+        return G, chi, core.fused_sub_steps(geom, D, wf.dt), True, \
+            np.unique(np.asarray(wf.echo_indices, int))
+    gap = core._replay_gap(geom, return_positions=False, return_compartments=False,
+                           return_walker_signals=False, diffusivity=D)
+    rep = gap is None and core._replay_auto_allowed(geom)
+    S = core.replay_sub_steps(geom, D, wf.dt) if rep else core.fused_sub_steps(geom, D, wf.dt)
+    return G, chi, S, not rep, None
+
+
+def _leg_flops(geom, n_meas, S, fused):
+    """Algorithmic FP32 FLOPs per walker-step: direction 20, the geometry's wall test (free 0,
+    cylinder 18, sphere 20, packed cylinders 22 per object within reach x 4), +10 with surface
+    relaxivity or permeability, the phase 6 M per waveform sample (G is constant over a sample's
+    sub-steps, so sum_s g.r_s = g.sum_s r_s) spread over its S sub-steps, +3 for the position sum
+    of the fused engine."""
+    kind = type(geom).__name__
+    f_geom = {"FreeDiffusion": 0.0, "Cylinder": 18.0, "Sphere": 20.0,
+              "PackedCylinders": 88.0, "PackedSpheres": 176.0}.get(kind, 0.0)
+    if getattr(geom, "surface_relaxivity_t2", None) or getattr(geom, "permeability", None):
+        f_geom += 10.0
+    return 20.0 + f_geom + 6.0 * n_meas / S + (3.0 if fused else 0.0)
+
+
+def _leg_cpu(geom, G, wf, S, fused, chi, T2, echo, threads, budget_s=4.0):
+    """The oracle (CPU restatement, every host thread) on a bounded walker sample of a leg."""
+    from oracle import oracle as O
+    og = O.geom_from(geom)
+    rho = getattr(geom, "surface_relaxivity_t2", None)
+    kappa = getattr(geom, "permeability", None)
+    wall = O.PERMEATE if kappa is not None else (O.RELAX if rho is not None else O.REFLECT)
+    kw = dict(G=G, dt=wf.dt, sub_steps=S, phase_per_substep=fused, wall=wall, chi=chi, T2=T2,
+              rho_over_D=0.0 if rho is None else rho / D,
+              kappa_over_D=0.0 if kappa is None else kappa / D, D=D, echo_idx=echo,
+              n_threads=threads)
+    n = max(threads, 16)
+    O.walk(og, n_walkers=threads, seed=0, **kw)          # loads the oracle library
+    t0 = time.perf_counter()
+    O.walk(og, n_walkers=n, seed=1, **kw)
+    dt1 = time.perf_counter() - t0
+    n2 = int(max(threads, min(200_000, n * budget_s / max(dt1, 1e-3))))
+    t0 = time.perf_counter()
+    O.walk(og, n_walkers=n2, seed=2, **kw)
+    el = time.perf_counter() - t0
+    steps = float(n2) * G.shape[1] * S
+    return {"value": steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n2} walkers x {G.shape[1]} samples x {S} sub-steps in {el:.1f} s"}
+
+
+def legs_measure(dev, peak_tflops, cpu=True):
+    """walker-steps/s of every other configuration of the metric at its own size, inputs
+    resident, timed with CUDA events (a 512 MB L2 flush between launches), with its roofline
+    fraction against the measured FP32 rate and the oracle's CPU rate beside it."""
+    import torch
+    from dmipy_sim_gb300 import core
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    out = {}
+    for name, (geom, wf, api, n, T2, engine, steps) in leg_workloads().items():
+        G, chi, S, fused, echo = _leg_plan(geom, wf, api, engine)
+        walk = core.PreparedWalk(geom, n_walkers=n, diffusivity=D, G=G, dt=wf.dt, sub_steps=S,
+                                 phase_per_substep=fused, seed=77, chi=chi, T2=T2,
+                                 echo_idx=echo, use_basis=engine != "direct")
+        walk.launch()
+        torch.cuda.synchronize(dev)
+        ms = []
+        for k in range(steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            walk.launch()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        res = walk.result()
+        sec = float(np.mean(ms)) * 1e-3
+        ws = float(n) * G.shape[1] * S
+        F = _leg_flops(geom, G.shape[0], S, fused)
+        ach = ws * F / sec / 1e12
+        leg = {"walker_steps_per_s": ws / sec, "ms_per_walk": sec * 1e3, "walkers": n,
+               "n_t": int(G.shape[1]), "n_meas": int(G.shape[0]), "sub_steps": int(S),
+               "engine": ("fused" if fused else "replay semantics") +
+                         (", direct phase form" if engine == "direct" else ""),
+               "roofline": {"bound": "fp32", "achieved": ach, "peak": peak_tflops,
+                            "unit": "TFLOP/s", "frac": ach / peak_tflops,
+                            "flops_per_walker_step": F},
+               "gpu_launches_per_walk": walk.launches_per_call, "timed_walks": steps,
+               "signal_first": float(res.signal.ravel()[0]), "status": res.status}
+        if cpu:
+            leg["cpu_baseline"] = _leg_cpu(geom, G, wf, S, fused, chi, T2, echo,
+                                           os.cpu_count() or 1)
+        out[name] = leg
+        del walk
+    del flush
+    return out
+
+
 N_SE_005 = 20_000   # walkers with sqrt(max var / N) <= 0.005 (var of w cos(phi) is at most 0.5)
 SURROGATE = ROOT / "dmipy_sim_gb300" / "data" / "surrogate_packed_cylinders.npz"
 SURROGATE_REPORT = ROOT / "dmipy_sim_gb300" / "data" / "surrogate_packed_cylinders.json"
@@ -182,6 +349,7 @@ def batched_measure(dev, walkers=2000):
     kinds = {k: sum(1 for p in params if p["kind"] == k) for k in ("PackedCylinders",
                                                                    "PackedSpheres", "Mesh")}
     out = {"signals_per_s": n_sig / sec, "signals": n_sig, "seconds": sec,
+           "signals_per_s_incl_host_setup": n_sig / (sec + host_s),
            "walker_steps_per_s": b.walker_steps() / sec, "instances": len(full),
            "walkers_per_instance": int(walkers), "max_stderr": max_se,
            "signals_per_s_at_0.005_err": n_sig / sec * (int(walkers) / N_SE_005),
@@ -438,7 +606,8 @@ def gpu_arm(a):
     per_launch_s = kernel_s / a.steps
     achieved = walker_steps * F / per_launch_s / 1e12
     sm_max = clocks.get("sm_max_mhz") or 2070.0
-    peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12          # FP32 FMA pipes at the max SM clock
+    nominal = 152 * 128 * 2 * sm_max * 1e6 / 1e12       # FP32 FMA pipes at the max SM clock
+    peak = fp32_peak_tflops(dev)                         # measured: FMA-chain kernel, this GPU
     traffic = None
     tpath = ROOT / "profiles" / "walk_packed_cylinders_traffic.txt"
     if tpath.exists():
@@ -458,9 +627,10 @@ def gpu_arm(a):
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "flops_per_walker_step": F,
-                     "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the "
-                                    "sampled max SM clock; MEASURED_PEAKS.json has no FP32 "
-                                    "figure"},
+                     "peak_source": "measured: FP32 FMA-chain kernel (dmsim_fp32_fma_peak) "
+                                    "timed with CUDA events in this process (MEASURED_PEAKS.json "
+                                    "has no FP32 figure)",
+                     "nominal_peak": nominal},
         "e2e": {"value": walker_steps * world / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": int(wf.G.nbytes + 4 * wf.G.shape[1]),
                 "d2h_bytes_per_step": int(8 * 3 * m + 4 * 8)},
@@ -473,6 +643,8 @@ def gpu_arm(a):
         v, sample = cpu_baseline(geom, wf, S, os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": sample}
+    if world == 1 and not a.no_legs:
+        out["legs"] = legs_measure(dev, peak, cpu=not a.no_cpu_baseline)
     if world == 1 and not a.no_batched:
         try:
             out["batched"], _ = batched_measure(dev, a.batched_walkers)
@@ -533,10 +705,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="skip the other configurations (free, cylinder, sphere, permeable "
+                         "lattice, CPMG, direct phase form)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-walk and surrogate measurements")
-    ap.add_argument("--batched-walkers", type=int, default=2000,
-                    help="walkers per instance of the batched study (20000: <= 0.005 error)")
+    ap.add_argument("--batched-walkers", type=int, default=N_SE_005,
+                    help="walkers per instance of the batched study (the default 20000 bounds "
+                         "every signal's standard error by 0.005)")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per GPU (smaller only for profiling captures)")
     ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched", "bloch", "mt", "rbloch"],

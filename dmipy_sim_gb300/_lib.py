@@ -32,7 +32,8 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
             "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes",
             "dmsim_bloch_workspace_bytes", "dmsim_bloch", "dmsim_bloch_mt_workspace_bytes",
-            "dmsim_bloch_mt", "dmsim_replay_bloch_workspace_bytes", "dmsim_replay_bloch")
+            "dmsim_bloch_mt", "dmsim_replay_bloch_workspace_bytes", "dmsim_replay_bloch",
+            "dmsim_fp32_fma_peak")
 
 EPI_STORE_F32, EPI_BIAS_GELU, EPI_GELU_BWD = range(3)
 
@@ -182,6 +183,8 @@ def load():
     lib.dmsim_replay_bloch.restype = C.c_int
     lib.dmsim_replay_bloch.argtypes = [C.POINTER(ReplayBlochParams), C.c_void_p, C.c_size_t,
                                        C.c_void_p]
+    lib.dmsim_fp32_fma_peak.restype = C.c_int
+    lib.dmsim_fp32_fma_peak.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     lib.dmsim_walk_noalloc.restype = C.c_int
     lib.dmsim_walk_noalloc.argtypes = [C.POINTER(WalkParams), C.POINTER(Geometry),
                                        C.POINTER(WalkOutputs), C.c_void_p]

@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .core import (PreparedWalk, WalkResult, _replay_auto_allowed, _replay_gap,
+from .core import (PreparedWalk, WalkResult, _replay_auto_allowed, _replay_gap, _to_frame,
                    _waveform_arrays, fused_sub_steps, replay_sub_steps)
 
 
@@ -26,7 +26,8 @@ from .core import (PreparedWalk, WalkResult, _replay_auto_allowed, _replay_gap,
 class Instance:
     """One simulate() call of a batch.  ``want_positions`` / ``want_walker_signals`` keep the
     walk-frame final positions / per-walker (log_w, phi) in :meth:`PreparedBatch.results`;
-    ``sub_steps`` overrides the engine's sub-step rule."""
+    ``sub_steps`` overrides the engine's sub-step rule; ``r0`` (n_walkers, 3), lab frame, gives
+    the start positions (simulate()'s ``r0``) instead of the geometry's seeding."""
     n_walkers: int
     diffusivity: float
     waveform: Any
@@ -38,6 +39,7 @@ class Instance:
     want_positions: bool = False
     want_walker_signals: bool = False
     sub_steps: Optional[int] = None
+    r0: Optional[Any] = None
 
 
 @dataclass
@@ -91,7 +93,8 @@ def _resolve(inst: Instance):
     kw = dict(n_walkers=int(inst.n_walkers), diffusivity=inst.diffusivity, G=G, dt=dt,
               sub_steps=S, phase_per_substep=not use_replay, seed=inst.seed, chi=chi,
               T2=inst.T2, T1=inst.T1, want_positions=bool(inst.want_positions),
-              want_walker_signals=bool(inst.want_walker_signals))
+              want_walker_signals=bool(inst.want_walker_signals),
+              r0=None if inst.r0 is None else _to_frame(geom, inst.r0))
     return kw, bool(getattr(wf, 'stimulated_echo', False))
 
 

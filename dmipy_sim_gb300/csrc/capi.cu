@@ -14,6 +14,7 @@
 #include "dmsim.h"
 #include "mt_kernel.cuh"
 #include "walk_kernel.cuh"
+#include "walk_wide.cuh"
 
 namespace dmsim {
 WalkFn walk_fn_free(int wall, int pm, int width, bool tsm);
@@ -31,6 +32,9 @@ WalkFn walk_batch_fn_box1d(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_slab(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_shell(int wall, int pm, int width, bool tsm);
 WalkFn walk_fn_ellipsoid(int wall, int pm, int width, bool tsm);
+WideFn wide_fn_pcyl_reflect(int rt, bool psub, int nt);
+WideFn wide_fn_pcyl_relax(int rt, bool psub, int nt);
+WideFn wide_fn_pcyl_permeate(int rt, bool psub, int nt);
 WalkFn walk_batch_fn_ellipsoid(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
@@ -63,6 +67,7 @@ size_t pad16(size_t v) { return (v + 15) & ~(size_t)15; }
 // Largest shared-memory footprint for which the cell list is staged into shared memory; larger
 // lists are read through L1 from global memory.
 constexpr size_t kTabSmemBudget = 96 * 1024;
+constexpr size_t kWideSmemMax = 227 * 1024;  // dynamic shared memory one block may take
 
 // Direct form: measurements per pass.  Basis form: shapes held per thread.
 int pick_mt(int M) {
@@ -76,6 +81,9 @@ constexpr int kMaxBasisMeas = 512;
 
 struct Plan {
   WalkFn fn = nullptr;
+  WideFn wide = nullptr;  // packed cylinders, basis form: the wide-block kernel
+  int grid_wide = 0, nt_wide = 0;
+  size_t smem_wide = 0;
   int pm = 0;      // 0 direct, 1 basis, 2 vector Bloch (direct waveform)
   int width = 0;   // MT (direct) or RT (basis)
   int mt = 0;      // measurements per pass (direct) or 1 (basis: a single pass of all M)
@@ -241,7 +249,40 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
   if (grid > n_tiles) grid = n_tiles;
   if (grid < 1) grid = 1;
   pl->grid = (int)grid;
-
+  // Packed cylinders in the basis form with the cell list on chip walk on the wide-block kernel
+  // (walk_wide.cuh: one block of 1024, else 512, threads per SM) when launch_single sees no
+  // trajectory, boundary-weight or occupancy export.  The partial buffer is sized for the larger
+  // of the two grids.
+  int64_t grid_part = grid;
+  if (g->kind == DMSIM_GEOM_PACKED_CYLINDERS && pl->tsm && pl->pm == 1 && !bloch) {
+    const bool psub = p->phase_per_substep != 0;
+    for (int nt : {1024, 512}) {
+      WideFn fn = g->wall_mode == DMSIM_WALL_REFLECT ? wide_fn_pcyl_reflect(pl->width, psub, nt)
+                  : g->wall_mode == DMSIM_WALL_RELAX ? wide_fn_pcyl_relax(pl->width, psub, nt)
+                                                     : wide_fn_pcyl_permeate(pl->width, psub, nt);
+      const size_t smem = wide_layout(nt, pl->width, p->n_meas, pl->tab_cs + pl->tab_cand).total;
+      int nbw = 0;
+      if (!fn || smem > kWideSmemMax ||
+          cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbw, (const void*)fn, nt, smem) !=
+              cudaSuccess ||
+          nbw < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      const int64_t tiles_w = (p->n_walkers + nt - 1) / nt;
+      int64_t gw = (int64_t)nbw * n_sm;
+      if (gw > tiles_w) gw = tiles_w;
+      if (gw < 1) gw = 1;
+      pl->wide = fn;
+      pl->nt_wide = nt;
+      pl->smem_wide = smem;
+      pl->grid_wide = (int)gw;
+      grid_part = std::max(grid_part, gw);
+      break;
+    }
+  }
   const int Mp = pl->pm == 1 ? p->n_meas : pl->n_pass * pl->mt;
   size_t off = 0;
   pl->off_gp = off;
@@ -251,7 +292,7 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
   pl->off_cp = off;
   off = align256(off + (pl->pm == 1 ? (size_t)p->n_meas * 3 * pl->width * 4 : 0));
   pl->off_part = off;
-  off = align256(off + (size_t)pl->grid * p->n_echo * Mp * 3 * 8);
+  off = align256(off + (size_t)grid_part * p->n_echo * Mp * 3 * 8);
   pl->total = off;
   return DMSIM_OK;
 }
@@ -708,14 +749,20 @@ int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dms
   }
   BatchCtl none;
   memset(&none, 0, sizeof(none));
+  const bool wide = pl.wide != nullptr && bl == nullptr && o->traj == nullptr &&
+                    o->dlog_unit == nullptr && o->comp_occ == nullptr;
+  const int grid = wide ? pl.grid_wide : pl.grid;
   for (int pass = 0; pass < pl.n_pass; ++pass) {
     a.pass = pass;
     a.Gp = Gp + (size_t)pass * t_pad * pl.row;
     a.active = act + (size_t)pass * p->n_t;
-    pl.fn<<<pl.grid, kBlock, pl.smem, st>>>(a, none);
+    if (wide)
+      pl.wide<<<grid, pl.nt_wide, pl.smem_wide, st>>>(a);
+    else
+      pl.fn<<<grid, kBlock, pl.smem, st>>>(a, none);
   }
   const int nred = p->n_echo * p->n_meas * 3;
-  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, pl.grid, p->n_echo, a.Mp, p->n_meas,
+  k_reduce<<<(nred + 255) / 256, 256, 0, st>>>(part, grid, p->n_echo, a.Mp, p->n_meas,
                                                o->sums);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(DMSIM_ECUDA, "launch failed: %s", cudaGetErrorString(err));

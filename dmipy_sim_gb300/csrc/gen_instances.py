@@ -51,11 +51,35 @@ def _table(stem, enum, walls, packed, batch):
     return "\n".join(lines)
 
 
+WIDE_WALLS = [(0, "reflect"), (1, "relax"), (2, "permeate")]
+WIDE_RANKS = [2, 4, 8]
+WIDE_BLOCKS = [1024, 512]
+
+
+def _wide_table(wall, name):
+    """The wide-block packed-cylinder kernels of one wall mode: shape rank x phase per sub-step x
+    block size."""
+    lines = [f"// Instantiations of the wide-block packed-cylinder walk kernel, wall mode {name}: "
+             "basis rank x phase per sub-step x block size.",
+             "// Written by gen_instances.py.",
+             '#include "walk_wide.cuh"', "", "namespace dmsim {", "",
+             f"WideFn wide_fn_pcyl_{name}(int rt, bool psub, int nt) {{"]
+    for rt in WIDE_RANKS:
+        for psub in ("false", "true"):
+            for nt in WIDE_BLOCKS:
+                lines.append(f"  if (rt == {rt} && psub == {psub} && nt == {nt}) "
+                             f"return k_pcyl_wide<{wall}, {rt}, {psub}, {nt}>;")
+    lines += ["  return nullptr;", "}", "", "}  // namespace dmsim", ""]
+    return "\n".join(lines)
+
+
 def main():
     for stem, enum, walls, packed, batched in KINDS:
         (HERE / f"walk_{stem}.cu").write_text(_table(stem, enum, walls, packed, False))
         if batched:
             (HERE / f"walk_batch_{stem}.cu").write_text(_table(stem, enum, walls, packed, True))
+    for wall, name in WIDE_WALLS:
+        (HERE / f"walk_wide_{name}.cu").write_text(_wide_table(wall, name))
 
 
 if __name__ == "__main__":

@@ -710,63 +710,211 @@ __device__ __forceinline__ void fold(float& v, int& img, const GeoK& g) {
   }
 }
 
-// Packed cylinders (2-D cross-section; z is free).  cs/cand point at the cell list (shared or
-// global memory).
-template <int WALL>
-__device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, int& iy, float sx,
-                                                 float sy, float u, const GeoK& g,
-                                                 const uint32_t* __restrict__ cs,
-                                                 const float4* __restrict__ cand, Tally& tl) {
-  const float lxy = sqrtf(sx * sx + sy * sy);
-  float dx = 0.f, dy = 0.f;
+// Packed cylinders (2-D cross-section; z is free).  The step is assembled from the pieces below
+// (shared with the cooperative kernel of walk_coop.cuh, which runs them in separate phases):
+//   pcyl_dir     step length and unit direction in the cross-section;
+//   pcyl_test    one candidate's entry root and straight-end containment (geometries.py:1777-1805
+//                / 2054-2081 for the root, 1851-1877 for the containment);
+//   pcyl_graze   the FP64 re-solve of a grazing winning root;
+//   pcyl_hit     the wall's action on the winner: specular reflection (+ boundary weight) or the
+//                Powles decision with its snapped, side-clamped reflection (geometries.py:1810-1842,
+//                1943-1967, 2083-2165);
+//   pcyl_clamp   the fold-first safety clamp over a cell's candidates (geometries.py:1851-1877).
+
+// Crossing of one candidate by the segment from (x, y) along (dx, dy) of length lxy.
+struct PcylRoot {
+  float t, disc;  // entry (or, from inside, exit) distance; discriminant of the root
+  bool valid;     // a forward crossing within the step
+  bool ins;       // the walker starts inside the candidate (permeable walls only)
+  bool end_in;    // the straight end point (ex, ey) lies inside (reflecting walls only)
+};
+
+__device__ __forceinline__ void pcyl_dir(float sx, float sy, float& lxy, float& dx, float& dy) {
+  lxy = sqrtf(sx * sx + sy * sy);
+  dx = 0.f;
+  dy = 0.f;
   if (lxy > 0.f) {
     const float inv = 1.f / lxy;
     dx = sx * inv;
     dy = sy * inv;
   }
-  const int c = cell_of(y, g) * g.n + cell_of(x, g);
-  const uint32_t kb = cs[c], ke = cs[c + 1];
+}
 
-  // Nearest wall crossing over the candidates (geometries.py:1777-1805 / 2054-2081).  The same
-  // pass also evaluates the fold-first safety clamp (geometries.py:1851-1877) for the straight
-  // end point x + s, which is the end point whenever no wall is hit.  A grazing root of the
-  // winning candidate is re-solved in FP64 after the pass.
-  float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hR = 1.f;
-  bool hit_in = false;
-  const float ex = x + sx, ey = y + sy;
+template <int WALL>
+__device__ __forceinline__ PcylRoot pcyl_test(const float4 C, float x, float y, float ex, float ey,
+                                              float dx, float dy, float lxy, const GeoK& g) {
+  PcylRoot r;
+  const float R2 = C.w * C.w;
+  r.end_in = false;
+  if constexpr (WALL != kPermeate) {
+    const float fx = ex - C.x, fy = ey - C.y;
+    const float d2 = fx * fx + fy * fy;
+    r.end_in = d2 < R2 && (!g.mi || (min_image(fx, g) && min_image(fy, g)));
+  }
+  const float qx = x - C.x, qy = y - C.y;
+  const bool mi_ok = !g.mi || (min_image(qx, g) && min_image(qy, g));
+  const float dp = dx * qx + dy * qy;
+  const float q2 = qx * qx + qy * qy;
+  r.disc = dp * dp - (q2 - R2);
+  r.ins = (WALL == kPermeate) && (q2 < R2);
+  const float sq = sqrtf(fmaxf(r.disc, 0.f));
+  r.t = r.ins ? -dp + sq : -dp - sq;
+  // an entry root with dp >= 0 is -dp - sqrt(disc) <= 0: no forward crossing
+  r.valid = mi_ok && (r.ins || dp < 0.f) && (r.disc > 0.f) && (r.t > g.eps) && (r.t < lxy) &&
+            (lxy > 0.f);
+  return r;
+}
+
+// A winning root whose discriminant is within kGrazeTol R^2 of grazing, re-solved in FP64; the
+// hit may vanish (tbest = INFINITY).
+__device__ __forceinline__ void pcyl_graze(float x, float y, float dx, float dy, float lxy,
+                                           float hcx, float hcy, float hR, bool hit_in,
+                                           const GeoK& g, float& tbest, float& disc_hit,
+                                           Tally& tl) {
+  const double qxd = (double)(x - hcx), qyd = (double)(y - hcy);
+  const double dpd = (double)dx * qxd + (double)dy * qyd;
+  const double dd = dpd * dpd - ((qxd * qxd + qyd * qyd) - (double)hR * hR);
+  const double sd = sqrt(fmax(dd, 0.0));
+  const float t = (float)(hit_in ? -dpd + sd : -dpd - sd);
+  disc_hit = (float)dd;
+  tbest = ((dd > 0.0) && (t > g.eps) && (t < lxy)) ? t : INFINITY;
+  ++tl.graze;
+}
+
+// The wall's action on a hit at distance tbest of candidate (hcx, hcy, hR): the new position in
+// the start cell's frame and the boundary log-weight at rho/D = 1.
+template <int WALL>
+__device__ __forceinline__ void pcyl_hit(float x, float y, float sx, float sy, float dx, float dy,
+                                         float lxy, float u, float tbest, float disc_hit,
+                                         float hcx, float hcy, float hR, bool hit_in,
+                                         const GeoK& g, Tally& tl, float& nxp, float& nyp,
+                                         float& dlog) {
+  dlog = 0.f;
+  const float qcx = x - hcx, qcy = y - hcy;
+  if constexpr (WALL != kPermeate) {
+    // geometries.py:1810-1842 / 1943-1967
+    const float nx = (qcx + tbest * dx) / hR, ny = (qcy + tbest * dy) / hR;
+    const float dn = dx * nx + dy * ny;
+    float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
+    const float rn = sqrtf(rx * rx + ry * ry);
+    if (rn > 0.f) {
+      rx /= fmaxf(rn, 1e-30f);
+      ry /= fmaxf(rn, 1e-30f);
+    } else {
+      rx = 0.f;
+      ry = 0.f;
+    }
+    const float remr = lxy - tbest;
+    const float f = fmaxf(remr - g.nudge, 0.f);
+    nxp = (x + tbest * dx) + g.nudge * nx + rx * f;
+    nyp = (y + tbest * dy) + g.nudge * ny + ry * f;
+    if constexpr (WALL == kRelax) dlog = -2.f * (remr * (sqrtf(fmaxf(disc_hit, 0.f)) / hR));
+  } else {
+    // geometries.py:2083-2165
+    const float hrx = qcx + tbest * dx, hry = qcy + tbest * dy;
+    const float hl = fmaxf(sqrtf(hrx * hrx + hry * hry), 1e-30f);
+    const float nx = hrx / hl, ny = hry / hl;
+    const float rem = lxy - tbest;
+    const float dperp = rem * (sqrtf(fmaxf(disc_hit, 0.f)) / hR);
+    const float p = fminf(1.f, 2.f * g.kod * dperp);
+    if (u < p) {
+      nxp = x + sx;
+      nyp = y + sy;
+      ++tl.transmit;
+    } else {
+      const float dn = dx * nx + dy * ny;
+      float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
+      const float rn = sqrtf(rx * rx + ry * ry);
+      if (rn > 0.f) {
+        rx /= fmaxf(rn, 1e-30f);
+        ry /= fmaxf(rn, 1e-30f);
+      } else {
+        rx = 0.f;
+        ry = 0.f;
+      }
+      const float sgn = hit_in ? -1.f : 1.f;
+      const float f = fmaxf(rem - g.nudge, 0.f);
+      float ox = hR * nx + g.nudge * sgn * nx + rx * f;
+      float oy = hR * ny + g.nudge * sgn * ny + ry * f;
+      const float on = sqrtf(ox * ox + oy * oy);
+      const bool wrong = hit_in ? (on >= hR) : (on <= hR);
+      if (wrong) {
+        const float s = (hit_in ? hR - g.nudge : hR + g.nudge) / fmaxf(on, 1e-30f);
+        ox *= s;
+        oy *= s;
+        ++tl.clamp;
+      }
+      nxp = x + (ox - qcx);
+      nyp = y + (oy - qcy);
+      dlog = -2.f * dperp;
+    }
+  }
+}
+
+// Fold-first safety clamp (geometries.py:1851-1877): push (nxp, nyp) out of the candidate it
+// penetrates most deeply (relative to R^2).  The start cell's list covers every object within
+// reach of the end point.
+__device__ __forceinline__ void pcyl_clamp(float& nxp, float& nyp, uint32_t kb, uint32_t ke,
+                                           const GeoK& g, const float4* __restrict__ cand,
+                                           Tally& tl) {
   float pe = 1.f, pqx = 0.f, pqy = 0.f, pR = 1.f;
-  auto visit = [&](const float4 C) {
-    const float R2 = C.w * C.w;
-    if constexpr (WALL != kPermeate) {
-      const float fx = ex - C.x, fy = ey - C.y;
-      const float d2 = fx * fx + fy * fy;
-      if (d2 < R2 && (!g.mi || (min_image(fx, g) && min_image(fy, g)))) {
-        const float pen = d2 / R2;
-        if (pen < pe) {
-          pe = pen;
-          pqx = fx;
-          pqy = fy;
-          pR = C.w;
-        }
+  auto pen_of = [&](const float4 C) {
+    const float qx = nxp - C.x, qy = nyp - C.y;
+    const float d2 = qx * qx + qy * qy, R2 = C.w * C.w;
+    if (d2 < R2 && (!g.mi || (min_image(qx, g) && min_image(qy, g)))) {
+      const float pen = d2 / R2;
+      if (pen < pe) {
+        pe = pen;
+        pqx = qx;
+        pqy = qy;
+        pR = C.w;
       }
     }
-    const float qx = x - C.x, qy = y - C.y;
-    if (g.mi && !(min_image(qx, g) && min_image(qy, g))) return;
-    const float dp = dx * qx + dy * qy;
-    const float q2 = qx * qx + qy * qy;
-    float disc = dp * dp - (q2 - R2);
-    const bool ins = (WALL == kPermeate) && (q2 < R2);
-    if (!ins && dp >= 0.f) return;  // entry root -dp - sqrt(disc) <= 0: no forward crossing
-    const float sq = sqrtf(fmaxf(disc, 0.f));
-    const float t = ins ? -dp + sq : -dp - sq;
-    const bool valid = (disc > 0.f) && (t > g.eps) && (t < lxy) && (lxy > 0.f);
-    if (valid && t < tbest) {
-      tbest = t;
-      disc_hit = disc;
+  };
+  if (g.kmax == 2) {
+#pragma unroll
+    for (uint32_t j = 0; j < 2u; ++j)
+      pen_of(kb + j < ke ? cand[kb + j] : make_float4(kFarAway, kFarAway, kFarAway, 0.f));
+  } else {
+#pragma unroll 1
+    for (uint32_t k = kb; k < ke; ++k) pen_of(cand[k]);
+  }
+  if (pe < 1.f) {
+    const float dcl = sqrtf(pqx * pqx + pqy * pqy);
+    const float s = (pR + g.nudge) / fmaxf(dcl, g.nudge);
+    nxp += pqx * (s - 1.f);
+    nyp += pqy * (s - 1.f);
+    ++tl.clamp;
+  }
+}
+
+// One sub-step of a walker: the nearest crossing over the cell's candidates (branch free; the
+// straight end point's containment is noted in the same pass, so the clamp scan runs only after a
+// reflection or when that end point lies inside a candidate), the grazing re-solve, the wall's
+// action, the clamp, and the fold back into the periodic cell.  cs/cand point at the cell list
+// (shared or global memory).
+template <int WALL>
+__device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, int& iy, float sx,
+                                                 float sy, float u, const GeoK& g,
+                                                 const uint32_t* __restrict__ cs,
+                                                 const float4* __restrict__ cand, Tally& tl) {
+  float lxy, dx, dy;
+  pcyl_dir(sx, sy, lxy, dx, dy);
+  const int c = cell_of(y, g) * g.n + cell_of(x, g);
+  const uint32_t kb = cs[c], ke = cs[c + 1];
+  float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hR = 1.f;
+  bool hit_in = false, end_in = false;
+  const float ex = x + sx, ey = y + sy;
+  auto visit = [&](const float4 C) {
+    const PcylRoot r = pcyl_test<WALL>(C, x, y, ex, ey, dx, dy, lxy, g);
+    end_in |= r.end_in;
+    if (r.valid && r.t < tbest) {
+      tbest = r.t;
+      disc_hit = r.disc;
       hcx = C.x;
       hcy = C.y;
       hR = C.w;
-      hit_in = ins;
+      hit_in = r.ins;
     }
   };
   if (g.kmax == 2) {
@@ -780,115 +928,15 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
 #pragma unroll 1
     for (uint32_t k = kb; k < ke; ++k) visit(cand[k]);
   }
-  if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR) {
-    const double qxd = (double)(x - hcx), qyd = (double)(y - hcy);
-    const double dpd = (double)dx * qxd + (double)dy * qyd;
-    const double dd = dpd * dpd - ((qxd * qxd + qyd * qyd) - (double)hR * hR);
-    const double sd = sqrt(fmax(dd, 0.0));
-    const float t = (float)(hit_in ? -dpd + sd : -dpd - sd);
-    disc_hit = (float)dd;
-    tbest = ((dd > 0.0) && (t > g.eps) && (t < lxy)) ? t : INFINITY;
-    ++tl.graze;
-  }
+  if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR)
+    pcyl_graze(x, y, dx, dy, lxy, hcx, hcy, hR, hit_in, g, tbest, disc_hit, tl);
 
-  float nxp, nyp;  // new position in the start cell's frame
-  float dlog = 0.f;
-  if (tbest < INFINITY) {
-    const float qcx = x - hcx, qcy = y - hcy;
-    if constexpr (WALL != kPermeate) {
-      // geometries.py:1810-1842 / 1943-1967
-      const float nx = (qcx + tbest * dx) / hR, ny = (qcy + tbest * dy) / hR;
-      const float dn = dx * nx + dy * ny;
-      float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
-      const float rn = sqrtf(rx * rx + ry * ry);
-      if (rn > 0.f) {
-        rx /= fmaxf(rn, 1e-30f);
-        ry /= fmaxf(rn, 1e-30f);
-      } else {
-        rx = 0.f;
-        ry = 0.f;
-      }
-      const float remr = lxy - tbest;
-      const float f = fmaxf(remr - g.nudge, 0.f);
-      nxp = (x + tbest * dx) + g.nudge * nx + rx * f;
-      nyp = (y + tbest * dy) + g.nudge * ny + ry * f;
-      if constexpr (WALL == kRelax) dlog = -2.f * (remr * (sqrtf(fmaxf(disc_hit, 0.f)) / hR));
-    } else {
-      // geometries.py:2083-2165
-      const float hrx = qcx + tbest * dx, hry = qcy + tbest * dy;
-      const float hl = fmaxf(sqrtf(hrx * hrx + hry * hry), 1e-30f);
-      const float nx = hrx / hl, ny = hry / hl;
-      const float rem = lxy - tbest;
-      const float dperp = rem * (sqrtf(fmaxf(disc_hit, 0.f)) / hR);
-      const float p = fminf(1.f, 2.f * g.kod * dperp);
-      if (u < p) {
-        nxp = x + sx;
-        nyp = y + sy;
-        ++tl.transmit;
-      } else {
-        const float dn = dx * nx + dy * ny;
-        float rx = dx - 2.f * dn * nx, ry = dy - 2.f * dn * ny;
-        const float rn = sqrtf(rx * rx + ry * ry);
-        if (rn > 0.f) {
-          rx /= fmaxf(rn, 1e-30f);
-          ry /= fmaxf(rn, 1e-30f);
-        } else {
-          rx = 0.f;
-          ry = 0.f;
-        }
-        const float sgn = hit_in ? -1.f : 1.f;
-        const float f = fmaxf(rem - g.nudge, 0.f);
-        float ox = hR * nx + g.nudge * sgn * nx + rx * f;
-        float oy = hR * ny + g.nudge * sgn * ny + ry * f;
-        const float on = sqrtf(ox * ox + oy * oy);
-        const bool wrong = hit_in ? (on >= hR) : (on <= hR);
-        if (wrong) {
-          const float s = (hit_in ? hR - g.nudge : hR + g.nudge) / fmaxf(on, 1e-30f);
-          ox *= s;
-          oy *= s;
-          ++tl.clamp;
-        }
-        nxp = x + (ox - qcx);
-        nyp = y + (oy - qcy);
-        dlog = -2.f * dperp;
-      }
-    }
-  } else {
-    nxp = x + sx;
-    nyp = y + sy;
-  }
-
-  if constexpr (WALL != kPermeate) {
-    // Fold-first safety clamp (geometries.py:1851-1877): push the walker out of the object it
-    // penetrates most deeply (relative to R^2).  Without a hit the end point is x + s, already
-    // tested above; after a reflection the start cell's list (which covers every object within
-    // reach of the end point) is scanned again.
-    if (tbest < INFINITY) {
-      pe = 1.f;
-#pragma unroll 1
-      for (uint32_t k = kb; k < ke; ++k) {
-        const float4 C = cand[k];
-        const float qx = nxp - C.x, qy = nyp - C.y;
-        const float d2 = qx * qx + qy * qy, R2 = C.w * C.w;
-        if (d2 < R2 && (!g.mi || (min_image(qx, g) && min_image(qy, g)))) {
-          const float pen = d2 / R2;
-          if (pen < pe) {
-            pe = pen;
-            pqx = qx;
-            pqy = qy;
-            pR = C.w;
-          }
-        }
-      }
-    }
-    if (pe < 1.f) {
-      const float dcl = sqrtf(pqx * pqx + pqy * pqy);
-      const float s = (pR + g.nudge) / fmaxf(dcl, g.nudge);
-      nxp += pqx * (s - 1.f);
-      nyp += pqy * (s - 1.f);
-      ++tl.clamp;
-    }
-  }
+  float nxp = x + sx, nyp = y + sy, dlog = 0.f;  // new position in the start cell's frame
+  if (tbest < INFINITY)
+    pcyl_hit<WALL>(x, y, sx, sy, dx, dy, lxy, u, tbest, disc_hit, hcx, hcy, hR, hit_in, g, tl,
+                   nxp, nyp, dlog);
+  if constexpr (WALL != kPermeate)
+    if (tbest < INFINITY || end_in) pcyl_clamp(nxp, nyp, kb, ke, g, cand, tl);
   x = nxp;
   y = nyp;
   fold(x, ix, g);

@@ -95,8 +95,10 @@ def test_permeability_limits(cuda):
 
 
 def test_tortuosity_square_lattice(cuda):
-    """D_self/D0 -> 1/(1+f) for tracer diffusion among impermeable cylinders on a square lattice
-    (reference README: MC within 1.4%)."""
+    """D_self/D0 -> 1/(1+f) for tracer diffusion among impermeable cylinders on a square lattice,
+    within the reference's own bar of 1.4 % (README: MC within 1.4 %), at 1,000,000 walkers (the
+    statistical error of the slope is ~0.1 %; Rayleigh's correction to 1/(1+f) at f = 0.3 is
+    +0.2 %)."""
     f, a = 0.3, 4e-6
     r = a * np.sqrt(f / np.pi)
     cen = np.array([[(i + 0.5) * a - a, (j + 0.5) * a - a] for i in range(2) for j in range(2)])
@@ -105,13 +107,13 @@ def test_tortuosity_square_lattice(cuda):
     G = np.zeros((1, n_t, 3), np.float32)
     dt = T / n_t
     S = core.replay_sub_steps(g, D, dt)
-    n = 40_000
+    n = 1_000_000
     r0 = g.init_positions(n, key=3)
     traj = torch.empty((n, n_t, 3), dtype=torch.float32, device=cuda)
     core.run_walk(g, n_walkers=n, diffusivity=D, G=G, dt=dt, sub_steps=S,
                   phase_per_substep=False, seed=10, r0=r0, traj=traj, traj_f16=False)
-    x = traj.cpu().numpy()
-    msd = np.mean(np.sum((x[:, :, :2] - r0[:, None, :2]) ** 2, axis=2), axis=0)
+    start = torch.from_numpy(np.asarray(r0[:, :2], np.float32)).to(cuda)
     i1, i2 = 19, 59                                     # t = 100 ms and 300 ms
-    d_perp = (msd[i2] - msd[i1]) / (4 * dt * (i2 - i1))
-    assert abs(d_perp / D * (1 + f) - 1) < 0.03, d_perp / D
+    msd = [float(((traj[:, i, :2] - start) ** 2).sum(dim=1).double().mean()) for i in (i1, i2)]
+    d_perp = (msd[1] - msd[0]) / (4 * dt * (i2 - i1))
+    assert abs(d_perp / D * (1 + f) - 1) < 0.014, d_perp / D
