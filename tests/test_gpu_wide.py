@@ -63,12 +63,18 @@ def test_wide_kernel_walks_the_general_kernels_walkers(cuda, case):
     identity is asked for over short walks only."""
     wide, gen = _walks(case, 400, 8000, 12, 9, keep=3)     # 40 us samples, <= 36 sub-steps
     pl, pg = wide.extras["pos"].cpu().numpy(), gen.extras["pos"].cpu().numpy()
-    same = np.all(np.abs(pl - pg) <= 1e-4 * 0.9e-6, axis=1)
+    pos_tol = 1e-4 * 0.9e-6
+    same = np.all(np.abs(pl - pg) <= pos_tol, axis=1)
     assert same.mean() >= 0.99, same.mean()
     np.testing.assert_allclose(wide.extras["phi"].cpu().numpy()[same],
                                gen.extras["phi"].cpu().numpy()[same], rtol=1e-5, atol=1e-5)
+    # a wall hit costs 2 rho/D x (penetration depth) of log-weight, and the depth is a
+    # difference of two near-equal radii: walkers that agree to pos_tol may differ by
+    # 2 rho/D pos_tol per hit (a few hits in this short walk)
+    rho = CASES[case][0].get("surface_relaxivity_t2", 0.0)
     np.testing.assert_allclose(wide.extras["log_w"].cpu().numpy()[same],
-                               gen.extras["log_w"].cpu().numpy()[same], rtol=1e-5, atol=1e-7)
+                               gen.extras["log_w"].cpu().numpy()[same], rtol=1e-5,
+                               atol=1e-7 + 4 * 2 * rho / D * pos_tol)
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
