@@ -19,6 +19,9 @@ TILE_WALKERS = 320
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
  GEOM_MYELIN, GEOM_PMYELIN, GEOM_BOX1D, GEOM_SLAB, GEOM_SHELL, GEOM_ELLIPSOID) = range(12)
 WALL_REFLECT, WALL_RELAX, WALL_PERMEATE = range(3)
+SCHED_LOCKSTEP, SCHED_FREE_FLIGHT, SCHED_SCAN_EVERY = range(3)
+SCHEDULES = {"lockstep": SCHED_LOCKSTEP, "free_flight": SCHED_FREE_FLIGHT,
+             "scan_every": SCHED_SCAN_EVERY}
 
 STATUS_NAMES = ("nonfinite", "clamped", "init_fail", "bounce_budget", "escape_reject",
                 "wait_timeout", "graze_fp64", "transmit")
@@ -77,7 +80,7 @@ class WalkParams(C.Structure):
         ("t2_decay", C.c_float), ("t1_decay", C.c_float), ("has_weight", C.c_int32),
         ("n_echo", C.c_int32), ("echo_idx", C.POINTER(C.c_int32)), ("G", C.c_void_p),
         ("chi", C.c_void_p), ("r0", C.c_void_p), ("basis_rank", C.c_int32),
-        ("pad1", C.c_int32), ("basis_V", C.c_void_p), ("basis_C", C.c_void_p),
+        ("schedule", C.c_int32), ("basis_V", C.c_void_p), ("basis_C", C.c_void_p),
     ]
 
 

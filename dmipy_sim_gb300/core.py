@@ -262,7 +262,7 @@ class PreparedWalk:
                  seed, chi=None, T2=None, T1=None, echo_idx=None, r0=None, walker_offset=0,
                  want_positions=False, want_walker_signals=False, want_compartments=False,
                  traj=None, traj_f16=True, want_dlog=False, want_comp_occ=False,
-                 use_basis=True, allocate_workspace=True, total_walkers=None):
+                 use_basis=True, allocate_workspace=True, total_walkers=None, schedule="lockstep"):
         self.lib = _lib.load()
         dev = self.dev = _lib.device()
         G = np.asarray(G, dtype=np.float32)
@@ -339,6 +339,13 @@ class PreparedWalk:
             p.basis_rank = self.basis_rank = V.shape[1]
             p.basis_V = self.V_dev.data_ptr()
             p.basis_C = self.C_dev.data_ptr()
+        # packed cylinders in the basis form: "lockstep" (default) walks every lane of a warp on
+        # the same sub-step; "free_flight" lets lanes step independently and skips the wall scan
+        # while a walker stays inside a wall-free disc; "scan_every" is that kernel scanning every
+        # sub-step (bit-identical to "free_flight")
+        if schedule not in _lib.SCHEDULES:
+            raise ValueError(f"schedule must be one of {sorted(_lib.SCHEDULES)}")
+        p.schedule = _lib.SCHEDULES[schedule]
         p.chi = None if self.chi_dev is None else self.chi_dev.data_ptr()
         p.r0 = None if self.r0_dev is None else self.r0_dev.data_ptr()
         self.sums = torch.zeros((len(echo), n_meas, 3), dtype=torch.float64, device=dev)

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -14,6 +15,7 @@
 #include "dmsim.h"
 #include "mt_kernel.cuh"
 #include "walk_kernel.cuh"
+#include "walk_ff.cuh"
 #include "walk_wide.cuh"
 
 namespace dmsim {
@@ -35,6 +37,9 @@ WalkFn walk_fn_ellipsoid(int wall, int pm, int width, bool tsm);
 WideFn wide_fn_pcyl_reflect(int rt, bool psub, int nt);
 WideFn wide_fn_pcyl_relax(int rt, bool psub, int nt);
 WideFn wide_fn_pcyl_permeate(int rt, bool psub, int nt);
+FfFn ff_fn_pcyl_reflect(int rt, bool psub, int nt);
+FfFn ff_fn_pcyl_relax(int rt, bool psub, int nt);
+FfFn ff_fn_pcyl_permeate(int rt, bool psub, int nt);
 WalkFn walk_batch_fn_ellipsoid(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_free(int wall, int pm, int width, bool tsm);
 WalkFn walk_batch_fn_cyl(int wall, int pm, int width, bool tsm);
@@ -68,6 +73,35 @@ size_t pad16(size_t v) { return (v + 15) & ~(size_t)15; }
 // lists are read through L1 from global memory.
 constexpr size_t kTabSmemBudget = 96 * 1024;
 constexpr size_t kWideSmemMax = 227 * 1024;  // dynamic shared memory one block may take
+constexpr size_t kFfPartialMax = (size_t)32 << 20;  // largest per-warp partial buffer (bytes)
+
+// Free-flight walk: lanes that wait for a wall scan, a hit resolution and a sample update before
+// the warp runs that stage.  DMSIM_FF_QUORUM="scan,hit,sample" overrides them, and
+// DMSIM_FF_BLOCK (512 or 1024) the block size tried first (tuning knobs).
+struct FfTuning {
+  int q[3] = {12, 6, 8};
+  int block = 0;
+  FfTuning() {
+    if (const char* v = getenv("DMSIM_FF_QUORUM")) {
+      int a = 0, b = 0, c = 0;
+      if (sscanf(v, "%d,%d,%d", &a, &b, &c) == 3 && a >= 1 && b >= 1 && c >= 1 && a <= 32 &&
+          b <= 32 && c <= 32) {
+        q[0] = a;
+        q[1] = b;
+        q[2] = c;
+      }
+    }
+    if (const char* v = getenv("DMSIM_FF_BLOCK")) {
+      const int n = atoi(v);
+      if (n == 512 || n == 1024) block = n;
+    }
+  }
+};
+const FfTuning& ff_tuning() {
+  static const FfTuning t;
+  return t;
+}
+int ff_block_override() { return ff_tuning().block; }
 
 // Direct form: measurements per pass.  Basis form: shapes held per thread.
 int pick_mt(int M) {
@@ -84,6 +118,9 @@ struct Plan {
   WideFn wide = nullptr;  // packed cylinders, basis form: the wide-block kernel
   int grid_wide = 0, nt_wide = 0;
   size_t smem_wide = 0;
+  FfFn ff = nullptr;  // packed cylinders, basis form, free flight: the free-flight kernel
+  int grid_ff = 0, nt_ff = 0;
+  size_t smem_ff = 0;
   int pm = 0;      // 0 direct, 1 basis, 2 vector Bloch (direct waveform)
   int width = 0;   // MT (direct) or RT (basis)
   int mt = 0;      // measurements per pass (direct) or 1 (basis: a single pass of all M)
@@ -174,6 +211,8 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
   }
   if (p->basis_rank < 0 || p->basis_rank > kMaxBasisRank)
     return fail(DMSIM_EINVAL, "basis_rank must be in [0, %d]", kMaxBasisRank);
+  if (p->schedule < DMSIM_SCHED_LOCKSTEP || p->schedule > DMSIM_SCHED_SCAN_EVERY)
+    return fail(DMSIM_EINVAL, "schedule must be one of DMSIM_SCHED_*");
   if (bloch) {
     if (p->G == nullptr) return fail(DMSIM_EINVAL, "G is null");
     pl->pm = 2;
@@ -281,6 +320,40 @@ int make_plan(const dmsim_walk_params* p, const dmsim_geometry* g, Plan* pl,
       pl->grid_wide = (int)gw;
       grid_part = std::max(grid_part, gw);
       break;
+    }
+    // The free-flight kernel (walk_ff.cuh), when asked for, walks the same walkers with fewer
+    // wall scans; it keeps one FP64 partial slice per warp, so it is taken while those slices
+    // stay small.
+    if (pl->wide && p->schedule != DMSIM_SCHED_LOCKSTEP) {
+      for (int nt : {ff_block_override(), 1024, 512}) {
+        if (nt <= 0) continue;
+        FfFn fn = g->wall_mode == DMSIM_WALL_REFLECT ? ff_fn_pcyl_reflect(pl->width, psub, nt)
+                  : g->wall_mode == DMSIM_WALL_RELAX ? ff_fn_pcyl_relax(pl->width, psub, nt)
+                                                     : ff_fn_pcyl_permeate(pl->width, psub, nt);
+        const size_t smem = ff_layout(nt, pl->width, p->n_meas, pl->tab_cs + pl->tab_cand).total;
+        int nbf = 0;
+        if (!fn || smem > kWideSmemMax ||
+            cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbf, (const void*)fn, nt, smem) !=
+                cudaSuccess ||
+            nbf < 1) {
+          cudaGetLastError();
+          continue;
+        }
+        const int64_t blocks = (p->n_walkers + nt - 1) / nt;
+        int64_t gf = (int64_t)nbf * n_sm;
+        if (gf > blocks) gf = blocks;
+        if (gf < 1) gf = 1;
+        const int64_t slots = gf * (nt / 32);
+        if ((size_t)slots * p->n_echo * p->n_meas * 3 * 8 > kFfPartialMax) break;
+        pl->ff = fn;
+        pl->nt_ff = nt;
+        pl->smem_ff = smem;
+        pl->grid_ff = (int)gf;
+        grid_part = std::max(grid_part, slots);
+        break;
+      }
     }
   }
   const int Mp = pl->pm == 1 ? p->n_meas : pl->n_pass * pl->mt;
@@ -638,6 +711,8 @@ GeoK make_geok(const dmsim_geometry* g) {
   gk.r_out = g->shell_r_out;
   gk.cyl = g->shell_cyl ? 1 : 0;
   for (int a = 0; a < 3; ++a) gk.e2[a] = g->ell_inv2[a];
+  gk.h = packed ? g->cell_h : 0.f;
+  gk.reach = packed ? g->reach : 0.f;
   return gk;
 }
 
@@ -751,12 +826,18 @@ int launch_single(const dmsim_walk_params* p, const dmsim_geometry* g, const dms
   memset(&none, 0, sizeof(none));
   const bool wide = pl.wide != nullptr && bl == nullptr && o->traj == nullptr &&
                     o->dlog_unit == nullptr && o->comp_occ == nullptr;
-  const int grid = wide ? pl.grid_wide : pl.grid;
+  const bool ff = wide && pl.ff != nullptr;
+  // partial slices to reduce: one per warp (free flight), else one per block
+  const int grid = ff ? pl.grid_ff * (pl.nt_ff / 32) : wide ? pl.grid_wide : pl.grid;
+  for (int k = 0; k < 3; ++k) a.ff_quorum[k] = ff_tuning().q[k];
+  a.ff_skip = p->schedule == DMSIM_SCHED_FREE_FLIGHT ? 1 : 0;
   for (int pass = 0; pass < pl.n_pass; ++pass) {
     a.pass = pass;
     a.Gp = Gp + (size_t)pass * t_pad * pl.row;
     a.active = act + (size_t)pass * p->n_t;
-    if (wide)
+    if (ff)
+      pl.ff<<<pl.grid_ff, pl.nt_ff, pl.smem_ff, st>>>(a);
+    else if (wide)
       pl.wide<<<grid, pl.nt_wide, pl.smem_wide, st>>>(a);
     else
       pl.fn<<<grid, kBlock, pl.smem, st>>>(a, none);

@@ -73,6 +73,26 @@ def _wide_table(wall, name):
     return "\n".join(lines)
 
 
+FF_BLOCKS = [1024]
+
+
+def _ff_table(wall, name):
+    """The free-flight packed-cylinder kernels of one wall mode: shape rank x phase per sub-step
+    x block size."""
+    lines = [f"// Instantiations of the free-flight packed-cylinder walk kernel, wall mode {name}: "
+             "basis rank x phase per sub-step x block size.",
+             "// Written by gen_instances.py.",
+             '#include "walk_ff.cuh"', "", "namespace dmsim {", "",
+             f"FfFn ff_fn_pcyl_{name}(int rt, bool psub, int nt) {{"]
+    for rt in WIDE_RANKS:
+        for psub in ("false", "true"):
+            for nt in FF_BLOCKS:
+                lines.append(f"  if (rt == {rt} && psub == {psub} && nt == {nt}) "
+                             f"return k_pcyl_ff<{wall}, {rt}, {psub}, {nt}>;")
+    lines += ["  return nullptr;", "}", "", "}  // namespace dmsim", ""]
+    return "\n".join(lines)
+
+
 def main():
     for stem, enum, walls, packed, batched in KINDS:
         (HERE / f"walk_{stem}.cu").write_text(_table(stem, enum, walls, packed, False))
@@ -80,6 +100,7 @@ def main():
             (HERE / f"walk_batch_{stem}.cu").write_text(_table(stem, enum, walls, packed, True))
     for wall, name in WIDE_WALLS:
         (HERE / f"walk_wide_{name}.cu").write_text(_wide_table(wall, name))
+        (HERE / f"walk_ff_{name}.cu").write_text(_ff_table(wall, name))
 
 
 if __name__ == "__main__":

@@ -51,6 +51,7 @@ struct GeoK {
   float r_out;  // shell: the reflecting outer wall
   int cyl;      // shell: radii from the z axis (1) or the origin (0)
   float e2[3];  // ellipsoid: 1 / semi-axis^2
+  float h, reach;  // packed: cell side; the reach (step + margin) the cell lists cover
 };
 
 // Myelinated cylinder: two concentric walls (axis z) around three compartments.

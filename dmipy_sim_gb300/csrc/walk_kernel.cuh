@@ -90,6 +90,10 @@ struct KArgs {
   float frot[9], fpar[8];
   int fdims[3];
   float fgdt;
+  // free-flight kernel: lanes waiting for a wall scan, a hit resolution and a sample update
+  // before the warp runs that stage
+  int ff_quorum[3];
+  int ff_skip;  // 1: free flight inside the wall-free disc; 0: a scan on every sub-step
   int echo[kMaxEcho];
 };
 

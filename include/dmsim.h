@@ -184,6 +184,19 @@ typedef struct dmsim_geometry {
   float ell_pad;
 } dmsim_geometry;
 
+/* Walk schedules of packed cylinders in the basis phase form (dmsim_walk_params.schedule).
+   LOCKSTEP (the default): every lane of a warp on the same sub-step, a wall scan on each.
+   FREE_FLIGHT: lanes step independently and skip the wall scan while the walker stays inside the
+   wall-free disc of its last scan; SCAN_EVERY: the same kernel with a scan on every sub-step
+   (bit-identical walks: the check of the skip).  On GB300 the lock-step kernel is the faster one
+   on dense packings: the independent lanes' divergence costs more than the skipped scans.
+   Other geometries and forms always walk lock-step. */
+enum dmsim_schedule {
+  DMSIM_SCHED_LOCKSTEP = 0,
+  DMSIM_SCHED_FREE_FLIGHT = 1,
+  DMSIM_SCHED_SCAN_EVERY = 2
+};
+
 /* ---- walk parameters -------------------------------------------------------------------------- */
 typedef struct dmsim_walk_params {
   int64_t n_walkers;     /* walkers in this call                                                */
@@ -209,7 +222,8 @@ typedef struct dmsim_walk_params {
      the measurements are built from r time shapes, G[t, m, k] = sum_j C[m, k, j] V[t, j], and the
      walk accumulates 3 r phase moments instead of n_meas phases; G is then ignored. */
   int32_t basis_rank;
-  int32_t pad1;
+  int32_t schedule;          /* enum dmsim_schedule: how packed cylinders in the basis form are
+                                walked (0, the default, is lock-step)                          */
   const float* basis_V;      /* (n_t, basis_rank)                                               */
   const float* basis_C;      /* (n_meas, 3, basis_rank)                                         */
 } dmsim_walk_params;
