@@ -26,6 +26,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "dmsim.h"
 
 namespace dmsim {
@@ -741,7 +743,9 @@ __device__ __forceinline__ void pcyl_dir(float sx, float sy, float& lxy, float& 
   }
 }
 
-template <int WALL>
+// MI = false compiles the test for cell lists that never list two images of one object
+// (g.mi == 0), where the minimum-image test always passes.
+template <int WALL, bool MI = true>
 __device__ __forceinline__ PcylRoot pcyl_test(const float4 C, float x, float y, float ex, float ey,
                                               float dx, float dy, float lxy, const GeoK& g) {
   PcylRoot r;
@@ -750,10 +754,10 @@ __device__ __forceinline__ PcylRoot pcyl_test(const float4 C, float x, float y, 
   if constexpr (WALL != kPermeate) {
     const float fx = ex - C.x, fy = ey - C.y;
     const float d2 = fx * fx + fy * fy;
-    r.end_in = d2 < R2 && (!g.mi || (min_image(fx, g) && min_image(fy, g)));
+    r.end_in = d2 < R2 && (!(MI && g.mi) || (min_image(fx, g) && min_image(fy, g)));
   }
   const float qx = x - C.x, qy = y - C.y;
-  const bool mi_ok = !g.mi || (min_image(qx, g) && min_image(qy, g));
+  const bool mi_ok = !(MI && g.mi) || (min_image(qx, g) && min_image(qy, g));
   const float dp = dx * qx + dy * qy;
   const float q2 = qx * qx + qy * qy;
   r.disc = dp * dp - (q2 - R2);
@@ -855,6 +859,7 @@ __device__ __forceinline__ void pcyl_hit(float x, float y, float sx, float sy, f
 // Fold-first safety clamp (geometries.py:1851-1877): push (nxp, nyp) out of the candidate it
 // penetrates most deeply (relative to R^2).  The start cell's list covers every object within
 // reach of the end point.
+template <bool MI = true>
 __device__ __forceinline__ void pcyl_clamp(float& nxp, float& nyp, uint32_t kb, uint32_t ke,
                                            const GeoK& g, const float4* __restrict__ cand,
                                            Tally& tl) {
@@ -862,7 +867,7 @@ __device__ __forceinline__ void pcyl_clamp(float& nxp, float& nyp, uint32_t kb, 
   auto pen_of = [&](const float4 C) {
     const float qx = nxp - C.x, qy = nyp - C.y;
     const float d2 = qx * qx + qy * qy, R2 = C.w * C.w;
-    if (d2 < R2 && (!g.mi || (min_image(qx, g) && min_image(qy, g)))) {
+    if (d2 < R2 && (!(MI && g.mi) || (min_image(qx, g) && min_image(qy, g)))) {
       const float pen = d2 / R2;
       if (pen < pe) {
         pe = pen;
@@ -906,8 +911,8 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
   float tbest = INFINITY, disc_hit = 0.f, hcx = 0.f, hcy = 0.f, hR = 1.f;
   bool hit_in = false, end_in = false;
   const float ex = x + sx, ey = y + sy;
-  auto visit = [&](const float4 C) {
-    const PcylRoot r = pcyl_test<WALL>(C, x, y, ex, ey, dx, dy, lxy, g);
+  auto visit = [&](const float4 C, auto mi) {
+    const PcylRoot r = pcyl_test<WALL, decltype(mi)::value>(C, x, y, ex, ey, dx, dy, lxy, g);
     end_in |= r.end_in;
     if (r.valid && r.t < tbest) {
       tbest = r.t;
@@ -918,16 +923,18 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
       hit_in = r.ins;
     }
   };
-  if (g.kmax == 2) {
-    // every cell lists at most two candidates: two slots for every lane, no divergent trip
-    // count; the slot past a shorter list holds a zero-radius object far outside the cell,
-    // which no test can select
+  // every cell lists at most two candidates and no two images of one object: two slots for every
+  // lane, no divergent trip count and no minimum-image tests; the slot past a shorter list holds
+  // a zero-radius object far outside the cell, which no test can select
+  const bool two = g.kmax == 2 && !g.mi;
+  if (two) {
 #pragma unroll
     for (uint32_t j = 0; j < 2u; ++j)
-      visit(kb + j < ke ? cand[kb + j] : make_float4(kFarAway, kFarAway, kFarAway, 0.f));
+      visit(kb + j < ke ? cand[kb + j] : make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+            std::false_type());
   } else {
 #pragma unroll 1
-    for (uint32_t k = kb; k < ke; ++k) visit(cand[k]);
+    for (uint32_t k = kb; k < ke; ++k) visit(cand[k], std::true_type());
   }
   if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR)
     pcyl_graze(x, y, dx, dy, lxy, hcx, hcy, hR, hit_in, g, tbest, disc_hit, tl);
@@ -937,7 +944,12 @@ __device__ __forceinline__ float packed_cyl_step(float& x, float& y, int& ix, in
     pcyl_hit<WALL>(x, y, sx, sy, dx, dy, lxy, u, tbest, disc_hit, hcx, hcy, hR, hit_in, g, tl,
                    nxp, nyp, dlog);
   if constexpr (WALL != kPermeate)
-    if (tbest < INFINITY || end_in) pcyl_clamp(nxp, nyp, kb, ke, g, cand, tl);
+    if (tbest < INFINITY || end_in) {
+      if (two)
+        pcyl_clamp<false>(nxp, nyp, kb, ke, g, cand, tl);
+      else
+        pcyl_clamp<true>(nxp, nyp, kb, ke, g, cand, tl);
+    }
   x = nxp;
   y = nyp;
   fold(x, ix, g);
