@@ -31,7 +31,8 @@ STATUS_WORDS = len(STATUS_NAMES)
 EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "dmsim_walk",
             "dmsim_walk_noalloc", "dmsim_step_kat", "dmsim_replay_workspace_bytes",
             "dmsim_replay", "dmsim_batch_create", "dmsim_batch_bind", "dmsim_batch_launch",
-            "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_pack",
+            "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_forward",
+            "dmsim_mlp_pack",
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
             "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes",
             "dmsim_bloch_workspace_bytes", "dmsim_bloch", "dmsim_bloch_mt_workspace_bytes",
@@ -151,6 +152,15 @@ class Gemm(C.Structure):
     ]
 
 
+class MlpFwd(C.Structure):
+    _fields_ = [
+        ("x", C.c_void_p), ("rows", C.c_int64), ("n_in", C.c_int32), ("depth", C.c_int32),
+        ("shift", C.c_void_p), ("scale", C.c_void_p), ("W", C.c_void_p * 8),
+        ("bias", C.c_void_p * 8), ("w_head", C.c_void_p), ("b_head", C.c_void_p),
+        ("y", C.c_void_p), ("err", C.c_void_p),
+    ]
+
+
 _lib = None
 
 
@@ -216,6 +226,8 @@ def load():
     vp, i32, i64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_float
     lib.dmsim_gemm_bf16.restype = C.c_int
     lib.dmsim_gemm_bf16.argtypes = [C.POINTER(Gemm), vp]
+    lib.dmsim_mlp_forward.restype = C.c_int
+    lib.dmsim_mlp_forward.argtypes = [C.POINTER(MlpFwd), vp]
     lib.dmsim_mlp_pack.restype = C.c_int
     lib.dmsim_mlp_pack.argtypes = [vp, i64, i32, i32, vp, vp, vp, vp, i64, vp]
     lib.dmsim_mlp_head.restype = C.c_int

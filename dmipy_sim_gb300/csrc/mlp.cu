@@ -130,14 +130,49 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// GELU with the exact normal CDF, and its derivative.
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) (Hendrycks and Gimpel,
+// "Gaussian Error Linear Units", 2016), with the tensor-core-era MUFU tanh (PTX tanh.approx.f32,
+// relative error about 2^-11, far below the bf16 rounding of the stored activations), and its
+// derivative 0.5 (1 + t) + 0.5 x (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 x^2).
+__device__ __forceinline__ float tanh_mufu(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2 / pi)
+constexpr float kGeluC1 = 0.044715f;
 __device__ __forceinline__ float gelu(float x) {
-  return 0.5f * x * (1.f + erff(x * 0.70710678118654752f));
+  const float x2 = x * x;
+  const float t = tanh_mufu(kGeluC0 * x * fmaf(kGeluC1, x2, 1.f));
+  const float hx = 0.5f * x;
+  return fmaf(hx, t, hx);
+}
+// GELU of two values at once (the fused forward pass's epilogue works on column pairs).
+__device__ __forceinline__ void gelu2(float a, float b, float& ya, float& yb) {
+  ya = gelu(a);
+  yb = gelu(b);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  const float x2 = x * x;
+  const float t = tanh_mufu(kGeluC0 * x * fmaf(kGeluC1, x2, 1.f));
+  const float du = kGeluC0 * fmaf(3.f * kGeluC1, x2, 1.f);
+  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * du;
 }
 
 struct GemmArgs {
@@ -396,6 +431,366 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// ---- fused forward pass -------------------------------------------------------------------------
+// The whole network on one 128-row tile of queries per step, on chip: the packed inputs and every
+// hidden layer's activations live in shared memory in the K-major, 128-byte-swizzled layout the
+// tensor core reads (the layout a TMA box of 64 bf16 columns writes: the 16-byte chunk c of row r
+// of a 64-column K slice sits at r * 128 + ((c ^ (r & 7)) * 16), 8-row groups 1024 bytes apart),
+// the accumulator of the current layer lives in tensor memory, and the weights stream from L2 by
+// TMA in 16 KB slices (128 output rows x 64 K columns).  Only the fp32 inputs are read from and
+// the fp32 outputs written to global memory.
+//   warp 0      TMA producer of the weight slices (a ring of kFwdStages), in the order the
+//               tensor core consumes them: per tile, per layer, per 64-wide K slice, both
+//               128-row halves of the output;
+//   warp 1      allocates 256 tensor-memory columns; one lane issues tcgen05.mma (M = 128,
+//               N = 128, K = 16) into the two 128-column halves of the accumulator, commits each
+//               weight slot back to the producer and each finished layer to the epilogue;
+//   warps 2..9  pack each tile's inputs ((x - shift) * scale as bf16), and after each layer read
+//               the accumulator (warp w owns tensor-memory lanes 32 (w % 4) .. + 31 = those tile
+//               rows, and one 128-column half), add the bias, apply GELU and write the next
+//               layer's operand back into shared memory; after the last layer they form the head
+//               y = H w + b (bf16-rounded activations, fp32 sums) and store y.
+// Two CTAs fit on an SM (about 103 KB of shared memory, 256 tensor-memory columns each), so one
+// CTA's epilogue overlaps the other's tensor-core work.  Every wait is bounded.
+constexpr int kFwdWidth = 256;
+constexpr int kFwdKp = 128;
+constexpr int kFwdMaxDepth = 8;
+constexpr int kFwdStages = 2;
+constexpr uint32_t kFwdSlice = 128 * BK * 2;       // 16 KB
+constexpr uint32_t kFwdAct = BM * kFwdWidth * 2;   // 64 KB: 4 K slices of 16 KB
+constexpr uint32_t kFwdBars = 256;  // mbarriers and flags, after the ring
+// then the parameters the epilogue reads as broadcasts: shift and scale (kFwdKp each), the head
+// weights (kFwdWidth) and each layer's bias (kFwdWidth)
+__host__ __device__ constexpr uint32_t fwd_smem(int depth) {
+  return kFwdAct + kFwdStages * kFwdSlice + kFwdBars + (2 * kFwdKp + kFwdWidth) * 4 +
+         (uint32_t)depth * kFwdWidth * 4;
+}
+constexpr int kFwdEpiWarps = 8;
+constexpr int kFwdThreads = 64 + 32 * kFwdEpiWarps;
+
+struct FwdArgs {
+  int64_t rows;
+  int n_in, depth;
+  const float* x;
+  const float* shift;
+  const float* scale;
+  const float* bias[kFwdMaxDepth];
+  const float* w_head;
+  const float* b_head;
+  float* y;
+  unsigned int* err;
+};
+struct FwdMaps {
+  CUtensorMap w[kFwdMaxDepth];
+};
+
+__device__ __forceinline__ uint32_t swz128(int r, int c16) {
+  return (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u + (uint32_t)((c16 ^ (r & 7)) * 16);
+}
+__device__ __forceinline__ void fence_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 2)
+    k_mlp_forward(const __grid_constant__ FwdMaps maps, const __grid_constant__ FwdArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* act = smem;
+  uint8_t* ring = smem + kFwdAct;
+  uint64_t* w_full = reinterpret_cast<uint64_t*>(ring + kFwdStages * kFwdSlice);
+  uint64_t* w_empty = w_full + kFwdStages;
+  uint64_t& acc_full = w_empty[kFwdStages];
+  uint64_t& act_ready = w_empty[kFwdStages + 1];
+  uint64_t& head_ready = w_empty[kFwdStages + 2];
+  uint32_t* flags = reinterpret_cast<uint32_t*>(&w_empty[kFwdStages + 3]);
+  uint32_t& tmem_slot = flags[0];
+  uint32_t& abort_flag = flags[1];
+  int& issued_s = reinterpret_cast<int&>(flags[2]);
+  int& consumed_s = reinterpret_cast<int&>(flags[3]);
+  int& committed_s = reinterpret_cast<int&>(flags[4]);
+  // the second column half's head partials (K slice 3 of the operand is free from the last
+  // layer's epilogue until the next tile's first epilogue)
+  float* head_part = reinterpret_cast<float*>(act + 3 * (BM * BK * 2));
+  float* s_shift = reinterpret_cast<float*>(ring + kFwdStages * kFwdSlice + kFwdBars);
+  float* s_scale = s_shift + kFwdKp;
+  float* s_whead = s_scale + kFwdKp;
+  float* s_bias = s_whead + kFwdWidth;  // [depth][kFwdWidth]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n_tiles = (g.rows + BM - 1) / BM;
+
+  if ((s_addr(smem) & 1023u) != 0u) {  // the swizzled layout needs 1024-byte alignment
+    if (threadIdx.x == 0) atomicAdd(g.err, 1u);
+    return;
+  }
+  for (int i = threadIdx.x; i < kFwdKp; i += blockDim.x) {
+    s_shift[i] = (g.shift && i < g.n_in) ? __ldg(g.shift + i) : 0.f;
+    s_scale[i] = (g.scale && i < g.n_in) ? __ldg(g.scale + i) : 1.f;
+  }
+  for (int i = threadIdx.x; i < kFwdWidth; i += blockDim.x) s_whead[i] = __ldg(g.w_head + i);
+  for (int l = 0; l < g.depth; ++l)
+    for (int i = threadIdx.x; i < kFwdWidth; i += blockDim.x)
+      s_bias[l * kFwdWidth + i] = __ldg(g.bias[l] + i);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kFwdStages; ++s) {
+      bar_init(&w_full[s], 1);
+      bar_init(&w_empty[s], 1);
+    }
+    bar_init(&acc_full, 1);
+    bar_init(&act_ready, kFwdEpiWarps);
+    bar_init(&head_ready, kFwdEpiWarps / 2);
+    abort_flag = 0;
+    issued_s = consumed_s = 0;
+    committed_s = -1;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     s_addr(&tmem_slot)),
+                 "r"(kFwdWidth)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  volatile uint32_t* abort_v = &abort_flag;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int q = 0;
+      for (int64_t tile = blockIdx.x; tile < n_tiles && !*abort_v; tile += gridDim.x) {
+        for (int l = 0; l < g.depth && !*abort_v; ++l) {
+          const int nk = (l == 0 ? kFwdKp : kFwdWidth) / BK;
+          for (int ks = 0; ks < nk; ++ks)
+            for (int nh = 0; nh < 2; ++nh, ++q) {
+              const int st = q % kFwdStages;
+              if (!bar_wait(&w_empty[st], ((q / kFwdStages) & 1) ^ 1)) {
+                *abort_v = 1;
+                goto producer_done;
+              }
+              bar_expect(&w_full[st], kFwdSlice);
+              tma_load_2d(ring + st * kFwdSlice, &maps.w[l], ks * BK, nh * 128, &w_full[st]);
+              issued_s = q + 1;
+            }
+        }
+      }
+    producer_done:;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = instr_desc(BM, 128);
+      int q = 0, layer_it = 0;
+      for (int64_t tile = blockIdx.x; tile < n_tiles && !*abort_v; tile += gridDim.x) {
+        for (int l = 0; l < g.depth; ++l, ++layer_it) {
+          if (!bar_wait(&act_ready, layer_it & 1)) {
+            *abort_v = 1;
+            goto mma_done;
+          }
+          tc_fence_after();
+          const int nk = (l == 0 ? kFwdKp : kFwdWidth) / BK;
+          for (int ks = 0; ks < nk; ++ks)
+            for (int nh = 0; nh < 2; ++nh, ++q) {
+              const int st = q % kFwdStages;
+              if (!bar_wait(&w_full[st], (q / kFwdStages) & 1)) {
+                *abort_v = 1;
+                tc_commit(&acc_full);
+                committed_s = layer_it;
+                goto mma_done;
+              }
+              tc_fence_after();
+              const uint32_t a0 = s_addr(act + ks * (BM * BK * 2));
+              const uint32_t b0 = s_addr(ring + st * kFwdSlice);
+#pragma unroll
+              for (int kk = 0; kk < BK / 16; ++kk)
+                mma_bf16(tmem + (uint32_t)(nh * 128), smem_desc(a0 + kk * 32),
+                         smem_desc(b0 + kk * 32), idesc, (ks > 0 || kk > 0) ? 1u : 0u);
+              tc_commit(&w_empty[st]);
+              consumed_s = q + 1;
+            }
+          tc_commit(&acc_full);
+          committed_s = layer_it;
+        }
+      }
+    mma_done:;
+    }
+  } else {
+    // epilogue warps: tile rows 32 * (warp % 4) + lane, accumulator / operand columns
+    // [128 * half, 128 * half + 128)
+    const int quarter = warp & 3, half = (warp - 2) >> 2;
+    const int r = quarter * 32 + lane;
+    const uint32_t t_row = tmem + ((uint32_t)(quarter * 32) << 16);
+    int layer_it = 0, tile_it = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++tile_it) {
+      const int64_t row = tile * BM + r;
+      // ---- pack the inputs: the two warps of each lane quarter read its 32 rows (one contiguous
+      // run of 32 n_in floats) with coalesced loads, 36 in flight per lane, normalise them and
+      // scatter them as bf16 into K slices 0 and 1 of the operand; the first-half warp writes
+      // the zero padding of columns n_in .. 127 (addresses no scattered value touches)
+      {
+        const int64_t row0 = tile * BM + quarter * 32;
+        const int nrow = (int)(g.rows - row0 < 32 ? (g.rows - row0 > 0 ? g.rows - row0 : 0) : 32);
+        if (half == 0) {
+          const bool live = lane < nrow;
+          for (int c = g.n_in; c < kFwdKp; ++c) {
+            if ((c & 7) == 0 && c + 8 <= kFwdKp) {  // a whole 16-byte chunk of padding
+              *reinterpret_cast<uint4*>(act + (c >> 6) * (BM * BK * 2) + swz128(r, (c & 63) >> 3)) =
+                  make_uint4(0u, 0u, 0u, 0u);
+              c += 7;
+              continue;
+            }
+            *reinterpret_cast<__nv_bfloat16*>(act + (c >> 6) * (BM * BK * 2) +
+                                              swz128(r, (c & 63) >> 3) + (c & 7) * 2) =
+                __float2bfloat16_rn(0.f);
+          }
+          if (!live) {  // rows past the end: zero inputs
+            for (int c = 0; c < g.n_in; ++c)
+              *reinterpret_cast<__nv_bfloat16*>(act + (c >> 6) * (BM * BK * 2) +
+                                                swz128(r, (c & 63) >> 3) + (c & 7) * 2) =
+                  __float2bfloat16_rn(0.f);
+          }
+        }
+        const int n = nrow * g.n_in;
+        const int e_lo = half * (n / 2), e_hi = half ? n : n / 2;
+        const float* src = g.x + (size_t)row0 * g.n_in;
+        // row of element e: floor((e + 0.5) / n_in) in FP32 is exact for e < 32 * 128 (the
+        // fraction stays at least 0.5 / n_in >= 1/256 from an integer)
+        const float inv_n = 1.f / (float)g.n_in;
+        constexpr int kIn = 36;  // loads in flight per lane: a 69-input half-block in one trip
+        for (int e0 = e_lo; e0 < e_hi; e0 += 32 * kIn) {
+          float v0[kIn];
+#pragma unroll
+          for (int k = 0; k < kIn; ++k) {
+            const int e = e0 + lane + 32 * k;
+            v0[k] = e < e_hi ? __ldg(src + e) : 0.f;
+          }
+#pragma unroll
+          for (int k = 0; k < kIn; ++k) {
+            const int e = e0 + lane + 32 * k;
+            if (e < e_hi) {
+              const int rr = (int)(((float)e + 0.5f) * inv_n), c = e - rr * g.n_in;
+              const float v = (v0[k] - s_shift[c]) * s_scale[c];
+              *reinterpret_cast<__nv_bfloat16*>(act + (c >> 6) * (BM * BK * 2) +
+                                                swz128(quarter * 32 + rr, (c & 63) >> 3) +
+                                                (c & 7) * 2) = __float2bfloat16_rn(v);
+            }
+          }
+        }
+      }
+      fence_async_shared();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) bar_arrive(&act_ready);
+      float head = 0.f;
+      for (int l = 0; l < g.depth; ++l, ++layer_it) {
+        if (!bar_wait(&acc_full, layer_it & 1) || *abort_v) {
+          *abort_v = 1;
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const bool last = l == g.depth - 1;
+        const float* bl = s_bias + l * kFwdWidth;
+        if (last) {
+          // this CTA's next tile's inputs (one contiguous block): into L2 while the head runs
+          const int64_t nt = tile + gridDim.x;
+          if (nt < n_tiles) {
+            const int64_t e0 = nt * BM * g.n_in;
+            const int64_t e1 = min((nt + 1) * BM, g.rows) * g.n_in;
+            for (int64_t e = e0 + (int64_t)(threadIdx.x - 64) * 32; e < e1;
+                 e += (int64_t)32 * kFwdEpiWarps * 32)
+              asm volatile("prefetch.global.L2 [%0];" ::"l"(g.x + e));
+          }
+        }
+        // two 32-column loads in flight per wait; the second chunk is processed from registers
+        // while nothing is pending
+        uint32_t u[2][32];
+#pragma unroll 1
+        for (int cc = half * 128; cc < half * 128 + 128; cc += 64) {
+          tmem_ld32_nowait(t_row + (uint32_t)cc, u[0]);
+          tmem_ld32_nowait(t_row + (uint32_t)(cc + 32), u[1]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+          const int c0 = cc + 32 * hh;
+          float v[32];
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(u[hh][i]);
+#pragma unroll
+          for (int i = 0; i < 32; i += 4) {
+            const float4 b4 = *reinterpret_cast<const float4*>(bl + c0 + i);
+            gelu2(v[i] + b4.x, v[i + 1] + b4.y, v[i], v[i + 1]);
+            gelu2(v[i + 2] + b4.z, v[i + 3] + b4.w, v[i + 2], v[i + 3]);
+          }
+          if (last) {
+#pragma unroll
+            for (int i = 0; i < 32; i += 4) {
+              const float4 w4 = *reinterpret_cast<const float4*>(s_whead + c0 + i);
+              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i])), w4.x, head);
+              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i + 1])), w4.y, head);
+              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i + 2])), w4.z, head);
+              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i + 3])), w4.w, head);
+            }
+          } else {
+            uint8_t* base = act + (c0 >> 6) * (BM * BK * 2);
+            const int cs = (c0 & 63) >> 3;  // first 16-byte chunk of these 32 columns
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              uint32_t pk[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                const __nv_bfloat162 b = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
+                pk[j] = *reinterpret_cast<const uint32_t*>(&b);
+              }
+              *reinterpret_cast<uint4*>(base + swz128(r, cs + k)) =
+                  make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            }
+          }
+          }
+        }
+        if (!last) {
+          // the next layer's operand is in place and this layer's accumulator is read out
+          fence_async_shared();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) bar_arrive(&act_ready);
+        }
+      }
+      if (!ok) break;
+      // ---- head: the second half's partial sums reach the first half through shared memory
+      if (half == 1) {
+        head_part[r] = head;
+        __syncwarp();
+        if (lane == 0) bar_arrive(&head_ready);
+      } else {
+        if (!bar_wait(&head_ready, tile_it & 1)) {
+          *abort_v = 1;
+          break;
+        }
+        if (row < g.rows) g.y[row] = (head + head_part[r]) + __ldg(g.b_head);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (*abort_v) {
+    // drain before leaving: the weight loads still in flight, then the last committed MMAs
+    if (threadIdx.x == 0) {
+      atomicAdd(g.err, 1u);
+      for (int k = consumed_s; k < issued_s; ++k)
+        bar_wait(&w_full[k % kFwdStages], (k / kFwdStages) & 1);
+    }
+    if (warp == 1 && lane == 0 && committed_s >= 0) bar_wait(&acc_full, committed_s & 1);
+    __syncthreads();
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kFwdWidth)
+                 : "memory");
+  }
+}
+
 // ---- small kernels ------------------------------------------------------------------------------
 // Inputs (rows, F) fp32 -> (x - shift) * scale as bf16 (rows, Kp), zero padded; optional
 // transpose (Kp, ldt).
@@ -639,6 +1034,67 @@ int dmsim_gemm_bf16(const dmsim_gemm* g, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   return BN == 256 ? launch_gemm<256, 3>(ma, mb, a, g->M, g->N, splits, st)
                    : launch_gemm<128, 5>(ma, mb, a, g->M, g->N, splits, st);
+}
+
+int dmsim_mlp_forward(const dmsim_mlp_fwd* f, void* stream) {
+  if (!f || !f->x || !f->y || !f->w_head || !f->b_head || !f->err || f->rows < 0)
+    return err(DMSIM_EINVAL, "mlp_forward: null argument");
+  if (f->depth < 1 || f->depth > kFwdMaxDepth || f->n_in < 1 || f->n_in > kFwdKp)
+    return err(DMSIM_EINVAL, "mlp_forward: need 1 <= depth <= 8 and 1 <= n_in <= 128");
+  if ((uintptr_t)f->w_head & 15) return err(DMSIM_EINVAL, "mlp_forward: w_head not 16-byte aligned");
+  for (int l = 0; l < f->depth; ++l)
+    if (!f->W[l] || !f->bias[l] || ((uintptr_t)f->W[l] & 15) || ((uintptr_t)f->bias[l] & 15))
+      return err(DMSIM_EINVAL, "mlp_forward: missing or unaligned layer weights / bias");
+  if (f->rows == 0) return DMSIM_OK;
+  FwdMaps maps;
+  memset(&maps, 0, sizeof(maps));
+  for (int l = 0; l < f->depth; ++l) {
+    const int K = l == 0 ? kFwdKp : kFwdWidth;
+    if (!make_map(&maps.w[l], f->W[l], kFwdWidth, K, K, 128))
+      return err(DMSIM_ECUDA, "mlp_forward: tensor map encoding failed");
+  }
+  FwdArgs a;
+  memset(&a, 0, sizeof(a));
+  a.rows = f->rows;
+  a.n_in = f->n_in;
+  a.depth = f->depth;
+  a.x = f->x;
+  a.shift = f->shift;
+  a.scale = f->scale;
+  for (int l = 0; l < f->depth; ++l) a.bias[l] = f->bias[l];
+  a.w_head = f->w_head;
+  a.b_head = f->b_head;
+  a.y = f->y;
+  a.err = f->err;
+  const uint32_t smem = fwd_smem(f->depth);
+  static bool attr = false;
+  static int n_sm = 0;
+  if (!attr) {
+    if (cudaFuncSetAttribute((const void*)k_mlp_forward,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fwd_smem(kFwdMaxDepth)) != cudaSuccess ||
+        cudaFuncSetAttribute((const void*)k_mlp_forward,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+      return err(DMSIM_ECUDA, "mlp_forward: cudaFuncSetAttribute failed");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm < 1) n_sm = 1;
+    attr = true;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_mlp_forward,
+                                                    kFwdThreads, smem) != cudaSuccess ||
+      per_sm < 1)
+    return err(DMSIM_ECUDA, "mlp_forward: the kernel does not fit on an SM");
+  // the kernel is sized for two resident CTAs per SM (registers, shared and tensor memory); the
+  // occupancy query may count one under the default shared-memory carveout
+  const int64_t tiles = (f->rows + BM - 1) / BM;
+  const int64_t slots = (int64_t)2 * n_sm;
+  const int grid = (int)(tiles < slots ? tiles : slots);
+  k_mlp_forward<<<grid, kFwdThreads, smem, (cudaStream_t)stream>>>(maps, a);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? DMSIM_OK : err(DMSIM_ECUDA, cudaGetErrorString(e));
 }
 
 int dmsim_mlp_pack(const float* x, int64_t rows, int32_t features, int32_t kp, const float* shift,

@@ -1,8 +1,10 @@
 """The surrogate's multilayer perceptron on the GB300 tensor cores.
 
-``depth`` hidden layers of ``width`` units with GELU, a linear head to one output, bf16 weights
-and activations with fp32 accumulation, trained with AdamW on the mean squared error.  Every
-matrix product is ``dmsim_gemm_bf16`` (tcgen05, csrc/mlp.cu) with its epilogue fused:
+``depth`` hidden layers of ``width`` units with GELU (tanh form), a linear head to one output,
+bf16 weights and activations with fp32 accumulation, trained with AdamW on the mean squared
+error.  Inference (:meth:`MLP.predict`) is one launch of ``dmsim_mlp_forward``, the whole network
+per 128-row tile on chip.  In training every matrix product is ``dmsim_gemm_bf16`` (tcgen05,
+csrc/mlp.cu) with its epilogue fused:
 
 forward   H_l = gelu(X_l W_l^T + b_l)            BIAS_GELU (stores P_l and H_l^T when training)
 head      y = H_L w + b; dy = 2 (y - t) / B; dP_L = dy w gelu'(P_L)       dmsim_mlp_head
@@ -210,8 +212,39 @@ class MLP:
                                        p.numel(), p.numel(), hp, None, None, 1, s), "adamw")
 
     # ---- public -------------------------------------------------------------------------------
+    def fused(self):
+        """Whether :meth:`predict` runs the one-launch forward pass (width 256, up to 128
+        inputs, up to 8 layers)."""
+        return self.width == 256 and self.kp == 128 and self.depth <= 8
+
     def predict(self, x, chunk=1 << 20):
-        """y (B,) for inputs x (B, n_in) (numpy or tensor, fp32)."""
+        """y (B,) for inputs x (B, n_in) (numpy or tensor, fp32): the fused forward pass
+        (``dmsim_mlp_forward``: one launch, activations on chip) when the shape allows, else the
+        layer-by-layer GEMMs."""
+        x = torch.as_tensor(np.asarray(x, np.float32) if not torch.is_tensor(x) else x)
+        x = x.to(self.dev, torch.float32)
+        if self.fused():
+            return self.predict_fused(x)
+        return self.predict_layers(x, chunk)
+
+    def predict_fused(self, x, out=None):
+        """The one-launch forward pass on a contiguous fp32 device tensor x (B, n_in)."""
+        x = x.contiguous()
+        y = torch.empty(len(x), device=self.dev) if out is None else out
+        f = _lib.MlpFwd()
+        f.x, f.rows, f.n_in, f.depth = x.data_ptr(), len(x), self.n_in, self.depth
+        f.shift, f.scale = self.shift.data_ptr(), self.scale.data_ptr()
+        for l in range(self.depth):
+            f.W[l] = self.Wb[l].data_ptr()
+            f.bias[l] = self.b[l].data_ptr()
+        f.w_head, f.b_head = self.w_head.data_ptr(), self.b_head.data_ptr()
+        f.y, f.err = y.data_ptr(), self.err.data_ptr()
+        _lib.check(self.lib.dmsim_mlp_forward(ctypes.byref(f), _lib.stream_handle()),
+                   "dmsim_mlp_forward")
+        return y
+
+    def predict_layers(self, x, chunk=1 << 20):
+        """The forward pass as layer-by-layer tensor-core GEMMs (the training path)."""
         x = torch.as_tensor(np.asarray(x, np.float32) if not torch.is_tensor(x) else x)
         x = x.to(self.dev, torch.float32)
         out = torch.empty(len(x), device=self.dev)

@@ -558,6 +558,31 @@ typedef struct dmsim_gemm {
 
 int dmsim_gemm_bf16(const dmsim_gemm* g, void* stream);
 
+/* The surrogate's whole forward pass in one launch (no counterpart in the reference: the learned
+   surrogate is this project's own): y = head(gelu(... gelu(pack(x) W_0^T + b_0) ...)) for depth
+   hidden layers of width 256 (GELU in its tanh form), on 128-row tiles kept on chip -- packed
+   inputs and activations in shared memory, the accumulator in tensor memory, the bf16 weights
+   streamed from L2 by TMA.  x (rows, n_in) fp32 with n_in <= 128, normalised as
+   (x - shift) * scale (either may be NULL) and zero padded to 128 columns; W[0] bf16 (256, 128),
+   W[l > 0] bf16 (256, 256), all 16-byte aligned; bias[l] and w_head fp32 (256), 16-byte
+   aligned; b_head one fp32 value in device memory; y (rows) fp32.  A tensor-core pipeline that
+   stalls past its bounded waits adds 1 to *err (device memory). */
+typedef struct dmsim_mlp_fwd {
+  const float* x;
+  int64_t rows;
+  int32_t n_in, depth;
+  const float* shift;
+  const float* scale;
+  const void* W[8];
+  const float* bias[8];
+  const float* w_head;
+  const float* b_head;
+  float* y;
+  uint32_t* err;
+} dmsim_mlp_fwd;
+
+int dmsim_mlp_forward(const dmsim_mlp_fwd* f, void* stream);
+
 /* Input packing: out[r, c] = bf16((x[r, c] - shift[c]) * scale[c]) for c < features, 0 up to kp;
    out_t (kp, ldt) is the optional transpose.  shift / scale may be NULL. */
 int dmsim_mlp_pack(const float* x, int64_t rows, int32_t features, int32_t kp, const float* shift,

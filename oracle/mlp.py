@@ -11,13 +11,8 @@ import math
 
 import numpy as np
 
-_SQRT1_2 = 1.0 / math.sqrt(2.0)
-_INV_SQRT_2PI = 1.0 / math.sqrt(2.0 * math.pi)
-
-try:
-    from scipy.special import erf as _erf
-except ImportError:                      # pragma: no cover
-    _erf = np.vectorize(math.erf)
+_C0 = math.sqrt(2.0 / math.pi)
+_C1 = 0.044715
 
 
 def bf16(x):
@@ -29,11 +24,13 @@ def bf16(x):
 
 
 def gelu(p):
-    return 0.5 * p * (1.0 + _erf(p * _SQRT1_2))
+    """GELU in its tanh form: 0.5 p (1 + tanh(sqrt(2/pi) (p + 0.044715 p^3)))."""
+    return 0.5 * p * (1.0 + np.tanh(_C0 * (p + _C1 * p ** 3)))
 
 
 def gelu_grad(p):
-    return 0.5 * (1.0 + _erf(p * _SQRT1_2)) + p * _INV_SQRT_2PI * np.exp(-0.5 * p * p)
+    t = np.tanh(_C0 * (p + _C1 * p ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * p * (1.0 - t * t) * _C0 * (1.0 + 3.0 * _C1 * p * p)
 
 
 def pack(x, kp, shift=None, scale=None):

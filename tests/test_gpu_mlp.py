@@ -70,7 +70,7 @@ def test_gemm_bias_gelu_and_transpose(cuda):
     np.testing.assert_allclose(P, p_ref, rtol=1e-5, atol=1e-4)
     H = out["H"].float().cpu().numpy()
     h_ref = OM.bf16(OM.gelu(P.astype(np.float64)).astype(np.float32))
-    # the kernel's erff and the oracle's erf may round one bf16 step apart
+    # the kernel's MUFU tanh and the oracle's tanh may round one bf16 step apart
     np.testing.assert_allclose(H, h_ref, rtol=8e-3, atol=1e-6)
     assert np.mean(H == h_ref) > 0.99
     HT = out["HT"].float().cpu().numpy()
@@ -109,6 +109,47 @@ def test_mlp_forward_matches_oracle(cuda):
     y = net.predict(x).cpu().numpy()
     Ws, bs, wh, bh = _oracle_params(net)
     y_ref, _ = OM.forward(OM.pack(x, net.kp), Ws, bs, wh, bh)
+    np.testing.assert_allclose(y, y_ref, atol=2e-2 * np.std(y_ref) + 1e-3)
+    assert np.corrcoef(y, y_ref)[0, 1] > 0.9999
+
+
+def _randomise(net, seed):
+    g = torch.Generator().manual_seed(seed)
+    for b in net.b:
+        b.copy_(torch.randn(b.shape, generator=g) * 0.3)
+    net.b_head.copy_(torch.randn(1, generator=g))
+    net.set_normalisation(np.linspace(-0.5, 0.5, net.n_in), np.linspace(0.5, 2.0, net.n_in))
+
+
+@pytest.mark.parametrize("rows", [1, 127, 128, 129, 4099, 300_001])
+def test_fused_forward_matches_the_layer_by_layer_pass(cuda, rows):
+    """The one-launch forward pass (activations on chip) against the four GEMMs + head on the
+    same bf16 weights: the two differ only in fp32 summation order, which can flip a bf16
+    rounding of an activation now and then."""
+    net = _net(5)
+    _randomise(net, 6)
+    assert net.fused()
+    x = torch.as_tensor(np.random.default_rng(7).normal(size=(rows, 69)).astype(np.float32),
+                        device=cuda)
+    y_f = net.predict_fused(x).cpu().numpy()
+    y_l = net.predict_layers(x).cpu().numpy()
+    torch.cuda.synchronize()
+    net.check_errors()
+    assert np.all(np.isfinite(y_f))
+    np.testing.assert_allclose(y_f, y_l, atol=2e-3 * np.std(y_l) + 2e-3)
+    if rows > 1000:
+        assert np.corrcoef(y_f, y_l)[0, 1] > 0.99999
+
+
+def test_fused_forward_matches_oracle_with_biases(cuda):
+    net = _net(8)
+    _randomise(net, 9)
+    x = np.random.default_rng(10).normal(size=(2000, 69)).astype(np.float32)
+    y = net.predict_fused(torch.as_tensor(x, device=cuda)).cpu().numpy()
+    net.check_errors()
+    Ws, bs, wh, bh = _oracle_params(net)
+    xs = OM.pack(x, net.kp, net.shift.cpu().numpy(), net.scale.cpu().numpy())
+    y_ref, _ = OM.forward(xs, Ws, bs, wh, bh)
     np.testing.assert_allclose(y, y_ref, atol=2e-2 * np.std(y_ref) + 1e-3)
     assert np.corrcoef(y, y_ref)[0, 1] > 0.9999
 
