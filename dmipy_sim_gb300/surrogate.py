@@ -5,8 +5,9 @@ relaxivity, diffusivity -- plus a 64-number waveform encoding (the dephasing q(t
 times, along and across the cylinder axis; :func:`substrates.q_encoding`) to one signal, with the
 tensor-core MLP of :mod:`mlp` (4 x 256 GELU, bf16 weights, fp32 accumulation, AdamW).
 
-Scope: packed parallel cylinders (the axis is the encoding's reference axis), with the parameters
-inside the hull it was trained on (:data:`HULL`) and echo times up to ``t_max``.  Every query
+Scope: one surrogate per substrate kind -- packed parallel cylinders (the axis is the encoding's
+reference axis) and packed spheres -- with the parameters inside the hull it was trained on
+(:data:`HULLS`) and echo times up to ``t_max``.  Every query
 outside the hull -- another substrate kind, a parameter out of range, a longer waveform -- is
 answered by the batched Monte-Carlo walk (:meth:`Surrogate.signals` does the routing), and the
 same walk at 1e6 walkers is what the surrogate's error on held-out substrates is measured against.
@@ -23,8 +24,20 @@ from .mlp import MLP
 
 N_Q = 32
 T_MAX = 0.08
-HULL = {"radius": (0.5e-6, 5e-6), "f": (0.3, 0.70), "kappa": (0.0, 1e-4), "rho": (0.0, 5e-6),
-        "D": (1e-9, 3e-9), "TE": (0.03, 0.08), "b": (0.0, 3e9)}
+# the training hull of each substrate kind a surrogate exists for (the batched study's ranges;
+# random sequential addition of a few spheres jams near f = 0.38)
+HULLS = {
+    "PackedCylinders": {"radius": (0.5e-6, 5e-6), "f": (0.3, 0.70), "kappa": (0.0, 1e-4),
+                        "rho": (0.0, 5e-6), "D": (1e-9, 3e-9), "TE": (0.03, 0.08),
+                        "b": (0.0, 3e9)},
+    "PackedSpheres": {"radius": (0.5e-6, 5e-6), "f": (0.2, 0.38), "kappa": (0.0, 1e-4),
+                      "rho": (0.0, 5e-6), "D": (1e-9, 3e-9), "TE": (0.03, 0.08),
+                      "b": (0.0, 3e9)},
+}
+HULL = HULLS["PackedCylinders"]
+# objects per training substrate: enough that one packing's signal is close to the mean over
+# packings of the same radius and volume fraction
+N_OBJECTS = {"PackedCylinders": 64, "PackedSpheres": 27}
 # substrate inputs in natural units (um, 1, 1e-5 m/s, 1e-6 m/s, 1e-9 m^2/s)
 _UNITS = np.array([1e6, 1.0, 1e5, 1e6, 1e9])
 
@@ -51,11 +64,12 @@ def features(params, wf, form="dimensionless"):
     return np.concatenate([np.repeat(sub[None, :], len(q), 0), q], axis=1).astype(np.float32)
 
 
-def in_hull(params, wf=None):
-    if params.get("kind", "PackedCylinders") != "PackedCylinders":
+def in_hull(params, wf=None, kind="PackedCylinders"):
+    if params.get("kind", "PackedCylinders") != kind or kind not in HULLS:
         return False
+    hull = HULLS[kind]
     for k in ("radius", "f", "kappa", "rho", "D"):
-        lo, hi = HULL[k]
+        lo, hi = hull[k]
         if not (lo <= params[k] <= hi):
             return False
     if wf is not None and (np.asarray(wf.G).shape[1] - 1) * wf.dt > T_MAX:
@@ -63,34 +77,35 @@ def in_hull(params, wf=None):
     return True
 
 
-def draw_instances(n, seed, n_meas=256, n_t=200, n_walkers=8192, n_objects=64,
-                   radius_sampling="uniform"):
-    """``n`` packed-cylinder instances with parameters uniform in the hull and free waveform
+def draw_instances(n, seed, n_meas=256, n_t=200, n_walkers=8192, n_objects=None,
+                   radius_sampling="uniform", kind="PackedCylinders"):
+    """``n`` packed instances of ``kind`` with parameters uniform in its hull and free waveform
     sets of ``n_meas`` measurements; returns (instances, params).  Each substrate holds
-    ``n_objects`` cylinders, enough that one packing's signal is close to the mean over packings
-    of the same radius and volume fraction (the 5 substrate inputs do not name the packing).
-    ``radius_sampling="mixture"`` draws half the radii log-uniformly instead, putting more
-    substrates at small radii, where the signal changes fastest with the parameters."""
+    ``n_objects`` objects (default :data:`N_OBJECTS`), enough that one packing's signal is close
+    to the mean over packings of the same radius and volume fraction (the 5 substrate inputs do
+    not name the packing).  ``radius_sampling="mixture"`` draws half the radii log-uniformly
+    instead, putting more substrates at small radii, where the signal changes fastest with the
+    parameters."""
     rng = np.random.default_rng(int(seed))
     insts, params = [], []
-    lo, hi = HULL["radius"]
+    hull = HULLS[kind]
+    n_objects = N_OBJECTS[kind] if n_objects is None else int(n_objects)
+    lo, hi = hull["radius"]
     for i in range(n):
         if radius_sampling == "mixture" and rng.uniform() < 0.5:
             r = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
         else:
             r = rng.uniform(lo, hi)
-        f = rng.uniform(*HULL["f"])
-        kappa = rng.uniform(*HULL["kappa"])
-        rho = rng.uniform(*HULL["rho"])
-        D = rng.uniform(*HULL["D"])
-        te = rng.uniform(*HULL["TE"])
-        wf, _, _, _ = S.free_waveform_set(n_meas, n_t, te, rng, b_max=HULL["b"][1])
-        geom, fa = S.packed_substrate("PackedCylinders", r, f, rng, n_objects=n_objects, rho=rho,
-                                      kappa=kappa)
+        f = rng.uniform(*hull["f"])
+        kappa = rng.uniform(*hull["kappa"])
+        rho = rng.uniform(*hull["rho"])
+        D = rng.uniform(*hull["D"])
+        te = rng.uniform(*hull["TE"])
+        wf, _, _, _ = S.free_waveform_set(n_meas, n_t, te, rng, b_max=hull["b"][1])
+        geom, fa = S.packed_substrate(kind, r, f, rng, n_objects=n_objects, rho=rho, kappa=kappa)
         radius = float(np.mean(geom._radii_np))
         insts.append(Instance(int(n_walkers), D, wf, geom, seed=int(rng.integers(1, 2 ** 62))))
-        params.append(dict(kind="PackedCylinders", radius=radius, f=fa, kappa=kappa, rho=rho,
-                           D=D, TE=te))
+        params.append(dict(kind=kind, radius=radius, f=fa, kappa=kappa, rho=rho, D=D, TE=te))
     return insts, params
 
 
@@ -118,11 +133,14 @@ def monte_carlo(insts, tuning=None, chunk=256, log=None):
 
 class Surrogate:
     def __init__(self, width=256, depth=4, seed=0, lr=1e-3, weight_decay=1e-5,
-                 form="dimensionless"):
+                 form="dimensionless", kind="PackedCylinders"):
+        if kind not in HULLS:
+            raise ValueError(f"no surrogate hull for {kind!r}")
         self.net = MLP(5 + 2 * N_Q, width=width, depth=depth, seed=seed, lr=lr,
                        weight_decay=weight_decay)
         self.lr0 = lr
         self.form = form
+        self.kind = kind
 
     # ---- training -----------------------------------------------------------------------------
     def fit(self, X, y, epochs=40, batch=8192, val=None, log=None, seed=0):
@@ -173,7 +191,7 @@ class Surrogate:
         feats, owners = [], []
         for i, (inst, p) in enumerate(zip(instances, params)):
             wf = inst.waveform.waveform if hasattr(inst.waveform, "waveform") else inst.waveform
-            ok = in_hull(p, wf)
+            ok = in_hull(p, wf, self.kind)
             flags.append(ok)
             if ok:
                 feats.append(features(p, wf, self.form))
@@ -198,13 +216,15 @@ class Surrogate:
                             **{f"b{l}": b.numpy() for l, b in enumerate(sd["b"])},
                             w_head=sd["w_head"].numpy(), b_head=sd["b_head"].numpy(),
                             shift=sd["shift"].numpy(), scale=sd["scale"].numpy(),
-                            shape=np.array(sd["shape"]), form=np.array(self.form))
+                            shape=np.array(sd["shape"]), form=np.array(self.form),
+                            kind=np.array(self.kind))
 
     @classmethod
     def load(cls, path):
         z = np.load(path)
         n_in, width, depth = (int(x) for x in z["shape"])
-        s = cls(width=width, depth=depth, form=str(z["form"]) if "form" in z else "raw")
+        s = cls(width=width, depth=depth, form=str(z["form"]) if "form" in z else "raw",
+                kind=str(z["kind"]) if "kind" in z else "PackedCylinders")
         sd = {"W": [torch.as_tensor(z[f"W{l}"]) for l in range(depth)],
               "b": [torch.as_tensor(z[f"b{l}"]) for l in range(depth)],
               "w_head": torch.as_tensor(z["w_head"]), "b_head": torch.as_tensor(z["b_head"]),
@@ -214,11 +234,12 @@ class Surrogate:
 
 
 def build_training_set(n_instances, seed=0, n_meas=256, n_t=200, n_walkers=8192, log=None,
-                       tuning=None, form="dimensionless", radius_sampling="uniform"):
+                       tuning=None, form="dimensionless", radius_sampling="uniform",
+                       kind="PackedCylinders"):
     """(X, y, se, params, GPU seconds) from ``n_instances`` batched-walk instances."""
     t0 = time.time()
     insts, params = draw_instances(n_instances, seed, n_meas, n_t, n_walkers,
-                                   radius_sampling=radius_sampling)
+                                   radius_sampling=radius_sampling, kind=kind)
     if log is not None:
         log(f"  drew {n_instances} instances in {time.time() - t0:.1f} s")
     sig, se, gpu_s = monte_carlo(insts, tuning, log=log)
@@ -226,5 +247,5 @@ def build_training_set(n_instances, seed=0, n_meas=256, n_t=200, n_walkers=8192,
     return X, np.concatenate(sig), np.concatenate(se), params, gpu_s
 
 
-__all__ = ["Surrogate", "HULL", "features", "in_hull", "draw_instances", "monte_carlo",
-           "build_training_set"]
+__all__ = ["Surrogate", "HULL", "HULLS", "N_OBJECTS", "features", "in_hull", "draw_instances",
+           "monte_carlo", "build_training_set"]

@@ -1,5 +1,5 @@
-"""Train the packed-cylinder surrogate from batched Monte-Carlo signals and judge it against the
-walk at high walker counts on held-out substrates.
+"""Train a packed-substrate surrogate (``--kind``: cylinders or spheres) from batched Monte-Carlo
+signals and judge it against the walk at high walker counts on held-out substrates.
 
     python -m dmipy_sim_gb300.train_surrogate --instances 20000 --out surrogate.npz
 
@@ -34,6 +34,7 @@ def main(argv=None):
     ap.add_argument("--form", default="dimensionless", choices=["dimensionless", "raw"])
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--radius-sampling", default="mixture", choices=["uniform", "mixture"])
+    ap.add_argument("--kind", default="PackedCylinders", choices=sorted(SG.HULLS))
     ap.add_argument("--out", default="surrogate.npz")
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
@@ -46,12 +47,13 @@ def main(argv=None):
     X, y, se, params, gpu_train_mc = SG.build_training_set(a.instances, a.seed, a.meas,
                                                            n_walkers=a.walkers, log=log,
                                                            form=a.form,
-                                                           radius_sampling=a.radius_sampling)
+                                                           radius_sampling=a.radius_sampling,
+                                                           kind=a.kind)
     log(f"  {len(y)} signals, median SE {np.median(se):.4f}, MC {gpu_train_mc:.1f} GPU s")
     # validation split: the last 5 % of instances
     n_val = max(1, a.instances // 20) * a.meas
     Xtr, ytr, Xva, yva = X[:-n_val], y[:-n_val], X[-n_val:], y[-n_val:]
-    sur = SG.Surrogate(seed=a.seed, lr=a.lr, form=a.form)
+    sur = SG.Surrogate(seed=a.seed, lr=a.lr, form=a.form, kind=a.kind)
     t1 = time.time()
     hist = sur.fit(Xtr, ytr, epochs=a.epochs, batch=a.batch, val=(Xva, yva), log=log)
     torch.cuda.synchronize()
@@ -61,7 +63,7 @@ def main(argv=None):
 
     # judge: held-out substrates at high walker counts
     insts, hp = SG.draw_instances(a.held_out, a.seed + 10_000, a.judge_meas,
-                                  n_walkers=a.judge_walkers)
+                                  n_walkers=a.judge_walkers, kind=a.kind)
     ref, ref_se, gpu_judge = SG.monte_carlo(insts, chunk=8, log=log)
     Xh = np.concatenate([SG.features(p, i.waveform, a.form) for p, i in zip(hp, insts)])
     pred = sur.predict(Xh)
@@ -80,7 +82,8 @@ def main(argv=None):
     e1.synchronize()
     sur_s = e0.elapsed_time(e1) * 1e-3
     rep = {
-        "instances": a.instances, "signals": int(len(y)), "walkers": a.walkers, "form": a.form,
+        "kind": a.kind, "instances": a.instances, "signals": int(len(y)), "walkers": a.walkers,
+        "form": a.form,
         "radius_sampling": a.radius_sampling,
         "train_mc_gpu_s": gpu_train_mc, "train_s": train_s, "epochs": a.epochs,
         "final_train_mse": hist[-1][0], "val_mae_vs_training_mc": hist[-1][1],
