@@ -13,35 +13,46 @@ from dmipy_sim_gb300 import surrogate as SG
 from dmipy_sim_gb300.batched import Instance
 
 pytestmark = pytest.mark.gpu
-WEIGHTS = Path(__file__).resolve().parent.parent / "dmipy_sim_gb300" / "data" / \
-    "surrogate_packed_cylinders.npz"
+DATA = Path(__file__).resolve().parent.parent / "dmipy_sim_gb300" / "data"
+WEIGHTS = DATA / "surrogate_packed_cylinders.npz"
+KINDS = {"PackedCylinders": DATA / "surrogate_packed_cylinders.npz",
+         "PackedSpheres": DATA / "surrogate_packed_spheres.npz"}
+
+
+def _load(kind):
+    if not KINDS[kind].exists():
+        pytest.skip(f"no trained {kind} surrogate weights")
+    return SG.Surrogate.load(KINDS[kind])
 
 
 @pytest.fixture(scope="module")
 def sur(cuda):
-    if not WEIGHTS.exists():
-        pytest.skip("no trained surrogate weights")
-    return SG.Surrogate.load(WEIGHTS)
+    return _load("PackedCylinders")
 
 
-@pytest.fixture(scope="module")
-def held_out(cuda):
-    # substrates drawn from a seed the training set never used, walked at 2e5 walkers
-    insts, params = SG.draw_instances(6, 777, n_meas=48, n_walkers=200_000)
+def _held_out(kind, n_walkers):
+    # substrates drawn from a seed the training set never used
+    insts, params = SG.draw_instances(6, 777, n_meas=48, n_walkers=n_walkers, kind=kind)
     sig, se, gpu_s = SG.monte_carlo(insts)
     return insts, params, np.concatenate(sig), np.concatenate(se), gpu_s
 
 
-def test_surrogate_error_on_held_out_substrates(sur, held_out):
-    insts, params, ref, se, _ = held_out
-    X = np.concatenate([SG.features(p, i.waveform, sur.form) for p, i in zip(params, insts)])
-    err = np.abs(sur.predict(X) - ref)
-    # the walk's own noise at 2e5 walkers (median SE) sits inside the measured error
-    assert np.median(se) < 0.003
-    # the training report's judge (24 substrates at 1e6 walkers) measured MAE 0.0047; six
-    # substrates at 2e5 walkers carry more sampling noise, hence the margin
-    assert err.mean() < 0.008, (err.mean(), np.percentile(err, 95))
-    assert np.percentile(err, 95) < 0.03
+@pytest.fixture(scope="module")
+def held_out(cuda):
+    return _held_out("PackedCylinders", 200_000)
+
+
+@pytest.mark.parametrize("kind", sorted(KINDS))
+def test_surrogate_error_on_held_out_substrates(cuda, kind):
+    """Mean absolute error at most 0.005 against the walk at 1e6 walkers (whose own standard
+    error, ~6e-4, is a small part of it) on six substrates the training never saw."""
+    s = _load(kind)
+    insts, params, ref, se, _ = _held_out(kind, 1_000_000)
+    X = np.concatenate([SG.features(p, i.waveform, s.form) for p, i in zip(params, insts)])
+    err = np.abs(s.predict(X) - ref)
+    assert np.median(se) < 0.0015
+    assert err.mean() <= 0.005, (kind, err.mean(), np.percentile(err, 95))
+    assert np.percentile(err, 95) < 0.03, (kind, err.mean(), np.percentile(err, 95))
 
 
 def test_surrogate_gain_over_the_walk(sur, held_out):
