@@ -416,7 +416,9 @@ def profile_case(a):
               dt 20 us) in a 2 um sphere, 131,072 walkers x 1251 samples x 38 sub-steps, FP64
               magnetisation, no burn-in (times the sequence walk alone);
     rbloch    the vector-Bloch replay of a stored float16 walk, 262,144 walkers x 500 samples,
-              4 measurements, a spin echo with T2 and T1 (FP64)."""
+              4 measurements, a spin echo with T2 and T1 (FP64);
+    free_flight / lockstep   the permeable 16x16 lattice (kappa = 2e-5 m/s, 461 sub-steps per
+              sample, 64 measurements) at 20,000 walkers in either packed-cylinder schedule."""
     import dataclasses
     import torch
     import dmipy_sim_gb300 as d
@@ -511,6 +513,15 @@ def profile_case(a):
                 walk = core.PreparedWalk(g, n_walkers=8192, diffusivity=D, G=G, dt=wf.dt,
                                          sub_steps=Sm, phase_per_substep=True, seed=5)
             walk.launch()
+        elif a.profile_case in ("free_flight", "lockstep"):
+            if _ == 0:
+                geom, wf, api, _n, T2, engine, _st = leg_workloads()["c3_lattice_kappa2e-5"]
+                G, chi, Sk, fused, echo = _leg_plan(geom, wf, api, engine)
+                walk = core.PreparedWalk(geom, n_walkers=20_000, diffusivity=D, G=G, dt=wf.dt,
+                                         sub_steps=Sk, phase_per_substep=fused, seed=77,
+                                         chi=chi, schedule=a.profile_case)
+                extra = {"walker_steps_per_launch": 20_000 * G.shape[1] * Sk}
+            walk.launch()
         elif a.profile_case == "mlp":
             if _ == 0:
                 from dmipy_sim_gb300.mlp import MLP
@@ -531,6 +542,8 @@ def profile_case(a):
     ms = e0.elapsed_time(e1) / max(1, a.steps)
     if a.profile_case == "bloch":
         extra["bloch_walker_steps_per_s"] = extra["walker_steps_per_launch"] / (ms * 1e-3)
+    if a.profile_case in ("free_flight", "lockstep"):
+        extra["walker_steps_per_s"] = extra["walker_steps_per_launch"] / (ms * 1e-3)
     print(json.dumps(dict({"profile_case": a.profile_case, "ok": True, "ms_per_step": ms},
                           **extra)))
 
@@ -721,7 +734,8 @@ def main():
                          "every signal's standard error below 0.005)")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per GPU (smaller only for profiling captures)")
-    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched", "bloch", "mt", "rbloch"],
+    ap.add_argument("--profile-case", choices=["mesh", "mlp", "batched", "bloch", "mt", "rbloch",
+                                               "free_flight", "lockstep"],
                     default=None,
                     help="run one small kernel case for a profiler capture and exit")
     a = ap.parse_args()
