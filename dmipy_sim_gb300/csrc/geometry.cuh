@@ -714,7 +714,7 @@ __device__ __forceinline__ void fold(float& v, int& img, const GeoK& g) {
 }
 
 // Packed cylinders (2-D cross-section; z is free).  The step is assembled from the pieces below
-// (shared with the cooperative kernel of walk_coop.cuh, which runs them in separate phases):
+// (shared with the free-flight kernel of walk_ff.cuh, which runs them in separate stages):
 //   pcyl_dir     step length and unit direction in the cross-section;
 //   pcyl_test    one candidate's entry root and straight-end containment (geometries.py:1777-1805
 //                / 2054-2081 for the root, 1851-1877 for the containment);
