@@ -623,56 +623,43 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
     bool ok = true;
     for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++tile_it) {
       const int64_t row = tile * BM + r;
-      // ---- pack the inputs: the two warps of each lane quarter read its 32 rows (one contiguous
-      // run of 32 n_in floats) with coalesced loads, 36 in flight per lane, normalise them and
-      // scatter them as bf16 into K slices 0 and 1 of the operand; the first-half warp writes
-      // the zero padding of columns n_in .. 127 (addresses no scattered value touches)
+      // ---- pack the inputs: the two warps of each lane quarter take 16 of its 32 rows each;
+      // lane l owns columns l, l + 32, l + 64, l + 96, so every load reads 32 consecutive floats
+      // of one row and every store lands in one 128-byte row of the operand; columns from n_in
+      // to 127 and rows past the end are written as zeros
       {
-        const int64_t row0 = tile * BM + quarter * 32;
-        const int nrow = (int)(g.rows - row0 < 32 ? (g.rows - row0 > 0 ? g.rows - row0 : 0) : 32);
-        if (half == 0) {
-          const bool live = lane < nrow;
-          for (int c = g.n_in; c < kFwdKp; ++c) {
-            if ((c & 7) == 0 && c + 8 <= kFwdKp) {  // a whole 16-byte chunk of padding
-              *reinterpret_cast<uint4*>(act + (c >> 6) * (BM * BK * 2) + swz128(r, (c & 63) >> 3)) =
-                  make_uint4(0u, 0u, 0u, 0u);
-              c += 7;
-              continue;
-            }
-            *reinterpret_cast<__nv_bfloat16*>(act + (c >> 6) * (BM * BK * 2) +
-                                              swz128(r, (c & 63) >> 3) + (c & 7) * 2) =
-                __float2bfloat16_rn(0.f);
-          }
-          if (!live) {  // rows past the end: zero inputs
-            for (int c = 0; c < g.n_in; ++c)
-              *reinterpret_cast<__nv_bfloat16*>(act + (c >> 6) * (BM * BK * 2) +
-                                                swz128(r, (c & 63) >> 3) + (c & 7) * 2) =
-                  __float2bfloat16_rn(0.f);
-          }
+        const int64_t row_base = tile * BM + quarter * 32 + half * 16;
+        float sh[4], sc[4];
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+          const int c = 32 * gq + lane;
+          sh[gq] = s_shift[c];
+          sc[gq] = s_scale[c];
         }
-        const int n = nrow * g.n_in;
-        const int e_lo = half * (n / 2), e_hi = half ? n : n / 2;
-        const float* src = g.x + (size_t)row0 * g.n_in;
-        // row of element e: floor((e + 0.5) / n_in) in FP32 is exact for e < 32 * 128 (the
-        // fraction stays at least 0.5 / n_in >= 1/256 from an integer)
-        const float inv_n = 1.f / (float)g.n_in;
-        constexpr int kIn = 36;  // loads in flight per lane: a 69-input half-block in one trip
-        for (int e0 = e_lo; e0 < e_hi; e0 += 32 * kIn) {
-          float v0[kIn];
+#pragma unroll 1
+        for (int r0 = 0; r0 < 16; r0 += 8) {
+          float v[8][4];
 #pragma unroll
-          for (int k = 0; k < kIn; ++k) {
-            const int e = e0 + lane + 32 * k;
-            v0[k] = e < e_hi ? __ldg(src + e) : 0.f;
+          for (int rr = 0; rr < 8; ++rr) {
+            const int64_t row = row_base + r0 + rr;
+#pragma unroll
+            for (int gq = 0; gq < 4; ++gq) {
+              const int c = 32 * gq + lane;
+              v[rr][gq] = (row < g.rows && c < g.n_in) ? __ldg(g.x + (size_t)row * g.n_in + c)
+                                                        : 0.f;
+            }
           }
 #pragma unroll
-          for (int k = 0; k < kIn; ++k) {
-            const int e = e0 + lane + 32 * k;
-            if (e < e_hi) {
-              const int rr = (int)(((float)e + 0.5f) * inv_n), c = e - rr * g.n_in;
-              const float v = (v0[k] - s_shift[c]) * s_scale[c];
+          for (int rr = 0; rr < 8; ++rr) {
+            const int64_t row = row_base + r0 + rr;
+            const int rt = quarter * 32 + half * 16 + r0 + rr;
+#pragma unroll
+            for (int gq = 0; gq < 4; ++gq) {
+              const int c = 32 * gq + lane;
+              const float val = (row < g.rows && c < g.n_in) ? (v[rr][gq] - sh[gq]) * sc[gq] : 0.f;
               *reinterpret_cast<__nv_bfloat16*>(act + (c >> 6) * (BM * BK * 2) +
-                                                swz128(quarter * 32 + rr, (c & 63) >> 3) +
-                                                (c & 7) * 2) = __float2bfloat16_rn(v);
+                                                swz128(rt, (c & 63) >> 3) + (c & 7) * 2) =
+                  __float2bfloat16_rn(val);
             }
           }
         }
