@@ -395,11 +395,15 @@ def surrogate_measure(dev, mc_signals_per_s):
            "speedup_vs_batched_mc": (1e6 / sec) / mc_signals_per_s if mc_signals_per_s else None,
            "forward": "fused (one launch)" if sur.net.fused() else "layer by layer",
            "gpu_launches_per_query_batch": 1 if sur.net.fused() else sur.net.depth + 2}
+    keys = ("held_out_instances", "held_out_signals", "judge_walkers", "mae", "p95_abs_err",
+            "max_abs_err", "signals")
     if SURROGATE_REPORT.exists():
         rep = json.loads(SURROGATE_REPORT.read_text())
-        out["held_out"] = {k: rep.get(k) for k in ("held_out_instances", "held_out_signals",
-                                                   "judge_walkers", "mae", "p95_abs_err",
-                                                   "max_abs_err", "signals")}
+        out["held_out"] = {k: rep.get(k) for k in keys}
+    sph = SURROGATE.parent / "surrogate_packed_spheres.json"
+    if sph.exists():   # the packed-sphere surrogate's training report (same network and judge)
+        rep = json.loads(sph.read_text())
+        out["packed_spheres_held_out"] = {k: rep.get(k) for k in keys}
     return out
 
 
