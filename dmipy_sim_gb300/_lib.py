@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 9
+DMSIM_ABI_VERSION = 10
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 9
+#define DMSIM_ABI_VERSION 10
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0

@@ -40,9 +40,9 @@ CONFIGS = {
     "c2_sph_kappa": dict(geom=("c2_sph",), wf=("c2_pgse30",), api="simulate", engine="auto",
                          n=48_000, chunk=4_000),
     "c3_lattice_auto": dict(geom=("lattice16", None), wf=("bench64",), api="simulate",
-                            engine="auto", n=40_000, chunk=2_000),
+                            engine="auto", n=80_000, chunk=2_000),
     "c3_lattice_kappa": dict(geom=("lattice16", 2e-5), wf=("lat_short",), api="simulate",
-                             engine="auto", n=24_000, chunk=2_000),
+                             engine="auto", n=42_000, chunk=2_000),
     "c3_lattice_cpmg": dict(geom=("lattice16", None), wf=("cpmg16",), api="cpmg", T2=0.08,
                             n=48_000, chunk=4_000),
 }

@@ -53,7 +53,8 @@ def _c_layout(struct, fields):
                                           ("dmsim_bloch_params", "BlochParams"),
                                           ("dmsim_mt_params", "MtParams"),
                                           ("dmsim_replay_bloch_params", "ReplayBlochParams"),
-                                          ("dmsim_gemm", "Gemm")])
+                                          ("dmsim_gemm", "Gemm"),
+                                          ("dmsim_mlp_fwd", "MlpFwd")])
 def test_struct_layout_matches_header(cname, pyname):
     from dmipy_sim_gb300 import _lib
     py = getattr(_lib, pyname)

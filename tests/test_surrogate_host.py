@@ -51,6 +51,25 @@ def test_hull_routing_rules():
     assert not SG.in_hull(p, long_wf)
 
 
+def test_each_surrogate_routes_only_its_own_kind():
+    ps = dict(kind="PackedSpheres", radius=2e-6, f=0.3, kappa=1e-5, rho=1e-6, D=2e-9)
+    assert SG.in_hull(ps, kind="PackedSpheres")
+    assert not SG.in_hull(ps)                                   # the cylinder surrogate's hull
+    assert not SG.in_hull({**ps, "f": 0.5}, kind="PackedSpheres")   # beyond what RSA packs
+    assert not SG.in_hull(ps, kind="Mesh")
+    with pytest.raises(ValueError):
+        SG.Surrogate.__init__(object.__new__(SG.Surrogate), kind="Mesh")
+
+
+def test_sphere_training_instances_are_drawn_in_their_hull():
+    insts, params = SG.draw_instances(4, 5, n_meas=8, n_walkers=64, kind="PackedSpheres")
+    for inst, p in zip(insts, params):
+        assert type(inst.geometry).__name__ == "PackedSpheres"
+        assert len(inst.geometry._radii_np) == SG.N_OBJECTS["PackedSpheres"]
+        assert p["kind"] == "PackedSpheres"
+        assert SG.in_hull(p, inst.waveform, kind="PackedSpheres") or p["f"] < 0.2
+
+
 def test_instance_mix_is_seeded_and_in_range():
     a, pa = S.instance_mix(12, seed=3, kinds=("PackedCylinders", "PackedSpheres"))
     b, pb = S.instance_mix(12, seed=3, kinds=("PackedCylinders", "PackedSpheres"))
