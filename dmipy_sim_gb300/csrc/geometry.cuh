@@ -977,44 +977,53 @@ __device__ __forceinline__ float packed_sph_step(float& x, float& y, float& z, i
   bool hit_in = false;
   const float ex = x + sx, ey = y + sy, ez = z + sz;
   float pe = 1.f, pqx = 0.f, pqy = 0.f, pqz = 0.f, pR = 1.f;
+  // the candidate scan, compiled twice: with the minimum-image tests, and without them for cell
+  // lists that never list two images of one object (g.mi == 0, where the tests always pass)
+  auto scan = [&](auto mi_c) {
+    constexpr bool MI = decltype(mi_c)::value;
 #pragma unroll 1
-  for (uint32_t k = kb; k < ke; ++k) {
-    const float4 C = cand[k];
-    const float R2 = C.w * C.w;
-    if constexpr (WALL != kPermeate) {
-      const float fx = ex - C.x, fy = ey - C.y, fz = ez - C.z;
-      const float d2 = fx * fx + fy * fy + fz * fz;
-      if (d2 < R2 && (!g.mi || (min_image(fx, g) && min_image(fy, g) && min_image(fz, g)))) {
-        const float pen = d2 / R2;
-        if (pen < pe) {
-          pe = pen;
-          pqx = fx;
-          pqy = fy;
-          pqz = fz;
-          pR = C.w;
+    for (uint32_t k = kb; k < ke; ++k) {
+      const float4 C = cand[k];
+      const float R2 = C.w * C.w;
+      if constexpr (WALL != kPermeate) {
+        const float fx = ex - C.x, fy = ey - C.y, fz = ez - C.z;
+        const float d2 = fx * fx + fy * fy + fz * fz;
+        if (d2 < R2 && (!MI || (min_image(fx, g) && min_image(fy, g) && min_image(fz, g)))) {
+          const float pen = d2 / R2;
+          if (pen < pe) {
+            pe = pen;
+            pqx = fx;
+            pqy = fy;
+            pqz = fz;
+            pR = C.w;
+          }
         }
       }
+      const float qx = x - C.x, qy = y - C.y, qz = z - C.z;
+      if (MI && !(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
+      const float dp = dx * qx + dy * qy + dz * qz;
+      const float q2 = qx * qx + qy * qy + qz * qz;
+      float disc = dp * dp - (q2 - R2);
+      const bool ins = (WALL == kPermeate) && (q2 < R2);
+      if (!ins && dp >= 0.f) continue;
+      const float sq = sqrtf(fmaxf(disc, 0.f));
+      const float t = ins ? -dp + sq : -dp - sq;
+      const bool valid = (disc > 0.f) && (t > g.eps) && (t < l) && (l > 0.f);
+      if (valid && t < tbest) {
+        tbest = t;
+        disc_hit = disc;
+        hcx = C.x;
+        hcy = C.y;
+        hcz = C.z;
+        hR = C.w;
+        hit_in = ins;
+      }
     }
-    const float qx = x - C.x, qy = y - C.y, qz = z - C.z;
-    if (g.mi && !(min_image(qx, g) && min_image(qy, g) && min_image(qz, g))) continue;
-    const float dp = dx * qx + dy * qy + dz * qz;
-    const float q2 = qx * qx + qy * qy + qz * qz;
-    float disc = dp * dp - (q2 - R2);
-    const bool ins = (WALL == kPermeate) && (q2 < R2);
-    if (!ins && dp >= 0.f) continue;
-    const float sq = sqrtf(fmaxf(disc, 0.f));
-    const float t = ins ? -dp + sq : -dp - sq;
-    const bool valid = (disc > 0.f) && (t > g.eps) && (t < l) && (l > 0.f);
-    if (valid && t < tbest) {
-      tbest = t;
-      disc_hit = disc;
-      hcx = C.x;
-      hcy = C.y;
-      hcz = C.z;
-      hR = C.w;
-      hit_in = ins;
-    }
-  }
+  };
+  if (g.mi)
+    scan(std::true_type());
+  else
+    scan(std::false_type());
   if (tbest < INFINITY && disc_hit < kGrazeTol * hR * hR) {
     const double qxd = (double)(x - hcx), qyd = (double)(y - hcy), qzd = (double)(z - hcz);
     const double dpd = (double)dx * qxd + (double)dy * qyd + (double)dz * qzd;
