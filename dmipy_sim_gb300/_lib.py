@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 10
+DMSIM_ABI_VERSION = 11
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
@@ -34,7 +34,8 @@ EXPORTED = ("dmsim_version", "dmsim_last_error", "dmsim_walk_workspace_bytes", "
             "dmsim_batch_info", "dmsim_batch_destroy", "dmsim_gemm_bf16", "dmsim_mlp_forward",
             "dmsim_mlp_pack",
             "dmsim_mlp_head", "dmsim_rowdot_bf16", "dmsim_sum_f32", "dmsim_adamw",
-            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_project_modes",
+            "dmsim_adam_advance", "dmsim_mesh_neighbourhoods", "dmsim_mesh_hit_lists",
+            "dmsim_project_modes",
             "dmsim_bloch_workspace_bytes", "dmsim_bloch", "dmsim_bloch_mt_workspace_bytes",
             "dmsim_bloch_mt", "dmsim_replay_bloch_workspace_bytes", "dmsim_replay_bloch",
             "dmsim_fp32_fma_peak")
@@ -60,7 +61,8 @@ class Geometry(C.Structure):
         ("seed_inside", C.c_int32), ("pad1", C.c_int32),
         ("tri", C.c_void_p), ("tri_vn", C.c_void_p), ("mesh_cell_start", C.c_void_p),
         ("mesh_cell_tri", C.c_void_p), ("mesh_nb_start", C.c_void_p), ("mesh_nb_tri", C.c_void_p),
-        ("tri_bs", C.c_void_p),
+        ("tri_bs", C.c_void_p), ("mesh_hit_start", C.c_void_p), ("mesh_hit_tri", C.c_void_p),
+        ("mesh_hit_reach", C.c_float), ("mesh_hit_pad", C.c_int32),
         ("myelin_r_out", C.c_float), ("myelin_step", C.c_float * 3),
         ("myelin_kin_over_D", C.c_float * 3), ("myelin_kout_over_D", C.c_float * 3),
         ("myelin_t2dec", C.c_float * 3), ("myelin_logw0", C.c_float * 3),
@@ -240,6 +242,8 @@ def load():
     lib.dmsim_adamw.argtypes = [vp, vp, vp, vp, i32, i64, i32, vp, vp, vp, i32, vp]
     lib.dmsim_mesh_neighbourhoods.restype = C.c_int
     lib.dmsim_mesh_neighbourhoods.argtypes = [C.POINTER(Geometry), vp, vp, vp]
+    lib.dmsim_mesh_hit_lists.restype = C.c_int
+    lib.dmsim_mesh_hit_lists.argtypes = [C.POINTER(Geometry), C.c_float, vp, vp, vp]
     lib.dmsim_adam_advance.restype = C.c_int
     lib.dmsim_adam_advance.argtypes = [vp, vp]
     lib.dmsim_project_modes.restype = C.c_int

@@ -39,6 +39,9 @@ struct MeshK {
   const uint32_t* ctri;
   const uint32_t* nbstart;  // optional neighbourhood lists (see mesh_neighbourhood): one list
   const uint32_t* nbtri;    // per cell with the distinct triangles of its 27-cell gather
+  const uint32_t* hstart;   // optional hit lists (see mesh_hit_list): the neighbourhood list's
+  const uint32_t* htri;     // triangles within hreach of the cell, for the nearest-hit search
+  float hreach;
 };
 
 struct Tri {
@@ -109,6 +112,101 @@ __device__ __forceinline__ uint32_t mesh_neighbourhood(const uint32_t* __restric
       if (out) out[n] = t;
       ++n;
     }
+  }
+  return n;
+}
+
+// Separating-axis test of a triangle (vertices relative to the box centre) against the box of
+// half-extents h: false when a face axis of the box, the triangle's normal or one of the nine
+// edge x box-axis cross products separates them.  A zero axis (degenerate triangle) separates
+// nothing, so the test only errs towards overlap.
+__device__ __forceinline__ bool tri_box_overlap(const double (&v)[3][3], const double (&h)[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double lo = fmin(v[0][a], fmin(v[1][a], v[2][a]));
+    const double hi = fmax(v[0][a], fmax(v[1][a], v[2][a]));
+    if (lo > h[a] || hi < -h[a]) return false;
+  }
+  double e[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) e[i][a] = v[(i + 1) % 3][a] - v[i][a];
+  {
+    // the triangle's plane: normal e0 x (v2 - v0) = -(e0 x e2)
+    const double nx = e[2][1] * e[0][2] - e[2][2] * e[0][1];
+    const double ny = e[2][2] * e[0][0] - e[2][0] * e[0][2];
+    const double nz = e[2][0] * e[0][1] - e[2][1] * e[0][0];
+    const double d = nx * v[0][0] + ny * v[0][1] + nz * v[0][2];
+    const double r = fabs(nx) * h[0] + fabs(ny) * h[1] + fabs(nz) * h[2];
+    if (fabs(d) > r) return false;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      // axis = e_i x unit_a
+      double ax[3];
+      ax[a] = 0.0;
+      ax[(a + 1) % 3] = e[i][(a + 2) % 3];
+      ax[(a + 2) % 3] = -e[i][(a + 1) % 3];
+      const double p0 = ax[0] * v[0][0] + ax[1] * v[0][1] + ax[2] * v[0][2];
+      const double p1 = ax[0] * v[1][0] + ax[1] * v[1][1] + ax[2] * v[1][2];
+      const double p2 = ax[0] * v[2][0] + ax[1] * v[2][1] + ax[2] * v[2][2];
+      const double r = fabs(ax[0]) * h[0] + fabs(ax[1]) * h[1] + fabs(ax[2]) * h[2];
+      if (fmin(p0, fmin(p1, p2)) > r || fmax(p0, fmax(p1, p2)) < -r) return false;
+    }
+  }
+  return true;
+}
+
+// The hit list of grid cell `cid` for steps no longer than `reach`: the entries of its
+// neighbourhood list whose triangle overlaps the cell widened by reach + margin on every side.
+// A step starting in the cell keeps its path (every bounce and nudge included) within its length
+// of the start, so a triangle it can hit overlaps that box; the list keeps the neighbourhood
+// order, so the first of equal hits is the same triangle.  The cells on the grid's faces also hold
+// the positions clamped into the grid and keep their whole list.  Writes to `out` when given;
+// returns the length.
+__device__ __forceinline__ uint32_t mesh_hit_list(const uint32_t* __restrict__ nbs,
+                                                  const uint32_t* __restrict__ nbt,
+                                                  const float* __restrict__ tri, const int* dims,
+                                                  const float* gmin, float cs, float reach,
+                                                  int64_t cid, uint32_t* __restrict__ out) {
+  const int c[3] = {(int)(cid / ((int64_t)dims[1] * dims[2])), (int)((cid / dims[2]) % dims[1]),
+                    (int)(cid % dims[2])};
+  const uint32_t kb = nbs[cid], ke = nbs[cid + 1];
+  bool face = false;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) face |= c[a] == 0 || c[a] == dims[a] - 1;
+  // widening: the reach, a relative allowance for the length of a float32 step, and an absolute
+  // one far above the rounding of float32 positions, cell indices and hit points
+  const double w = (double)reach * 1.001 + 4e-9 + 1e-5 * (double)cs;
+  double ctr[3], h[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ctr[a] = (double)gmin[a] + ((double)c[a] + 0.5) * (double)cs;
+    h[a] = 0.5 * (double)cs + w;
+  }
+  uint32_t n = 0;
+#pragma unroll 1
+  for (uint32_t k = kb; k < ke; ++k) {
+    const uint32_t t = nbt[k];
+    bool keep = face;
+    if (!keep) {
+      const float* r = tri + 16 * (size_t)t;
+      double v[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double A = (double)r[a];
+        v[0][a] = A - ctr[a];
+        v[1][a] = A + (double)r[3 + a] - ctr[a];
+        v[2][a] = A + (double)r[6 + a] - ctr[a];
+      }
+      keep = tri_box_overlap(v, h);
+    }
+    if (!keep) continue;
+    if (out) out[n] = t;
+    ++n;
   }
   return n;
 }
@@ -327,16 +425,18 @@ __device__ __forceinline__ int scratch_owner(const MeshScratch* w, uint32_t j) {
 }
 
 __device__ __forceinline__ MeshHit mesh_nearest_coop(const MeshK& m, MeshScratch* w, bool need,
-                                                     float gx, float gy, float gz, float r0x,
-                                                     float r0y, float r0z, float dx, float dy,
-                                                     float dz, float rem) {
+                                                     bool hit_lists, float gx, float gy,
+                                                     float gz, float r0x, float r0y, float r0z,
+                                                     float dx, float dy, float dz, float rem) {
   const int lane = threadIdx.x & 31;
+  const uint32_t* __restrict__ lst = hit_lists ? m.hstart : m.nbstart;
+  const uint32_t* __restrict__ ltri = hit_lists ? m.htri : m.nbtri;
   uint32_t ls = 0, cnt = 0;
   if (need) {
     const int cid = (mesh_cell(gx, 0, m) * m.dims[1] + mesh_cell(gy, 1, m)) * m.dims[2] +
                     mesh_cell(gz, 2, m);
-    ls = m.nbstart[cid];
-    cnt = m.nbstart[cid + 1] - ls;
+    ls = lst[cid];
+    cnt = lst[cid + 1] - ls;
   }
   const uint32_t incl = warp_incl_scan(cnt, lane);
   const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
@@ -355,7 +455,7 @@ __device__ __forceinline__ MeshHit mesh_nearest_coop(const MeshK& m, MeshScratch
     if (j < total) {
       const int L = scratch_owner(w, j);
       const uint32_t pos = j - (L ? w->incl[L - 1] : 0u);
-      const uint32_t k = m.nbtri[w->ls[L] + pos];
+      const uint32_t k = ltri[w->ls[L] + pos];
       const float ox = w->rx[L], oy = w->ry[L], oz = w->rz[L];
       const float ux = w->dx[L], uy = w->dy[L], uz = w->dz[L], rm = w->rem[L];
       bool test = true;
@@ -379,7 +479,7 @@ __device__ __forceinline__ MeshHit mesh_nearest_coop(const MeshK& m, MeshScratch
   const unsigned long long b = w->best[lane];
   __syncwarp();
   if (need && b != ~0ull) {
-    const uint32_t k = m.nbtri[ls + (uint32_t)(b & 0xffffffffull)];
+    const uint32_t k = ltri[ls + (uint32_t)(b & 0xffffffffull)];
     const Tri T = load_tri(m, k);
     float u, v;
     h.t = mt_hit(T, r0x, r0y, r0z, dx, dy, dz, u, v);
@@ -440,6 +540,9 @@ __device__ __forceinline__ float mesh_step(float& x, float& y, float& z, int& ix
                                            MeshScratch* ws) {
   const bool coop = m.nbstart != nullptr;
   const float l = sqrtf(sx * sx + sy * sy + sz * sz);
+  // the hit lists serve the warp's searches when every lane's step is within their reach
+  const bool hit_lists =
+      coop && m.hstart != nullptr && __all_sync(0xffffffffu, l <= m.hreach);
   float dx = sx / l, dy = sy / l, dz = sz / l;
   float r0x = x, r0y = y, r0z = z, rem = l;
   float dsum = 0.f;
@@ -449,8 +552,8 @@ __device__ __forceinline__ float mesh_step(float& x, float& y, float& z, int& ix
 #pragma unroll 1
   for (int it = 0; it < m.maxb; ++it) {
     if (coop ? !__any_sync(0xffffffffu, active) : !active) break;
-    const MeshHit h = coop ? mesh_nearest_coop(m, ws, active, x, y, z, r0x, r0y, r0z, dx, dy,
-                                               dz, rem)
+    const MeshHit h = coop ? mesh_nearest_coop(m, ws, active, hit_lists, x, y, z, r0x, r0y,
+                                               r0z, dx, dy, dz, rem)
                            : mesh_nearest(m, x, y, z, r0x, r0y, r0z, dx, dy, dz, rem);
     if (!active) continue;
     const bool hit = h.t < INFINITY;

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 10
+#define DMSIM_ABI_VERSION 11
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -138,6 +138,14 @@ typedef struct dmsim_geometry {
                                       each triangle; a candidate whose sphere misses the step's
                                       segment is skipped before the Moller-Trumbore test.  The
                                       radius must cover the float32 vertices (it only prunes). */
+  const uint32_t* mesh_hit_start;  /* optional hit lists (NULL: the neighbourhood lists serve  */
+  const uint32_t* mesh_hit_tri;    /* the hit search too): per cell, the neighbourhood list's
+                                      triangles that come within mesh_hit_reach of the cell,
+                                      in the same order, from dmsim_mesh_hit_lists().  Used by
+                                      the nearest-hit search of a step no longer than the reach;
+                                      classification always reads the neighbourhood lists.    */
+  float mesh_hit_reach;            /* the reach (m) the hit lists were built for              */
+  int32_t mesh_hit_pad;
 
   /* myelinated cylinder (DMSIM_GEOM_MYELIN): compartments 0 intra-axonal (r < radius), 1 myelin
      (radius <= r < myelin_r_out), 2 extra-axonal, r the distance from the frame z axis.  Each
@@ -307,6 +315,18 @@ int dmsim_step_kat(const dmsim_geometry* g, int64_t n, const float* r_in, const 
    again with nb_tri of `total` entries. */
 int dmsim_mesh_neighbourhoods(const dmsim_geometry* g, uint32_t* nb_start, uint32_t* nb_tri,
                               void* stream);
+
+/* Hit lists of a mesh grid for steps no longer than `reach` (m): for each cell, the entries of its
+   neighbourhood list (g->mesh_nb_start / mesh_nb_tri, from dmsim_mesh_neighbourhoods) whose
+   triangle (g->tri: A, A + E1, A + E2) overlaps the cell's box widened on every side by reach
+   plus a rounding margin, by a separating-axis test in float64; the cells on the grid's faces
+   (which also hold the positions clamped into the grid) keep their whole list.  A step's path,
+   bounces included, stays within its length of its start, so every triangle the 27-cell gather
+   of mesh.py:208-215 could report as hit within the step is kept, in the gather's order.  Two
+   calls, as dmsim_mesh_neighbourhoods: with hit_tri == NULL the list lengths go to
+   hit_start[0 .. n_cells); then with the offsets in hit_start and hit_tri of `total` entries. */
+int dmsim_mesh_hit_lists(const dmsim_geometry* g, float reach, uint32_t* hit_start,
+                         uint32_t* hit_tri, void* stream);
 
 /* Replay operator on saved trajectories, trajectories.py:360-641 without relaxation terms:
    phi[m,w] = gamma_dt * sum_t G[t,m,:] . traj[w,t,:]  (trajectories.py:550-552) and

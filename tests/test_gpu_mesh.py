@@ -79,33 +79,43 @@ def test_mesh_sphere_matches_analytic_sphere(cuda):
     np.testing.assert_allclose(s_mesh, s_ana, atol=0.02)
 
 
-@pytest.mark.parametrize("mode", ["reflect", "perm"])
+@pytest.mark.parametrize("mode", ["reflect", "relax", "perm"])
 def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
-    """The per-cell neighbourhood lists (each candidate once) and the bounding-sphere pruning
-    walk exactly like the 27-cell gather that tests a triangle once per grid cell it overlaps."""
+    """The per-cell hit lists (candidates within the step's reach of the cell), the neighbourhood
+    lists (each candidate of the 27-cell gather once) and the bounding-sphere pruning walk exactly
+    like the 27-cell gather that tests a triangle once per grid cell it overlaps."""
     from dmipy_sim_gb300 import substrates as S
     mesh, _ = S.ellipsoid_cell_mesh(n_cells=8, faces_per_cell=600, box=24e-6,
                                     radius_range=(2e-6, 4e-6), permeable=mode == "perm")
-    g = mesh.with_walls(None, 1e-5 if mode == "perm" else None)
+    g = mesh.with_walls(2e-6 if mode == "relax" else None, 1e-5 if mode == "perm" else None)
     rng = np.random.default_rng(3)
     wf, _, _, _ = S.free_waveform_set(4, 40, 0.02, rng, n_shapes=1)
     G, _ = core._waveform_arrays(wf, g)
     S_ = core.fused_sub_steps(g, D, wf.dt)
+    if mode != "perm":
+        S_ *= 16    # steps of about a quarter of the grid cell, as permeable walls give
     res = []
-    for use_lists in (True, False):
+    for lists in ("hit", "neighbourhood", "none"):
         w = core.PreparedWalk(g, n_walkers=4096, diffusivity=D, G=G, dt=wf.dt, sub_steps=S_,
                               phase_per_substep=True, seed=9, want_positions=True,
                               want_walker_signals=True)
-        if not use_lists:
+        if lists == "hit":
+            assert w.gdesc.mesh_hit_start and w.gdesc.mesh_hit_reach >= w.p.step_length
+        if lists != "hit":
+            w.gdesc.mesh_hit_start = None
+            w.gdesc.mesh_hit_tri = None
+        if lists == "none":
             w.gdesc.mesh_nb_start = None
             w.gdesc.mesh_nb_tri = None
             w.gdesc.tri_bs = None
         w.launch()
         res.append(w.result())
     assert g.n_neighbourhood_entries < len(mesh._cell_tri) * 27
-    for k in ("pos", "phi", "log_w"):
-        assert np.array_equal(res[0].extras[k].cpu().numpy(), res[1].extras[k].cpu().numpy()), k
-    assert res[0].status == res[1].status
+    assert g.n_hit_entries < 0.7 * g.n_neighbourhood_entries
+    for r in res[1:]:
+        for k in ("pos", "phi", "log_w"):
+            assert np.array_equal(res[0].extras[k].cpu().numpy(), r.extras[k].cpu().numpy()), k
+        assert res[0].status == r.status
 
 
 def _inside_points(V, F, n, seed):
