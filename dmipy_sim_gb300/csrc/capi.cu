@@ -641,6 +641,7 @@ MeshK make_meshk(const dmsim_geometry* g) {
   if (g->mesh_nb_start && g->mesh_hit_start && g->mesh_hit_tri && g->mesh_hit_reach > 0.f) {
     m.hstart = g->mesh_hit_start;
     m.htri = g->mesh_hit_tri;
+    m.hbs = g->tri_bs ? reinterpret_cast<const float4*>(g->mesh_hit_bs) : nullptr;
     m.hreach = g->mesh_hit_reach;
   }
   return m;
@@ -663,16 +664,18 @@ __global__ void k_mesh_nb(const uint32_t* __restrict__ cs, const uint32_t* __res
 __global__ void k_mesh_hit(const uint32_t* __restrict__ nbs, const uint32_t* __restrict__ nbt,
                            const float* __restrict__ tri, int d0, int d1, int d2, float g0,
                            float g1, float g2, float cs, float reach,
-                           const uint32_t* __restrict__ start, uint32_t* __restrict__ out) {
+                           const uint32_t* __restrict__ start, uint32_t* __restrict__ out,
+                           const float4* __restrict__ bs, float4* __restrict__ out_bs) {
   const int dims[3] = {d0, d1, d2};
   const float gmin[3] = {g0, g1, g2};
   const int64_t n = (int64_t)d0 * d1 * d2;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
     if (start)
-      mesh_hit_list(nbs, nbt, tri, dims, gmin, cs, reach, c, out + start[c]);
+      mesh_hit_list(nbs, nbt, tri, dims, gmin, cs, reach, c, out + start[c], bs,
+                    out_bs ? out_bs + start[c] : nullptr);
     else
-      out[c] = mesh_hit_list(nbs, nbt, tri, dims, gmin, cs, reach, c, nullptr);
+      out[c] = mesh_hit_list(nbs, nbt, tri, dims, gmin, cs, reach, c, nullptr, nullptr, nullptr);
   }
 }
 
@@ -1140,7 +1143,9 @@ int dmsim_mesh_neighbourhoods(const dmsim_geometry* g, uint32_t* nb_start, uint3
 }
 
 int dmsim_mesh_hit_lists(const dmsim_geometry* g, float reach, uint32_t* hit_start,
-                         uint32_t* hit_tri, void* stream) {
+                         uint32_t* hit_tri, float* hit_bs, void* stream) {
+  if (hit_bs && (!hit_tri || !g || !g->tri_bs))
+    return fail(DMSIM_EINVAL, "mesh_hit_lists: hit_bs needs hit_tri and g->tri_bs");
   if (!g || !hit_start || !g->tri || !g->mesh_nb_start || !g->mesh_nb_tri ||
       g->mesh_dims[0] < 1 || g->mesh_dims[1] < 1 || g->mesh_dims[2] < 1 ||
       !(g->mesh_cell > 0.f) || !(reach > 0.f) || !isfinite(reach))
@@ -1150,7 +1155,8 @@ int dmsim_mesh_hit_lists(const dmsim_geometry* g, float reach, uint32_t* hit_sta
   k_mesh_hit<<<blocks, 256, 0, (cudaStream_t)stream>>>(
       g->mesh_nb_start, g->mesh_nb_tri, g->tri, g->mesh_dims[0], g->mesh_dims[1],
       g->mesh_dims[2], g->grid_min[0], g->grid_min[1], g->grid_min[2], g->mesh_cell, reach,
-      hit_tri ? hit_start : nullptr, hit_tri ? hit_tri : hit_start);
+      hit_tri ? hit_start : nullptr, hit_tri ? hit_tri : hit_start,
+      reinterpret_cast<const float4*>(g->tri_bs), reinterpret_cast<float4*>(hit_bs));
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess)
     return fail(DMSIM_ECUDA, "mesh_hit_lists launch failed: %s", cudaGetErrorString(err));

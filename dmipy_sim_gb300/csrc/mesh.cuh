@@ -41,6 +41,7 @@ struct MeshK {
   const uint32_t* nbtri;    // per cell with the distinct triangles of its 27-cell gather
   const uint32_t* hstart;   // optional hit lists (see mesh_hit_list): the neighbourhood list's
   const uint32_t* htri;     // triangles within hreach of the cell, for the nearest-hit search
+  const float4* hbs;        // optional: the hit-list entries' bounding spheres, in list order
   float hreach;
 };
 
@@ -171,7 +172,9 @@ __device__ __forceinline__ uint32_t mesh_hit_list(const uint32_t* __restrict__ n
                                                   const uint32_t* __restrict__ nbt,
                                                   const float* __restrict__ tri, const int* dims,
                                                   const float* gmin, float cs, float reach,
-                                                  int64_t cid, uint32_t* __restrict__ out) {
+                                                  int64_t cid, uint32_t* __restrict__ out,
+                                                  const float4* __restrict__ bs,
+                                                  float4* __restrict__ out_bs) {
   const int c[3] = {(int)(cid / ((int64_t)dims[1] * dims[2])), (int)((cid / dims[2]) % dims[1]),
                     (int)(cid % dims[2])};
   const uint32_t kb = nbs[cid], ke = nbs[cid + 1];
@@ -206,6 +209,7 @@ __device__ __forceinline__ uint32_t mesh_hit_list(const uint32_t* __restrict__ n
     }
     if (!keep) continue;
     if (out) out[n] = t;
+    if (out_bs) out_bs[n] = bs[t];
     ++n;
   }
   return n;
@@ -431,6 +435,7 @@ __device__ __forceinline__ MeshHit mesh_nearest_coop(const MeshK& m, MeshScratch
   const int lane = threadIdx.x & 31;
   const uint32_t* __restrict__ lst = hit_lists ? m.hstart : m.nbstart;
   const uint32_t* __restrict__ ltri = hit_lists ? m.htri : m.nbtri;
+  const float4* __restrict__ lbs = hit_lists ? m.hbs : nullptr;  // spheres in list order
   uint32_t ls = 0, cnt = 0;
   if (need) {
     const int cid = (mesh_cell(gx, 0, m) * m.dims[1] + mesh_cell(gy, 1, m)) * m.dims[2] +
@@ -455,12 +460,13 @@ __device__ __forceinline__ MeshHit mesh_nearest_coop(const MeshK& m, MeshScratch
     if (j < total) {
       const int L = scratch_owner(w, j);
       const uint32_t pos = j - (L ? w->incl[L - 1] : 0u);
-      const uint32_t k = ltri[w->ls[L] + pos];
+      const uint32_t li = w->ls[L] + pos;
+      const uint32_t k = ltri[li];
       const float ox = w->rx[L], oy = w->ry[L], oz = w->rz[L];
       const float ux = w->dx[L], uy = w->dy[L], uz = w->dz[L], rm = w->rem[L];
       bool test = true;
       if (m.bs != nullptr) {
-        const float4 b = __ldg(m.bs + k);
+        const float4 b = lbs != nullptr ? __ldg(lbs + li) : __ldg(m.bs + k);
         const float cx = b.x - ox, cy = b.y - oy, cz = b.z - oz;
         const float s = fminf(fmaxf(cx * ux + cy * uy + cz * uz, 0.f), rm);
         const float ex = cx - s * ux, ey = cy - s * uy, ez = cz - s * uz;

@@ -507,22 +507,24 @@ class Mesh(Geometry):
             g.grid_min[:] = [float(np.float32(x)) for x in self.grid_min]
             g.mesh_cell = float(np.float32(self.cell_size))
             g.tri = tt["tri"].data_ptr()
+            g.tri_bs = tt["bs"].data_ptr()
             g.mesh_nb_start = tt["nbs"].data_ptr()
             g.mesh_nb_tri = tt["nbt"].data_ptr()
             n_cells = int(np.prod(self.dims))
             dev = tt["tri"].device
             counts = torch.empty(n_cells + 1, dtype=torch.int32, device=dev)
             s = _lib.stream_handle()
-            _lib.check(lib.dmsim_mesh_hit_lists(g, reach, _lib.ptr(counts), None, s),
+            _lib.check(lib.dmsim_mesh_hit_lists(g, reach, _lib.ptr(counts), None, None, s),
                        "dmsim_mesh_hit_lists")
             start = torch.zeros(n_cells + 1, dtype=torch.int64, device=dev)
             start[1:] = torch.cumsum(counts[:n_cells].to(torch.int64), 0)
             total = int(start[-1].item())
             hs = start.to(torch.int32)
             ht = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
-            _lib.check(lib.dmsim_mesh_hit_lists(g, reach, _lib.ptr(hs), _lib.ptr(ht), s),
-                       "dmsim_mesh_hit_lists")
-            cache[reach] = (hs, ht, total)
+            hb = torch.empty((max(total, 1), 4), dtype=torch.float32, device=dev)
+            _lib.check(lib.dmsim_mesh_hit_lists(g, reach, _lib.ptr(hs), _lib.ptr(ht),
+                                                _lib.ptr(hb), s), "dmsim_mesh_hit_lists")
+            cache[reach] = (hs, ht, hb, total)
         return reach, cache[reach]
 
     def _desc(self, step_length, wall_mode, rho_over_D, kappa_over_D, dev):
@@ -556,9 +558,10 @@ class Mesh(Geometry):
         g.mesh_nb_tri = tt["nbt"].data_ptr()
         hl = self._hit_lists(tt, float(step_length)) if self.use_hit_lists else None
         if hl is not None:
-            reach, (hs, ht, total) = hl
+            reach, (hs, ht, hb, total) = hl
             g.mesh_hit_start = hs.data_ptr()
             g.mesh_hit_tri = ht.data_ptr()
+            g.mesh_hit_bs = hb.data_ptr()
             g.mesh_hit_reach = reach
             self.n_hit_entries = total
         return g, (tt,)

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 11
+#define DMSIM_ABI_VERSION 12
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -144,6 +144,8 @@ typedef struct dmsim_geometry {
                                       in the same order, from dmsim_mesh_hit_lists().  Used by
                                       the nearest-hit search of a step no longer than the reach;
                                       classification always reads the neighbourhood lists.    */
+  const float* mesh_hit_bs;        /* optional: tri_bs of each hit-list entry, in list order
+                                      (4 floats per entry), read beside the index             */
   float mesh_hit_reach;            /* the reach (m) the hit lists were built for              */
   int32_t mesh_hit_pad;
 
@@ -324,9 +326,10 @@ int dmsim_mesh_neighbourhoods(const dmsim_geometry* g, uint32_t* nb_start, uint3
    bounces included, stays within its length of its start, so every triangle the 27-cell gather
    of mesh.py:208-215 could report as hit within the step is kept, in the gather's order.  Two
    calls, as dmsim_mesh_neighbourhoods: with hit_tri == NULL the list lengths go to
-   hit_start[0 .. n_cells); then with the offsets in hit_start and hit_tri of `total` entries. */
+   hit_start[0 .. n_cells); then with the offsets in hit_start and hit_tri of `total` entries,
+   and hit_bs (4 x `total` floats, or NULL) for the entries' bounding spheres from g->tri_bs. */
 int dmsim_mesh_hit_lists(const dmsim_geometry* g, float reach, uint32_t* hit_start,
-                         uint32_t* hit_tri, void* stream);
+                         uint32_t* hit_tri, float* hit_bs, void* stream);
 
 /* Replay operator on saved trajectories, trajectories.py:360-641 without relaxation terms:
    phi[m,w] = gamma_dt * sum_t G[t,m,:] . traj[w,t,:]  (trajectories.py:550-552) and

@@ -81,9 +81,10 @@ def test_mesh_sphere_matches_analytic_sphere(cuda):
 
 @pytest.mark.parametrize("mode", ["reflect", "relax", "perm"])
 def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
-    """The per-cell hit lists (candidates within the step's reach of the cell), the neighbourhood
-    lists (each candidate of the 27-cell gather once) and the bounding-sphere pruning walk exactly
-    like the 27-cell gather that tests a triangle once per grid cell it overlaps."""
+    """The per-cell hit lists (candidates within the step's reach of the cell, with their bounding
+    spheres in list order or read by triangle index), the neighbourhood lists (each candidate of
+    the 27-cell gather once) and the bounding-sphere pruning walk exactly like the 27-cell gather
+    that tests a triangle once per grid cell it overlaps."""
     from dmipy_sim_gb300 import substrates as S
     mesh, _ = S.ellipsoid_cell_mesh(n_cells=8, faces_per_cell=600, box=24e-6,
                                     radius_range=(2e-6, 4e-6), permeable=mode == "perm")
@@ -95,13 +96,16 @@ def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
     if mode != "perm":
         S_ *= 16    # steps of about a quarter of the grid cell, as permeable walls give
     res = []
-    for lists in ("hit", "neighbourhood", "none"):
+    for lists in ("hit", "hit, spheres by index", "neighbourhood", "none"):
         w = core.PreparedWalk(g, n_walkers=4096, diffusivity=D, G=G, dt=wf.dt, sub_steps=S_,
                               phase_per_substep=True, seed=9, want_positions=True,
                               want_walker_signals=True)
-        if lists == "hit":
-            assert w.gdesc.mesh_hit_start and w.gdesc.mesh_hit_reach >= w.p.step_length
-        if lists != "hit":
+        if lists.startswith("hit"):
+            assert w.gdesc.mesh_hit_start and w.gdesc.mesh_hit_bs
+            assert w.gdesc.mesh_hit_reach >= w.p.step_length
+        if lists == "hit, spheres by index":
+            w.gdesc.mesh_hit_bs = None
+        if not lists.startswith("hit"):
             w.gdesc.mesh_hit_start = None
             w.gdesc.mesh_hit_tri = None
         if lists == "none":
