@@ -239,6 +239,19 @@ def _closed_surface(F):
     return bool(np.all(cnt == 2))
 
 
+def hit_reach(step_length, cell_size):
+    """The reach (a float32 value) of the hit lists that serve steps of ``step_length``: at least
+    1.001 x the step, rounded up to the ladder cell_size x 2^(q/16); None when that is not below
+    the cell size or the step is not a positive number."""
+    if not (step_length > 0.0) or not np.isfinite(step_length):
+        return None
+    q = int(np.ceil(16.0 * np.log2(step_length * 1.001 / cell_size)))
+    reach = float(np.float32(cell_size * 2.0 ** (q / 16.0)))
+    if reach < step_length * 1.001:
+        reach = float(np.nextafter(np.float32(step_length * 1.001), np.float32(np.inf)))
+    return reach if reach < cell_size else None
+
+
 class Mesh(Geometry):
     """Reflecting / relaxing / permeable triangle-mesh substrate (mesh.py:257-907).
 
@@ -490,14 +503,8 @@ class Mesh(Geometry):
         reach rounded up to a ladder of 1/16 octave steps from the grid cell, so that walks of
         similar step lengths share one set; None when the reach is not below the cell size (the
         neighbourhood lists then serve)."""
-        cs = float(self.cell_size)
-        if not (step_length > 0.0) or not np.isfinite(step_length):
-            return None
-        q = int(np.ceil(16.0 * np.log2(step_length * 1.001 / cs)))
-        reach = float(np.float32(cs * 2.0 ** (q / 16.0)))
-        if reach < step_length * 1.001:
-            reach = float(np.nextafter(np.float32(step_length * 1.001), np.float32(np.inf)))
-        if reach >= cs:
+        reach = hit_reach(step_length, float(self.cell_size))
+        if reach is None:
             return None
         cache = tt.setdefault("hit", {})
         if reach not in cache:

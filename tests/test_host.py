@@ -177,3 +177,28 @@ def test_tensor_encodings_and_invariants(kat):
     np.testing.assert_allclose(bd, kat["wf_inv_bdelta"], atol=1e-9)
     np.testing.assert_allclose(be, kat["wf_inv_beta"], atol=1e-9)
     assert abs(bd[0]) < 1e-6 and abs(bd[1] + 0.5) < 1e-6 and abs(bd[2] - 1.0) < 1e-6
+
+
+def test_mesh_hit_list_reach():
+    """The hit lists' reach covers the float32 step with the relative margin, lies on the
+    1/16-octave ladder of the grid cell (so that walks of similar steps share one set), and is
+    not used at or above the cell size (the neighbourhood lists then serve)."""
+    from dmipy_sim_gb300.mesh import hit_reach
+    cs = 3.2e-7
+    rng = np.random.default_rng(0)
+    for step in np.concatenate([rng.uniform(1e-9, 0.99 * cs / 1.001, 2000),
+                                [cs / 4, 0.2412 * cs, 0.25 * cs, cs / 1.001 * 0.999]]):
+        r = hit_reach(float(np.float32(step)), cs)
+        if r is None:
+            assert float(np.float32(step)) * 1.001 > cs * 2 ** (-1 / 16) * (1 - 1e-6)
+            continue
+        assert r == float(np.float32(r))
+        assert r >= float(np.float32(step)) * 1.001
+        assert r < cs
+        assert r <= max(float(np.float32(step)) * 1.001 * 2 ** (1 / 16) * (1 + 1e-6),
+                        float(np.nextafter(np.float32(step * 1.001), np.float32(np.inf))))
+    # the study's steps (a quarter of the grid cell, within 4 %) share at most two sets
+    steps = np.linspace(0.241, 0.2503, 100) * cs
+    assert len({hit_reach(float(s), cs) for s in steps}) <= 2
+    for bad in (0.0, -1.0, float("nan"), float("inf"), cs, 2 * cs):
+        assert hit_reach(bad, cs) is None
