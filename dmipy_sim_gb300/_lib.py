@@ -13,7 +13,7 @@ import torch
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdmsim.so"
 
-DMSIM_ABI_VERSION = 12
+DMSIM_ABI_VERSION = 13
 TILE_WALKERS = 320
 
 (GEOM_FREE, GEOM_CYLINDER, GEOM_SPHERE, GEOM_PACKED_CYLINDERS, GEOM_PACKED_SPHERES, GEOM_MESH,
@@ -62,7 +62,8 @@ class Geometry(C.Structure):
         ("tri", C.c_void_p), ("tri_vn", C.c_void_p), ("mesh_cell_start", C.c_void_p),
         ("mesh_cell_tri", C.c_void_p), ("mesh_nb_start", C.c_void_p), ("mesh_nb_tri", C.c_void_p),
         ("tri_bs", C.c_void_p), ("mesh_hit_start", C.c_void_p), ("mesh_hit_tri", C.c_void_p),
-        ("mesh_hit_bs", C.c_void_p), ("mesh_hit_reach", C.c_float), ("mesh_hit_pad", C.c_int32),
+        ("mesh_hit_bs", C.c_void_p), ("mesh_nb_cent", C.c_void_p), ("mesh_hit_reach", C.c_float),
+        ("mesh_hit_pad", C.c_int32),
         ("myelin_r_out", C.c_float), ("myelin_step", C.c_float * 3),
         ("myelin_kin_over_D", C.c_float * 3), ("myelin_kout_over_D", C.c_float * 3),
         ("myelin_t2dec", C.c_float * 3), ("myelin_logw0", C.c_float * 3),

@@ -638,6 +638,7 @@ MeshK make_meshk(const dmsim_geometry* g) {
   m.ctri = g->mesh_cell_tri;
   m.nbstart = g->mesh_nb_start;
   m.nbtri = g->mesh_nb_tri;
+  m.nbc = g->mesh_nb_start ? reinterpret_cast<const float4*>(g->mesh_nb_cent) : nullptr;
   if (g->mesh_nb_start && g->mesh_hit_start && g->mesh_hit_tri && g->mesh_hit_reach > 0.f) {
     m.hstart = g->mesh_hit_start;
     m.htri = g->mesh_hit_tri;

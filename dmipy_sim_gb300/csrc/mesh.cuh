@@ -42,6 +42,7 @@ struct MeshK {
   const uint32_t* hstart;   // optional hit lists (see mesh_hit_list): the neighbourhood list's
   const uint32_t* htri;     // triangles within hreach of the cell, for the nearest-hit search
   const float4* hbs;        // optional: the hit-list entries' bounding spheres, in list order
+  const float4* nbc;        // optional: the neighbourhood-list entries' centroids, in list order
   float hreach;
 };
 
@@ -518,8 +519,8 @@ __device__ __forceinline__ int mesh_classify_coop(const MeshK& m, MeshScratch* w
     if (j < total) {
       const int L = scratch_owner(w, j);
       const uint32_t pos = j - (L ? w->incl[L - 1] : 0u);
-      const uint32_t k = m.nbtri[w->ls[L] + pos];
-      const float4 c = m.tri[4 * k + 3];
+      const uint32_t li = w->ls[L] + pos;
+      const float4 c = m.nbc != nullptr ? __ldg(m.nbc + li) : m.tri[4 * m.nbtri[li] + 3];
       const float ddx = w->rx[L] - c.x, ddy = w->ry[L] - c.y, ddz = w->rz[L] - c.z;
       const float d = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
       atomicMin(&w->best[L], ((unsigned long long)__float_as_uint(d) << 32) | pos);

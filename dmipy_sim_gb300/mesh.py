@@ -496,6 +496,10 @@ class Mesh(Geometry):
         _lib.check(lib.dmsim_mesh_neighbourhoods(g, _lib.ptr(nb_start), _lib.ptr(nb_tri), s),
                    "dmsim_mesh_neighbourhoods")
         tt["nbs"], tt["nbt"] = nb_start, nb_tri
+        # each entry's centroid record in list order: the classification reads it beside the
+        # list position instead of through the triangle index
+        tt["nbc"] = tt["tri"][nb_tri.to(torch.int64), 12:16].contiguous() if total else \
+            torch.zeros((1, 4), dtype=torch.float32, device=dev)
         self.n_neighbourhood_entries = total
 
     def _hit_lists(self, tt, step_length):
@@ -563,6 +567,7 @@ class Mesh(Geometry):
         g.mesh_cell_tri = tt["ct"].data_ptr()
         g.mesh_nb_start = tt["nbs"].data_ptr()
         g.mesh_nb_tri = tt["nbt"].data_ptr()
+        g.mesh_nb_cent = tt["nbc"].data_ptr()
         hl = self._hit_lists(tt, float(step_length)) if self.use_hit_lists else None
         if hl is not None:
             reach, (hs, ht, hb, total) = hl

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define DMSIM_ABI_VERSION 12
+#define DMSIM_ABI_VERSION 13
 
 /* ---- error codes ---------------------------------------------------------------------------- */
 #define DMSIM_OK 0
@@ -146,6 +146,9 @@ typedef struct dmsim_geometry {
                                       classification always reads the neighbourhood lists.    */
   const float* mesh_hit_bs;        /* optional: tri_bs of each hit-list entry, in list order
                                       (4 floats per entry), read beside the index             */
+  const float* mesh_nb_cent;       /* optional: the centroid record (tri[16 k + 12 .. 16]) of
+                                      each neighbourhood-list entry, in list order, for the
+                                      nearest-centroid classification                         */
   float mesh_hit_reach;            /* the reach (m) the hit lists were built for              */
   int32_t mesh_hit_pad;
 

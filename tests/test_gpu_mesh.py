@@ -83,8 +83,9 @@ def test_mesh_sphere_matches_analytic_sphere(cuda):
 def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
     """The per-cell hit lists (candidates within the step's reach of the cell, with their bounding
     spheres in list order or read by triangle index), the neighbourhood lists (each candidate of
-    the 27-cell gather once) and the bounding-sphere pruning walk exactly like the 27-cell gather
-    that tests a triangle once per grid cell it overlaps."""
+    the 27-cell gather once, with the centroids the classification reads in list order or by
+    triangle index) and the bounding-sphere pruning walk exactly like the 27-cell gather that
+    tests a triangle once per grid cell it overlaps."""
     from dmipy_sim_gb300 import substrates as S
     mesh, _ = S.ellipsoid_cell_mesh(n_cells=8, faces_per_cell=600, box=24e-6,
                                     radius_range=(2e-6, 4e-6), permeable=mode == "perm")
@@ -96,7 +97,7 @@ def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
     if mode != "perm":
         S_ *= 16    # steps of about a quarter of the grid cell, as permeable walls give
     res = []
-    for lists in ("hit", "hit, spheres by index", "neighbourhood", "none"):
+    for lists in ("hit", "hit, spheres by index", "neighbourhood", "centroids by index", "none"):
         w = core.PreparedWalk(g, n_walkers=4096, diffusivity=D, G=G, dt=wf.dt, sub_steps=S_,
                               phase_per_substep=True, seed=9, want_positions=True,
                               want_walker_signals=True)
@@ -105,6 +106,8 @@ def test_neighbourhood_lists_give_the_27_cell_walk(cuda, mode):
             assert w.gdesc.mesh_hit_reach >= w.p.step_length
         if lists == "hit, spheres by index":
             w.gdesc.mesh_hit_bs = None
+        if lists == "centroids by index":
+            w.gdesc.mesh_nb_cent = None
         if not lists.startswith("hit"):
             w.gdesc.mesh_hit_start = None
             w.gdesc.mesh_hit_tri = None
