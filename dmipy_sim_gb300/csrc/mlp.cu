@@ -163,10 +163,44 @@ __device__ __forceinline__ float gelu(float x) {
   const float hx = 0.5f * x;
   return fmaf(hx, t, hx);
 }
-// GELU of two values at once (the fused forward pass's epilogue works on column pairs).
-__device__ __forceinline__ void gelu2(float a, float b, float& ya, float& yb) {
-  ya = gelu(a);
-  yb = gelu(b);
+// Two fp32 lanes in one 64-bit register and Blackwell's packed add / mul / fma on them: each
+// lane is an IEEE round-to-nearest fp32 operation, so a packed sequence gives exactly the
+// scalar sequence's results with half the instructions.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void up2(uint64_t r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// gelu(a + ba), gelu(b + bb) by the same operations as gelu() on each lane
+__device__ __forceinline__ void gelu2_bias(float a, float b, float ba, float bb, float& ya,
+                                           float& yb) {
+  const uint64_t x = add2(pk2(a, b), pk2(ba, bb));
+  const uint64_t x2 = mul2(x, x);
+  const uint64_t p = fma2(pk2(kGeluC1, kGeluC1), x2, pk2(1.f, 1.f));
+  const uint64_t arg = mul2(mul2(pk2(kGeluC0, kGeluC0), x), p);
+  float a0, a1;
+  up2(arg, a0, a1);
+  const uint64_t t = pk2(tanh_mufu(a0), tanh_mufu(a1));
+  const uint64_t hx = mul2(pk2(0.5f, 0.5f), x);
+  up2(fma2(hx, t, hx), ya, yb);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
   const float x2 = x * x;
@@ -668,7 +702,7 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) bar_arrive(&act_ready);
-      float head = 0.f;
+      uint64_t head2 = pk2(0.f, 0.f);
       for (int l = 0; l < g.depth; ++l, ++layer_it) {
         if (!bar_wait(&acc_full, layer_it & 1) || *abort_v) {
           *abort_v = 1;
@@ -706,17 +740,18 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
 #pragma unroll
           for (int i = 0; i < 32; i += 4) {
             const float4 b4 = *reinterpret_cast<const float4*>(bl + c0 + i);
-            gelu2(v[i] + b4.x, v[i + 1] + b4.y, v[i], v[i + 1]);
-            gelu2(v[i + 2] + b4.z, v[i + 3] + b4.w, v[i + 2], v[i + 3]);
+            gelu2_bias(v[i], v[i + 1], b4.x, b4.y, v[i], v[i + 1]);
+            gelu2_bias(v[i + 2], v[i + 3], b4.z, b4.w, v[i + 2], v[i + 3]);
           }
           if (last) {
+            // the head on the bf16 activations: even and odd columns in the two lanes
 #pragma unroll
             for (int i = 0; i < 32; i += 4) {
               const float4 w4 = *reinterpret_cast<const float4*>(s_whead + c0 + i);
-              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i])), w4.x, head);
-              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i + 1])), w4.y, head);
-              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i + 2])), w4.z, head);
-              head = fmaf(__bfloat162float(__float2bfloat16_rn(v[i + 3])), w4.w, head);
+              const float2 a01 = __bfloat1622float2(__floats2bfloat162_rn(v[i], v[i + 1]));
+              const float2 a23 = __bfloat1622float2(__floats2bfloat162_rn(v[i + 2], v[i + 3]));
+              head2 = fma2(pk2(a01.x, a01.y), pk2(w4.x, w4.y), head2);
+              head2 = fma2(pk2(a23.x, a23.y), pk2(w4.z, w4.w), head2);
             }
           } else {
             uint8_t* base = act + (c0 >> 6) * (BM * BK * 2);
@@ -744,6 +779,9 @@ __global__ void __launch_bounds__(kFwdThreads, 2)
         }
       }
       if (!ok) break;
+      float head0, head1;
+      up2(head2, head0, head1);
+      const float head = head0 + head1;
       // ---- head: the second half's partial sums reach the first half through shared memory
       if (half == 1) {
         head_part[r] = head;
